@@ -1,0 +1,289 @@
+/*
+ * jitter_gpu.h — C ABI of the GB300 contact pipeline (narrowphase, contact cache,
+ * coloured sequential-impulse solve, integration) for Jitter Physics 2 worlds.
+ *
+ * All entry points are extern "C", take plain pointers and sizes, return an int
+ * status (JG_OK = 0, negative JG_ERR_* on failure) and never throw.  The library
+ * owns every device buffer; the caller passes host buffers that are copied in or
+ * out.  One host thread drives one jg_world (the reference contract "a World has a
+ * single external owner", docfx/docs/documentation/world.md:75-97).
+ *
+ * Each declaration names the reference code it replaces (paths inside the
+ * Jitter2 source tree, src/Jitter2/...).
+ */
+#ifndef JITTER_GPU_H
+#define JITTER_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------- */
+#define JG_OK                 0
+#define JG_ERR_INVALID_ARG   -1  /* ArgumentException, World.Step.cs:157-165            */
+#define JG_ERR_CAPACITY      -2  /* a device pool is full; grow it and retry            */
+#define JG_ERR_NONFINITE     -3  /* NaN/Inf in uploaded or simulated state              */
+#define JG_ERR_TIMEOUT       -4  /* a bounded device-side wait gave up                  */
+#define JG_ERR_CUDA          -5  /* a CUDA runtime call failed                          */
+#define JG_ERR_NOT_SUPPORTED -6  /* feature not available (e.g. no sm_103a device)     */
+#define JG_ERR_INVALID_SHAPE -7  /* InvalidCollisionTypeException, World.Detect.cs:29-59 */
+
+/* ---- enumerations mirroring the reference ---------------------------------------- */
+/* MotionType, Dynamics/RigidBody.cs:75-95 */
+#define JG_MOTION_DYNAMIC   0
+#define JG_MOTION_KINEMATIC 1
+#define JG_MOTION_STATIC    2
+
+/* Shape kinds: BoxShape, SphereShape, CapsuleShape, CylinderShape, ConeShape,
+ * PointCloudShape (VertexSupportMap), TriangleShape (files under Collision/Shapes) */
+#define JG_SHAPE_BOX        0
+#define JG_SHAPE_SPHERE     1
+#define JG_SHAPE_CAPSULE    2
+#define JG_SHAPE_CYLINDER   3
+#define JG_SHAPE_CONE       4
+#define JG_SHAPE_POINTCLOUD 5
+#define JG_SHAPE_TRIANGLE   6
+
+/* Body flag bits (RigidBodyData.Flags layout, Dynamics/RigidBody.cs:180-250) */
+#define JG_BODY_ACTIVE            (1 << 2)
+#define JG_BODY_GYROSCOPIC        (1 << 3)
+#define JG_BODY_LOCKS_SHIFT       4       /* 6 bits: locked motion axes (MotionAxes ^ All) */
+#define JG_BODY_NO_GRAVITY        (1 << 12)
+
+/* Warm start of newly created contacts (no counterpart in the reference, which
+ * always starts new contacts from zero: Contact.cs:727) */
+#define JG_WARMSTART_ZERO   0
+#define JG_WARMSTART_CACHED 1   /* reference behaviour: new = 0, cached = previous impulse */
+#define JG_WARMSTART_MLP    2   /* cached contacts as reference, new contacts from the MLP */
+
+/* Constraint kinds (Dynamics/Constraints/BallSocket.cs, HingeAngle.cs) */
+#define JG_CONSTRAINT_BALLSOCKET 1
+#define JG_CONSTRAINT_HINGEANGLE 2
+
+/* ---- plain data structures ------------------------------------------------------- */
+
+/* World settings (World.cs:333-416, World.Detect.cs:88-122). */
+typedef struct jg_world_params {
+    float   gravity[3];                 /* default (0,-9.81,0), World.cs:389           */
+    int32_t substeps;                   /* SubstepCount, default 1                      */
+    int32_t solver_iterations;          /* SolverIterations.solver, default 6           */
+    int32_t relax_iterations;           /* SolverIterations.relaxation, default 4       */
+    int32_t enable_auxiliary_contacts;  /* EnableAuxiliaryContactPoints, default 1      */
+    int32_t persistent_manifold;        /* PersistentContactManifold, default 1         */
+    float   speculative_relaxation;     /* SpeculativeRelaxationFactor, default 0.9     */
+    int32_t edge_filter;                /* default TriangleEdgeCollisionFilter present  */
+    int32_t warm_start_mode;            /* JG_WARMSTART_*                               */
+    int32_t max_bodies;                 /* device pool capacities (0 = derive)          */
+    int32_t max_shapes;
+    int32_t max_pairs;
+    int32_t max_arbiters;
+    int32_t max_constraints;
+    int32_t solver_block;               /* threads per CTA of the solver (0 = tuned)    */
+    int32_t solver_ctas_per_sm;         /* persistent CTAs per SM (0 = tuned)           */
+    int32_t narrow_tile;                /* lanes per pair in the narrowphase (32)       */
+    int32_t use_graph;                  /* capture the step in a CUDA graph             */
+    int32_t record_residual;            /* record the per-iteration residual (metric)   */
+    int32_t deterministic;              /* sort new arbiters by key every step          */
+} jg_world_params;
+
+/* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the
+ * per-body settings the per-step update reads (RigidBody.cs:380-409, :716-764). */
+typedef struct jg_body_desc {
+    float   position[3];
+    float   orientation[4];             /* quaternion x,y,z,w                            */
+    float   velocity[3];
+    float   angular_velocity[3];
+    float   delta_velocity[3];          /* DeltaVelocity queued by the last update       */
+    float   delta_angular_velocity[3];  /* DeltaAngularVelocity                          */
+    float   inv_inertia[6];             /* local inverse inertia M11 M12 M13 M22 M23 M33 */
+    float   inv_mass;
+    float   friction;                   /* default 0.2                                   */
+    float   restitution;                /* default 0                                     */
+    float   linear_damping;             /* multiplier, default 0.998                     */
+    float   angular_damping;            /* multiplier, default 0.995                     */
+    float   force[3];                   /* cleared after each step (RigidBody.cs:760)    */
+    float   torque[3];
+    int32_t motion_type;                /* JG_MOTION_*                                   */
+    int32_t flags;                      /* JG_BODY_* bits                                */
+    int32_t world;                      /* world index for batched worlds (0 otherwise)  */
+} jg_body_desc;
+
+/* One collision shape attached to a body.  The shape index in the uploaded array is
+ * the reference's ShapeId order (World.Detect.cs:141-144 orders pairs by it). */
+typedef struct jg_shape_desc {
+    int32_t kind;                       /* JG_SHAPE_*                                    */
+    int32_t body;                       /* owning body index                             */
+    float   dims[4];                    /* box: half extents; sphere: r; capsule: r, half length;
+                                           cylinder: r, height; cone: r, height;
+                                           pointcloud: shift xyz                         */
+    float   center[3];                  /* GetCenter(): point cloud centre of mass       */
+    int32_t data_offset;                /* pointcloud: first vertex; triangle: triangle id */
+    int32_t data_count;                 /* pointcloud: vertex count                      */
+} jg_shape_desc;
+
+/* One triangle of a TriangleMesh (Collision/Shapes/TriangleMesh.cs:194-319): mesh-local
+ * vertices, unit normal and the neighbour across edges A (c-b), B (a-c), C (b-a). */
+typedef struct jg_triangle_desc {
+    float   a[3], b[3], c[3];
+    float   normal[3];
+    int32_t neighbor[3];                /* triangle ids, -1 for an open edge             */
+    int32_t pad;
+} jg_triangle_desc;
+
+/* Read-only view of one cached contact point (Contact.cs:585-700). */
+typedef struct jg_contact_view {
+    int32_t shape1, shape2;             /* ArbiterKey (Arbiter.cs:67-103)                */
+    int32_t body1, body2;
+    int32_t slot;                       /* 0..3 within the ContactData                   */
+    int32_t usage_mask;                 /* ContactData.UsageMask                         */
+    int32_t color;                      /* solver colour of the arbiter                  */
+    int32_t flags;
+    float   normal[3], tangent1[3], tangent2[3];
+    float   rel_pos1[3], rel_pos2[3];   /* RelativePosition1/2 (world offsets)           */
+    float   pos1_local[3], pos2_local[3];
+    float   accumulated[3];             /* normal, tangent1, tangent2 impulses           */
+    float   mass[3];
+    float   bias, penalty_bias;
+    float   friction, restitution;
+} jg_contact_view;
+
+/* Per-step counters (SceneBenchmark records pairs/contacts, other/SceneBenchmark/Program.cs:64-71). */
+typedef struct jg_counters {
+    int64_t pairs;                      /* broadphase pairs                              */
+    int64_t colliding;                  /* pairs MPR/EPA reported as colliding           */
+    int64_t manifold_points;            /* contact points written by the manifold        */
+    int64_t arbiters;                   /* arbiters after the step                       */
+    int64_t contacts;                   /* active contact points solved (UsageMask bits) */
+    int64_t new_contacts;
+    int64_t colors;                     /* solver colours                                */
+    int64_t epa_calls;
+    int64_t epa_failures;               /* EPA fell back to MPR (NarrowPhase.cs:82-84)   */
+    int64_t exact_fallbacks;            /* FP64 orientation/normal evaluations           */
+    int64_t status;                     /* JG_ERR_* raised on the device, 0 if none      */
+    int64_t created_arbiters;
+    int64_t removed_arbiters;
+} jg_counters;
+
+/* Stage timings in milliseconds (World.DebugTimings buckets, World.Step.cs:44-81). */
+typedef struct jg_timings {
+    float broadphase, narrowphase, add_arbiter, coloring, solve, update_contacts,
+          update_bodies, total;
+} jg_timings;
+
+typedef struct jg_world jg_world;
+typedef struct jg_batch jg_batch;
+
+/* ---- lifetime ---------------------------------------------------------------------- */
+
+/* Fills defaults equal to a freshly constructed World (World.cs:333-416). */
+int jg_default_params(jg_world_params* params);
+
+/* new World(...) (World.cs:166-230); allocates the device pools. */
+int jg_create(const jg_world_params* params, jg_world** out_world);
+/* World.Dispose (World.cs:281-299). */
+int jg_destroy(jg_world* world);
+
+/* ---- state upload / download -------------------------------------------------------- */
+
+/* World.CreateRigidBody + RigidBody setters (World.cs:930-965, RigidBody.cs:503-760). */
+int jg_upload_bodies(jg_world* world, const jg_body_desc* bodies, int32_t count);
+int jg_download_bodies(jg_world* world, jg_body_desc* bodies, int32_t count);
+
+/* RigidBody.AddShape (RigidBody.cs:1440-1520); vertices for point clouds, triangles
+ * for meshes.  Uploading shapes clears the contact cache. */
+int jg_upload_shapes(jg_world* world, const jg_shape_desc* shapes, int32_t count,
+                     const float* hull_vertices, int32_t hull_vertex_count,
+                     const jg_triangle_desc* triangles, int32_t triangle_count);
+
+/* RigidBody.Position/Orientation/Velocity setters; field: 0 position, 1 orientation,
+ * 2 velocity, 3 angular velocity, 4 force, 5 torque.  Position/orientation follow
+ * RigidBody.Move (RigidBody.cs:637-648): the body's contact cache is cleared. */
+int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value);
+
+/* World.CreateConstraint<BallSocket/HingeAngle> + Initialize (BallSocket.cs:120-138,
+ * HingeAngle.cs:84-110).  init: BallSocket anchor xyz; HingeAngle axis xyz, min, max. */
+int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,
+                      const float* init, int32_t* out_id);
+
+/* ---- the step ------------------------------------------------------------------------- */
+
+/* World.Step(dt) from DynamicTree.EnumerateOverlaps through DynamicTree.Update
+ * (World.Step.cs:153-296): broadphase, narrowphase + manifold, arbiter merge,
+ * colouring, substepped solve + integration, contact and body update. */
+int jg_step(jg_world* world, float dt);
+
+/* Like jg_step but with the body state taken from and returned to host buffers
+ * (copies included), the call a host that keeps its own bodies makes. */
+int jg_step_host(jg_world* world, float dt, jg_body_desc* bodies, int32_t count);
+
+/* ---- inspection ------------------------------------------------------------------------ */
+
+/* Arbiter/ContactData view (World.RawData, World.cs:95-141).  Writes up to capacity
+ * entries; *out_count receives the number of active contact points. */
+int jg_get_contacts(jg_world* world, jg_contact_view* out, int32_t capacity, int32_t* out_count);
+/* Arbiter keys created and removed during the last step (BeginCollide/EndCollide). */
+int jg_get_arbiter_events(jg_world* world, int32_t* created_pairs, int32_t created_capacity,
+                          int32_t* n_created, int32_t* removed_pairs, int32_t removed_capacity,
+                          int32_t* n_removed);
+int jg_get_counters(jg_world* world, jg_counters* out);
+int jg_get_timings(jg_world* world, jg_timings* out);
+/* Per-iteration residual of the first substep of the last step (record_residual=1):
+ * r_k = |lambda_k - lambda_{k-1}| / max(|lambda_k|, 1e-12) over all contact rows. */
+int jg_get_residuals(jg_world* world, float* out, int32_t capacity, int32_t* out_count);
+
+/* Full state dump for checkpoints and one-step comparisons (no reference counterpart;
+ * World.Stabilize, World.Step.cs:318-392, re-solves restored contacts). */
+int jg_export_state(jg_world* world, void* buffer, int64_t capacity, int64_t* out_size);
+int jg_import_state(jg_world* world, const void* buffer, int64_t size);
+
+/* ---- learned warm start (no reference counterpart) ---------------------------------------- */
+
+/* Loads MLP weights 24->64->64->3 (BF16 stored, given as float): W1[64x24], b1[64],
+ * W2[64x64], b2[64], W3[3x64], b3[3], plus feature mean/scale[24] and output scale[3]. */
+int jg_mlp_load(jg_world* world, const float* params, int32_t count);
+/* Predicts impulses for n feature rows (24 floats each), writes 3 floats per row. */
+int jg_mlp_predict(jg_world* world, const float* features, int32_t n, float* out);
+/* One Adam step over a minibatch of (features, targets) held in host memory;
+ * returns the mean squared error of the minibatch before the update. */
+int jg_mlp_train_step(jg_world* world, const float* features, const float* targets,
+                      int32_t n, float learning_rate, float* out_loss);
+/* Exports the current float parameters in the jg_mlp_load layout. */
+int jg_mlp_export(jg_world* world, float* params, int32_t capacity, int32_t* out_count);
+/* Gradients of the minibatch MSE with respect to every parameter (jg_mlp_load layout). */
+int jg_mlp_gradients(jg_world* world, const float* features, const float* targets,
+                     int32_t n, float* out_grads, int32_t capacity, float* out_loss);
+/* Collects (features, converged impulse) training pairs of contacts created during
+ * the last step: up to capacity rows of 24 + 3 floats. */
+int jg_collect_training(jg_world* world, float* features, float* targets, int32_t capacity,
+                        int32_t* out_count);
+
+/* ---- batched worlds (no reference counterpart) ---------------------------------------------- */
+
+/* Many independent worlds stepped by one captured launch sequence.  Bodies, shapes and
+ * constraints carry their world index; all worlds share params and dt. */
+int jg_batch_create(const jg_world_params* params, int32_t n_worlds, jg_world** out_world);
+int jg_batch_step(jg_world* world, float dt);
+/* Autotunes solver block shape / CTAs per SM and narrowphase tile for this world by
+ * timing a few steps of a copy of its state; writes the chosen values into params. */
+int jg_autotune(jg_world* world, float dt, int32_t steps, jg_world_params* chosen);
+
+/* ---- host utilities ------------------------------------------------------------------------- */
+
+/* Shape mass properties, CalculateMassInertia of each shape (BoxShape.cs:188-199,
+ * SphereShape.cs:100-111, CapsuleShape.cs:112-129, CylinderShape.cs:122-133,
+ * ConeShape.cs:128-138, ShapeHelper.cs:399-412 for point clouds).  Host only. */
+int jg_shape_mass_inertia(const jg_shape_desc* shape, const float* hull_vertices,
+                          float* inertia6, float* com3, float* mass);
+
+/* Last CUDA error string of this thread (static storage). */
+const char* jg_last_error(void);
+/* Library version string. */
+const char* jg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JITTER_GPU_H */

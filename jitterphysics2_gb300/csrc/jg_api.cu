@@ -1,0 +1,780 @@
+// The C ABI (include/jitter_gpu.h): world lifetime, state upload/download, the step
+// driver and inspection.  One jg_world owns one CUDA stream and all of its device pools;
+// every call returns a status and never throws.  The step is a fixed launch sequence
+// whose sizes live in device memory, so it can be captured once per arbiter-buffer parity
+// into a CUDA graph and replayed.
+#include "jg_world.cuh"
+#include <cstring>
+#include <cmath>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include <chrono>
+
+void jg_contacts_set_scratch(int2* created, int2* removed, int* remaining, int* dst_index);
+void jg_flip_store(WorldDev& w);
+void jg_launch_count_contacts(WorldDev& w, cudaStream_t s, int nsm);
+void jg_launch_update_contacts(WorldDev& w, cudaStream_t s, int nsm);
+void jg_solver_reset_launch_cache();
+int jg_mlp_alloc(WorldDev& w);
+int jg_mlp_launch_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+
+static thread_local std::string g_err;
+
+struct jg_world {
+    jg_world_params prm{};
+    WorldDev d{};
+    cudaStream_t stream = nullptr;
+    int device = 0, nsm = 0;
+    DevCounters* h_ctr = nullptr;     // pinned
+    int2 *ev_created = nullptr, *ev_removed = nullptr;
+    int* remaining = nullptr;
+    int* dst_index = nullptr;
+    std::vector<jg_body_desc> host_bodies;
+    std::vector<jg_shape_desc> host_shapes;
+    int nj_host = 0;
+    cudaEvent_t ev[9]{};
+    jg_timings timings{};
+    jg_counters counters{};
+    cudaGraphExec_t graph[2]{nullptr, nullptr};
+    float graph_dt[2]{-1.f, -1.f};
+    int nworlds = 1;
+    std::vector<void*> allocs;
+    bool mlp_ready = false;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return JG_ERR_CUDA;
+}
+#define CK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return cuda_fail(_e, #x); } while (0)
+
+template <class T> int dalloc(jg_world* w, T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    cudaMemsetAsync(*p, 0, sizeof(T) * count, w->stream);
+    w->allocs.push_back(*p);
+    return JG_OK;
+}
+#define DA(ptr, n) do { int _r = dalloc(w, &(ptr), (size_t)(n)); if (_r) return _r; } while (0)
+
+int alloc_store(jg_world* w, ArbStore& A, int cap) {
+    DA(A.key, cap); DA(A.body, cap); DA(A.info, cap); DA(A.mat, cap);
+    DA(A.cn, 4 * cap); DA(A.ct1, 4 * cap); DA(A.ct2, 4 * cap); DA(A.cr1, 4 * cap);
+    DA(A.cr2, 4 * cap); DA(A.cacc, 4 * cap); DA(A.cp1, 4 * cap); DA(A.cp2, 4 * cap);
+    return JG_OK;
+}
+
+int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
+
+int allocate(jg_world* w) {
+    WorldDev& d = w->d;
+    const jg_world_params& p = w->prm;
+    d.cap_bodies = std::max(p.max_bodies, 16);
+    d.cap_shapes = std::max(p.max_shapes, 16);
+    d.cap_pairs = std::max(p.max_pairs, 1024);
+    d.cap_arb = std::max(p.max_arbiters, 1024);
+    d.cap_joints = std::max(p.max_constraints, 16);
+    d.cap_hull = 64;
+    d.cap_tris = 16;
+    DA(d.body, d.cap_bodies); DA(d.pos, d.cap_bodies); DA(d.q, d.cap_bodies); DA(d.dv, d.cap_bodies);
+    DA(d.dw, d.cap_bodies); DA(d.il0, d.cap_bodies); DA(d.il1, d.cap_bodies); DA(d.force, d.cap_bodies);
+    DA(d.torque, d.cap_bodies); DA(d.mat, d.cap_bodies); DA(d.binfo, d.cap_bodies);
+    DA(d.sinfo, d.cap_shapes); DA(d.sdims, d.cap_shapes); DA(d.scenter, d.cap_shapes);
+    DA(d.amin, d.cap_shapes); DA(d.amax, d.cap_shapes);
+    DA(d.mkey, d.cap_shapes); DA(d.mkey_alt, d.cap_shapes); DA(d.midx, d.cap_shapes); DA(d.midx_alt, d.cap_shapes);
+    int rs_blocks = (d.cap_shapes + 2047) / 2048;
+    DA(d.hist, std::max(256 * rs_blocks + 1, 8192));
+    DA(d.node, d.cap_shapes); DA(d.node_range, d.cap_shapes); DA(d.nmin, d.cap_shapes); DA(d.nmax, d.cap_shapes);
+    DA(d.leaf_parent, d.cap_shapes); DA(d.node_flag, d.cap_shapes);
+    DA(d.scene_box, 2);
+    DA(d.pairs, d.cap_pairs);
+    DA(d.cs_key, d.cap_pairs); DA(d.cs_n, d.cap_pairs); DA(d.cs_pa, 4 * (size_t)d.cap_pairs); DA(d.cs_pb, 4 * (size_t)d.cap_pairs);
+    int r;
+    if ((r = alloc_store(w, d.arb[0], d.cap_arb))) return r;
+    if ((r = alloc_store(w, d.arb[1], d.cap_arb))) return r;
+    d.cur = 0;
+    d.hcap = next_pow2(2 * d.cap_arb);
+    DA(d.hkeys, d.hcap); DA(d.hvals, d.hcap);
+    DA(d.cstat, d.cap_arb + d.cap_joints);
+    DA(d.bmask, 2 * (size_t)d.cap_bodies);
+    DA(d.adj_off, d.cap_bodies + 1);
+    DA(d.adj, 2 * ((size_t)d.cap_arb + d.cap_joints));
+    DA(d.deg, d.cap_bodies);
+    DA(d.color_count, JG_MAX_COLORS + 1); DA(d.color_start, JG_MAX_COLORS + 1); DA(d.jcolor_start, JG_MAX_COLORS + 1);
+    DA(d.color_cursor, JG_MAX_COLORS + 1);
+    DA(d.jorder, d.cap_joints + JG_MAX_COLORS);
+    DA(d.joints, d.cap_joints);
+    DA(d.bar_count, 2); d.bar_gen = d.bar_count + 1;
+    DA(d.resid, 2 * 64);
+    DA(d.ctr, 1);
+    DA(w->ev_created, d.cap_arb); DA(w->ev_removed, d.cap_arb); DA(w->remaining, 2); DA(w->dst_index, d.cap_arb);
+    CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));
+    memset(w->h_ctr, 0, sizeof(DevCounters));
+    return JG_OK;
+}
+
+int ensure_hull(jg_world* w, int n) {
+    if (n <= w->d.cap_hull && w->d.hull) return JG_OK;
+    w->d.cap_hull = std::max(n, 64);
+    DA(w->d.hull, w->d.cap_hull);
+    return JG_OK;
+}
+int ensure_tris(jg_world* w, int n) {
+    if (n <= w->d.cap_tris && w->d.tris) return JG_OK;
+    w->d.cap_tris = std::max(n, 16);
+    DA(w->d.tris, w->d.cap_tris);
+    return JG_OK;
+}
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+float host_int_as_float(int i) { float f; memcpy(&f, &i, 4); return f; }
+int host_float_as_int(float f) { int i; memcpy(&i, &f, 4); return i; }
+
+// RigidBody.UpdateWorldInertia (RigidBody.cs:903-923) on the host, for uploads.
+void host_world_inertia(const jg_body_desc& b, float* i0, float* i1, float* imv) {
+    float x = b.orientation[0], y = b.orientation[1], z = b.orientation[2], ww = b.orientation[3];
+    m33 R;
+    R.m[0][0] = 1.0f - 2.0f * (y * y + z * z); R.m[0][1] = 2.0f * (x * y - z * ww); R.m[0][2] = 2.0f * (x * z + y * ww);
+    R.m[1][0] = 2.0f * (x * y + z * ww); R.m[1][1] = 1.0f - 2.0f * (x * x + z * z); R.m[1][2] = 2.0f * (y * z - x * ww);
+    R.m[2][0] = 2.0f * (x * z - y * ww); R.m[2][1] = 2.0f * (y * z + x * ww); R.m[2][2] = 1.0f - 2.0f * (x * x + y * y);
+    sym6 L{b.inv_inertia[0], b.inv_inertia[1], b.inv_inertia[2], b.inv_inertia[3], b.inv_inertia[4], b.inv_inertia[5]};
+    sym6 I = sym_transform(L, R);
+    int axes = 63 ^ ((b.flags >> 4) & 63);
+    if (((b.flags >> 4) & 56) != 0) {
+        if ((axes & 56) == 0) { I = sym6{0, 0, 0, 0, 0, 0}; }
+        else {
+            if (!(axes & 8)) { if (I.m11 > 0) { float xy = I.m12 / I.m11, xz = I.m13 / I.m11; I.m22 -= xy * I.m12; I.m23 -= xy * I.m13; I.m33 -= xz * I.m13; } I.m11 = I.m12 = I.m13 = 0; }
+            if (!(axes & 16)) { if (I.m22 > 0) { float xy = I.m12 / I.m22, yz = I.m23 / I.m22; I.m11 -= xy * I.m12; I.m13 -= xy * I.m23; I.m33 -= yz * I.m23; } I.m12 = I.m22 = I.m23 = 0; }
+            if (!(axes & 32)) { if (I.m33 > 0) { float xz = I.m13 / I.m33, yz = I.m23 / I.m33; I.m11 -= xz * I.m13; I.m12 -= xz * I.m23; I.m22 -= yz * I.m23; } I.m13 = I.m23 = I.m33 = 0; }
+        }
+    }
+    imv[0] = imv[1] = imv[2] = b.inv_mass;
+    if (!(axes & 1)) imv[0] = 0;
+    if (!(axes & 2)) imv[1] = 0;
+    if (!(axes & 4)) imv[2] = 0;
+    if (b.motion_type != JG_MOTION_DYNAMIC) { I = sym6{0, 0, 0, 0, 0, 0}; imv[0] = imv[1] = imv[2] = 0; }
+    i0[0] = I.m11; i0[1] = I.m12; i0[2] = I.m13; i0[3] = I.m22;
+    i1[0] = I.m23; i1[1] = I.m33;
+}
+
+__global__ void k_reset_counters(DevCounters* c) {
+    int narb = c->narb;
+    DevCounters z;
+    memset(&z, 0, sizeof(z));
+    z.narb = narb;
+    *c = z;
+}
+
+StepParams make_params(const jg_world* w, float dt) {
+    StepParams sp;
+    const jg_world_params& p = w->prm;
+    sp.dt = dt;
+    sp.substeps = p.substeps;
+    sp.sub_dt = dt / (float)p.substeps;
+    sp.inv_dt = dt > 0 ? 1.0f / dt : 0;
+    sp.inv_sub_dt = sp.sub_dt > 0 ? 1.0f / sp.sub_dt : 0;
+    sp.gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    sp.iterations = p.solver_iterations;
+    sp.relax = p.relax_iterations;
+    sp.aux_contacts = p.enable_auxiliary_contacts;
+    sp.persistent = p.persistent_manifold;
+    sp.edge_filter = p.edge_filter;
+    sp.spec_relax = p.speculative_relaxation;
+    sp.warm_start = p.warm_start_mode;
+    sp.record_residual = p.record_residual;
+    return sp;
+}
+
+// The launch sequence of one step.  `timed` records stage events (not inside graphs).
+int launch_step(jg_world* w, const StepParams& sp, bool timed) {
+    WorldDev& d = w->d;
+    cudaStream_t s = w->stream;
+    jg_contacts_set_scratch(w->ev_created, w->ev_removed, w->remaining, w->dst_index);
+    if (timed) cudaEventRecord(w->ev[0], s);
+    k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
+    if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 128, s);
+    jg_launch_aabb(d, s);
+    jg_launch_broadphase(d, s, w->nsm);
+    if (timed) cudaEventRecord(w->ev[1], s);
+    jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
+    if (timed) cudaEventRecord(w->ev[2], s);
+    jg_launch_merge(d, sp, s, w->nsm);
+    if (sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) jg_mlp_launch_warmstart(d, sp, s, w->nsm);
+    if (timed) cudaEventRecord(w->ev[3], s);
+    jg_launch_color(d, s, w->nsm);
+    jg_flip_store(d);
+    if (timed) cudaEventRecord(w->ev[4], s);
+    jg_launch_count_contacts(d, s, w->nsm);
+    if (jg_launch_solve(d, sp, s, w->nsm, w->prm.solver_block, w->prm.solver_ctas_per_sm) < 0) {
+        g_err = "cooperative launch of the solver failed";
+        return JG_ERR_CUDA;
+    }
+    if (timed) cudaEventRecord(w->ev[5], s);
+    jg_launch_update_contacts(d, s, w->nsm);
+    if (timed) cudaEventRecord(w->ev[6], s);
+    jg_launch_update(d, sp, s, w->nsm);
+    if (timed) cudaEventRecord(w->ev[7], s);
+    return JG_OK;
+}
+
+int finish_step(jg_world* w, bool timed) {
+    CK(cudaMemcpyAsync(w->h_ctr, w->d.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    CK(cudaGetLastError());
+    const DevCounters& c = *w->h_ctr;
+    jg_counters& o = w->counters;
+    o.pairs = c.npairs; o.colliding = c.nstream; o.manifold_points = c.points; o.arbiters = c.narb;
+    o.contacts = c.contacts; o.new_contacts = c.new_contacts; o.colors = c.ncolors; o.epa_calls = c.nepa;
+    o.epa_failures = c.epa_fail; o.exact_fallbacks = c.exact; o.status = c.status;
+    o.created_arbiters = c.nnew; o.removed_arbiters = c.nremoved;
+    if (timed) {
+        float t[8];
+        for (int i = 0; i < 7; i++) cudaEventElapsedTime(&t[i], w->ev[i], w->ev[i + 1]);
+        jg_timings& tm = w->timings;
+        tm.broadphase = t[0]; tm.narrowphase = t[1]; tm.add_arbiter = t[2]; tm.coloring = t[3];
+        tm.solve = t[4]; tm.update_contacts = t[5]; tm.update_bodies = t[6];
+        cudaEventElapsedTime(&tm.total, w->ev[0], w->ev[7]);
+    }
+    if (c.status != 0) {
+        g_err = "device status " + std::to_string(c.status);
+        return c.status;
+    }
+    return JG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* jg_last_error(void) { return g_err.c_str(); }
+const char* jg_version(void) { return "jitter-gb300 0.1 (sm_103a)"; }
+
+int jg_default_params(jg_world_params* p) {
+    if (!p) return JG_ERR_INVALID_ARG;
+    memset(p, 0, sizeof(*p));
+    p->gravity[0] = 0; p->gravity[1] = -9.81f; p->gravity[2] = 0;
+    p->substeps = 1;
+    p->solver_iterations = 6;
+    p->relax_iterations = 4;
+    p->enable_auxiliary_contacts = 1;
+    p->persistent_manifold = 1;
+    p->speculative_relaxation = 0.9f;
+    p->edge_filter = 1;
+    p->warm_start_mode = JG_WARMSTART_CACHED;
+    p->narrow_tile = 32;
+    return JG_OK;
+}
+
+int jg_create(const jg_world_params* params, jg_world** out) {
+    if (!params || !out) return JG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (params->substeps < 1 || params->solver_iterations < 1 || params->relax_iterations < 0) return JG_ERR_INVALID_ARG;
+    if (params->solver_iterations > 64) return JG_ERR_INVALID_ARG;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) { g_err = "no CUDA device"; return JG_ERR_NOT_SUPPORTED; }
+    jg_world* w = new jg_world();
+    w->prm = *params;
+    cudaGetDevice(&w->device);
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, w->device);
+    if (prop.major < 10) { delete w; g_err = "needs an sm_103a (Blackwell) device"; return JG_ERR_NOT_SUPPORTED; }
+    w->nsm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { delete w; return JG_ERR_CUDA; }
+    for (int i = 0; i < 9; i++) cudaEventCreate(&w->ev[i]);
+    int r = allocate(w);
+    if (r) { jg_destroy(w); return r; }
+    w->d.nworlds = 1;
+    cudaStreamSynchronize(w->stream);
+    *out = w;
+    return JG_OK;
+}
+
+int jg_batch_create(const jg_world_params* params, int32_t n_worlds, jg_world** out) {
+    if (n_worlds < 1) return JG_ERR_INVALID_ARG;
+    int r = jg_create(params, out);
+    if (r) return r;
+    (*out)->nworlds = n_worlds;
+    (*out)->d.nworlds = n_worlds;
+    return JG_OK;
+}
+
+int jg_destroy(jg_world* w) {
+    if (!w) return JG_ERR_INVALID_ARG;
+    for (int i = 0; i < 2; i++) if (w->graph[i]) cudaGraphExecDestroy(w->graph[i]);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (void* p : w->allocs) cudaFree(p);
+    if (w->h_ctr) cudaFreeHost(w->h_ctr);
+    for (int i = 0; i < 9; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return JG_OK;
+}
+
+static void invalidate_graphs(jg_world* w) {
+    for (int i = 0; i < 2; i++) {
+        if (w->graph[i]) cudaGraphExecDestroy(w->graph[i]);
+        w->graph[i] = nullptr;
+        w->graph_dt[i] = -1.f;
+    }
+}
+
+int jg_upload_bodies(jg_world* w, const jg_body_desc* b, int32_t n) {
+    if (!w || (!b && n > 0) || n < 0) return JG_ERR_INVALID_ARG;
+    if (n > w->d.cap_bodies) return JG_ERR_CAPACITY;
+    std::vector<SBody> sb(n);
+    std::vector<float4> pos(n), q(n), dv(n), dw(n), il0(n), il1(n), force(n), torque(n), mat(n);
+    std::vector<int4> info(n);
+    int maxworld = 0;
+    for (int i = 0; i < n; i++) {
+        const jg_body_desc& d = b[i];
+        if (!finite3(d.position) || !finite3(d.velocity) || !finite3(d.angular_velocity) ||
+            !std::isfinite(d.orientation[3]) || !finite3(d.orientation) || !std::isfinite(d.inv_mass))
+            return JG_ERR_NONFINITE;
+        if (d.motion_type < 0 || d.motion_type > 2) return JG_ERR_INVALID_ARG;
+        if (d.world < 0 || d.world >= w->nworlds) return JG_ERR_INVALID_ARG;
+        maxworld = std::max(maxworld, d.world);
+        float i0[4], i1[2], imv[3];
+        host_world_inertia(d, i0, i1, imv);
+        int fl = 0;
+        if (d.motion_type == JG_MOTION_DYNAMIC) fl |= SB_DYNAMIC;
+        if (d.motion_type == JG_MOTION_DYNAMIC && ((d.flags >> 4) & 7)) fl |= SB_LINLOCK;
+        sb[i].v = make_float4(d.velocity[0], d.velocity[1], d.velocity[2], imv[0]);
+        sb[i].w = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], imv[1]);
+        sb[i].i0 = make_float4(i0[0], i0[1], i0[2], i0[3]);
+        sb[i].i1 = make_float4(i1[0], i1[1], imv[2], host_int_as_float(fl));
+        pos[i] = make_float4(d.position[0], d.position[1], d.position[2], 0.f);
+        q[i] = make_float4(d.orientation[0], d.orientation[1], d.orientation[2], d.orientation[3]);
+        dv[i] = make_float4(d.delta_velocity[0], d.delta_velocity[1], d.delta_velocity[2], 0.f);
+        dw[i] = make_float4(d.delta_angular_velocity[0], d.delta_angular_velocity[1], d.delta_angular_velocity[2], 0.f);
+        il0[i] = make_float4(d.inv_inertia[0], d.inv_inertia[1], d.inv_inertia[2], d.inv_inertia[3]);
+        il1[i] = make_float4(d.inv_inertia[4], d.inv_inertia[5], d.inv_mass, 0.f);
+        force[i] = make_float4(d.force[0], d.force[1], d.force[2], 0.f);
+        torque[i] = make_float4(d.torque[0], d.torque[1], d.torque[2], 0.f);
+        mat[i] = make_float4(d.friction, d.restitution, d.linear_damping, d.angular_damping);
+        info[i] = make_int4(d.motion_type, d.flags, d.world, 0);
+    }
+    WorldDev& D = w->d;
+    cudaStream_t s = w->stream;
+    CK(cudaMemcpyAsync(D.body, sb.data(), sizeof(SBody) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.pos, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.q, q.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.dv, dv.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.dw, dw.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.il0, il0.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.il1, il1.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.force, force.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.torque, torque.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.mat, mat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.binfo, info.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    if (D.nb != n) invalidate_graphs(w);
+    D.nb = n;
+    w->host_bodies.assign(b, b + n);
+    return JG_OK;
+}
+
+int jg_download_bodies(jg_world* w, jg_body_desc* b, int32_t n) {
+    if (!w || (!b && n > 0) || n < 0 || n > w->d.nb) return JG_ERR_INVALID_ARG;
+    WorldDev& D = w->d;
+    std::vector<SBody> sb(n);
+    std::vector<float4> pos(n), q(n), dv(n), dw(n);
+    cudaStream_t s = w->stream;
+    CK(cudaMemcpyAsync(sb.data(), D.body, sizeof(SBody) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(pos.data(), D.pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(q.data(), D.q, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(dv.data(), D.dv, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(dw.data(), D.dw, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; i++) {
+        jg_body_desc& o = b[i];
+        if (i < (int)w->host_bodies.size()) o = w->host_bodies[i];
+        o.position[0] = pos[i].x; o.position[1] = pos[i].y; o.position[2] = pos[i].z;
+        o.orientation[0] = q[i].x; o.orientation[1] = q[i].y; o.orientation[2] = q[i].z; o.orientation[3] = q[i].w;
+        o.velocity[0] = sb[i].v.x; o.velocity[1] = sb[i].v.y; o.velocity[2] = sb[i].v.z;
+        o.angular_velocity[0] = sb[i].w.x; o.angular_velocity[1] = sb[i].w.y; o.angular_velocity[2] = sb[i].w.z;
+        o.delta_velocity[0] = dv[i].x; o.delta_velocity[1] = dv[i].y; o.delta_velocity[2] = dv[i].z;
+        o.delta_angular_velocity[0] = dw[i].x; o.delta_angular_velocity[1] = dw[i].y; o.delta_angular_velocity[2] = dw[i].z;
+        o.force[0] = o.force[1] = o.force[2] = 0;
+        o.torque[0] = o.torque[1] = o.torque[2] = 0;
+    }
+    return JG_OK;
+}
+
+int jg_upload_shapes(jg_world* w, const jg_shape_desc* sh, int32_t n, const float* hull, int32_t nh,
+                     const jg_triangle_desc* tris, int32_t nt) {
+    if (!w || n < 0 || nh < 0 || nt < 0 || (n > 0 && !sh)) return JG_ERR_INVALID_ARG;
+    if (n > w->d.cap_shapes) return JG_ERR_CAPACITY;
+    std::vector<int4> info(n);
+    std::vector<float4> dims(n), cen(n);
+    for (int i = 0; i < n; i++) {
+        const jg_shape_desc& s = sh[i];
+        if (s.kind < 0 || s.kind > JG_SHAPE_TRIANGLE) { g_err = "invalid shape kind"; return JG_ERR_INVALID_SHAPE; }
+        if (s.body < 0 || s.body >= w->d.nb) return JG_ERR_INVALID_ARG;
+        if (s.kind == JG_SHAPE_POINTCLOUD) {
+            if (s.data_offset < 0 || s.data_count < 1 || s.data_offset + s.data_count > nh) return JG_ERR_INVALID_ARG;
+        }
+        if (s.kind == JG_SHAPE_TRIANGLE && (s.data_offset < 0 || s.data_offset >= nt)) return JG_ERR_INVALID_ARG;
+        info[i] = make_int4(s.kind, s.body, s.data_offset, s.data_count);
+        dims[i] = make_float4(s.dims[0], s.dims[1], s.dims[2], s.dims[3]);
+        cen[i] = make_float4(s.center[0], s.center[1], s.center[2], 0.f);
+    }
+    int r;
+    if ((r = ensure_hull(w, nh))) return r;
+    if ((r = ensure_tris(w, nt))) return r;
+    std::vector<float4> hv(nh);
+    for (int i = 0; i < nh; i++) hv[i] = make_float4(hull[3 * i], hull[3 * i + 1], hull[3 * i + 2], 0.f);
+    std::vector<TriDev> td(nt);
+    for (int i = 0; i < nt; i++) {
+        const jg_triangle_desc& t = tris[i];
+        td[i].a = make_float4(t.a[0], t.a[1], t.a[2], 0.f);
+        td[i].b = make_float4(t.b[0], t.b[1], t.b[2], 0.f);
+        td[i].c = make_float4(t.c[0], t.c[1], t.c[2], 0.f);
+        td[i].n = make_float4(t.normal[0], t.normal[1], t.normal[2], 0.f);
+        for (int k = 0; k < 3; k++) {
+            int nb = t.neighbor[k];
+            if (nb >= 0 && nb < nt) td[i].nb[k] = make_float4(tris[nb].normal[0], tris[nb].normal[1], tris[nb].normal[2], 1.f);
+            else td[i].nb[k] = make_float4(0, 0, 0, 0.f);
+        }
+    }
+    WorldDev& D = w->d;
+    cudaStream_t s = w->stream;
+    CK(cudaMemcpyAsync(D.sinfo, info.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.sdims, dims.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.scenter, cen.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    if (nh) CK(cudaMemcpyAsync(D.hull, hv.data(), sizeof(float4) * nh, cudaMemcpyHostToDevice, s));
+    if (nt) CK(cudaMemcpyAsync(D.tris, td.data(), sizeof(TriDev) * nt, cudaMemcpyHostToDevice, s));
+    // new shape ids: the contact cache starts empty
+    int zero = 0;
+    CK(cudaMemcpyAsync(&D.ctr->narb, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    D.ns = n; D.nhull = nh; D.ntris = nt;
+    w->host_shapes.assign(sh, sh + n);
+    invalidate_graphs(w);
+    return JG_OK;
+}
+
+int jg_set_body(jg_world* w, int32_t body, int32_t field, const float* v) {
+    if (!w || !v || body < 0 || body >= w->d.nb || field < 0 || field > 5) return JG_ERR_INVALID_ARG;
+    jg_body_desc d;
+    int r = jg_download_bodies(w, w->host_bodies.data(), w->d.nb);
+    if (r) return r;
+    d = w->host_bodies[body];
+    switch (field) {
+        case 0: memcpy(d.position, v, 12); break;
+        case 1: memcpy(d.orientation, v, 16); break;
+        case 2: memcpy(d.velocity, v, 12); break;
+        case 3: memcpy(d.angular_velocity, v, 12); break;
+        case 4: memcpy(d.force, v, 12); break;
+        case 5: memcpy(d.torque, v, 12); break;
+    }
+    w->host_bodies[body] = d;
+    std::vector<jg_body_desc> all = w->host_bodies;
+    r = jg_upload_bodies(w, all.data(), (int)all.size());
+    if (r) return r;
+    if (field <= 1) {
+        // RigidBody.Move (RigidBody.cs:637-648): clear the contact cache of the body
+        std::vector<int2> bodies(w->d.ctr ? 0 : 0);
+        WorldDev& D = w->d;
+        int narb = 0;
+        CK(cudaMemcpy(&narb, &D.ctr->narb, sizeof(int), cudaMemcpyDeviceToHost));
+        if (narb > 0) {
+            std::vector<int2> bb(narb);
+            std::vector<int4> info(narb);
+            const ArbStore& A = D.arb[D.cur];
+            CK(cudaMemcpy(bb.data(), A.body, sizeof(int2) * narb, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(info.data(), A.info, sizeof(int4) * narb, cudaMemcpyDeviceToHost));
+            for (int a = 0; a < narb; a++) if (bb[a].x == body || bb[a].y == body) info[a].x = 0;
+            CK(cudaMemcpy(A.info, info.data(), sizeof(int4) * narb, cudaMemcpyHostToDevice));
+        }
+    }
+    return JG_OK;
+}
+
+int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
+    if (!w || !init) return JG_ERR_INVALID_ARG;
+    if (kind != JG_CONSTRAINT_BALLSOCKET && kind != JG_CONSTRAINT_HINGEANGLE) return JG_ERR_INVALID_ARG;
+    if (b1 < 0 || b2 < 0 || b1 >= w->d.nb || b2 >= w->d.nb || b1 == b2) return JG_ERR_INVALID_ARG;
+    if (w->nj_host >= w->d.cap_joints) return JG_ERR_CAPACITY;
+    jg_body_desc bd[2];
+    int r;
+    std::vector<jg_body_desc> all(w->d.nb);
+    if ((r = jg_download_bodies(w, all.data(), w->d.nb))) return r;
+    bd[0] = all[b1]; bd[1] = all[b2];
+    JointDev J;
+    memset(&J, 0, sizeof(J));
+    J.hdr = make_int4(kind, b1, b2, 0);
+    q4 q1{bd[0].orientation[0], bd[0].orientation[1], bd[0].orientation[2], bd[0].orientation[3]};
+    q4 q2{bd[1].orientation[0], bd[1].orientation[1], bd[1].orientation[2], bd[1].orientation[3]};
+    v3 p1 = mk3(bd[0].position[0], bd[0].position[1], bd[0].position[2]);
+    v3 p2 = mk3(bd[1].position[0], bd[1].position[1], bd[1].position[2]);
+    if (kind == JG_CONSTRAINT_BALLSOCKET) {
+        // BallSocket.Initialize (BallSocket.cs:120-138)
+        v3 anchor = mk3(init[0], init[1], init[2]);
+        J.la1 = f4(rotate_inv(anchor - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(anchor - p2, q2), 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+    } else {
+        // HingeAngle.Initialize (HingeAngle.cs:84-110)
+        v3 axis = normalize(mk3(init[0], init[1], init[2]));
+        float from = init[3], to = init[4];
+        J.prm = make_float4(0.2f, 0.001f, 0.1f, 0.001f);
+        J.lim = make_float4(from / 2.0f, to / 2.0f, 0.25f * from + 0.25f * to, 0.f);
+        J.axis = f4(rotate_inv(axis, q2), 0.f);
+        J.q0 = f4(qmul(qconj(q2), q1));
+    }
+    CK(cudaMemcpy(w->d.joints + w->nj_host, &J, sizeof(J), cudaMemcpyHostToDevice));
+    if (out_id) *out_id = w->nj_host;
+    w->nj_host++;
+    w->d.nj = w->nj_host;
+    invalidate_graphs(w);
+    return JG_OK;
+}
+
+int jg_step(jg_world* w, float dt) {
+    if (!w) return JG_ERR_INVALID_ARG;
+    if (!std::isfinite(dt)) return JG_ERR_NONFINITE;
+    if (dt < 0) return JG_ERR_INVALID_ARG;
+    if (dt < 1.401298e-45f) return JG_OK;
+    StepParams sp = make_params(w, dt);
+    if (w->d.ns == 0 && w->d.nb == 0) return JG_OK;
+    int parity = w->d.cur;
+    if (w->prm.use_graph) {
+        if (!w->graph[parity] || w->graph_dt[parity] != dt) {
+            if (w->graph[parity]) { cudaGraphExecDestroy(w->graph[parity]); w->graph[parity] = nullptr; }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+            int r = launch_step(w, sp, false);
+            cudaError_t e = cudaStreamEndCapture(w->stream, &g);
+            if (r) return r;
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            CK(cudaGraphInstantiate(&w->graph[parity], g, 0));
+            cudaGraphDestroy(g);
+            w->graph_dt[parity] = dt;
+        } else {
+            jg_flip_store(w->d);
+        }
+        CK(cudaGraphLaunch(w->graph[parity], w->stream));
+        return finish_step(w, false);
+    }
+    int r = launch_step(w, sp, true);
+    if (r) return r;
+    return finish_step(w, true);
+}
+
+int jg_batch_step(jg_world* w, float dt) { return jg_step(w, dt); }
+
+int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
+    if (!w || !bodies || n != w->d.nb) return JG_ERR_INVALID_ARG;
+    int r = jg_upload_bodies(w, bodies, n);
+    if (r) return r;
+    r = jg_step(w, dt);
+    if (r) return r;
+    return jg_download_bodies(w, bodies, n);
+}
+
+int jg_get_counters(jg_world* w, jg_counters* out) {
+    if (!w || !out) return JG_ERR_INVALID_ARG;
+    *out = w->counters;
+    return JG_OK;
+}
+int jg_get_timings(jg_world* w, jg_timings* out) {
+    if (!w || !out) return JG_ERR_INVALID_ARG;
+    *out = w->timings;
+    return JG_OK;
+}
+
+int jg_get_residuals(jg_world* w, float* out, int32_t cap, int32_t* n) {
+    if (!w || !out || !n) return JG_ERR_INVALID_ARG;
+    float h[128];
+    CK(cudaMemcpy(h, w->d.resid, sizeof(h), cudaMemcpyDeviceToHost));
+    int k = std::min(w->prm.solver_iterations, 64);
+    *n = k;
+    for (int i = 0; i < k && i < cap; i++) out[i] = (float)(std::sqrt((double)h[2 * i]) / std::max(std::sqrt((double)h[2 * i + 1]), 1e-12));
+    return JG_OK;
+}
+
+int jg_get_contacts(jg_world* w, jg_contact_view* out, int32_t cap, int32_t* count) {
+    if (!w || !count) return JG_ERR_INVALID_ARG;
+    WorldDev& D = w->d;
+    int narb = 0;
+    CK(cudaMemcpy(&narb, &D.ctr->narb, sizeof(int), cudaMemcpyDeviceToHost));
+    narb = std::min(narb, D.cap_arb);
+    const ArbStore& A = D.arb[D.cur];
+    int c = D.cap_arb;
+    std::vector<int2> key(narb), body(narb);
+    std::vector<int4> info(narb);
+    std::vector<float4> mat(narb);
+    std::vector<float4> f[8];
+    CK(cudaMemcpy(key.data(), A.key, sizeof(int2) * narb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(body.data(), A.body, sizeof(int2) * narb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(info.data(), A.info, sizeof(int4) * narb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(mat.data(), A.mat, sizeof(float4) * narb, cudaMemcpyDeviceToHost));
+    float4* src[8] = {A.cn, A.ct1, A.ct2, A.cr1, A.cr2, A.cacc, A.cp1, A.cp2};
+    for (int k = 0; k < 8; k++) {
+        f[k].resize(4 * (size_t)narb);
+        for (int s = 0; s < 4; s++)
+            CK(cudaMemcpy(f[k].data() + (size_t)s * narb, src[k] + (size_t)s * c, sizeof(float4) * narb, cudaMemcpyDeviceToHost));
+    }
+    int n = 0;
+    for (int a = 0; a < narb; a++)
+        for (int s = 0; s < 4; s++) {
+            if (!(info[a].x & (0x11 << s))) continue;
+            if (out && n < cap) {
+                jg_contact_view& v = out[n];
+                size_t i = (size_t)s * narb + a;
+                v.shape1 = key[a].x; v.shape2 = key[a].y; v.body1 = body[a].x; v.body2 = body[a].y;
+                v.slot = s; v.usage_mask = info[a].x; v.color = info[a].z;
+                v.flags = host_float_as_int(f[2][i].w);
+                auto put = [](float* o, float4 x) { o[0] = x.x; o[1] = x.y; o[2] = x.z; };
+                put(v.normal, f[0][i]); put(v.tangent1, f[1][i]); put(v.tangent2, f[2][i]);
+                put(v.rel_pos1, f[3][i]); put(v.rel_pos2, f[4][i]); put(v.pos1_local, f[6][i]); put(v.pos2_local, f[7][i]);
+                v.accumulated[0] = f[5][i].x; v.accumulated[1] = f[5][i].y; v.accumulated[2] = f[5][i].z;
+                v.mass[0] = f[3][i].w; v.mass[1] = f[4][i].w; v.mass[2] = f[5][i].w;
+                v.bias = f[0][i].w; v.penalty_bias = f[1][i].w;
+                v.friction = mat[a].x; v.restitution = mat[a].y;
+            }
+            n++;
+        }
+    *count = n;
+    return JG_OK;
+}
+
+int jg_get_arbiter_events(jg_world* w, int32_t* created, int32_t ccap, int32_t* nc, int32_t* removed, int32_t rcap,
+                          int32_t* nr) {
+    if (!w || !nc || !nr) return JG_ERR_INVALID_ARG;
+    int a = (int)std::min<int64_t>(w->counters.created_arbiters, w->d.cap_arb);
+    int b = (int)std::min<int64_t>(w->counters.removed_arbiters, w->d.cap_arb);
+    *nc = a; *nr = b;
+    if (created && ccap > 0) CK(cudaMemcpy(created, w->ev_created, sizeof(int2) * std::min(a, ccap), cudaMemcpyDeviceToHost));
+    if (removed && rcap > 0) CK(cudaMemcpy(removed, w->ev_removed, sizeof(int2) * std::min(b, rcap), cudaMemcpyDeviceToHost));
+    return JG_OK;
+}
+
+// State blob: header, bodies (jg_body_desc), arbiter store of the live buffer, joints.
+struct StateHeader { int magic, version, nb, narb, nj, cap_arb; };
+
+int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
+    if (!w || !size) return JG_ERR_INVALID_ARG;
+    WorldDev& D = w->d;
+    int narb = 0;
+    CK(cudaMemcpy(&narb, &D.ctr->narb, sizeof(int), cudaMemcpyDeviceToHost));
+    narb = std::min(narb, D.cap_arb);
+    size_t per_arb = sizeof(int2) * 2 + sizeof(int4) + sizeof(float4) + 32 * sizeof(float4);
+    int64_t need = sizeof(StateHeader) + sizeof(jg_body_desc) * (int64_t)D.nb + (int64_t)per_arb * narb + sizeof(JointDev) * (int64_t)D.nj;
+    *size = need;
+    if (!buf) return JG_OK;
+    if (cap < need) return JG_ERR_CAPACITY;
+    char* p = (char*)buf;
+    StateHeader h{0x4a475331, 1, D.nb, narb, D.nj, D.cap_arb};
+    memcpy(p, &h, sizeof(h)); p += sizeof(h);
+    int r = jg_download_bodies(w, (jg_body_desc*)p, D.nb);
+    if (r) return r;
+    p += sizeof(jg_body_desc) * D.nb;
+    const ArbStore& A = D.arb[D.cur];
+    auto cp = [&](const void* src, size_t bytes) -> int {
+        cudaError_t e = cudaMemcpy(p, src, bytes, cudaMemcpyDeviceToHost);
+        p += bytes;
+        return e == cudaSuccess ? 0 : cuda_fail(e, "export");
+    };
+    if ((r = cp(A.key, sizeof(int2) * narb))) return r;
+    if ((r = cp(A.body, sizeof(int2) * narb))) return r;
+    if ((r = cp(A.info, sizeof(int4) * narb))) return r;
+    if ((r = cp(A.mat, sizeof(float4) * narb))) return r;
+    float4* fs[8] = {A.cn, A.ct1, A.ct2, A.cr1, A.cr2, A.cacc, A.cp1, A.cp2};
+    for (int k = 0; k < 8; k++)
+        for (int s = 0; s < 4; s++)
+            if ((r = cp(fs[k] + (size_t)s * D.cap_arb, sizeof(float4) * narb))) return r;
+    if ((r = cp(D.joints, sizeof(JointDev) * D.nj))) return r;
+    return JG_OK;
+}
+
+int jg_import_state(jg_world* w, const void* buf, int64_t size) {
+    if (!w || !buf || size < (int64_t)sizeof(StateHeader)) return JG_ERR_INVALID_ARG;
+    const char* p = (const char*)buf;
+    StateHeader h;
+    memcpy(&h, p, sizeof(h)); p += sizeof(h);
+    if (h.magic != 0x4a475331 || h.version != 1) return JG_ERR_INVALID_ARG;
+    WorldDev& D = w->d;
+    if (h.nb != D.nb) return JG_ERR_INVALID_ARG;
+    if (h.narb > D.cap_arb || h.nj > D.cap_joints) return JG_ERR_CAPACITY;
+    int r = jg_upload_bodies(w, (const jg_body_desc*)p, h.nb);
+    if (r) return r;
+    p += sizeof(jg_body_desc) * h.nb;
+    const ArbStore& A = D.arb[D.cur];
+    int narb = h.narb;
+    auto cp = [&](void* dst, size_t bytes) -> int {
+        cudaError_t e = cudaMemcpy(dst, p, bytes, cudaMemcpyHostToDevice);
+        p += bytes;
+        return e == cudaSuccess ? 0 : cuda_fail(e, "import");
+    };
+    if ((r = cp(A.key, sizeof(int2) * narb))) return r;
+    if ((r = cp(A.body, sizeof(int2) * narb))) return r;
+    if ((r = cp(A.info, sizeof(int4) * narb))) return r;
+    if ((r = cp(A.mat, sizeof(float4) * narb))) return r;
+    float4* fs[8] = {A.cn, A.ct1, A.ct2, A.cr1, A.cr2, A.cacc, A.cp1, A.cp2};
+    for (int k = 0; k < 8; k++)
+        for (int s = 0; s < 4; s++)
+            if ((r = cp(fs[k] + (size_t)s * D.cap_arb, sizeof(float4) * narb))) return r;
+    if ((r = cp(D.joints, sizeof(JointDev) * h.nj))) return r;
+    CK(cudaMemcpy(&D.ctr->narb, &narb, sizeof(int), cudaMemcpyHostToDevice));
+    D.nj = h.nj;
+    w->nj_host = h.nj;
+    invalidate_graphs(w);
+    return JG_OK;
+}
+
+int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
+    if (!w || steps < 1) return JG_ERR_INVALID_ARG;
+    int64_t size = 0;
+    int r = jg_export_state(w, nullptr, 0, &size);
+    if (r) return r;
+    std::vector<char> snap(size);
+    if ((r = jg_export_state(w, snap.data(), size, &size))) return r;
+    const int blocks[] = {128, 256, 512};
+    const int ctas[] = {1, 2, 4};
+    float best = 1e30f;
+    int bb = 256, bc = 2;
+    jg_world_params saved = w->prm;
+    for (int b : blocks)
+        for (int c : ctas) {
+            w->prm.solver_block = b;
+            w->prm.solver_ctas_per_sm = c;
+            w->prm.use_graph = 0;
+            jg_solver_reset_launch_cache();
+            if ((r = jg_import_state(w, snap.data(), size))) return r;
+            if ((r = jg_step(w, dt))) continue;  // warm-up
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0); cudaEventCreate(&e1);
+            cudaEventRecord(e0, w->stream);
+            bool ok = true;
+            for (int s = 0; s < steps && ok; s++) ok = jg_step(w, dt) == JG_OK;
+            cudaEventRecord(e1, w->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            if (ok && ms < best) { best = ms; bb = b; bc = c; }
+        }
+    w->prm = saved;
+    w->prm.solver_block = bb;
+    w->prm.solver_ctas_per_sm = bc;
+    jg_solver_reset_launch_cache();
+    invalidate_graphs(w);
+    r = jg_import_state(w, snap.data(), size);
+    if (chosen) *chosen = w->prm;
+    return r;
+}
+
+}  // extern "C"
+
+// accessors for the MLP translation unit
+WorldDev& jg_world_dev(jg_world* w) { return w->d; }
+cudaStream_t jg_world_stream(jg_world* w) { return w->stream; }
+int jg_world_nsm(jg_world* w) { return w->nsm; }
+void jg_world_set_mlp_ready(jg_world* w, bool r) { w->mlp_ready = r; }
+int jg_world_iterations(jg_world* w) { return w->prm.solver_iterations; }

@@ -1,0 +1,375 @@
+// Device BallSocket (Dynamics/Constraints/BallSocket.cs:140-252) and HingeAngle
+// (Dynamics/Constraints/HingeAngle.cs:133-364) rows, solved in the same colours as the
+// contacts.  Included by the solver translation unit.  Matrices are row-major float[3][3].
+#pragma once
+
+struct M3x { float a[3][3]; };
+__device__ __forceinline__ M3x mzero() { M3x m; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) m.a[i][j] = 0.f; return m; }
+__device__ __forceinline__ M3x mskew(v3 v) {
+    M3x m = mzero();
+    m.a[0][1] = -v.z; m.a[0][2] = v.y; m.a[1][0] = v.z; m.a[1][2] = -v.x; m.a[2][0] = -v.y; m.a[2][1] = v.x;
+    return m;
+}
+__device__ __forceinline__ v3 mv(const M3x& M, v3 v) {
+    return mk3(v.x * M.a[0][0] + v.y * M.a[0][1] + v.z * M.a[0][2], v.x * M.a[1][0] + v.y * M.a[1][1] + v.z * M.a[1][2],
+               v.x * M.a[2][0] + v.y * M.a[2][1] + v.z * M.a[2][2]);
+}
+__device__ __forceinline__ v3 mtv(const M3x& M, v3 v) {
+    return mk3(v.x * M.a[0][0] + v.y * M.a[1][0] + v.z * M.a[2][0], v.x * M.a[0][1] + v.y * M.a[1][1] + v.z * M.a[2][1],
+               v.x * M.a[0][2] + v.y * M.a[1][2] + v.z * M.a[2][2]);
+}
+__device__ __forceinline__ M3x mmulx(const M3x& x, const M3x& y) {
+    M3x o;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) o.a[i][j] = x.a[i][0] * y.a[0][j] + x.a[i][1] * y.a[1][j] + x.a[i][2] * y.a[2][j];
+    return o;
+}
+__device__ __forceinline__ float mdetx(const M3x& m) {
+    const auto& a = m.a;
+    return a[0][0] * a[1][1] * a[2][2] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+           a[2][0] * a[1][1] * a[0][2] - a[2][1] * a[1][2] * a[0][0] - a[2][2] * a[1][0] * a[0][1];
+}
+__device__ __forceinline__ bool mfin(const M3x& m) {
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) if (!isfinite(m.a[i][j])) return false;
+    return true;
+}
+// JMatrix.TryInverseUnscaled / Inverse (JMatrix.cs:404-478)
+__device__ bool minv_u(const M3x& m, M3x& o) {
+    float idet = 1.0f / mdetx(m);
+    if (!(isfinite(idet) && fabsf(idet) >= 1.17549435e-38f)) { o = mzero(); return false; }
+    const auto& a = m.a;
+    o.a[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) * idet;
+    o.a[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * idet;
+    o.a[0][2] = (a[0][1] * a[1][2] - a[1][1] * a[0][2]) * idet;
+    o.a[1][0] = (a[1][2] * a[2][0] - a[2][2] * a[1][0]) * idet;
+    o.a[1][1] = (a[0][0] * a[2][2] - a[2][0] * a[0][2]) * idet;
+    o.a[1][2] = (a[0][2] * a[1][0] - a[1][2] * a[0][0]) * idet;
+    o.a[2][0] = (a[1][0] * a[2][1] - a[2][0] * a[1][1]) * idet;
+    o.a[2][1] = (a[0][1] * a[2][0] - a[2][1] * a[0][0]) * idet;
+    o.a[2][2] = (a[0][0] * a[1][1] - a[1][0] * a[0][1]) * idet;
+    return mfin(o);
+}
+__device__ bool minvx(const M3x& m, M3x& o) {
+    if (minv_u(m, o)) return true;
+    float s = 0.f;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) s = fmaxf(s, fabsf(m.a[i][j]));
+    if (s > 0 && isfinite(s)) {
+        M3x n;
+        for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) n.a[i][j] = m.a[i][j] / s;
+        if (minv_u(n, o)) {
+            for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] /= s;
+            if (mfin(o)) return true;
+        }
+    }
+    o = mzero();
+    return false;
+}
+// MathHelper.JacobiRotate (MathHelper.cs:374-406)
+__device__ bool jacobi(float* a, float* basis, int p, int q, float tol) {
+    float off = a[3 * p + q];
+    if (fabsf(off) <= tol) return false;
+    float tau = (a[3 * q + q] - a[3 * p + p]) / (2.0f * off);
+    float tg = copysignf(1.0f, tau) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+    float cs = 1.0f / sqrtf(1.0f + tg * tg);
+    float sn = tg * cs;
+    a[3 * p + p] -= tg * off;
+    a[3 * q + q] += tg * off;
+    a[3 * p + q] = a[3 * q + p] = 0;
+    for (int k = 0; k < 3; k++) {
+        if (k != p && k != q) {
+            float akp = a[3 * k + p], akq = a[3 * k + q];
+            a[3 * k + p] = a[3 * p + k] = cs * akp - sn * akq;
+            a[3 * k + q] = a[3 * q + k] = sn * akp + cs * akq;
+        }
+        float vkp = basis[3 * k + p], vkq = basis[3 * k + q];
+        basis[3 * k + p] = cs * vkp - sn * vkq;
+        basis[3 * k + q] = sn * vkp + cs * vkq;
+    }
+    return true;
+}
+// MathHelper.PseudoInverseSymmetric (MathHelper.cs:282-325)
+__device__ M3x pinv_sym(const M3x& m) {
+    float s = fmaxf(fabsf(m.a[0][0]), fmaxf(fabsf(m.a[1][1]), fabsf(m.a[2][2])));
+    if (!(s > 0) || !isfinite(s)) return mzero();
+    float n11 = m.a[0][0] / s, n12 = m.a[0][1] / s, n13 = m.a[0][2] / s, n22 = m.a[1][1] / s, n23 = m.a[1][2] / s, n33 = m.a[2][2] / s;
+    const float tol = 1e-6f;
+    float nd = n11 * (n22 * n33 - n23 * n23) + n12 * (n23 * n13 - n12 * n33) + n13 * (n12 * n23 - n22 * n13);
+    M3x inv;
+    if (fabsf(nd) > tol && minvx(m, inv)) return inv;
+    float a[9] = {n11, n12, n13, n12, n22, n23, n13, n23, n33};
+    float basis[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int sw = 0; sw < 8; sw++) {
+        bool ch = jacobi(a, basis, 0, 1, tol);
+        ch |= jacobi(a, basis, 0, 2, tol);
+        ch |= jacobi(a, basis, 1, 2, tol);
+        if (!ch) break;
+    }
+    float r11 = 0, r12 = 0, r13 = 0, r22 = 0, r23 = 0, r33 = 0;
+    for (int i = 0; i < 3; i++) {
+        float ev = a[3 * i + i];
+        if (!(ev > tol)) continue;
+        float wgt = (1.0f / ev) / s;
+        v3 ax = mk3(basis[i], basis[3 + i], basis[6 + i]);
+        r11 += wgt * (ax.x * ax.x); r12 += wgt * (ax.x * ax.y); r13 += wgt * (ax.x * ax.z);
+        r22 += wgt * (ax.y * ax.y); r23 += wgt * (ax.y * ax.z); r33 += wgt * (ax.z * ax.z);
+    }
+    M3x o;
+    o.a[0][0] = r11; o.a[0][1] = r12; o.a[0][2] = r13;
+    o.a[1][0] = r12; o.a[1][1] = r22; o.a[1][2] = r23;
+    o.a[2][0] = r13; o.a[2][1] = r23; o.a[2][2] = r33;
+    return o;
+}
+// MathHelper.InverseSymmetric (MathHelper.cs:328-365)
+__device__ M3x inv_symmetric(const M3x& m) {
+    const float tol = 1e-6f;
+    float dp = m.a[0][0] * m.a[1][1] * m.a[2][2];
+    M3x inv;
+    if (mdetx(m) / dp > tol && minvx(m, inv)) return inv;
+    float x = m.a[0][0] > 0 ? sqrtf(m.a[0][0]) : 0, y = m.a[1][1] > 0 ? sqrtf(m.a[1][1]) : 0, z = m.a[2][2] > 0 ? sqrtf(m.a[2][2]) : 0;
+    if (x == 0 && y == 0 && z == 0) return mzero();
+    float xy = x > 0 && y > 0 ? m.a[0][1] / x / y : 0, xz = x > 0 && z > 0 ? m.a[0][2] / x / z : 0, yz = y > 0 && z > 0 ? m.a[1][2] / y / z : 0;
+    M3x nrm;
+    nrm.a[0][0] = 1; nrm.a[0][1] = xy; nrm.a[0][2] = xz;
+    nrm.a[1][0] = xy; nrm.a[1][1] = 1; nrm.a[1][2] = yz;
+    nrm.a[2][0] = xz; nrm.a[2][1] = yz; nrm.a[2][2] = 1;
+    M3x r = pinv_sym(nrm);
+    xy = x > 0 && y > 0 ? r.a[0][1] / x / y : 0;
+    xz = x > 0 && z > 0 ? r.a[0][2] / x / z : 0;
+    yz = y > 0 && z > 0 ? r.a[1][2] / y / z : 0;
+    M3x o;
+    o.a[0][0] = x > 0 ? r.a[0][0] / x / x : 0; o.a[0][1] = xy; o.a[0][2] = xz;
+    o.a[1][0] = xy; o.a[1][1] = y > 0 ? r.a[1][1] / y / y : 0; o.a[1][2] = yz;
+    o.a[2][0] = xz; o.a[2][1] = yz; o.a[2][2] = z > 0 ? r.a[2][2] / z / z : 0;
+    return mfin(o) ? o : mzero();
+}
+
+__device__ __forceinline__ void jstore_m(float4* dst, const M3x& m) {
+    for (int r = 0; r < 3; r++) dst[r] = make_float4(m.a[r][0], m.a[r][1], m.a[r][2], 0.f);
+}
+__device__ __forceinline__ M3x jload_m(const float4* src) {
+    M3x m;
+    for (int r = 0; r < 3; r++) { float4 v = src[r]; m.a[r][0] = v.x; m.a[r][1] = v.y; m.a[r][2] = v.z; }
+    return m;
+}
+// JSymmetricMatrix.Transform(S, T) = T S T^T with a full T (JSymmetricMatrix.cs:247-260)
+__device__ __forceinline__ M3x sym_transform_full(const sym6& S, const M3x& T) {
+    m33 t;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) t.m[i][j] = T.a[i][j];
+    sym6 r = sym_transform(S, t);
+    M3x o;
+    o.a[0][0] = r.m11; o.a[0][1] = r.m12; o.a[0][2] = r.m13;
+    o.a[1][0] = r.m12; o.a[1][1] = r.m22; o.a[1][2] = r.m23;
+    o.a[2][0] = r.m13; o.a[2][1] = r.m23; o.a[2][2] = r.m33;
+    return o;
+}
+
+// BallSocket.PrepareForIterationBallSocket (BallSocket.cs:140-183)
+__device__ void ballsocket_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 r1 = rotate(mk3(J.la1), q1), r2 = rotate(mk3(J.la2), q2);
+    v3 p1 = mk3(w.pos[i1]) + r1, p2 = mk3(w.pos[i2]) + r2;
+    M3x cr1 = mskew(r1), cr2 = mskew(r2);
+    M3x t1 = sym_transform_full(b1.I, cr1), t2 = sym_transform_full(b2.I, cr2);
+    // ((Scale(m1) + T1) + Scale(m2)) + T2, component-wise, in the reference's order
+    M3x e;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) e.a[i][j] = t1.a[i][j] + t2.a[i][j];
+    e.a[0][0] = ((b1.im.x + t1.a[0][0]) + b2.im.x) + t2.a[0][0];
+    e.a[1][1] = ((b1.im.y + t1.a[1][1]) + b2.im.y) + t2.a[1][1];
+    e.a[2][2] = ((b1.im.z + t1.a[2][2]) + b2.im.z) + t2.a[2][2];
+    float soft = J.prm.y * sp.inv_sub_dt;
+    e.a[0][0] += soft; e.a[1][1] += soft; e.a[2][2] += soft;
+    M3x eff = inv_symmetric(e);
+    v3 bias = (p2 - p1) * J.prm.x * sp.inv_dt;
+    v3 acc = mk3(J.acc);
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v - cmul(acc, b1.im);
+        b1.w = b1.w - sym_mul(b1.I, mv(cr1, acc));
+        store_vel(w.body, i1, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(acc, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, mv(cr2, acc));
+        store_vel(w.body, i2, b2);
+    }
+    J.r1 = f4(r1, 0.f); J.r2 = f4(r2, 0.f);
+    J.bias = f4(bias, 0.f);
+    jstore_m(J.eff, eff);
+}
+// BallSocket.IterateBallSocket (BallSocket.cs:223-252)
+__device__ void ballsocket_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    M3x cr1 = mskew(mk3(J.r1)), cr2 = mskew(mk3(J.r2));
+    v3 acc = mk3(J.acc);
+    v3 sv = acc * J.prm.y * sp.inv_sub_dt;
+    v3 jv = -b1.v + mv(cr1, b1.w) + b2.v - mv(cr2, b2.w);
+    M3x eff = jload_m(J.eff);
+    v3 lambda = -1.0f * mv(eff, jv + mk3(J.bias) + sv);
+    J.acc = f4(acc + lambda, 0.f);
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v - cmul(lambda, b1.im);
+        b1.w = b1.w - sym_mul(b1.I, mv(cr1, lambda));
+        store_vel(w.body, i1, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(lambda, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, mv(cr2, lambda));
+        store_vel(w.body, i2, b2);
+    }
+}
+
+// AngularConstraintMath.CalculateJacobian (AngularConstraintMath.cs:65-95)
+__device__ M3x calc_jacobian(q4 left, q4 right, v3& err, int& hemi) {
+    q4 q = qmul(left, right);
+    hemi = q.w < 0 ? -1 : 1;
+    if (q.w < 0) { q.x = -q.x; q.y = -q.y; q.z = -q.z; q.w = -q.w; }
+    v3 qv = mk3(q.x, q.y, q.z);
+    float sine = sqrtf(len2(qv));
+    M3x der;
+    if (sine > 0) {
+        float half = StableMathF::atan2(sine, q.w);
+        v3 ax = qv * (1.0f / sine);
+        err = ax * half;
+        float diag = half * q.w / sine;
+        float od = 1.0f - diag;
+        M3x sk = mskew(err);
+        float outer[3][3] = {{ax.x * ax.x, ax.x * ax.y, ax.x * ax.z}, {ax.x * ax.y, ax.y * ax.y, ax.y * ax.z}, {ax.x * ax.z, ax.y * ax.z, ax.z * ax.z}};
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) der.a[i][j] = ((i == j ? diag : 0.f) + od * outer[i][j]) - sk.a[i][j];
+    } else {
+        err = mk3(0.f);
+        der = mzero();
+        der.a[0][0] = der.a[1][1] = der.a[2][2] = 1.f;
+    }
+    m33 R = mat_from_quat(left);
+    M3x Rm;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) Rm.a[i][j] = R.m[i][j];
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) der.a[i][j] = -0.5f * der.a[i][j];
+    return mmulx(der, Rm);
+}
+
+// HingeAngle.PrepareForIterationHingeAngle (HingeAngle.cs:133-220)
+__device__ void hinge_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 axis = mk3(J.axis);
+    v3 p0 = create_orthonormal(axis);
+    v3 p1 = cross(axis, p0);
+    v3 rot;
+    int hemi;
+    M3x m0 = calc_jacobian(qmul(mkq(J.q0), qconj(q1)), q2, rot, hemi);
+    v3 acc = mk3(J.acc);
+    int old_hemi = (int)J.bil.w;
+    if (old_hemi != 0 && old_hemi != hemi) acc = mk3(0.f);
+    v3 err = mk3(dot(p0, rot), dot(p1, rot), dot(axis, rot));
+    int clamp = 0;
+    v3 c0 = mtv(m0, p0), c1 = mtv(m0, p1), c2 = mtv(m0, axis);
+    M3x jac;  // columns c0 c1 c2 (JMatrix column-major UnsafeGet, JMatrix.cs:62-79)
+    jac.a[0][0] = c0.x; jac.a[1][0] = c0.y; jac.a[2][0] = c0.z;
+    jac.a[0][1] = c1.x; jac.a[1][1] = c1.y; jac.a[2][1] = c1.z;
+    jac.a[0][2] = c2.x; jac.a[1][2] = c2.y; jac.a[2][2] = c2.z;
+    sym6 Is;
+    Is.m11 = b1.I.m11 + b2.I.m11; Is.m12 = b1.I.m12 + b2.I.m12; Is.m13 = b1.I.m13 + b2.I.m13;
+    Is.m22 = b1.I.m22 + b2.I.m22; Is.m23 = b1.I.m23 + b2.I.m23; Is.m33 = b1.I.m33 + b2.I.m33;
+    M3x jt;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) jt.a[i][j] = jac.a[j][i];
+    M3x eff = sym_transform_full(Is, jt);
+    float soft = J.prm.y, lsoft = J.prm.w, bias_f = J.prm.x, lbias = J.prm.z;
+    eff.a[0][0] += soft * sp.inv_sub_dt;
+    eff.a[1][1] += soft * sp.inv_sub_dt;
+    eff.a[2][2] += lsoft * sp.inv_sub_dt;
+    float minA = J.lim.x, maxA = J.lim.y, fixedA = J.lim.z;
+    const float PI = 3.14159265358979323846f;
+    bool full = minA <= -PI / 2 && maxA >= PI / 2;
+    if (minA >= maxA) {
+        clamp = 3;
+        float ang = err.z - fixedA, half = PI / 2;
+        if (!(ang >= -half && ang <= half)) {
+            float period = 2 * half;
+            ang = fmodf(ang, period);
+            if (ang > half) ang -= period; else if (ang < -half) ang += period;
+        }
+        err.z = ang;
+    } else if (!full && err.z >= maxA) {
+        clamp = 1;
+        err.z -= maxA;
+    } else if (!full && err.z <= minA) {
+        clamp = 2;
+        err.z -= minA;
+    } else {
+        acc.z = 0;
+        eff.a[2][2] = 0;
+        eff.a[2][0] = eff.a[0][2] = 0;
+        eff.a[2][1] = eff.a[1][2] = 0;
+        jac.a[0][2] = jac.a[1][2] = jac.a[2][2] = 0;
+    }
+    v3 bil = mk3(0.f);
+    float cx = 0.f, cy = 0.f;
+    if (clamp == 1 || clamp == 2) {
+        acc.z = clamp == 1 ? fminf(acc.z, 0.f) : fmaxf(acc.z, 0.f);
+        M3x blk = mzero();
+        blk.a[0][0] = eff.a[0][0]; blk.a[0][1] = eff.a[0][1]; blk.a[1][0] = eff.a[0][1]; blk.a[1][1] = eff.a[1][1];
+        M3x bi = inv_symmetric(blk);
+        bil = mk3(bi.a[0][0], bi.a[0][1], bi.a[1][1]);
+        cx = eff.a[0][2];
+        cy = eff.a[1][2];
+    }
+    eff = inv_symmetric(eff);
+    v3 bias = err * sp.inv_dt;
+    bias.x *= bias_f; bias.y *= bias_f; bias.z *= lbias;
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, mv(jac, acc)); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, mv(jac, acc)); store_vel(w.body, i2, b2); }
+    J.acc = f4(acc, 0.f);
+    J.bias = f4(bias, 0.f);
+    jstore_m(J.eff, eff);
+    jstore_m(J.jac, jac);
+    J.lim.w = (float)clamp;
+    J.bil = make_float4(bil.x, bil.y, bil.z, (float)hemi);
+    J.cpl = make_float4(cx, cy, 0.f, 0.f);
+}
+// HingeAngle.IterateHingeAngle (HingeAngle.cs:313-364)
+__device__ void hinge_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    M3x jac = jload_m(J.jac), eff = jload_m(J.eff);
+    v3 jv = mtv(jac, b1.w - b2.w);
+    v3 acc = mk3(J.acc);
+    v3 soft = acc * sp.inv_sub_dt;
+    soft.x *= J.prm.y; soft.y *= J.prm.y; soft.z *= J.prm.w;
+    v3 res = jv + mk3(J.bias) + soft;
+    v3 lambda = -1.0f * mv(eff, res);
+    v3 orig = acc;
+    acc = acc + lambda;
+    int clamp = (int)J.lim.w;
+    if ((clamp == 1 && acc.z > 0) || (clamp == 2 && acc.z < 0)) {
+        lambda.z = -orig.z;
+        float x = res.x + J.cpl.x * lambda.z;
+        float y = res.y + J.cpl.y * lambda.z;
+        lambda.x = -(J.bil.x * x + J.bil.y * y);
+        lambda.y = -(J.bil.y * x + J.bil.z * y);
+        acc.x = orig.x + lambda.x;
+        acc.y = orig.y + lambda.y;
+        acc.z = 0;
+    } else if (clamp == 0) {
+        orig.z = 0;
+        acc.z = 0;
+    }
+    lambda = acc - orig;
+    J.acc = f4(acc, 0.f);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, mv(jac, lambda)); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, mv(jac, lambda)); store_vel(w.body, i2, b2); }
+}
+
+__device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
+    JointDev& J = w.joints[j];
+    if (J.hdr.x == JG_CONSTRAINT_BALLSOCKET) ballsocket_prepare(w, J, sp);
+    else hinge_prepare(w, J, sp);
+}
+__device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const StepParams& sp) {
+    JointDev& J = w.joints[j];
+    if (J.hdr.x == JG_CONSTRAINT_BALLSOCKET) ballsocket_iterate(w, J, sp);
+    else hinge_iterate(w, J, sp);
+}

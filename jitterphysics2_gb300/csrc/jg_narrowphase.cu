@@ -1,0 +1,941 @@
+// Narrowphase: one warp per broadphase pair.  MPR (NarrowPhase.cs:98-347), EPA with the
+// polytope in shared memory (NarrowPhase.cs:39-95, ConvexPolytope.cs), the triangle-edge
+// filter (TriangleEdgeCollisionFilter.cs:243-420) and the one-shot manifold
+// (CollisionManifold.cs:393-566) run fused; colliding pairs append one record (key,
+// normal, up to four point pairs) to the compacted contact stream.
+//
+// Lanes of a warp hold identical copies of the MPR state; point-cloud support maps, the
+// EPA face scans (closest face, visibility, fan construction) and the manifold's segment
+// intersections are split across lanes.  EPA keeps its face data in FP32; FP64 is used
+// only when a face normal is too cancelled to trust (exact expansion recomputation, as
+// the reference's ExpansionArithmetic.Normal) and when the FP32 orientation filter cannot
+// prove a sign (the reference's double filter, then exact expansions).  The device
+// polytope holds 64 vertices / 128 faces (the reference: 128 / 256); running out ends
+// EPA with the MPR result, the reference's behaviour on any EPA failure.
+//
+// The MPR follows code the reference adapted from XenoCollide (zlib license, (c) 2007-2014
+// Gary Snethen, http://xenocollide.com): provided 'as-is', without any express or implied
+// warranty; altered source versions must be plainly marked as such; this notice may not
+// be removed or altered from any source distribution.
+#include "jg_shapes.cuh"
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct MV { v3 V, A, B; };
+
+__device__ __forceinline__ void mk_support(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, v3 d, MV& v) {
+    v3 tmp = -d;
+    v.A = support(sa, d);
+    v3 tmp2 = rotate_inv(tmp, qb);
+    v.B = support(sb, tmp2);
+    v.B = rotate(v.B, qb);
+    v.B = v.B + pb;
+    v.V = v.A - v.B;
+}
+__device__ __forceinline__ void mk_center(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, MV& c) {
+    c.A = sa.center;
+    c.B = rotate(sb.center, qb);
+    c.B = pb + c.B;
+    c.V = c.A - c.B;
+}
+
+// ---- exact arithmetic (double expansions), used only on unresolved EPA predicates -------
+struct Exp {
+    __device__ static int diff(double a, double b, double* o) {
+        double v = a - b, vb = a - v;
+        double res = (a - (v + vb)) + (vb - b);
+        int n = 0;
+        if (res != 0) o[n++] = res;
+        if (v != 0) o[n++] = v;
+        return n;
+    }
+    __device__ static int grow(double* e, int len, double value) {
+        int cnt = 0;
+        for (int i = 0; i < len; i++) {
+            double part = e[i];
+            double sum = value + part;
+            double vp = sum - value;
+            double res = (value - (sum - vp)) + (part - vp);
+            if (res != 0) e[cnt++] = res;
+            value = sum;
+        }
+        if (value != 0) e[cnt++] = value;
+        return cnt;
+    }
+    __device__ static int addp(double* r, int len, const double* a, int na, const double* b, int nb, bool neg, int cap) {
+        for (int i = 0; i < na; i++)
+            for (int j = 0; j < nb; j++) {
+                double x = a[i], y = b[j];
+                double p = __dmul_rn(x, y);
+                double res = fma(x, y, -p);
+                if (neg) { p = -p; res = -res; }
+                if (res != 0 && len < cap) len = grow(r, len, res);
+                if (p != 0 && len < cap) len = grow(r, len, p);
+            }
+        return len;
+    }
+    __device__ static int crossterm(const double* a, int na, const double* b, int nb, const double* c, int nc,
+                                    const double* d, int nd, double* o) {
+        int len = addp(o, 0, a, na, b, nb, false, 16);
+        return addp(o, len, c, nc, d, nd, true, 16);
+    }
+    // ExpansionArithmetic.Side (ExactArithmetic/ExpansionArithmetic.cs:20-41)
+    __device__ static int side(v3 a, v3 b, v3 c, v3 p) {
+        double ux[2], uy[2], uz[2], vx[2], vy[2], vz[2], dx[2], dy[2], dz[2];
+        int nx = diff(a.x, b.x, ux), ny = diff(a.y, b.y, uy), nz = diff(a.z, b.z, uz);
+        int mx = diff(a.x, c.x, vx), my = diff(a.y, c.y, vy), mz = diff(a.z, c.z, vz);
+        int px = diff(p.x, a.x, dx), py = diff(p.y, a.y, dy), pz = diff(p.z, a.z, dz);
+        double cr[16], det[192];
+        int len = crossterm(uy, ny, vz, mz, uz, nz, vy, my, cr);
+        int cnt = addp(det, 0, cr, len, dx, px, false, 192);
+        len = crossterm(uz, nz, vx, mx, ux, nx, vz, mz, cr);
+        cnt = addp(det, cnt, cr, len, dy, py, false, 192);
+        len = crossterm(ux, nx, vy, my, uy, ny, vx, mx, cr);
+        cnt = addp(det, cnt, cr, len, dz, pz, false, 192);
+        if (cnt == 0) return 0;
+        double t = det[cnt - 1];
+        return t > 0 ? 1 : (t < 0 ? -1 : 0);
+    }
+    // ExpansionArithmetic.Normal (ExpansionArithmetic.cs:43-55)
+    __device__ static v3 normal(v3 a, v3 b, v3 c) {
+        double ux[2], uy[2], uz[2], vx[2], vy[2], vz[2], cr[16];
+        int nx = diff(a.x, b.x, ux), ny = diff(a.y, b.y, uy), nz = diff(a.z, b.z, uz);
+        int mx = diff(a.x, c.x, vx), my = diff(a.y, c.y, vy), mz = diff(a.z, c.z, vz);
+        double r[3];
+        int len = crossterm(uy, ny, vz, mz, uz, nz, vy, my, cr);
+        double s = 0; for (int i = 0; i < len; i++) s += cr[i]; r[0] = s;
+        len = crossterm(uz, nz, vx, mx, ux, nx, vz, mz, cr);
+        s = 0; for (int i = 0; i < len; i++) s += cr[i]; r[1] = s;
+        len = crossterm(ux, nx, vy, my, uy, ny, vx, mx, cr);
+        s = 0; for (int i = 0; i < len; i++) s += cr[i]; r[2] = s;
+        // scale by the largest component in double before rounding to float
+        double m = fmax(fabs(r[0]), fmax(fabs(r[1]), fabs(r[2])));
+        if (!(m > 0)) return mk3(0.f);
+        return mk3((float)(r[0] / m), (float)(r[1] / m), (float)(r[2] / m));
+    }
+};
+
+// PlaneFilter in double (ExactArithmetic/PlaneFilter.cs:29-70); the FP32 filter below
+// tries first.
+__device__ bool dfilter_side(v3 a, v3 b, v3 c, v3 p, int& sign) {
+    const double EF = 16 * 1.1102230246251565e-16;
+    double ux = (double)a.x - b.x, uy = (double)a.y - b.y, uz = (double)a.z - b.z;
+    double vx = (double)a.x - c.x, vy = (double)a.y - c.y, vz = (double)a.z - c.z;
+    double yz = uy * vz, zy = uz * vy, zx = uz * vx, xz = ux * vz, xy = ux * vy, yx = uy * vx;
+    double nx = yz - zy, ny = zx - xz, nz = xy - yx;
+    double ex = EF * (fabs(yz) + fabs(zy)), ey = EF * (fabs(zx) + fabs(xz)), ez = EF * (fabs(xy) + fabs(yx));
+    double dx = (double)p.x - a.x, dy = (double)p.y - a.y, dz = (double)p.z - a.z;
+    double x = nx * dx, y = ny * dy, z = nz * dz;
+    double value = (x + y) + z;
+    double round = EF * ((fabs(x) + fabs(y)) + fabs(z));
+    double coef = (ex * fabs(dx) + ey * fabs(dy)) + ez * fabs(dz);
+    if (fabs(value) <= round + 2 * coef) return false;
+    sign = value > 0 ? 1 : -1;
+    return true;
+}
+
+// FP32 version of the same filter: identical bound structure with u = 2^-24.
+__device__ __forceinline__ bool ffilter_side(v3 a, v3 b, v3 c, v3 p, int& sign) {
+    const float EF = 16.0f * 5.9604645e-08f;
+    float ux = a.x - b.x, uy = a.y - b.y, uz = a.z - b.z;
+    float vx = a.x - c.x, vy = a.y - c.y, vz = a.z - c.z;
+    float yz = uy * vz, zy = uz * vy, zx = uz * vx, xz = ux * vz, xy = ux * vy, yx = uy * vx;
+    float nx = yz - zy, ny = zx - xz, nz = xy - yx;
+    float ex = EF * (fabsf(yz) + fabsf(zy)), ey = EF * (fabsf(zx) + fabsf(xz)), ez = EF * (fabsf(xy) + fabsf(yx));
+    float dx = p.x - a.x, dy = p.y - a.y, dz = p.z - a.z;
+    float x = nx * dx, y = ny * dy, z = nz * dz;
+    float value = (x + y) + z;
+    float round = EF * ((fabsf(x) + fabsf(y)) + fabsf(z));
+    float coef = (ex * fabsf(dx) + ey * fabsf(dy)) + ez * fabsf(dz);
+    // the difference of two float coordinates is inexact in float: widen the bound for
+    // the extra rounding of the displacement (covered by the factor 4)
+    if (fabsf(value) <= 4.0f * (round + 2.0f * coef) || !isfinite(value)) return false;
+    sign = value > 0 ? 1 : -1;
+    return true;
+}
+
+struct EpaSmem {
+    float4 vV[JG_EPA_MAXV], vA[JG_EPA_MAXV], vB[JG_EPA_MAXV];
+    float4 fn[JG_EPA_MAXT];     // scaled normal xyz, normal_sq
+    float4 fc[JG_EPA_MAXT];     // closest point xyz, closest_sq
+    uchar4 fi[JG_EPA_MAXT];     // a, b, c, facing origin
+    unsigned char ea[3 * JG_EPA_MAXT], eb[3 * JG_EPA_MAXT];
+    unsigned lit[JG_EPA_MAXT / 32];
+    int nv, nt, ne, enclosed;
+    // manifold scratch
+    float4 mA[12], mB[12];
+    float4 left[6], right[6];
+};
+
+enum { ADDED = 0, NO_HORIZON = 1, DEGENERATE = 2, CAPACITY = 3, NUMERICAL = 4 };
+
+struct NpStats { int exact; };
+
+// ConvexPolytope.Side (ConvexPolytope.cs:321-327): orientation of point p relative to face (a,b,c).
+__device__ __forceinline__ int side_pt(v3 a, v3 b, v3 c, v3 p, NpStats& st) {
+    if (p == a || p == b || p == c) return 0;
+    int s;
+    if (ffilter_side(a, b, c, p, s)) return s;
+    st.exact++;
+    if (dfilter_side(a, b, c, p, s)) return s;
+    return Exp::side(a, b, c, p);
+}
+
+__device__ __forceinline__ bool safe_coord(float v) {
+    float a = fabsf(v);
+    return v == 0.f || (a >= 1e-30f && a <= 1e30f);
+}
+__device__ __forceinline__ bool is_safe(v3 p) { return safe_coord(p.x) && safe_coord(p.y) && safe_coord(p.z); }
+
+// ConvexPolytope.CalcBarycentric (ConvexPolytope.cs:328-395), in FP32.
+__device__ bool calc_bary(v3 a, v3 b, v3 c, v3 n, float nscale, float nsq, v3& out) {
+    v3 u = a - b, v = a - c;
+    float gamma = (dot(cross(u, a), n) / nsq) / nscale;
+    float beta = (dot(cross(a, v), n) / nsq) / nscale;
+    float alpha = 1.f - gamma - beta;
+    bool clamped = false;
+    if (alpha >= 0 && beta < 0) {
+        float t = dot(a, u);
+        if (gamma < 0 && t > 0) { beta = fminf(1.f, t / dot(u, u)); alpha = 1 - beta; gamma = 0; }
+        else { gamma = fminf(fmaxf(dot(a, v) / dot(v, v), 0.f), 1.f); alpha = 1 - gamma; beta = 0; }
+        clamped = true;
+    } else if (beta >= 0 && gamma < 0) {
+        v3 w = b - c;
+        float t = dot(b, w);
+        if (alpha < 0 && t > 0) { gamma = fminf(1.f, t / dot(w, w)); beta = 1 - gamma; alpha = 0; }
+        else { alpha = fminf(fmaxf(-dot(b, u) / dot(u, u), 0.f), 1.f); beta = 1 - alpha; gamma = 0; }
+        clamped = true;
+    } else if (gamma >= 0 && alpha < 0) {
+        v3 w = b - c;
+        float t = -dot(c, v);
+        if (beta < 0 && t > 0) { alpha = fminf(1.f, t / dot(v, v)); gamma = 1 - alpha; beta = 0; }
+        else { beta = fminf(fmaxf(-dot(c, w) / dot(w, w), 0.f), 1.f); gamma = 1 - beta; alpha = 0; }
+        clamped = true;
+    }
+    out = mk3(alpha, beta, gamma);
+    return clamped;
+}
+
+// ConvexPolytope.CreateTriangle (ConvexPolytope.cs:267-318), one lane per face.
+__device__ int create_tri(EpaSmem& E, int a, int b, int c, int slot, NpStats& st) {
+    v3 va = mk3(E.vV[a]), vb = mk3(E.vV[b]), vc = mk3(E.vV[c]);
+    int orient = 0;
+    for (int i = 0; i < 4 && orient == 0; i++) {
+        if (i == a || i == b || i == c) continue;
+        orient = -side_pt(va, vb, vc, mk3(E.vV[i]), st);
+    }
+    if (orient == 0) return DEGENERATE;
+    if (orient < 0) { int t = a; a = b; b = t; v3 tv = va; va = vb; vb = tv; }
+    bool facing = side_pt(va, vb, vc, mk3(0.f), st) <= 0;
+    // raw normal (a-b) x (a-c) with its filter error; recompute exactly when cancelled
+    float ux = va.x - vb.x, uy = va.y - vb.y, uz = va.z - vb.z;
+    float vx = va.x - vc.x, vy = va.y - vc.y, vz = va.z - vc.z;
+    float yz = uy * vz, zy = uz * vy, zx = uz * vx, xz = ux * vz, xy = ux * vy, yx = uy * vx;
+    v3 raw = mk3(yz - zy, zx - xz, xy - yx);
+    const float EF = 16.0f * 5.9604645e-08f;
+    float err = EF * fmaxf(fabsf(yz) + fabsf(zy), fmaxf(fabsf(zx) + fabsf(xz), fabsf(xy) + fabsf(yx)));
+    float nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
+    if (!(nmax > 4096.0f * err)) {
+        st.exact++;
+        raw = Exp::normal(va, vb, vc);
+        nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
+    }
+    if (!(nmax > 0) || !isfinite(nmax)) return NUMERICAL;
+    v3 sn = mk3(raw.x / nmax, raw.y / nmax, raw.z / nmax);
+    float nsq = dot(sn, sn);
+    v3 bc;
+    bool clamped = calc_bary(va, vb, vc, sn, nmax, nsq, bc);
+    v3 cl = clamped ? (va * bc.x + vb * bc.y) + vc * bc.z : sn * (dot(sn, va) / nsq);
+    float d2 = dot(cl, cl);
+    if (!isfinite(cl.x) || !isfinite(cl.y) || !isfinite(cl.z) || !isfinite(d2)) return NUMERICAL;
+    E.fi[slot] = make_uchar4((unsigned char)a, (unsigned char)b, (unsigned char)c, facing ? 1 : 0);
+    E.fn[slot] = f4(sn, len2(sn));
+    E.fc[slot] = f4(cl, d2);
+    return ADDED;
+}
+
+// ConvexPolytope.InitTetrahedron (ConvexPolytope.cs:113-132)
+__device__ bool epa_init(EpaSmem& E, NpStats& st) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) { E.nv = 4; E.nt = 0; E.enclosed = 0; }
+    __syncwarp();
+    bool safe = true;
+    for (int i = 0; i < 4; i++) safe = safe && is_safe(mk3(E.vV[i]));
+    if (!safe) return false;
+    const int idx[12] = {0, 2, 1, 0, 1, 3, 0, 3, 2, 1, 2, 3};
+    int r = ADDED;
+    if (lane < 4) r = create_tri(E, idx[3 * lane], idx[3 * lane + 1], idx[3 * lane + 2], lane, st);
+    bool ok = __all_sync(FULL, r == ADDED);
+    __syncwarp();
+    if (ok && lane == 0) E.nt = 4;
+    __syncwarp();
+    return ok;
+}
+
+// ConvexPolytope.GetClosestTriangle (ConvexPolytope.cs:147-166): first minimum wins.
+__device__ int epa_closest(EpaSmem& E) {
+    const int lane = threadIdx.x & 31;
+    float best = 3.402823466e+38f;
+    int bi = 0x7fffffff;
+    bool notfacing = false;
+    int nt = E.nt;
+    for (int i = lane; i < nt; i += 32) {
+        float d = E.fc[i].w;
+        if (d < best || (d == best && i < bi)) { best = d; bi = i; }
+        if (!E.fi[i].w) notfacing = true;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        float ob = __shfl_xor_sync(FULL, best, off);
+        int oi = __shfl_xor_sync(FULL, bi, off);
+        if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    bool any_nf = __any_sync(FULL, notfacing);
+    bool skip = E.enclosed != 0;
+    __syncwarp();
+    if (lane == 0) E.enclosed = any_nf ? (skip ? 1 : 0) : 1;
+    __syncwarp();
+    if (bi == 0x7fffffff) bi = 0;
+    return bi;
+}
+
+// ConvexPolytope.AddVertexDetailed (ConvexPolytope.cs:199-265)
+__device__ int epa_add(EpaSmem& E, const MV& v, NpStats& st) {
+    const int lane = threadIdx.x & 31;
+    if (E.nt == 0 || !is_safe(v.V)) return NUMERICAL;
+    int nv = E.nv;
+    if (nv == JG_EPA_MAXV) return CAPACITY;
+    if (lane == 0) { E.vV[nv] = f4(v.V, 0.f); E.vA[nv] = f4(v.A, 0.f); E.vB[nv] = f4(v.B, 0.f); }
+    __syncwarp();
+    int nt = E.nt;
+    // visibility of every face, lanes in parallel
+    for (int base = 0; base < nt; base += 32) {
+        int i = base + lane;
+        bool lit = false;
+        if (i < nt) {
+            uchar4 f = E.fi[i];
+            lit = side_pt(mk3(E.vV[f.x]), mk3(E.vV[f.y]), mk3(E.vV[f.z]), v.V, st) > 0;
+        }
+        unsigned m = __ballot_sync(FULL, lit);
+        if (lane == 0) E.lit[base >> 5] = m;
+    }
+    __syncwarp();
+    // horizon edges in the reference's order (faces from last to first), one lane
+    if (lane == 0) {
+        int ne = 0;
+        for (int index = nt; index-- > 0;) {
+            if (!((E.lit[index >> 5] >> (index & 31)) & 1u)) continue;
+            uchar4 f = E.fi[index];
+            unsigned char cs[3] = {f.x, f.y, f.z};
+            for (int k = 0; k < 3; k++) {
+                unsigned char A = cs[k], B = cs[(k + 1) % 3];
+                bool added = true;
+                for (int e = ne; e-- > 0;) {
+                    bool match = (E.ea[e] == A && E.eb[e] == B) || (E.ea[e] == B && E.eb[e] == A);
+                    if (!match) continue;
+                    --ne;
+                    E.ea[e] = E.ea[ne]; E.eb[e] = E.eb[ne];
+                    added = false;
+                    break;
+                }
+                if (added && ne < 3 * JG_EPA_MAXT) { E.ea[ne] = A; E.eb[ne] = B; ne++; }
+            }
+        }
+        E.ne = ne;
+    }
+    __syncwarp();
+    int ne = E.ne;
+    if (ne == 0) return NO_HORIZON;
+    int nlit = 0;
+    for (int k = 0; k < (nt + 31) / 32; k++) nlit += __popc(E.lit[k] & (k * 32 + 32 <= nt ? 0xffffffffu : ((1u << (nt & 31)) - 1u)));
+    if (nt - nlit + ne > JG_EPA_MAXT) return CAPACITY;
+    // order-preserving compaction of the surviving faces
+    int surv = 0;
+    for (int base = 0; base < nt; base += 32) {
+        int i = base + lane;
+        bool keep = i < nt && !((E.lit[i >> 5] >> (i & 31)) & 1u);
+        uchar4 fi; float4 fn, fc;
+        if (keep) { fi = E.fi[i]; fn = E.fn[i]; fc = E.fc[i]; }
+        unsigned m = __ballot_sync(FULL, keep);
+        int dst = surv + __popc(m & ((1u << lane) - 1u));
+        __syncwarp();
+        if (keep) { E.fi[dst] = fi; E.fn[dst] = fn; E.fc[dst] = fc; }
+        surv += __popc(m);
+        __syncwarp();
+    }
+    // the new fan, one face per lane
+    int res = ADDED;
+    for (int base = 0; base < ne; base += 32) {
+        int e = base + lane;
+        int r = ADDED;
+        if (e < ne) r = create_tri(E, E.ea[e], E.eb[e], nv, surv + e, st);
+        for (int off = 16; off > 0; off >>= 1) {
+            int o = __shfl_xor_sync(FULL, r, off);
+            if (o != ADDED && (r == ADDED || o < r)) r = o;
+        }
+        if (r != ADDED && res == ADDED) res = r;
+    }
+    __syncwarp();
+    if (res != ADDED) {
+        if (lane == 0) { E.nt = 0; E.enclosed = 0; }
+        __syncwarp();
+        return res;
+    }
+    if (lane == 0) { E.nt = surv + ne; E.nv = nv + 1; }
+    __syncwarp();
+    return ADDED;
+}
+
+// MprEpaSolver.SolveMprEpa (NarrowPhase.cs:39-95).  Seed vertices are in E.v*[0..3].
+__device__ bool solve_epa(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb,
+                          v3& p1, v3& p2, v3& n, float& pen, NpStats& st) {
+    const float eps = 1e-5f;
+    const int maxIter = 85;
+    if (!epa_init(E, st)) return false;
+    int iter = 0;
+    int ci = 0;
+    while (++iter < maxIter) {
+        ci = epa_closest(E);
+        float4 fc = E.fc[ci], fn = E.fn[ci];
+        v3 sd = mk3(fc), cl = mk3(fc);
+        float sdsq = fc.w;
+        if (!E.enclosed) sd = -sd;
+        if (fc.w < 1e-16f) { sd = mk3(fn); sdsq = fn.w; }
+        MV v;
+        mk_support(sa, sb, qb, pb, sd, v);
+        float delta = dot(cl - v.V, sd);
+        if (delta * delta <= eps * eps * sdsq) goto converged;
+        {
+            int r = epa_add(E, v, st);
+            if (r == NO_HORIZON) goto converged;
+            if (r != ADDED) return false;
+        }
+    }
+    return false;
+converged:
+    if (!E.enclosed) return false;
+    {
+        // ConvexPolytope.CalculatePoints (ConvexPolytope.cs:169-185)
+        uchar4 f = E.fi[ci];
+        float4 fn = E.fn[ci], fc = E.fc[ci];
+        v3 va = mk3(E.vV[f.x]), vb = mk3(E.vV[f.y]), vc = mk3(E.vV[f.z]);
+        v3 sn = mk3(fn);
+        // rebuild the normal scale the face was built with
+        float ux = va.x - vb.x, uy = va.y - vb.y, uz = va.z - vb.z;
+        float vx = va.x - vc.x, vy = va.y - vc.y, vz = va.z - vc.z;
+        v3 raw = mk3(uy * vz - uz * vy, uz * vx - ux * vz, ux * vy - uy * vx);
+        float nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
+        if (!(nmax > 0)) nmax = 1.f;
+        v3 bc;
+        calc_bary(va, vb, vc, sn, nmax, dot(sn, sn), bc);
+        p1 = (mk3(E.vA[f.x]) * bc.x + mk3(E.vA[f.y]) * bc.y) + mk3(E.vA[f.z]) * bc.z;
+        p2 = (mk3(E.vB[f.x]) * bc.x + mk3(E.vB[f.y]) * bc.y) + mk3(E.vB[f.z]) * bc.z;
+        n = sn * (1.0f / sqrtf(fn.w));
+        pen = sqrtf(fc.w);
+    }
+    return true;
+}
+
+// MprEpaSolver.SolveMpr (NarrowPhase.cs:98-347), all lanes redundantly.
+__device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, float epa_threshold,
+                          v3& pA, v3& pB, v3& normal, float& pen, NpStats& st, int& epa_calls, int& epa_fail) {
+    const float eps = 1e-5f;
+    const int maxIter = 34;
+    const float NumericEpsilon = 1e-16f;
+    MV v0, v1, v2, v3v, v4;
+    v3 t1, t2, t3;
+    pen = 0.0f;
+    mk_center(sa, sb, qb, pb, v0);
+    if (fabsf(v0.V.x) < NumericEpsilon && fabsf(v0.V.y) < NumericEpsilon && fabsf(v0.V.z) < NumericEpsilon) v0.V.x = 1e-05f;
+    normal = -v0.V;
+    mk_support(sa, sb, qb, pb, normal, v1);
+    pA = v1.A; pB = v1.B;
+    if (dot(v1.V, normal) <= 0.0f) return false;
+    normal = cross(v1.V, v0.V);
+    if (len2(normal) < 1e-12f) {
+        normal = v1.V - v0.V;
+        normal = normalize(normal);
+        t1 = v1.A - v1.B;
+        pen = dot(t1, normal);
+        return true;
+    }
+    mk_support(sa, sb, qb, pb, normal, v2);
+    if (dot(v2.V, normal) <= 0.0f) return false;
+    t1 = v1.V - v0.V;
+    t2 = v2.V - v0.V;
+    normal = cross(t1, t2);
+    float dist = dot(normal, v0.V);
+    if (dist > 0.0f) {
+        MV t = v1;
+        v1 = v2; v2 = t;
+        normal = -normal;
+    }
+    int phase2 = 0, phase1 = 0;
+    bool hit = false;
+    while (true) {
+        if (phase1 > maxIter) return false;
+        phase1++;
+        mk_support(sa, sb, qb, pb, normal, v3v);
+        if (dot(v3v.V, normal) <= 0.0f) return false;
+        t1 = cross(v1.V, v3v.V);
+        if (dot(t1, v0.V) < 0.0f) {
+            v2 = v3v;
+            t1 = v1.V - v0.V; t2 = v3v.V - v0.V;
+            normal = cross(t1, t2);
+            continue;
+        }
+        t1 = cross(v3v.V, v2.V);
+        if (dot(t1, v0.V) < 0.0f) {
+            v1 = v3v;
+            t1 = v3v.V - v0.V; t2 = v2.V - v0.V;
+            normal = cross(t1, t2);
+            continue;
+        }
+        break;
+    }
+    while (true) {
+        phase2++;
+        t1 = v2.V - v1.V;
+        t2 = v3v.V - v1.V;
+        normal = cross(t1, t2);
+        float nsq = len2(normal);
+        if (nsq < NumericEpsilon) return false;
+        if (!hit) {
+            float d = dot(normal, v1.V);
+            hit = d >= 0;
+        }
+        mk_support(sa, sb, qb, pb, normal, v4);
+        t3 = v4.V - v3v.V;
+        float delta = dot(t3, normal);
+        pen = dot(v4.V, normal);
+        if (delta * delta <= eps * eps * nsq || pen <= 0.0f || phase2 > maxIter) {
+            if (hit) {
+                float invn = 1.0f / sqrtf(nsq);
+                pen *= invn;
+                if (pen > epa_threshold) {
+                    const int lane = threadIdx.x & 31;
+                    if (lane == 0) {
+                        E.vV[0] = f4(v0.V, 0.f); E.vA[0] = f4(v0.A, 0.f); E.vB[0] = f4(v0.B, 0.f);
+                        E.vV[1] = f4(v1.V, 0.f); E.vA[1] = f4(v1.A, 0.f); E.vB[1] = f4(v1.B, 0.f);
+                        E.vV[2] = f4(v2.V, 0.f); E.vA[2] = f4(v2.A, 0.f); E.vB[2] = f4(v2.B, 0.f);
+                        E.vV[3] = f4(v3v.V, 0.f); E.vA[3] = f4(v3v.A, 0.f); E.vB[3] = f4(v3v.B, 0.f);
+                    }
+                    __syncwarp();
+                    epa_calls++;
+                    if (solve_epa(E, sa, sb, qb, pb, pA, pB, normal, pen, st)) return true;
+                    epa_fail++;
+                }
+                normal = normal * invn;
+                t3 = cross(v1.V, t1);
+                float gamma = dot(t3, normal) * invn;
+                t3 = cross(t2, v1.V);
+                float beta = dot(t3, normal) * invn;
+                float alpha = 1.0f - gamma - beta;
+                pA = alpha * v1.A + beta * v2.A + gamma * v3v.A;
+                pB = alpha * v1.B + beta * v2.B + gamma * v3v.B;
+            }
+            return hit;
+        }
+        t1 = cross(v4.V, v0.V);
+        float d = dot(t1, v1.V);
+        if (d >= 0.0f) {
+            d = dot(t1, v2.V);
+            if (d >= 0.0f) v1 = v4; else v3v = v4;
+        } else {
+            d = dot(t1, v3v.V);
+            if (d >= 0.0f) v2 = v4; else v1 = v4;
+        }
+    }
+}
+
+// NarrowPhase.MprEpa world-space wrapper (NarrowPhase.cs:902-927)
+__device__ bool mpr_epa_world(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qa, q4 qb, v3 pa, v3 pb,
+                              v3& pA, v3& pB, v3& n, float& pen, float threshold, NpStats& st, int& ec, int& ef) {
+    q4 q = qmul(qconj(qa), qb);
+    v3 p = rotate_inv(pb - pa, qa);
+    bool res = solve_mpr(E, sa, sb, q, p, threshold, pA, pB, n, pen, st, ec, ef);
+    pA = rotate(pA, qa); pA = pA + pa;
+    pB = rotate(pB, qa); pB = pB + pa;
+    n = rotate(n, qa);
+    return res;
+}
+
+// ---- TriangleEdgeCollisionFilter (TriangleEdgeCollisionFilter.cs:183-420) ---------------
+enum { KEEP = 0, DISCARD = 1, EDGE = 2 };
+__device__ int edge_evaluate(const WorldDev& w, int tri, q4 tq, v3 tp, bool tri_is_b, v3 cp, v3 n, v3& tn, v3& nn) {
+    const TriDev& T = w.tris[tri];
+    const float cosAngle = 0.999f, edgeThreshold = 0.01f;
+    tn = rotate(mk3(T.n), tq);
+    nn = mk3(0.f);
+    if (tri_is_b) tn = -tn;
+    if (dot(n, tn) < -cosAngle) return DISCARD;
+    v3 a = rotate(mk3(T.a), tq) + tp, b = rotate(mk3(T.b), tq) + tp, c = rotate(mk3(T.c), tq) + tp;
+    v3 pc = cp;
+    {
+        v3 ab = b - a, ac = c - a;
+        v3 pn = normalize(cross(ab, ac));
+        v3 ap = pc - a;
+        float d = dot(ap, pn);
+        pc = pc - d * pn;
+    }
+    v3 e = b - a, pma = pc - a;
+    float d0 = len2(pma - dot(pma, e) * e * (1.0f / len2(e)));
+    e = c - a; pma = pc - a;
+    float d1 = len2(pma - dot(pma, e) * e * (1.0f / len2(e)));
+    e = c - b; pma = pc - b;
+    float d2 = len2(pma - dot(pma, e) * e * (1.0f / len2(e)));
+    if (fminf(fminf(d0, d1), d2) > edgeThreshold * edgeThreshold) return KEEP;
+    int which;
+    if (d0 < d1 && d0 < d2) which = 2;
+    else if (d1 < d2) which = 1;
+    else which = 0;
+    float4 nb = T.nb[which];
+    if (nb.w == 0.f) return KEEP;
+    nn = rotate(mk3(nb), tq);
+    if (tri_is_b) nn = -nn;
+    return EDGE;
+}
+
+// ---- one-shot manifold (CollisionManifold.cs) --------------------------------------------
+__device__ __forceinline__ void push_pt(float4* arr, int& cnt, v3 v) {
+    if (cnt > 0 && len2(mk3(arr[0]) - v) < 0.001f) return;
+    if (cnt > 1 && len2(mk3(arr[cnt - 1]) - v) < 0.001f) return;
+    if ((threadIdx.x & 31) == 0) arr[cnt] = f4(v, 0.f);
+    cnt++;
+    __syncwarp();
+}
+__device__ bool polygon_sign(const float4* poly, int cnt, v3 n, float& sign) {
+    float area = 0.0f;
+    v3 prev = mk3(poly[cnt - 1]);
+    for (int i = 0; i < cnt; i++) { v3 cur = mk3(poly[i]); area += dot(cross(prev, cur), n); prev = cur; }
+    if (fabsf(area) <= 1e-6f) { sign = 0.f; return false; }
+    sign = area < 0.0f ? -1.0f : 1.0f;
+    return true;
+}
+__device__ bool contains_pt(const float4* poly, int cnt, v3 p, v3 n, float sign) {
+    v3 prev = mk3(poly[cnt - 1]);
+    for (int i = 0; i < cnt; i++) {
+        v3 cur = mk3(poly[i]);
+        float sd = sign * dot(cross(cur - prev, p - prev), n);
+        if (sd < -1e-3f) return false;
+        prev = cur;
+    }
+    return true;
+}
+__device__ int clip_segment(v3 s, v3 e, const float4* poly, int pc, v3 n, float sign, v3* out) {
+    const float eps = 1e-3f;
+    float enter = 0.0f, exit = 1.0f;
+    v3 delta = e - s;
+    for (int i = 0; i < pc; i++) {
+        v3 es = mk3(poly[i]), ee = mk3(poly[(i + 1) % pc]);
+        float ss = sign * dot(cross(ee - es, s - es), n);
+        float se = sign * dot(cross(ee - es, e - es), n);
+        bool si = ss >= -eps, ei = se >= -eps;
+        if (!si && !ei) return 0;
+        if (si && ei) continue;
+        float den = ss - se;
+        if (fabsf(den) <= eps) return 0;
+        float t = fminf(fmaxf(ss / den, 0.0f), 1.0f);
+        if (!si) enter = fmaxf(enter, t); else exit = fminf(exit, t);
+        if (exit < enter) return 0;
+    }
+    out[0] = s + enter * delta;
+    if (len2(s + exit * delta - out[0]) < eps) return 1;
+    out[1] = s + exit * delta;
+    return 2;
+}
+__device__ __forceinline__ float cross_along(v3 l, v3 r, v3 n) { return dot(cross(l, r), n); }
+__device__ int intersect_seg(v3 sA, v3 eA, v3 sB, v3 eB, v3 n, v3* cA, v3* cB) {
+    const float eps = 1e-3f;
+    v3 dA = eA - sA, dB = eB - sB, off = sB - sA;
+    float cr = cross_along(dA, dB, n);
+    if (fabsf(cr) <= eps) {
+        if (fabsf(cross_along(off, dA, n)) > eps) return 0;
+        float la = len2(dA), lb = len2(dB);
+        if (la <= eps || lb <= eps) return 0;
+        float b0 = dot(sB - sA, dA) / la, b1 = dot(eB - sA, dA) / la;
+        float enter = fmaxf(0.0f, fminf(b0, b1));
+        float exit = fminf(1.0f, fmaxf(b0, b1));
+        if (exit < enter - eps) return 0;
+        cA[0] = sA + enter * dA;
+        float a0 = fminf(fmaxf(dot(cA[0] - sB, dB) / lb, 0.0f), 1.0f);
+        cB[0] = sB + a0 * dB;
+        cA[1] = sA + exit * dA;
+        if (len2(cA[1] - cA[0]) <= eps) return 1;
+        float a1 = fminf(fmaxf(dot(cA[1] - sB, dB) / lb, 0.0f), 1.0f);
+        cB[1] = sB + a1 * dB;
+        return 2;
+    }
+    float t = cross_along(off, dB, n) / cr;
+    float u = cross_along(off, dA, n) / cr;
+    if (t < -eps || t > 1.0f + eps || u < -eps || u > 1.0f + eps) return 0;
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    u = fminf(fmaxf(u, 0.0f), 1.0f);
+    cA[0] = sA + t * dA;
+    cB[0] = sB + u * dB;
+    return 1;
+}
+__device__ bool is_dup(const float4* m, int cnt, v3 p) {
+    for (int i = 0; i < cnt; i++) if (len2(mk3(m[i]) - p) < 0.001f) return true;
+    return false;
+}
+struct MF {
+    EpaSmem* E;
+    int count;
+    __device__ void set(int i, v3 a, v3 b) {
+        if ((threadIdx.x & 31) == 0) { E->mA[i] = f4(a, 0.f); E->mB[i] = f4(b, 0.f); }
+        __syncwarp();
+    }
+    __device__ void on_a(v3 p, v3 pB, v3 n) {
+        if (count == 12) return;
+        float diff = dot(p - pB, n);
+        if (diff < 0.0f) return;
+        if (is_dup(E->mA, count, p)) return;
+        set(count, p, p - diff * n);
+        count++;
+    }
+    __device__ void on_b(v3 p, v3 pA, v3 n) {
+        if (count == 12) return;
+        float diff = dot(p - pA, n);
+        if (diff > 0.0f) return;
+        if (is_dup(E->mB, count, p)) return;
+        set(count, p - diff * n, p);
+        count++;
+    }
+    __device__ void pair(v3 a, v3 b, v3 n) {
+        if (count == 12) return;
+        if (dot(a - b, n) < 0.0f) return;
+        if (is_dup(E->mA, count, a)) return;
+        if (is_dup(E->mB, count, b)) return;
+        set(count, a, b);
+        count++;
+    }
+};
+
+__device__ int build_manifold(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qa, q4 qb, v3 pa, v3 pb,
+                              v3 pA, v3 pB, v3 n, v3* outA, v3* outB) {
+    const int lane = threadIdx.x & 31;
+    const float P = 0.01f, S = 0.86602540378f;
+    const float hx[12] = {1.0f, 0.0f, 0.5f, S, -0.5f, S, -1.0f, 0.0f, -0.5f, -S, 0.5f, -S};
+    v3 c1 = create_orthonormal(n);
+    v3 c2 = cross(n, c1);
+    v3 relB = pb - pa, pAl = pA - pa, pBl = pB - pa;
+    int lc = 0, rc = 0;
+    for (int e = 0; e < 6; e++) {
+        v3 pn = n + hx[2 * e + 0] * P * c1 + hx[2 * e + 1] * P * c2;
+        v3 np1 = rotate(support(sa, rotate_inv(pn, qa)), qa);
+        push_pt(E.left, lc, np1);
+        pn = -pn;
+        v3 np2 = rotate(support(sb, rotate_inv(pn, qb)), qb) + relB;
+        push_pt(E.right, rc, np2);
+    }
+    float ls = 0.f, rs = 0.f;
+    bool lp = lc > 2 && polygon_sign(E.left, lc, n, ls);
+    bool rp = rc > 2 && polygon_sign(E.right, rc, n, rs);
+    MF m; m.E = &E; m.count = 0;
+    if (lp) {
+        for (int e = 0; e < rc; e++) {
+            v3 p = mk3(E.right[e]);
+            if (!contains_pt(E.left, lc, p, n, ls)) continue;
+            m.on_b(p, pAl, n);
+            if (m.count == 12) goto finalize;
+        }
+        if (rc == 2) {
+            v3 cl[2];
+            int k = clip_segment(mk3(E.right[0]), mk3(E.right[1]), E.left, lc, n, ls, cl);
+            for (int i = 0; i < k; i++) { m.on_b(cl[i], pAl, n); if (m.count == 12) goto finalize; }
+        }
+    }
+    if (rp) {
+        for (int e = 0; e < lc; e++) {
+            v3 p = mk3(E.left[e]);
+            if (!contains_pt(E.right, rc, p, n, rs)) continue;
+            m.on_a(p, pBl, n);
+            if (m.count == 12) goto finalize;
+        }
+        if (lc == 2) {
+            v3 cl[2];
+            int k = clip_segment(mk3(E.left[0]), mk3(E.left[1]), E.right, rc, n, rs, cl);
+            for (int i = 0; i < k; i++) { m.on_a(cl[i], pBl, n); if (m.count == 12) goto finalize; }
+        }
+    }
+    if (lc == 2 && rc == 2) {
+        v3 cA[2], cB[2];
+        int k = intersect_seg(mk3(E.left[0]), mk3(E.left[1]), mk3(E.right[0]), mk3(E.right[1]), n, cA, cB);
+        for (int i = 0; i < k; i++) { m.pair(cA[i], cB[i], n); if (m.count == 12) goto finalize; }
+    }
+    if (lp && rp) {
+        // every (left edge, right edge) intersection, one lane per edge pair, inserted in
+        // the reference's (i, j) order
+        int total = lc * rc;
+        for (int base = 0; base < total; base += 32) {
+            int idx = base + lane;
+            v3 cA[2], cB[2];
+            int k = 0;
+            if (idx < total) {
+                int i = idx / rc, j = idx % rc;
+                k = intersect_seg(mk3(E.left[i]), mk3(E.left[(i + 1) % lc]), mk3(E.right[j]), mk3(E.right[(j + 1) % rc]), n, cA, cB);
+            }
+            unsigned any = __ballot_sync(FULL, k > 0);
+            while (any) {
+                int src = __ffs(any) - 1;
+                any &= any - 1;
+                int kk = __shfl_sync(FULL, k, src);
+                for (int q = 0; q < kk; q++) {
+                    v3 a, b;
+                    a.x = __shfl_sync(FULL, cA[q].x, src); a.y = __shfl_sync(FULL, cA[q].y, src); a.z = __shfl_sync(FULL, cA[q].z, src);
+                    b.x = __shfl_sync(FULL, cB[q].x, src); b.y = __shfl_sync(FULL, cB[q].y, src); b.z = __shfl_sync(FULL, cB[q].z, src);
+                    m.pair(a, b, n);
+                    if (m.count == 12) goto finalize;
+                }
+            }
+        }
+    }
+    if (m.count <= 1) { m.set(0, pAl, pBl); m.count = 1; }
+    else if (m.count < 4) { m.set(m.count, pAl, pBl); m.count++; }
+finalize:
+    int count = m.count;
+    if (count > 4) {
+        // ReduceManifold (CollisionManifold.cs:321-375)
+        v3 c = mk3(0.f);
+        for (int i = 0; i < count; i++) c = c + mk3(E.mA[i]);
+        c = c * (float)(1.0 / count);
+        v3 t1 = create_orthonormal(n);
+        v3 t2 = cross(n, t1);
+        float ang[12];
+        int order[12];
+        for (int i = 0; i < count; i++) {
+            v3 d = mk3(E.mA[i]) - c;
+            ang[i] = StableMathF::atan2(dot(d, t2), dot(d, t1));
+            order[i] = i;
+        }
+        for (int i = 1; i < count; i++) {
+            int cur = order[i];
+            float ca = ang[cur];
+            int j = i - 1;
+            while (j >= 0 && ang[order[j]] > ca) { order[j + 1] = order[j]; j--; }
+            order[j + 1] = cur;
+        }
+        for (int i = 0; i < 4; i++) {
+            int sel = order[((2 * i + 1) * count) / 8];
+            outA[i] = mk3(E.mA[sel]) + pa;
+            outB[i] = mk3(E.mB[sel]) + pa;
+        }
+        __syncwarp();
+        return 4;
+    }
+    for (int i = 0; i < count; i++) { outA[i] = mk3(E.mA[i]) + pa; outB[i] = mk3(E.mB[i]) + pa; }
+    __syncwarp();
+    return count;
+}
+
+constexpr int NP_WARPS = 4;
+
+__global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams sp) {
+    __shared__ EpaSmem smem[NP_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    EpaSmem& E = smem[wib];
+    NpStats st; st.exact = 0;
+    int epa_calls = 0, epa_fail = 0, written = 0, pts = 0;
+    int npairs = min(w.ctr->npairs, w.cap_pairs);
+    for (int p = blockIdx.x * NP_WARPS + wib; p < npairs; p += gridDim.x * NP_WARPS) {
+        int2 pr = w.pairs[p];
+        int s1 = pr.x, s2 = pr.y;  // s1 < s2: ShapeId order (World.Detect.cs:141-144)
+        ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
+        int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
+        int4 i1 = w.binfo[b1], i2 = w.binfo[b2];
+        if (!(i1.y & JG_BODY_ACTIVE) && !(i2.y & JG_BODY_ACTIVE)) continue;
+        if (i1.x != JG_MOTION_DYNAMIC && i2.x != JG_MOTION_DYNAMIC) continue;
+        q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+        v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+        v3 pA, pB, n;
+        float pen;
+        bool hit = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, n, pen, 0.02f, st, epa_calls, epa_fail);
+        if (!hit) continue;  // speculative contacts (off by default, RigidBody.cs:863) not handled
+        if (sp.edge_filter) {
+            bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
+            bool tri_dyn = c1 ? i1.x == JG_MOTION_DYNAMIC : i2.x == JG_MOTION_DYNAMIC;
+            if (c1 != c2 && !tri_dyn) {
+                int tri = c1 ? sa.tri : sb.tri;
+                q4 tq = c1 ? qa : qb;
+                v3 tp = c1 ? pa : pb;
+                v3 tn, nn;
+                int ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
+                if (ev == DISCARD) continue;
+                if (ev == EDGE) {
+                    bool spec = pen < 0.0f;
+                    bool keep = true, done = false;
+                    if (!spec) {
+                        bool res = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, n, pen, 0.0f, st, epa_calls, epa_fail);
+                        if (!res) keep = false;
+                        else {
+                            ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
+                            if (ev == DISCARD) keep = false;
+                            else if (ev == KEEP) done = true;
+                        }
+                    }
+                    if (!keep) continue;
+                    if (!done) {
+                        v3 mid = 0.5f * (pA + pB);
+                        if (dot(tn, nn) > 0.999f) {
+                            float f5 = dot(n, nn), f6 = dot(n, tn);
+                            if (!spec) { pen = 0; pA = pB = mid; }
+                            n = f5 > f6 ? nn : tn;
+                        } else {
+                            v3 cr = cross(nn, tn);
+                            float crl = len2(cr);
+                            v3 proj = n - (dot(cr, n) / crl) * cr;
+                            if (len2(proj) < 0.5f * 0.5f) continue;
+                            float f1 = dot(cross(proj, nn), cr);
+                            float f2 = dot(cross(proj, tn), cr);
+                            bool between = f1 <= 0.0f && f2 >= 0.0f;
+                            if (!between) {
+                                float f3 = dot(n, nn), f4v = dot(n, tn);
+                                if (!spec) { pen = 0; pA = pB = mid; }
+                                n = f3 > f4v ? nn : tn;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        v3 oA[4], oB[4];
+        int cnt;
+        if (sp.aux_contacts) cnt = build_manifold(E, sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
+        else { cnt = 1; oA[0] = pA; oB[0] = pB; }
+        if (lane == 0) {
+            int idx = atomicAdd(&w.ctr->nstream, 1);
+            if (idx < w.cap_pairs) {
+                w.cs_key[idx] = make_int2(s1, s2);
+                w.cs_n[idx] = f4(n, __int_as_float(cnt));
+                for (int k = 0; k < cnt; k++) {
+                    w.cs_pa[4 * idx + k] = f4(oA[k], 0.f);
+                    w.cs_pb[4 * idx + k] = f4(oB[k], 0.f);
+                }
+            } else {
+                atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY);
+            }
+        }
+        written++;
+        pts += cnt;
+    }
+    if (lane == 0) {
+        if (epa_calls) atomicAdd(&w.ctr->nepa, epa_calls);
+        if (epa_fail) atomicAdd(&w.ctr->epa_fail, epa_fail);
+        if (pts) atomicAdd(&w.ctr->points, pts);
+    }
+    int ex = st.exact;
+    for (int off = 16; off > 0; off >>= 1) ex += __shfl_xor_sync(FULL, ex, off);
+    if (lane == 0 && ex) atomicAdd(&w.ctr->exact, ex);
+    (void)written;
+}
+
+}  // namespace
+
+void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
+    (void)tile;
+    int blocks = nsm * 8;
+    k_narrow<<<blocks, NP_WARPS * 32, 0, s>>>(w, p);
+}

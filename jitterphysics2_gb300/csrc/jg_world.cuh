@@ -1,0 +1,162 @@
+// Device-resident world state of the GB300 contact pipeline and the launch entry points
+// of each stage.  Layout (all SoA or 64-byte records, 16-byte aligned):
+//   bodies    SBody[nb]      64 B solver record: v|invM.x, w|invM.y, I^-1 world (6), invM.z, flags
+//             pos/q/dv/dw/...  float4 per body, read by integration and the per-step update
+//   shapes    int4 info + float4 dims/centre, hull vertices float4, triangles TriDev
+//   arbiters  ArbStore (double-buffered): key, bodies, usage/mode/colour, material, and
+//             8 float4 fields per contact slot stored as [slot * capacity + arbiter]
+//   joints    JointDev records (BallSocket / HingeAngle)
+// Arbiters are kept sorted by solver colour: the colouring stage permutes them into the
+// other buffer, so each colour is a contiguous, coalesced range during the solve.
+#pragma once
+#include "jg_math.cuh"
+#include "../../include/jitter_gpu.h"
+
+#define JG_MAX_COLORS 128
+#define JG_HULL_MAX 64          // point-cloud vertices per shape handled on the device
+#define JG_EPA_MAXV 64          // EPA polytope capacity on the device (reference: 128/256)
+#define JG_EPA_MAXT 128
+
+struct __align__(16) SBody {
+    float4 v;   // velocity xyz, inverse mass x
+    float4 w;   // angular velocity xyz, inverse mass y
+    float4 i0;  // world inverse inertia M11 M12 M13 M22
+    float4 i1;  // M23 M33, inverse mass z, flags (int bits: 1 dynamic, 2 linear locks)
+};
+#define SB_DYNAMIC 1
+#define SB_LINLOCK 2
+
+struct __align__(16) TriDev {
+    float4 a, b, c;    // mesh-local vertices
+    float4 n;          // unit normal
+    float4 nb[3];      // neighbour normals across edges A, B, C; w = 1 when the neighbour exists
+};
+
+struct ArbStore {
+    int2* key;      // shape ids (ArbiterKey)
+    int2* body;     // body indices
+    int4* info;     // usage mask, solve mode, colour, created-this-step flag
+    float4* mat;    // friction, restitution, speculative relaxation, 0
+    float4* cn;     // normal xyz, Bias
+    float4* ct1;    // tangent1 xyz, PenaltyBias
+    float4* ct2;    // tangent2 xyz, contact flags (int bits)
+    float4* cr1;    // RelativePosition1 xyz, mass normal
+    float4* cr2;    // RelativePosition2 xyz, mass tangent1
+    float4* cacc;   // accumulated normal, tangent1, tangent2, mass tangent2
+    float4* cp1;    // Position1 (local) xyz, 0
+    float4* cp2;    // Position2 (local) xyz, 0
+};
+
+struct __align__(16) JointDev {
+    int4 hdr;        // kind, body1, body2, colour
+    float4 la1, la2; // BallSocket local anchors
+    float4 r1, r2;   // world anchors (prepare)
+    float4 acc;      // accumulated impulse
+    float4 bias;
+    float4 eff[3];   // effective mass rows
+    float4 jac[3];   // HingeAngle Jacobian columns
+    float4 axis;     // hinge axis (local to body 2)
+    float4 q0;       // hinge reference rotation
+    float4 lim;      // min, max, fixed angle, clamp (as float)
+    float4 prm;      // bias factor, softness, limit bias, limit softness
+    float4 bil;      // bilateral block inverse xyz, hemisphere
+    float4 cpl;      // coupling x, coupling y
+};
+
+struct DevCounters {
+    int npairs;
+    int nstream;      // colliding pairs written by the narrowphase
+    int nepa;         // pairs queued for EPA
+    int narb;         // arbiters in the current store
+    int nnew;         // arbiters created this step
+    int ncolors;
+    int nremoved;
+    int status;       // JG_ERR_* raised on the device
+    int epa_fail;
+    int exact;
+    int points;       // manifold points written
+    int contacts;     // active contact points after the merge
+    int new_contacts;
+    int color_rounds;
+    int pad[2];
+};
+
+struct WorldDev {
+    // capacities
+    int cap_bodies, cap_shapes, cap_pairs, cap_arb, cap_joints, cap_hull, cap_tris;
+    int nb, ns, nj, nhull, ntris, nworlds;
+    // bodies
+    SBody* body;
+    float4 *pos, *q, *dv, *dw, *il0, *il1, *force, *torque, *mat;
+    int4* binfo;                 // motion, flags, world, 0
+    // shapes
+    int4* sinfo;                 // kind, body, data offset, data count
+    float4 *sdims, *scenter, *hull;
+    TriDev* tris;
+    float4 *amin, *amax;         // world AABBs
+    // broadphase
+    unsigned long long *mkey, *mkey_alt;
+    int *midx, *midx_alt;
+    int *hist;                   // radix histograms
+    int4* node;                  // internal nodes: left, right, parent, first|last packed
+    int2* node_range;            // leaf range [first, last] per internal node
+    float4 *nmin, *nmax;         // internal node AABBs
+    int* leaf_parent;
+    int* node_flag;
+    float4* scene_box;           // [0] min, [1] max (reduction)
+    int2* pairs;
+    // narrowphase output (contact stream) and EPA queue
+    int2* cs_key;
+    float4* cs_n;                // normal xyz, count
+    float4* cs_pa;               // [4 * cap_pairs]
+    float4* cs_pb;
+    int* epa_pair;               // pair index
+    float4* epa_seed;            // [4 * 3 * cap] MPR portal vertices V, A, B
+    float4* epa_mpr;             // MPR fallback: pA, pB, n|pen
+    int* epa_flag;               // bit0: threshold-zero rerun from the edge filter
+    // arbiters
+    ArbStore arb[2];
+    int cur;                     // which ArbStore holds the live arbiters
+    unsigned long long* hkeys;   // hash table keys
+    int* hvals;
+    int hcap;
+    // colouring
+    int* cstat;                  // per constraint: colour or -1
+    unsigned long long* bmask;   // per body: used colours (2 words)
+    int* adj_off;                // CSR body -> constraints
+    int* adj;
+    int* deg;
+    int* color_count;            // [JG_MAX_COLORS + 1]
+    int* color_start;            // [JG_MAX_COLORS + 1] arbiters
+    int* jcolor_start;           // [JG_MAX_COLORS + 1] joints
+    int* color_cursor;
+    int* jorder;                 // joints sorted by colour
+    // joints
+    JointDev* joints;
+    // solver bookkeeping
+    unsigned* bar_count;         // grid barrier
+    unsigned* bar_gen;
+    float* resid;                // per iteration: sum dlambda^2, sum lambda^2 [2 * 64]
+    float* mlp_w;                // MLP parameters (device)
+    DevCounters* ctr;
+};
+
+struct StepParams {
+    float dt, sub_dt, inv_dt, inv_sub_dt;
+    float3 gravity;
+    int substeps, iterations, relax;
+    int aux_contacts, persistent, edge_filter;
+    float spec_relax;
+    int warm_start;
+    int record_residual;
+};
+
+// ---- stage launchers (each defined in its own translation unit) ------------------------
+void jg_launch_aabb(WorldDev& w, cudaStream_t s);
+int  jg_launch_broadphase(WorldDev& w, cudaStream_t s, int nsm);
+void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile);
+void jg_launch_merge(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+void jg_launch_color(WorldDev& w, cudaStream_t s, int nsm);
+int  jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm);
+void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+void jg_launch_mlp_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);

@@ -1,0 +1,178 @@
+"""Host-side mirror of the reference's World API for the contact hot path.
+
+`World` plays the part of Jitter2's `World` (src/Jitter2/World.cs, World.Step.cs): it
+owns a device-resident jg_world, takes bodies and shapes (as the reference's
+CreateRigidBody / AddShape / SetMassInertia / CreateConstraint calls would leave them)
+and steps with `step(dt)`, which raises the reference's exception types on the same
+conditions (ArgumentException for a negative dt, World.Step.cs:157-165).  Everything
+is routed through the C ABI; there is no CPU code path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+from .abi import check, ptr
+
+
+class ArgumentException(ValueError):
+    """World.Step's ArgumentException for an invalid time step."""
+
+
+class World:
+    def __init__(self, substeps=1, solver_iterations=6, relax_iterations=4, gravity=(0.0, -9.81, 0.0),
+                 max_bodies=1024, max_shapes=None, max_pairs=None, max_arbiters=None, max_constraints=1024,
+                 n_worlds=1, **params):
+        lib = abi.load()
+        max_shapes = max_shapes or max_bodies
+        p = abi.default_params(substeps=substeps, solver_iterations=solver_iterations,
+                               relax_iterations=relax_iterations, gravity=gravity, max_bodies=max_bodies,
+                               max_shapes=max_shapes, max_pairs=max_pairs or max(4096, 24 * max_shapes),
+                               max_arbiters=max_arbiters or max(4096, 8 * max_shapes),
+                               max_constraints=max_constraints, **params)
+        self.params = p
+        h = ctypes.c_void_p()
+        if n_worlds > 1:
+            check(lib.jg_batch_create(ctypes.byref(p), n_worlds, ctypes.byref(h)), "jg_batch_create")
+        else:
+            check(lib.jg_create(ctypes.byref(p), ctypes.byref(h)), "jg_create")
+        self._h = h
+        self._lib = lib
+        self.n_bodies = 0
+        self.n_shapes = 0
+        self.n_joints = 0
+
+    # -- lifetime ------------------------------------------------------------------------
+    def close(self):
+        if self._h:
+            self._lib.jg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- scene --------------------------------------------------------------------------
+    def set_bodies(self, bodies):
+        b = np.ascontiguousarray(bodies, abi.BODY_DTYPE)
+        check(self._lib.jg_upload_bodies(self._h, ptr(b), len(b)), "jg_upload_bodies")
+        self.n_bodies = len(b)
+
+    def set_shapes(self, shapes, hull=None, triangles=None):
+        s = np.ascontiguousarray(shapes, abi.SHAPE_DTYPE)
+        h = np.ascontiguousarray(hull if hull is not None else np.zeros((0, 3)), np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles if triangles is not None else np.zeros(0, abi.TRIANGLE_DTYPE),
+                                 abi.TRIANGLE_DTYPE)
+        check(self._lib.jg_upload_shapes(self._h, ptr(s), len(s), ptr(h), len(h), ptr(t), len(t)), "jg_upload_shapes")
+        self.n_shapes = len(s)
+
+    def add_constraint(self, kind, body1, body2, init):
+        v = np.ascontiguousarray(init, np.float32)
+        out = ctypes.c_int32()
+        check(self._lib.jg_add_constraint(self._h, kind, body1, body2, ptr(v), ctypes.byref(out)), "jg_add_constraint")
+        self.n_joints += 1
+        return out.value
+
+    def load_scene(self, scene):
+        self.set_bodies(scene["bodies"])
+        self.set_shapes(scene["shapes"], scene["hull"], scene["triangles"])
+        for kind, b1, b2, init in scene.get("joints", []):
+            if kind == abi.CONSTRAINT_BALLSOCKET:
+                self.add_constraint(kind, b1, b2, np.array(init, np.float32))
+            else:
+                self.add_constraint(kind, b1, b2, np.array(init, np.float32))
+
+    def set_body(self, index, field, value):
+        fields = {"position": 0, "orientation": 1, "velocity": 2, "angular_velocity": 3, "force": 4, "torque": 5}
+        v = np.ascontiguousarray(value, np.float32)
+        check(self._lib.jg_set_body(self._h, index, fields[field], ptr(v)), "jg_set_body")
+
+    # -- stepping -----------------------------------------------------------------------
+    def step(self, dt):
+        """World.Step(dt) (World.Step.cs:141-296) on the device."""
+        if not np.isfinite(dt):
+            raise ArgumentException("Time step must be finite.")
+        if dt < 0:
+            raise ArgumentException("Time step cannot be negative.")
+        check(self._lib.jg_step(self._h, ctypes.c_float(dt)), "jg_step")
+
+    def step_host(self, dt, bodies):
+        """One step with the body state copied in from and back to a host array."""
+        check(self._lib.jg_step_host(self._h, ctypes.c_float(dt), ptr(bodies), len(bodies)), "jg_step_host")
+
+    # -- inspection ---------------------------------------------------------------------
+    def bodies(self):
+        out = np.zeros(self.n_bodies, abi.BODY_DTYPE)
+        check(self._lib.jg_download_bodies(self._h, ptr(out), self.n_bodies), "jg_download_bodies")
+        return out
+
+    def contacts(self):
+        n = ctypes.c_int32()
+        check(self._lib.jg_get_contacts(self._h, None, 0, ctypes.byref(n)), "jg_get_contacts")
+        out = np.zeros(max(n.value, 1), abi.CONTACT_DTYPE)
+        check(self._lib.jg_get_contacts(self._h, ptr(out), len(out), ctypes.byref(n)), "jg_get_contacts")
+        return out[:n.value]
+
+    def counters(self):
+        buf = np.zeros(len(abi.COUNTER_NAMES), np.int64)
+        check(self._lib.jg_get_counters(self._h, ptr(buf)), "jg_get_counters")
+        return dict(zip(abi.COUNTER_NAMES, buf.tolist()))
+
+    def timings(self):
+        buf = np.zeros(len(abi.TIMING_NAMES), np.float32)
+        check(self._lib.jg_get_timings(self._h, ptr(buf)), "jg_get_timings")
+        return dict(zip(abi.TIMING_NAMES, buf.tolist()))
+
+    def residuals(self):
+        buf = np.zeros(64, np.float32)
+        n = ctypes.c_int32()
+        check(self._lib.jg_get_residuals(self._h, ptr(buf), 64, ctypes.byref(n)), "jg_get_residuals")
+        return buf[:n.value].copy()
+
+    def arbiter_events(self):
+        cap = 1 << 20
+        created = np.zeros((cap, 2), np.int32)
+        removed = np.zeros((cap, 2), np.int32)
+        nc, nr = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.jg_get_arbiter_events(self._h, ptr(created), cap, ctypes.byref(nc), ptr(removed), cap,
+                                              ctypes.byref(nr)), "jg_get_arbiter_events")
+        return created[:nc.value].copy(), removed[:nr.value].copy()
+
+    def export_state(self):
+        size = ctypes.c_int64()
+        check(self._lib.jg_export_state(self._h, None, 0, ctypes.byref(size)), "jg_export_state")
+        buf = np.zeros(size.value, np.uint8)
+        check(self._lib.jg_export_state(self._h, ptr(buf), size.value, ctypes.byref(size)), "jg_export_state")
+        return buf
+
+    def import_state(self, buf):
+        b = np.ascontiguousarray(buf, np.uint8)
+        check(self._lib.jg_import_state(self._h, ptr(b), len(b)), "jg_import_state")
+
+    def autotune(self, dt, steps=3):
+        chosen = abi.WorldParams()
+        check(self._lib.jg_autotune(self._h, ctypes.c_float(dt), steps, ctypes.byref(chosen)), "jg_autotune")
+        return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile")}
+
+    @property
+    def handle(self):
+        return self._h
+
+
+def world_for_scene(scene, **overrides):
+    """A World sized for a scene from jitterphysics2_gb300.scenes, with its solver settings."""
+    nb, ns = len(scene["bodies"]), len(scene["shapes"])
+    kw = dict(scene.get("params", {}))
+    kw.update(overrides)
+    w = World(max_bodies=nb, max_shapes=ns, max_constraints=max(16, len(scene.get("joints", []))),
+              n_worlds=scene.get("n_worlds", 1), **kw)
+    w.load_scene(scene)
+    return w

@@ -1,0 +1,394 @@
+// Oracle (test infrastructure only): CPU restatement of the two joint kinds the batched
+// world configuration uses: BallSocket (Dynamics/Constraints/BallSocket.cs:140-252) and
+// HingeAngle (Dynamics/Constraints/HingeAngle.cs:84-364), with their math helpers
+// (AngularConstraintMath.cs:13-95, MathHelper.cs:282-372, JMatrix.cs:391-478).
+#pragma once
+#include "jor_dynamics.hpp"
+
+namespace jor {
+
+template <class R> struct Mat {
+    R a[3][3];
+    Mat() { for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) a[i][j] = 0; }
+    static Mat ident() { Mat m; m.a[0][0] = m.a[1][1] = m.a[2][2] = 1; return m; }
+    static Mat skew(V3<R> v) { Mat m; m.a[0][1] = -v.z; m.a[0][2] = v.y; m.a[1][0] = v.z; m.a[1][2] = -v.x; m.a[2][0] = -v.y; m.a[2][1] = v.x; return m; }
+    static Mat from_sym(const Sym3<R>& s) {
+        Mat m;
+        m.a[0][0] = s.m11; m.a[0][1] = s.m12; m.a[0][2] = s.m13;
+        m.a[1][0] = s.m12; m.a[1][1] = s.m22; m.a[1][2] = s.m23;
+        m.a[2][0] = s.m13; m.a[2][1] = s.m23; m.a[2][2] = s.m33;
+        return m;
+    }
+    static Mat from_m3(const M3<R>& s) { Mat m; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) m.a[i][j] = s.m[i][j]; return m; }
+};
+// JMatrix.Multiply (JMatrix.cs:156-180)
+template <class R> Mat<R> mmul(const Mat<R>& x, const Mat<R>& y) {
+    Mat<R> o;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) o.a[i][j] = x.a[i][0] * y.a[0][j] + x.a[i][1] * y.a[1][j] + x.a[i][2] * y.a[2][j];
+    return o;
+}
+template <class R> Mat<R> madd(const Mat<R>& x, const Mat<R>& y) { Mat<R> o; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] = x.a[i][j] + y.a[i][j]; return o; }
+template <class R> Mat<R> msub(const Mat<R>& x, const Mat<R>& y) { Mat<R> o; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] = x.a[i][j] - y.a[i][j]; return o; }
+template <class R> Mat<R> mscale(R s, const Mat<R>& x) { Mat<R> o; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] = s * x.a[i][j]; return o; }
+template <class R> Mat<R> mtrans(const Mat<R>& x) { Mat<R> o; for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] = x.a[j][i]; return o; }
+template <class R> V3<R> mvec(const Mat<R>& M, V3<R> v) {
+    return {v.x * M.a[0][0] + v.y * M.a[0][1] + v.z * M.a[0][2], v.x * M.a[1][0] + v.y * M.a[1][1] + v.z * M.a[1][2],
+            v.x * M.a[2][0] + v.y * M.a[2][1] + v.z * M.a[2][2]};
+}
+template <class R> V3<R> mtvec(const Mat<R>& M, V3<R> v) {
+    return {v.x * M.a[0][0] + v.y * M.a[1][0] + v.z * M.a[2][0], v.x * M.a[0][1] + v.y * M.a[1][1] + v.z * M.a[2][1],
+            v.x * M.a[0][2] + v.y * M.a[1][2] + v.z * M.a[2][2]};
+}
+// JMatrix.Determinant (JMatrix.cs:391-395)
+template <class R> R mdet(const Mat<R>& m) {
+    const auto& a = m.a;
+    return a[0][0] * a[1][1] * a[2][2] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+           a[2][0] * a[1][1] * a[0][2] - a[2][1] * a[1][2] * a[0][0] - a[2][2] * a[1][0] * a[0][1];
+}
+template <class R> bool mfinite(const Mat<R>& m) { for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) if (!std::isfinite(m.a[i][j])) return false; return true; }
+// JMatrix.TryInverseUnscaled (JMatrix.cs:448-480)
+template <class R> bool minv_unscaled(const Mat<R>& m, Mat<R>& o) {
+    R idet = (R)1.0 / mdet(m);
+    if (!std::isnormal(idet)) { o = Mat<R>(); return false; }
+    const auto& a = m.a;
+    o.a[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) * idet;
+    o.a[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * idet;
+    o.a[0][2] = (a[0][1] * a[1][2] - a[1][1] * a[0][2]) * idet;
+    o.a[1][0] = (a[1][2] * a[2][0] - a[2][2] * a[1][0]) * idet;
+    o.a[1][1] = (a[0][0] * a[2][2] - a[2][0] * a[0][2]) * idet;
+    o.a[1][2] = (a[0][2] * a[1][0] - a[1][2] * a[0][0]) * idet;
+    o.a[2][0] = (a[1][0] * a[2][1] - a[2][0] * a[1][1]) * idet;
+    o.a[2][1] = (a[0][1] * a[2][0] - a[2][1] * a[0][0]) * idet;
+    o.a[2][2] = (a[0][0] * a[1][1] - a[1][0] * a[0][1]) * idet;
+    return mfinite(o);
+}
+// JMatrix.Inverse (JMatrix.cs:404-437)
+template <class R> bool minv(const Mat<R>& m, Mat<R>& o) {
+    if (minv_unscaled(m, o)) return true;
+    R s = 0;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) s = std::max(s, std::abs(m.a[i][j]));
+    if (s > 0 && std::isfinite(s)) {
+        Mat<R> n;
+        for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) n.a[i][j] = m.a[i][j] / s;
+        if (minv_unscaled(n, o)) {
+            for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.a[i][j] /= s;
+            if (mfinite(o)) return true;
+        }
+    }
+    o = Mat<R>();
+    return false;
+}
+template <class R> R tol() { return sizeof(R) == 8 ? (R)1e-12 : (R)1e-6; }
+// MathHelper.JacobiRotate (MathHelper.cs:374-406)
+template <class R> bool jacobi_rotate(R* a, R* basis, int p, int q, R t) {
+    R off = a[3 * p + q];
+    if (std::abs(off) <= t) return false;
+    R tau = (a[3 * q + q] - a[3 * p + p]) / ((R)2.0 * off);
+    R tg = std::copysign((R)1.0, tau) / (std::abs(tau) + std::sqrt((R)1.0 + tau * tau));
+    R cs = (R)1.0 / std::sqrt((R)1.0 + tg * tg);
+    R sn = tg * cs;
+    a[3 * p + p] -= tg * off;
+    a[3 * q + q] += tg * off;
+    a[3 * p + q] = a[3 * q + p] = 0;
+    for (int k = 0; k < 3; k++) {
+        if (k != p && k != q) {
+            R akp = a[3 * k + p], akq = a[3 * k + q];
+            a[3 * k + p] = a[3 * p + k] = cs * akp - sn * akq;
+            a[3 * k + q] = a[3 * q + k] = sn * akp + cs * akq;
+        }
+        R vkp = basis[3 * k + p], vkq = basis[3 * k + q];
+        basis[3 * k + p] = cs * vkp - sn * vkq;
+        basis[3 * k + q] = sn * vkp + cs * vkq;
+    }
+    return true;
+}
+// MathHelper.PseudoInverseSymmetric (MathHelper.cs:282-325)
+template <class R> Mat<R> pinv_sym(const Mat<R>& m) {
+    R s = std::max(std::abs(m.a[0][0]), std::max(std::abs(m.a[1][1]), std::abs(m.a[2][2])));
+    if (!(s > 0) || !std::isfinite(s)) return Mat<R>();
+    Sym3<R> n(m.a[0][0] / s, m.a[0][1] / s, m.a[0][2] / s, m.a[1][1] / s, m.a[1][2] / s, m.a[2][2] / s);
+    R t = tol<R>();
+    Mat<R> inv;
+    if (std::abs(sym_det(n)) > t && minv(m, inv)) return inv;
+    R a[9] = {n.m11, n.m12, n.m13, n.m12, n.m22, n.m23, n.m13, n.m23, n.m33};
+    R basis[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int sw = 0; sw < 8; sw++) {
+        bool ch = jacobi_rotate(a, basis, 0, 1, t);
+        ch |= jacobi_rotate(a, basis, 0, 2, t);
+        ch |= jacobi_rotate(a, basis, 1, 2, t);
+        if (!ch) break;
+    }
+    Sym3<R> r;
+    for (int i = 0; i < 3; i++) {
+        R ev = a[3 * i + i];
+        if (!(ev > t)) continue;
+        R wgt = ((R)1.0 / ev) / s;
+        V3<R> ax(basis[i], basis[3 + i], basis[6 + i]);
+        r.m11 += wgt * (ax.x * ax.x); r.m12 += wgt * (ax.x * ax.y); r.m13 += wgt * (ax.x * ax.z);
+        r.m22 += wgt * (ax.y * ax.y); r.m23 += wgt * (ax.y * ax.z); r.m33 += wgt * (ax.z * ax.z);
+    }
+    return Mat<R>::from_sym(r);
+}
+// MathHelper.InverseSymmetric (MathHelper.cs:328-365)
+template <class R> Mat<R> inverse_symmetric(const Mat<R>& m) {
+    R t = tol<R>();
+    R dp = m.a[0][0] * m.a[1][1] * m.a[2][2];
+    Mat<R> inv;
+    if (mdet(m) / dp > t && minv(m, inv)) return inv;
+    R x = m.a[0][0] > 0 ? std::sqrt(m.a[0][0]) : 0;
+    R y = m.a[1][1] > 0 ? std::sqrt(m.a[1][1]) : 0;
+    R z = m.a[2][2] > 0 ? std::sqrt(m.a[2][2]) : 0;
+    if (x == 0 && y == 0 && z == 0) return Mat<R>();
+    R xy = x > 0 && y > 0 ? m.a[0][1] / x / y : 0;
+    R xz = x > 0 && z > 0 ? m.a[0][2] / x / z : 0;
+    R yz = y > 0 && z > 0 ? m.a[1][2] / y / z : 0;
+    Mat<R> nrm;
+    nrm.a[0][0] = 1; nrm.a[0][1] = xy; nrm.a[0][2] = xz;
+    nrm.a[1][0] = xy; nrm.a[1][1] = 1; nrm.a[1][2] = yz;
+    nrm.a[2][0] = xz; nrm.a[2][1] = yz; nrm.a[2][2] = 1;
+    Mat<R> resp = pinv_sym(nrm);
+    xy = x > 0 && y > 0 ? resp.a[0][1] / x / y : 0;
+    xz = x > 0 && z > 0 ? resp.a[0][2] / x / z : 0;
+    yz = y > 0 && z > 0 ? resp.a[1][2] / y / z : 0;
+    Mat<R> r;
+    r.a[0][0] = x > 0 ? resp.a[0][0] / x / x : 0; r.a[0][1] = xy; r.a[0][2] = xz;
+    r.a[1][0] = xy; r.a[1][1] = y > 0 ? resp.a[1][1] / y / y : 0; r.a[1][2] = yz;
+    r.a[2][0] = xz; r.a[2][1] = yz; r.a[2][2] = z > 0 ? resp.a[2][2] / z / z : 0;
+    return mfinite(r) ? r : Mat<R>();
+}
+// MathHelper.InverseBilateralBlock (MathHelper.cs:367-372)
+template <class R> V3<R> inverse_bilateral(const Mat<R>& m) {
+    Mat<R> b;
+    b.a[0][0] = m.a[0][0]; b.a[0][1] = m.a[0][1]; b.a[1][0] = m.a[0][1]; b.a[1][1] = m.a[1][1];
+    Mat<R> inv = inverse_symmetric(b);
+    return V3<R>(inv.a[0][0], inv.a[0][1], inv.a[1][1]);
+}
+// AngularConstraintMath.ShortestAngle (AngularConstraintMath.cs:13-21)
+template <class R> R shortest_angle(R angle, R half) {
+    if (angle >= -half && angle <= half) return angle;
+    R period = (R)2 * half;
+    angle = std::fmod(angle, period);
+    if (angle > half) angle -= period;
+    else if (angle < -half) angle += period;
+    return angle;
+}
+// AngularConstraintMath.CalculateJacobian (AngularConstraintMath.cs:65-95)
+template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, short& hemi) {
+    Q4<R> q = qmul(left, right);
+    hemi = q.w < 0 ? (short)-1 : (short)1;
+    if (q.w < 0) q = Q4<R>(-q.x, -q.y, -q.z, -q.w);
+    V3<R> qv(q.x, q.y, q.z);
+    R sine = std::sqrt(len2(qv));
+    Mat<R> der;
+    if (sine > 0) {
+        R half = StableMath<R>::atan2(sine, q.w);
+        V3<R> ax = qv * ((R)1 / sine);
+        err = ax * half;
+        R diag = half * q.w / sine;
+        Sym3<R> outer(ax.x * ax.x, ax.x * ax.y, ax.x * ax.z, ax.y * ax.y, ax.y * ax.z, ax.z * ax.z);
+        der = msub(madd(mscale(diag, Mat<R>::ident()), mscale((R)1 - diag, Mat<R>::from_sym(outer))), Mat<R>::skew(err));
+    } else {
+        err = V3<R>();
+        der = Mat<R>::ident();
+    }
+    return mmul(mscale(-(R)0.5, der), Mat<R>::from_m3(mat_from_quat(left)));
+}
+
+enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2 };
+template <class R> struct Joint {
+    int kind = BALLSOCKET;
+    int b1 = 0, b2 = 0;
+    int color = 0;
+    // BallSocketData (BallSocket.cs:32-60)
+    V3<R> la1, la2, r1, r2, acc, bias;
+    R bias_factor = (R)0.2, softness = (R)0.00001;
+    Mat<R> eff;
+    // HingeAngleData (HingeAngle.cs:32-70)
+    R min_angle = 0, max_angle = 0, fixed_angle = 0, limit_bias = (R)0.1, limit_softness = (R)0.001;
+    V3<R> axis;
+    Q4<R> q0;
+    Mat<R> jac;
+    V3<R> bilateral;
+    R coupling_x = 0, coupling_y = 0;
+    int clamp = 0;
+    short hemisphere = 0;
+};
+
+// BallSocket.Initialize (BallSocket.cs:120-138)
+template <class R> void ballsocket_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> anchor) {
+    j.kind = BALLSOCKET;
+    j.la1 = rotate_inv(anchor - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(anchor - b[j.b2].pos, b[j.b2].q);
+    j.bias_factor = (R)0.2;
+    j.softness = (R)0.00001;
+}
+// HingeAngle.Initialize (HingeAngle.cs:84-110)
+template <class R> void hinge_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> axis, R from, R to) {
+    j.kind = HINGEANGLE;
+    j.softness = (R)0.001; j.limit_softness = (R)0.001;
+    j.bias_factor = (R)0.2; j.limit_bias = (R)0.1;
+    j.min_angle = from / (R)2.0;
+    j.max_angle = to / (R)2.0;
+    j.fixed_angle = (R)0.25 * from + (R)0.25 * to;
+    axis = normalize(axis);
+    j.axis = rotate_inv(axis, b[j.b2].q);
+    j.q0 = qmul(qconj(b[j.b2].q), b[j.b1].q);
+}
+
+// ((Scale(m1) + Transform(I1, [r1]x)) + Scale(m2)) + Transform(I2, [r2]x), component-wise
+// in the reference's left-to-right order (BallSocket.cs:158-161)
+template <class R> Mat<R> ballsocket_mass(const Body<R>& b1, V3<R> r1, const Body<R>& b2, V3<R> r2) {
+    auto tr = [](const Body<R>& bd, V3<R> r) {
+        Mat<R> cr = Mat<R>::skew(r);
+        M3<R> c3;
+        for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c3.m[i][k] = cr.a[i][k];
+        return sym_transform(bd.inv_inertia_world, c3);
+    };
+    Sym3<R> t1 = tr(b1, r1), t2 = tr(b2, r2);
+    Sym3<R> o;
+    o.m11 = ((b1.inv_mass_vec.x + t1.m11) + b2.inv_mass_vec.x) + t2.m11;
+    o.m12 = ((0 + t1.m12) + 0) + t2.m12;
+    o.m13 = ((0 + t1.m13) + 0) + t2.m13;
+    o.m22 = ((b1.inv_mass_vec.y + t1.m22) + b2.inv_mass_vec.y) + t2.m22;
+    o.m23 = ((0 + t1.m23) + 0) + t2.m23;
+    o.m33 = ((b1.inv_mass_vec.z + t1.m33) + b2.inv_mass_vec.z) + t2.m33;
+    return Mat<R>::from_sym(o);
+}
+
+// BallSocket.PrepareForIterationBallSocket (BallSocket.cs:140-183)
+template <class R> void ballsocket_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    j.r1 = rotate(j.la1, b1.q);
+    j.r2 = rotate(j.la2, b2.q);
+    V3<R> p1 = b1.pos + j.r1, p2 = b2.pos + j.r2;
+    Mat<R> cr1 = Mat<R>::skew(j.r1), cr2 = Mat<R>::skew(j.r2);
+    Mat<R> e = ballsocket_mass(b1, j.r1, b2, j.r2);
+    R soft = j.softness * ts.inv_sub_dt;
+    e.a[0][0] += soft; e.a[1][1] += soft; e.a[2][2] += soft;
+    j.eff = inverse_symmetric(e);
+    j.bias = (p2 - p1) * j.bias_factor * ts.inv_dt;
+    V3<R> acc = j.acc;
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel - cmul(acc, b1.inv_mass_vec);
+        b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, mvec(cr1, acc));
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(acc, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, mvec(cr2, acc));
+    }
+}
+// BallSocket.IterateBallSocket (BallSocket.cs:223-252)
+template <class R> void ballsocket_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    Mat<R> cr1 = Mat<R>::skew(j.r1), cr2 = Mat<R>::skew(j.r2);
+    V3<R> sv = j.acc * j.softness * ts.inv_sub_dt;
+    V3<R> jv = -b1.vel + mvec(cr1, b1.angvel) + b2.vel - mvec(cr2, b2.angvel);
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, jv + j.bias + sv);
+    j.acc = j.acc + lambda;
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel - cmul(lambda, b1.inv_mass_vec);
+        b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, mvec(cr1, lambda));
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(lambda, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, mvec(cr2, lambda));
+    }
+}
+// HingeAngle.PrepareForIterationHingeAngle (HingeAngle.cs:133-220)
+template <class R> void hinge_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> p0 = create_orthonormal(j.axis);
+    V3<R> p1 = cross(j.axis, p0);
+    V3<R> rot;
+    short hemi;
+    Mat<R> m0 = calc_jacobian(qmul(j.q0, qconj(b1.q)), b2.q, rot, hemi);
+    if (j.hemisphere != 0 && j.hemisphere != hemi) j.acc = V3<R>();
+    j.hemisphere = hemi;
+    V3<R> err(dot(p0, rot), dot(p1, rot), dot(j.axis, rot));
+    j.clamp = 0;
+    V3<R> r0 = mtvec(m0, p0), r1 = mtvec(m0, p1), r2 = mtvec(m0, j.axis);
+    // JMatrix is column-major: UnsafeGet(i) is column i (JMatrix.cs:62-79).
+    for (int k = 0; k < 3; k++) { j.jac.a[k][0] = (&r0.x)[k]; j.jac.a[k][1] = (&r1.x)[k]; j.jac.a[k][2] = (&r2.x)[k]; }
+    Sym3<R> isum(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                 b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                 b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+    Mat<R> jt = mtrans(j.jac);
+    M3<R> jt3;
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) jt3.m[i][k] = jt.a[i][k];
+    j.eff = Mat<R>::from_sym(sym_transform(isum, jt3));
+    j.eff.a[0][0] += j.softness * ts.inv_sub_dt;
+    j.eff.a[1][1] += j.softness * ts.inv_sub_dt;
+    j.eff.a[2][2] += j.limit_softness * ts.inv_sub_dt;
+    R maxA = j.max_angle, minA = j.min_angle;
+    const R PI = (R)3.14159265358979323846;
+    bool full = minA <= -PI / 2 && maxA >= PI / 2;
+    if (minA >= maxA) {
+        j.clamp = 3;
+        err.z = shortest_angle(err.z - j.fixed_angle, PI / 2);
+    } else if (!full && err.z >= maxA) {
+        j.clamp = 1;
+        err.z -= maxA;
+    } else if (!full && err.z <= minA) {
+        j.clamp = 2;
+        err.z -= minA;
+    } else {
+        j.acc.z = 0;
+        j.eff.a[2][2] = 0;
+        j.eff.a[2][0] = j.eff.a[0][2] = 0;
+        j.eff.a[2][1] = j.eff.a[1][2] = 0;
+        j.jac.a[0][2] = j.jac.a[1][2] = j.jac.a[2][2] = 0;
+    }
+    if (j.clamp == 1 || j.clamp == 2) {
+        j.acc.z = j.clamp == 1 ? std::min(j.acc.z, (R)0) : std::max(j.acc.z, (R)0);
+        j.bilateral = inverse_bilateral(j.eff);
+        j.coupling_x = j.eff.a[0][2];
+        j.coupling_y = j.eff.a[1][2];
+    }
+    j.eff = inverse_symmetric(j.eff);
+    j.bias = err * ts.inv_dt;
+    j.bias.x *= j.bias_factor;
+    j.bias.y *= j.bias_factor;
+    j.bias.z *= j.limit_bias;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, mvec(j.jac, j.acc));
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, mvec(j.jac, j.acc));
+}
+// HingeAngle.IterateHingeAngle (HingeAngle.cs:313-364)
+template <class R> void hinge_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> jv = mtvec(j.jac, b1.angvel - b2.angvel);
+    V3<R> soft = j.acc * ts.inv_sub_dt;
+    soft.x *= j.softness; soft.y *= j.softness; soft.z *= j.limit_softness;
+    V3<R> res = jv + j.bias + soft;
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, res);
+    V3<R> orig = j.acc;
+    j.acc = j.acc + lambda;
+    if ((j.clamp == 1 && j.acc.z > 0) || (j.clamp == 2 && j.acc.z < 0)) {
+        lambda.z = -orig.z;
+        R x = res.x + j.coupling_x * lambda.z;
+        R y = res.y + j.coupling_y * lambda.z;
+        lambda.x = -(j.bilateral.x * x + j.bilateral.y * y);
+        lambda.y = -(j.bilateral.y * x + j.bilateral.z * y);
+        j.acc.x = orig.x + lambda.x;
+        j.acc.y = orig.y + lambda.y;
+        j.acc.z = 0;
+    } else if (j.clamp == 0) {
+        orig.z = 0;
+        j.acc.z = 0;
+    }
+    lambda = j.acc - orig;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, mvec(j.jac, lambda));
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, mvec(j.jac, lambda));
+}
+template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
+    if (j.kind == BALLSOCKET) ballsocket_prepare(j, b, ts); else hinge_prepare(j, b, ts);
+}
+template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
+    if (j.kind == BALLSOCKET) ballsocket_iterate(j, b, ts); else hinge_iterate(j, b, ts);
+}
+
+}  // namespace jor

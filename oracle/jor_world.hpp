@@ -1,0 +1,349 @@
+// Oracle (test infrastructure only): a CPU world that strings the restated stages
+// together the way World.StepInternal does (World.Step.cs:153-296) with deactivation
+// disabled.  Pairs are every shape pair with non-disjoint exact world AABBs on different
+// bodies (DynamicTree.cs:266-286 + World.cs:447-455), found by sort-and-sweep.  Solve
+// order: the reference's deterministic order (contacts sorted by arbiter key, then
+// constraints by id; World.Deterministic.cs:142-203) or an external colour order
+// (colour by colour; inside a colour rows share no dynamic body, so their order does
+// not change the result).  A multithreaded variant restates the Regular mode's
+// batch + try-lock scheme (World.Step.cs:428-526, :924-986) for the CPU baseline.
+#pragma once
+#include "jor_dynamics.hpp"
+#include "jor_joints.hpp"
+#include <algorithm>
+#include <numeric>
+#include <condition_variable>
+
+namespace jor {
+
+template <class R> struct World {
+    std::vector<Body<R>> bodies;
+    std::vector<Shape<R>> shapes;
+    std::vector<int> shape_body;
+    std::vector<R> hull;                       // point cloud vertices
+    std::vector<ContactData<R>> arbiters;
+    std::unordered_map<uint64_t, int> arb_index;
+    std::vector<Joint<R>> joints;
+    V3<R> gravity = V3<R>(0, -(R)9.81, 0);
+    int substeps = 1, iterations = 6, relax = 4;
+    bool aux_contacts = true, persistent = true, edge_filter = true;
+    R spec_relax = (R)0.9;
+    bool external_order = false;               // use ContactData::color / Joint::color
+    bool record_residual = false;
+    std::vector<R> residuals;                  // first substep, one value per iteration
+    MprEpa<R> solver;
+    EdgeFilter<R> efilter;
+    int64_t n_pairs = 0, n_colliding = 0, n_points = 0;
+    int nthreads = 1;
+
+    static uint64_t key(int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
+
+    int find_or_create(int s1, int s2) {
+        uint64_t k = key(s1, s2);
+        auto it = arb_index.find(k);
+        if (it != arb_index.end()) return it->second;
+        ContactData<R> cd;
+        int b1 = shape_body[s1], b2 = shape_body[s2];
+        // ContactData.Init (Contact.cs:271-286)
+        cd.b1 = b1; cd.b2 = b2; cd.key1 = s1; cd.key2 = s2;
+        cd.friction = std::max(bodies[b1].friction, bodies[b2].friction);
+        cd.restitution = std::max(bodies[b1].restitution, bodies[b2].restitution);
+        cd.spec_relax = spec_relax;
+        cd.mode = 0; cd.usage = 0;
+        arbiters.push_back(cd);
+        int idx = (int)arbiters.size() - 1;
+        arb_index[k] = idx;
+        return idx;
+    }
+    // ContactData.ResetMode (Contact.cs:288-296)
+    void reset_mode(ContactData<R>& cd) {
+        cd.mode = (bodies[cd.b1].motion == DYNAMIC) ? 3 : 0;
+        cd.mode |= (bodies[cd.b2].motion == DYNAMIC) ? 12 : 0;
+    }
+
+    std::vector<Box3<R>> aabbs() {
+        std::vector<Box3<R>> out(shapes.size());
+        for (size_t i = 0; i < shapes.size(); i++) {
+            const Body<R>& b = bodies[shape_body[i]];
+            out[i] = shape_aabb(shapes[i], b.q, b.pos);
+        }
+        return out;
+    }
+    // The reference's pair contract, evaluated by sort-and-sweep on x.
+    std::vector<std::pair<int, int>> find_pairs() {
+        auto box = aabbs();
+        std::vector<int> ord(shapes.size());
+        std::iota(ord.begin(), ord.end(), 0);
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) { return box[a].mn.x < box[b].mn.x; });
+        std::vector<std::pair<int, int>> pairs;
+        for (size_t ii = 0; ii < ord.size(); ii++) {
+            int i = ord[ii];
+            for (size_t jj = ii + 1; jj < ord.size(); jj++) {
+                int j = ord[jj];
+                if (box[j].mn.x > box[i].mx.x) break;
+                if (disjoint(box[i], box[j])) continue;
+                int bi = shape_body[i], bj = shape_body[j];
+                if (bi == bj) continue;
+                if (bodies[bi].world != bodies[bj].world) continue;
+                if (!bodies[bi].active() && !bodies[bj].active()) continue;
+                if (bodies[bi].motion != DYNAMIC && bodies[bj].motion != DYNAMIC) continue;
+                pairs.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
+            }
+        }
+        std::sort(pairs.begin(), pairs.end());
+        return pairs;
+    }
+
+    struct DetectResult {
+        bool hit = false;
+        V3<R> n;
+        int count = 0;
+        V3<R> A[4], B[4];
+        V3<R> pA, pB;
+        R pen = 0;
+    };
+    // World.Detect (World.Detect.cs:125-218) up to, not including, RegisterContact.
+    DetectResult detect(int sA, int sB, MprEpa<R>& sol) {
+        DetectResult r;
+        const Body<R>& b1 = bodies[shape_body[sA]];
+        const Body<R>& b2 = bodies[shape_body[sB]];
+        if (!b1.active() && !b2.active()) return r;
+        if (b1.motion != DYNAMIC && b2.motion != DYNAMIC) return r;
+        V3<R> pA, pB, n;
+        R pen;
+        bool hit = sol.mpr_epa_world(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, pA, pB, n, pen);
+        if (!hit) return r;
+        if (edge_filter) {
+            bool tri_dyn = shapes[sA].is_triangle() ? b1.motion == DYNAMIC : b2.motion == DYNAMIC;
+            if (!efilter.filter(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, tri_dyn, sol, pA, pB, n, pen)) return r;
+        }
+        r.hit = true; r.n = n; r.pA = pA; r.pB = pB; r.pen = pen;
+        if (aux_contacts) {
+            Manifold<R> m;
+            m.build(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, pA, pB, n);
+            r.count = m.count;
+            for (int i = 0; i < m.count; i++) { r.A[i] = m.A[i]; r.B[i] = m.B[i]; }
+        } else {
+            r.count = 1; r.A[0] = pA; r.B[0] = pB;
+        }
+        return r;
+    }
+    // RegisterContact (World.Detect.cs:294-324)
+    void register_contact(int sA, int sB, const DetectResult& r) {
+        int ai = find_or_create(sA, sB);
+        ContactData<R>& cd = arbiters[ai];
+        if (!persistent) cd.usage = 0;
+        reset_mode(cd);
+        for (int e = 0; e < r.count; e++) add_contact(cd, bodies, r.A[e], r.B[e], r.n);
+    }
+
+    void narrowphase() {
+        auto pairs = find_pairs();
+        n_pairs = (int64_t)pairs.size();
+        n_colliding = 0; n_points = 0;
+        if (nthreads <= 1) {
+            for (auto& p : pairs) {
+                DetectResult r = detect(p.first, p.second, solver);
+                if (!r.hit) continue;
+                n_colliding++; n_points += r.count;
+                register_contact(p.first, p.second, r);
+            }
+            return;
+        }
+        std::vector<DetectResult> res(pairs.size());
+        parallel_for((int)pairs.size(), 64, [&](int b, int e) {
+            MprEpa<R> local;
+            for (int i = b; i < e; i++) res[i] = detect(pairs[i].first, pairs[i].second, local);
+        });
+        for (size_t i = 0; i < pairs.size(); i++) {
+            if (!res[i].hit) continue;
+            n_colliding++; n_points += res[i].count;
+            register_contact(pairs[i].first, pairs[i].second, res[i]);
+        }
+    }
+
+    // Solve order: indices into arbiters and joints, grouped by colour.
+    std::vector<std::vector<int>> order_arb, order_joint;
+    void build_order() {
+        order_arb.clear(); order_joint.clear();
+        if (!external_order) {
+            std::vector<int> a(arbiters.size());
+            std::iota(a.begin(), a.end(), 0);
+            std::sort(a.begin(), a.end(), [&](int x, int y) {
+                return std::make_pair(arbiters[x].key1, arbiters[x].key2) < std::make_pair(arbiters[y].key1, arbiters[y].key2);
+            });
+            std::vector<int> j(joints.size());
+            std::iota(j.begin(), j.end(), 0);
+            order_arb.push_back(a);
+            order_joint.push_back(std::vector<int>());
+            order_arb.push_back(std::vector<int>());
+            order_joint.push_back(j);
+            return;
+        }
+        int nc = 0;
+        for (auto& a : arbiters) nc = std::max(nc, a.color + 1);
+        for (auto& j : joints) nc = std::max(nc, j.color + 1);
+        order_arb.assign(nc, {});
+        order_joint.assign(nc, {});
+        for (size_t i = 0; i < arbiters.size(); i++) order_arb[arbiters[i].color].push_back((int)i);
+        for (size_t i = 0; i < joints.size(); i++) order_joint[joints[i].color].push_back((int)i);
+    }
+    R residual_norm(std::vector<R>& prev) {
+        double d2 = 0, l2 = 0;
+        size_t k = 0;
+        for (auto& cd : arbiters)
+            for (int c = 0; c < 4; c++) {
+                if (!(cd.usage & (1u << c))) continue;
+                for (int r = 0; r < 3; r++) {
+                    R v = cd.c[c].acc[r];
+                    if (k < prev.size()) { double d = (double)v - prev[k]; d2 += d * d; prev[k] = v; }
+                    else prev.push_back(v);
+                    l2 += (double)v * v;
+                    k++;
+                }
+            }
+        return (R)(std::sqrt(d2) / std::max(std::sqrt(l2), 1e-12));
+    }
+    std::vector<R> snapshot_acc() {
+        std::vector<R> v;
+        for (auto& cd : arbiters)
+            for (int c = 0; c < 4; c++)
+                if (cd.usage & (1u << c)) for (int r = 0; r < 3; r++) v.push_back(cd.c[c].acc[r]);
+        return v;
+    }
+
+    void solve_substep(const TimeStep<R>& ts, bool first) {
+        for (auto& b : bodies) integrate_forces(b);
+        // prepare (World.Step.cs:1155-1172)
+        for (size_t c = 0; c < order_arb.size(); c++) {
+            for (int i : order_arb[c]) contactdata_prepare(arbiters[i], bodies, ts);
+            for (int i : order_joint[c]) joint_prepare(joints[i], bodies, ts);
+        }
+        std::vector<R> prev;
+        if (first && record_residual) { prev = snapshot_acc(); residuals.clear(); }
+        for (int it = 0; it < iterations; it++) {
+            for (size_t c = 0; c < order_arb.size(); c++) {
+                for (int i : order_arb[c]) contactdata_iterate(arbiters[i], bodies, true);
+                for (int i : order_joint[c]) joint_iterate(joints[i], bodies, ts);
+            }
+            if (first && record_residual) residuals.push_back(residual_norm(prev));
+        }
+        for (auto& b : bodies) integrate_velocities(b, ts);
+        for (int it = 0; it < relax; it++)
+            for (size_t c = 0; c < order_arb.size(); c++)
+                for (int i : order_arb[c]) contactdata_iterate(arbiters[i], bodies, false);
+    }
+
+    // RemoveBrokenArbiters (World.Step.cs:839-860): arbiters still without contacts.
+    void remove_broken() {
+        std::vector<ContactData<R>> keep;
+        keep.reserve(arbiters.size());
+        for (auto& a : arbiters) if ((a.usage & 15u) != 0) keep.push_back(a);
+        arbiters.swap(keep);
+        arb_index.clear();
+        for (size_t i = 0; i < arbiters.size(); i++) arb_index[key(arbiters[i].key1, arbiters[i].key2)] = (int)i;
+    }
+
+    // World.StepInternal (World.Step.cs:153-296) with deactivation disabled.
+    // narrow=false skips detection (the caller registered contacts itself).
+    void step(R dt, bool narrow = true) {
+        if (dt < std::numeric_limits<R>::epsilon()) return;
+        TimeStep<R> ts(dt, substeps);
+        if (narrow) narrowphase();
+        build_order();
+        for (int s = 0; s < substeps; s++) solve_substep(ts, s == 0);
+        remove_broken();
+        for (auto& a : arbiters) contactdata_update_position(a, bodies);
+        for (auto& b : bodies) body_update(b, ts, gravity);
+    }
+
+    // --- threading for the multithreaded Regular-mode restatement ---------------------
+    void parallel_for(int n, int batch, const std::function<void(int, int)>& fn) {
+        std::atomic<int> next{0};
+        auto worker = [&]() {
+            while (true) {
+                int b = next.fetch_add(batch);
+                if (b >= n) break;
+                fn(b, std::min(n, b + batch));
+            }
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nthreads; t++) th.emplace_back(worker);
+        worker();
+        for (auto& t : th) t.join();
+    }
+};
+
+// Multithreaded Regular-mode step (World.Step.cs:428-526, :924-986): batches of 64
+// arbiters per task, a per-body try-lock, and a deferred queue for locked rows.  Used
+// only as the timed CPU baseline.
+template <class R> struct RegularSolver {
+    World<R>& w;
+    std::vector<std::atomic<int>> locks;
+    explicit RegularSolver(World<R>& world) : w(world), locks(world.bodies.size()) {
+        for (auto& l : locks) l.store(0);
+    }
+    bool try_lock_two(int a, int b) {
+        bool da = w.bodies[a].motion == DYNAMIC, db = w.bodies[b].motion == DYNAMIC;
+        int lo = std::min(a, b), hi = std::max(a, b);
+        bool dlo = lo == a ? da : db, dhi = hi == a ? da : db;
+        int z = 0;
+        if (dlo && !locks[lo].compare_exchange_strong(z, 1)) return false;
+        z = 0;
+        if (dhi && hi != lo && !locks[hi].compare_exchange_strong(z, 1)) {
+            if (dlo) locks[lo].store(0);
+            return false;
+        }
+        return true;
+    }
+    void unlock_two(int a, int b) {
+        if (w.bodies[a].motion == DYNAMIC) locks[a].store(0);
+        if (b != a && w.bodies[b].motion == DYNAMIC) locks[b].store(0);
+    }
+    template <class F> void sweep(const F& fn) {
+        int n = (int)w.arbiters.size();
+        w.parallel_for(n, 64, [&](int b, int e) {
+            std::vector<int> q;
+            for (int i = b; i < e; i++) {
+                auto& cd = w.arbiters[i];
+                if (!try_lock_two(cd.b1, cd.b2)) { q.push_back(i); continue; }
+                fn(cd);
+                unlock_two(cd.b1, cd.b2);
+            }
+            size_t h = 0;
+            while (h < q.size()) {
+                int i = q[h++];
+                auto& cd = w.arbiters[i];
+                if (!try_lock_two(cd.b1, cd.b2)) { q.push_back(i); continue; }
+                fn(cd);
+                unlock_two(cd.b1, cd.b2);
+            }
+        });
+    }
+    void step(R dt) {
+        TimeStep<R> ts(dt, w.substeps);
+        w.narrowphase();
+        locks = std::vector<std::atomic<int>>(w.bodies.size());
+        for (auto& l : locks) l.store(0);
+        int nb = (int)w.bodies.size();
+        for (int s = 0; s < w.substeps; s++) {
+            w.parallel_for(nb, 256, [&](int b, int e) { for (int i = b; i < e; i++) integrate_forces(w.bodies[i]); });
+            sweep([&](ContactData<R>& cd) { contactdata_prepare(cd, w.bodies, ts); });
+            for (auto& j : w.joints) joint_prepare(j, w.bodies, ts);
+            for (int it = 0; it < w.iterations; it++) {
+                sweep([&](ContactData<R>& cd) { contactdata_iterate(cd, w.bodies, true); });
+                for (auto& j : w.joints) joint_iterate(j, w.bodies, ts);
+            }
+            w.parallel_for(nb, 256, [&](int b, int e) { for (int i = b; i < e; i++) integrate_velocities(w.bodies[i], ts); });
+            for (int it = 0; it < w.relax; it++)
+                sweep([&](ContactData<R>& cd) { contactdata_iterate(cd, w.bodies, false); });
+        }
+        w.remove_broken();
+        w.parallel_for((int)w.arbiters.size(), 256, [&](int b, int e) {
+            for (int i = b; i < e; i++) contactdata_update_position(w.arbiters[i], w.bodies);
+        });
+        w.parallel_for(nb, 256, [&](int b, int e) { for (int i = b; i < e; i++) body_update(w.bodies[i], ts, w.gravity); });
+    }
+};
+
+}  // namespace jor

@@ -1,0 +1,447 @@
+"""Pins the CPU oracle to the reference's own known-answer tests for the hot path.
+
+Each test restates one test of src/JitterTests (cited per test) against the oracle, in
+both precisions where the reference runs both (CI matrix single/double,
+.github/workflows/jitter-tests.yml).  Values with explicit expectations in the
+reference (SAT depths, manifold corners, the analytic penalty bias, exact orientation
+signs) are checked with the reference's tolerances.
+"""
+import itertools
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi, scenes
+
+IDQ = np.array([0.0, 0.0, 0.0, 1.0])
+
+
+def qaxis(axis, angle):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    s = np.sin(angle / 2)
+    return np.array([axis[0] * s, axis[1] * s, axis[2] * s, np.cos(angle / 2)])
+
+
+def rotate(q, v):
+    x, y, z, w = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    return R @ np.asarray(v)
+
+
+def qmul(a, b):
+    ax, ay, az, aw = a
+    bx, by, bz, bw = b
+    return np.array([aw * bx + bw * ax + ay * bz - az * by, aw * by + bw * ay + az * bx - ax * bz,
+                     aw * bz + bw * az + ax * by - ay * bx, aw * bw - (ax * bx + ay * by + az * bz)])
+
+
+def box_sat_depth(ha, hb, q, p):
+    """Minimum penetration over the 15 SAT axes of two boxes, A at the origin
+    (ConvexPolytopeTests.MinimumBoxDepth, ConvexPolytopeTests.cs:176-196)."""
+    axA = np.eye(3)
+    axB = np.stack([rotate(q, e) for e in np.eye(3)])
+    axes = list(axA) + list(axB) + [np.cross(a, b) for a in axA for b in axB]
+
+    def sup(h, R, d, off):
+        return off + R @ (np.sign(np.where(R.T @ d == 0, 1, R.T @ d)) * h)
+
+    RA, RB = np.eye(3), axB.T
+    best = np.inf
+    for a in axes:
+        if a @ a < 1e-12:
+            continue
+        a = a / np.linalg.norm(a)
+        pos = sup(ha, RA, a, 0) - sup(hb, RB, -a, p)
+        neg = sup(ha, RA, -a, 0) - sup(hb, RB, a, p)
+        best = min(best, pos @ a, neg @ -a)
+    return best
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_collision_duplicate_support_matches_box_sat(real):
+    # ConvexPolytopeTests.Collision_DuplicateSupportRegressionMatchesBoxSat (ConvexPolytopeTests.cs:164-174)
+    a, b = O.box(2, 0.25, 1), O.box(0.5, 0.5, 0.5)
+    q = np.array([-0.34783155, 0.69148487, -0.5953642, -0.21541446])
+    pos = np.array([0.53918016, 0.12698002, -1.1122025])
+    exp = box_sat_depth(np.array([2, 0.25, 1]), np.array([0.5, 0.5, 0.5]), q, pos)
+    hit, _, _, n, depth, _ = O.collide(a, b, IDQ, q, np.zeros(3), pos, mode=1, real=real)
+    assert hit
+    assert abs(depth - exp) <= 1e-4
+    assert np.all(np.isfinite(n))
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("case", ["collinear", "oblique"])
+def test_mprepa_regressions_match_box_sat(real, case):
+    # ConvexPolytopeTests.MprEpa_CollinearSupportRegressionMatchesBoxSat / ObliqueBox (ConvexPolytopeTests.cs:198-233)
+    if case == "collinear":
+        h = np.array([0.3, 1.2, 0.7])
+        q = np.array([0, 0.99999815, 0, -0.0019342888]) if real == "f" else np.array([0, 0.999998129169539, 0, -0.0019343364293572605])
+        pos = np.array([0, 0.43866748, 0]) if real == "f" else np.array([0, 0.43866746976909576, 0])
+    else:
+        h = np.array([2, 0.25, 1])
+        q = np.array([-0.28864738, -0.1558499, 0.15853547, -0.931268]) if real == "f" else \
+            np.array([-0.28864726319747464, -0.15584983931147614, 0.15853538827229016, -0.9312680149669853])
+        pos = np.array([-0.7871254, 0.20686495, -0.014221248]) if real == "f" else \
+            np.array([-0.7871254097758174, 0.20686499835933464, -0.014221211987464191])
+    a = O.box(*h)
+    exp = box_sat_depth(h, h, q, pos)
+    hit, pA, pB, n, depth, _ = O.collide(a, a, IDQ, q, np.zeros(3), pos, mode=0, real=real)
+    assert hit
+    assert abs(depth - exp) <= 1e-4
+    # depth matches the Minkowski support along the normal
+    sa = O.support(a, n, real)
+    sb = rotate(q, O.support(a, rotate(np.array([-q[0], -q[1], -q[2], q[3]]), -n), real)) + pos
+    assert abs((sa - sb) @ n - depth) <= 1e-4
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("shape_name", ["cube", "cylinder", "flat box"])
+@pytest.mark.parametrize("threshold", [0.0, 0.02])
+def test_mprepa_floor_contacts_remain_exact(real, shape_name, threshold):
+    # ConvexPolytopeTests.MprEpa_FloorContactsRemainExact (ConvexPolytopeTests.cs:235-263)
+    shp = {"cube": O.box(0.5, 0.5, 0.5), "cylinder": O.cylinder(0.5, 1.0), "flat box": O.box(1.5, 0.1, 0.7)}[shape_name]
+    floor = O.box(20, 0.5, 20)
+    top = O.support(shp, [0, 1, 0], real)[1]
+    wrong = []
+    for depth in (0.001, 0.005, 0.01, 0.025, 0.05, 0.1):
+        for yaw in range(0, 90, 3):
+            q = qaxis([0, 1, 0], yaw * np.pi / 180)
+            for x in range(-2, 3):
+                for z in range(-2, 3):
+                    pos = np.array([x * 0.37, top - depth, z * 0.53])
+                    hit, _, _, n, actual, _ = O.collide(shp, floor, q, IDQ, pos, np.array([0, -0.5, 0]), threshold, 0, real)
+                    if hit and np.isfinite(actual) and abs(actual - depth) <= 1e-4 and abs(n[1]) >= 0.9999:
+                        continue
+                    wrong.append((depth, yaw, x, z, actual, n))
+    assert not wrong, wrong[:3]
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_mprepa_depth_always_matches_its_normal(real):
+    # ConvexPolytopeTests.MprEpa_DepthAlwaysMatchesItsNormal (ConvexPolytopeTests.cs:265-317); the
+    # reference draws from .NET Random(11), here a seeded numpy generator draws the same distribution.
+    shapes = [O.box(0.5, 0.5, 0.5), O.box(2, 0.25, 1), O.cylinder(0.5, 1.0), O.capsule(0.3, 0.5), O.sphere(0.5)]
+    rng = np.random.default_rng(11)
+
+    def rdir():
+        v = rng.random(3) - 0.5
+        return v / np.linalg.norm(v)
+
+    overlapping, wrong = 0, []
+    for i in range(4000):
+        a, b = shapes[rng.integers(5)], shapes[rng.integers(5)]
+        q = qaxis([0, 1, 0], rng.random() * 6) if i % 3 == 0 else qaxis(rdir(), rng.random() * 6)
+        d = np.array([0, 1.0, 0]) if i % 3 == 0 else rdir()
+        pos = d * (0.4 + rng.random() * 1.4)
+        if i % 2 == 1:
+            outside, inside = 6.0, 0.0
+            for _ in range(40):
+                mid = (outside + inside) * 0.5
+                if O.collide(a, b, IDQ, q, np.zeros(3), d * mid, 1e9, 0, real)[0]:
+                    inside = mid
+                else:
+                    outside = mid
+            pos = d * (inside - rng.random() * 0.03)
+        hit, _, _, n, pen, _ = O.collide(a, b, IDQ, q, np.zeros(3), pos, 0.02, 0, real)
+        if not hit:
+            continue
+        overlapping += 1
+        qc = np.array([-q[0], -q[1], -q[2], q[3]])
+        sv = O.support(a, n, real) - (rotate(q, O.support(b, rotate(qc, -n), real)) + pos)
+        if abs(sv @ n - pen) > 1e-3:
+            wrong.append((i, pen, sv @ n))
+    assert overlapping > 1000
+    assert not wrong, wrong[:3]
+
+
+# ---- CollisionManifold (Regression/CollisionManifoldTests.cs) --------------------------------
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("radius,sphere_first", [(0.5, False), (0.5, True), (1.0, False), (1.0, True)])
+def test_manifold_sphere_on_floor_keeps_original(real, radius, sphere_first):
+    # SphereAgainstFloor_PreservesOriginalContact (CollisionManifoldTests.cs:101-126)
+    floor, sph = O.box(100, 100, 100), O.sphere(radius)
+    fpos, spos = np.array([0, -100, 0.0]), np.array([3, radius - 0.005, -2])
+    fpt, spt = np.array([3, 0, -2.0]), np.array([3, -0.005, -2])
+    if sphere_first:
+        A, B = O.manifold(sph, floor, IDQ, IDQ, spos, fpos, spt, fpt, [0, -1, 0], real)
+        exp_a, exp_b = spt, fpt
+    else:
+        A, B = O.manifold(floor, sph, IDQ, IDQ, fpos, spos, fpt, spt, [0, 1, 0], real)
+        exp_a, exp_b = fpt, spt
+    assert len(A) == 1
+    assert np.abs(A[0] - exp_a).max() < 1e-5 and np.abs(B[0] - exp_b).max() < 1e-5
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("radius", [0.5, 1.0])
+def test_manifold_cylinder_on_floor(real, radius):
+    # CylinderAgainstFloor_PreservesEndpointsAndOriginalContact (CollisionManifoldTests.cs:128-153)
+    floor, cyl = O.box(100, 100, 100), O.cylinder(radius, 2.0)
+    fpos, cpos = np.array([0, -100, 0.0]), np.array([10, radius - 0.005, 0])
+    cq = qaxis([0, 0, 1], np.pi / 2)
+    hit, pA, pB, n, _, _ = O.collide(floor, cyl, IDQ, cq, fpos, cpos, 0.02, 0, real)
+    assert hit
+    A, B = O.manifold(floor, cyl, IDQ, cq, fpos, cpos, pA, pB, n, real)
+    assert len(A) == 3
+    assert abs(abs(A[0][0] - cpos[0]) - 1) < 1e-5 and abs(abs(A[1][0] - cpos[0]) - 1) < 1e-5
+    assert abs(A[0][0] - A[1][0]) > 1e-5
+    assert np.abs(A[2] - pA).max() < 1e-5 and np.abs(B[2] - pB).max() < 1e-5
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_manifold_equal_face_boxes_four_corners(real):
+    # EqualFaceBoxes_ProduceFourCornerContacts (CollisionManifoldTests.cs:155-180)
+    b = O.box(1, 1, 1)
+    pb = np.array([0, 1.9, 0])
+    hit, pA, pB, n, pen, _ = O.collide(b, b, IDQ, IDQ, np.zeros(3), pb, 0, 1, real)
+    assert hit
+    A, B = O.manifold(b, b, IDQ, IDQ, np.zeros(3), pb, pA, pB, n, real)
+    assert len(A) == 4
+    for a, bb in zip(A, B):
+        assert abs(a[1] - 1.0) < 1e-4 and abs(bb[1] - 0.9) < 1e-4
+        assert abs(abs(a[0]) - 1) < 1e-4 and abs(abs(a[2]) - 1) < 1e-4
+        assert abs((a - bb) @ n - pen) < 1e-4
+    d = np.linalg.norm(A[:, None] - A[None], axis=2) + np.eye(4)
+    assert d.min() > 1e-4
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("prism_first", [False, True])
+def test_manifold_triangular_prism(real, prism_first):
+    # TriangularFaceAgainstFloor_PreservesTriangleAndOriginalContact (CollisionManifoldTests.cs:182-209)
+    floor = O.box(2, 1, 2)
+    prism = O.hull([[-1, -1, -1], [1, -1, -1], [0, -1, 1], [-1, 1, -1], [1, 1, -1], [0, 1, 1]])
+    fpos, ppos = np.array([0, -1, 0.0]), np.array([0, 0.995, 0])
+    fpt, ppt = np.zeros(3), np.array([0, -0.005, 0])
+    if prism_first:
+        A, B = O.manifold(prism, floor, IDQ, IDQ, ppos, fpos, ppt, fpt, [0, -1, 0], real)
+        floor_pts, last_a, last_b = B, ppt, fpt
+    else:
+        A, B = O.manifold(floor, prism, IDQ, IDQ, fpos, ppos, fpt, ppt, [0, 1, 0], real)
+        floor_pts, last_a, last_b = A, fpt, ppt
+    assert len(A) == 4
+    expected = [np.array(v, float) for v in ([-1, 0, -1], [1, 0, -1], [0, 0, 1], [0, 0, 0])]
+    used = set()
+    for e in expected:
+        m = [i for i in range(4) if i not in used and np.sum((floor_pts[i] - e) ** 2) <= 1e-10]
+        assert m, (e, floor_pts)
+        used.add(m[0])
+    assert np.abs(A[3] - last_a).max() < 1e-5 and np.abs(B[3] - last_b).max() < 1e-5
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_manifold_rotated_boxes_cover_all_quadrants(real):
+    # RotatedFaceBoxes_IncludeIntersectionVertices / _ReductionSpansAllQuadrants
+    # (CollisionManifoldTests.cs:211-273)
+    b = O.box(1, 1, 1)
+    qb = qaxis([0, 1, 0], np.pi / 4)
+    pb = np.array([0, 1.9, 0])
+    hit, pA, pB, n, pen, _ = O.collide(b, b, IDQ, qb, np.zeros(3), pb, 0, 1, real)
+    assert hit
+    A, B = O.manifold(b, b, IDQ, qb, np.zeros(3), pb, pA, pB, n, real)
+    assert len(A) == 4
+    eps = 2e-4
+    quads = set()
+    qc = np.array([-qb[0], -qb[1], -qb[2], qb[3]])
+    for a, bb in zip(A, B):
+        assert abs(a[1] - 1) < eps and abs((a - bb) @ n - pen) < eps
+        assert abs(a[0]) <= 1 + eps and abs(a[2]) <= 1 + eps
+        lb = rotate(qc, bb - pb)
+        assert abs(lb[1] + 1) < eps and abs(lb[0]) <= 1 + eps and abs(lb[2]) <= 1 + eps
+        assert abs(a[0]) > 0.05 and abs(a[2]) > 0.05
+        quads.add((a[0] > 0, a[2] > 0))
+    assert len(quads) == 4
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_manifold_world_offset_invariance(real):
+    # RotatedFaceBoxes_AtLargeWorldOffset_MatchNearOriginContacts (CollisionManifoldTests.cs:275-321)
+    b = O.box(1, 1, 1)
+    qb = qaxis([0, 1, 0], np.pi / 4)
+    pb = np.array([0, 1.9, 0])
+    off = np.array([10000.0, -20000.0, 30000.0])
+    hit, pA, pB, n, _, _ = O.collide(b, b, IDQ, qb, np.zeros(3), pb, 0, 1, real)
+    A0, B0 = O.manifold(b, b, IDQ, qb, np.zeros(3), pb, pA, pB, n, real)
+    A1, B1 = O.manifold(b, b, IDQ, qb, off, off + pb, pA + off, pB + off, n, real)
+    assert len(A0) == len(A1)
+    for S0, S1 in ((A0, A1 - off), (B0, B1 - off)):
+        for p0 in S0:
+            assert np.min(np.sum((S1 - p0) ** 2, axis=1)) <= 1e-6
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("box_first", [True, False])
+def test_manifold_box_and_ridge(real, box_first):
+    # BoxFaceAndRidge / RidgeAndBoxFace (CollisionManifoldTests.cs:323-390)
+    bx = O.box(2, 2, 2)
+    ridge = O.hull([[-2, -1, 0], [2, -1, 0], [-2, 1, -1], [2, 1, -1], [-2, 1, 1], [2, 1, 1]])
+    if box_first:
+        A, B = O.manifold(bx, ridge, IDQ, IDQ, np.zeros(3), np.array([0, 2.9, 0]), [0, 2.0, 0], [0, 1.9, 0], [0, 1, 0], real)
+        ya, yb = 2.0, 1.9
+    else:
+        A, B = O.manifold(ridge, bx, IDQ, IDQ, np.array([0, 2.9, 0]), np.zeros(3), [0, 1.9, 0], [0, 2.0, 0], [0, -1, 0], real)
+        ya, yb = 1.9, 2.0
+    assert len(A) == 3
+    for i in range(2):
+        assert abs(A[i][1] - ya) < 1e-4 and abs(B[i][1] - yb) < 1e-4
+        assert abs(abs(A[i][0]) - 2) < 1e-4 and abs(A[i][2]) < 1e-4 and abs(B[i][2]) < 1e-4
+    assert np.allclose(A[2], [0, ya, 0]) and np.allclose(B[2], [0, yb, 0])
+
+
+# ---- exact predicates (Behavior/ExactPredicateTests.cs + DyadicReference.cs) ------------------
+def exact_sign(a, b, c, p):
+    A = [[Fraction(float(x)) for x in v] for v in (a, b, c, p)]
+    u = [A[0][i] - A[1][i] for i in range(3)]
+    v = [A[0][i] - A[2][i] for i in range(3)]
+    d = [A[3][i] - A[0][i] for i in range(3)]
+    n = [u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]]
+    s = n[0] * d[0] + n[1] * d[1] + n[2] * d[2]
+    return (s > 0) - (s < 0)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_exact_orientation_matches_rational_arithmetic(real):
+    lib = O.load()
+    rng = np.random.default_rng(3)
+    dt = np.float32 if real == "f" else np.float64
+    cases = []
+    for _ in range(300):
+        a, b, c = (rng.normal(size=3) * 10 ** rng.uniform(-3, 3, size=3)).astype(dt), rng.normal(size=3).astype(dt), rng.normal(size=3).astype(dt)
+        t, s = rng.random(), rng.random()
+        p = (a + t * (b - a) + s * (c - a)).astype(dt)   # on the plane up to rounding: the hard cases
+        cases.append((a, b, c, p))
+        cases.append((a, b, c, rng.normal(size=3).astype(dt)))
+    cases.append((np.array([0, 0, 0], dt), np.array([1, 0, 0], dt), np.array([0, 1, 0], dt), np.array([0.5, 0.5, 0], dt)))
+    for a, b, c, p in cases:
+        args = [np.ascontiguousarray(x, np.float64) for x in (a, b, c, p)]
+        got = getattr(lib, "jor_exact_side_" + real)(*[O.p(x) for x in args])
+        assert got == exact_sign(a, b, c, p)
+        sign = np.zeros(1, np.int32)
+        if getattr(lib, "jor_filter_side_" + real)(*[O.p(x) for x in args], O.p(sign)):
+            assert sign[0] == got  # the filter only reports proven signs (PlaneFilter.cs:56-70)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_stable_math_tracks_libm(real):
+    lib = O.load()
+    tol = 2e-6 if real == "f" else 1e-12
+    for a in np.linspace(-20, 20, 2001):
+        s, c = np.zeros(1), np.zeros(1)
+        getattr(lib, "jor_stable_sincos_" + real)(a, O.p(s), O.p(c))
+        assert abs(s[0] - np.sin(a)) < tol * max(1, abs(a)) and abs(c[0] - np.cos(a)) < tol * max(1, abs(a))
+    for y, x in itertools.product(np.linspace(-3, 3, 41), np.linspace(-3, 3, 41)):
+        # the reference truncates the atan series at order 17: ~3e-9 at |x| = tan(pi/8)
+        assert abs(getattr(lib, "jor_stable_atan2_" + real)(y, x) - np.arctan2(y, x)) < max(10 * tol, 1e-8)
+
+
+# ---- contact solver (Regression/ContactSubstepTests.cs, Behavior/ContactLifecycleTests.cs) ----
+def _two_body_scene(b1, b2):
+    bodies = scenes._body(2)
+    for i, b in enumerate((b1, b2)):
+        for k, v in b.items():
+            bodies[k][i] = v
+    shapes = np.zeros(2, abi.SHAPE_DTYPE)
+    shapes["kind"] = abi.SHAPE_SPHERE
+    shapes["dims"][:, 0] = 0.5
+    shapes["body"] = [0, 1]
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[], params={})
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_penalty_bias_follows_rotation_within_step(real):
+    # ContactSubstepTests.RotationWithinStep_UpdatesPenetrationWithoutAddingNormalTorque (ContactSubstepTests.cs:13-47)
+    tol = 1e-5 if real == "f" else 1e-12
+    null = dict(motion_type=abi.MOTION_STATIC, inv_mass=0.0, inv_inertia=np.zeros(6), friction=0.0)
+    inv_i = 1.0 / (0.4 * (4 / 3 * np.pi * 0.125) * 0.25)
+    sph = dict(position=(0, 0.45, 0), velocity=(0, -1, 0), inv_mass=1 / (4 / 3 * np.pi * 0.125),
+               inv_inertia=(inv_i, 0, 0, inv_i, 0, inv_i), friction=0.0)
+    w = O.OracleWorld(_two_body_scene(null, sph), real=real)
+    w.register_contact(0, 1, [0, 0, 0], [0, -0.05, 0], [0, 1, 0])
+    q = qaxis([0, 0, 1], 0.3).astype(np.float32)
+    w.fn("jor_world_set_orientation")(w.h, 1, O.p(q))
+    w.fn("jor_world_prepare")(w.h, 0.01, 3)
+    c = w.contacts()[0]
+    pen = 0.5 * np.cos(0.3) - 0.45
+    expected = 0.2 * 100.0 * (pen - 0.01)
+    assert abs(c["penalty_bias"] - expected) < 5 * tol + 1e-6
+    assert np.abs(c["rel_pos2"] + np.array([0, 0.5, 0])).max() < tol
+    w.fn("jor_world_iterate")(w.h, 1)
+    b = w.bodies()
+    assert abs(b["velocity"][1][1] - expected) < 5 * tol + 1e-6
+    assert np.linalg.norm(b["angular_velocity"][1]) < 1e-5
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("bias", [False, True])
+def test_contact_iteration_conserves_momentum(real, bias):
+    # ContactLifecycleTests.ContactIteration_ConservesLinearAndAngularMomentum (ContactLifecycleTests.cs:15-73)
+    tol = 1e-5 if real == "f" else 1e-12
+    q1 = qmul(qaxis([1, 0, 0], 0.4), qaxis([0, 0, 1], 0.7))
+    q2 = qmul(qaxis([0, 1, 0], 0.6), qaxis([1, 0, 0], 0.3))
+    b1 = dict(position=(-0.6, 0.3, 0.4), orientation=q1, velocity=(2, 3, -1), angular_velocity=(0.2, -0.4, 0.1),
+              inv_mass=0.5, inv_inertia=(1 / 3, 0, 0, 1 / 5, 0, 1 / 7), friction=0.75)
+    b2 = dict(position=(0.8, -0.2, -0.5), orientation=q2, velocity=(-1, -2, 0.5), angular_velocity=(-0.3, 0.1, 0.5),
+              inv_mass=1 / 3, inv_inertia=(1 / 4, 0, 0, 1 / 6, 0, 1 / 9), friction=0.75)
+    w = O.OracleWorld(_two_body_scene(b1, b2), real=real)
+    n = np.array([0.3, 1, -0.4]) / np.linalg.norm([0.3, 1, -0.4])
+    w.register_contact(0, 1, [0.1, 0.4, 0.5], [0.1, 0.4, 0.5], n)
+    w.fn("jor_world_prepare")(w.h, 0.01, 1)
+    w.fn("jor_world_set_penalty")(w.h, 0, 0, 1.0)
+
+    def inertia(i):
+        out = np.zeros(6)
+        w.fn("jor_world_inertia_world")(w.h, i, O.p(out))
+        m = np.array([[out[0], out[1], out[2]], [out[1], out[3], out[4]], [out[2], out[4], out[5]]])
+        return np.linalg.inv(m)
+
+    I1, I2 = inertia(0), inertia(1)
+    # the scene's inverse masses are stored as float32: use the masses they encode
+    m1, m2 = 1.0 / float(np.float32(0.5)), 1.0 / float(np.float32(1 / 3))
+
+    def momenta():
+        b = w.bodies_d()
+        lin = m1 * b[0, 7:10] + m2 * b[1, 7:10]
+        ang = np.cross(b[0, 0:3], m1 * b[0, 7:10]) + np.cross(b[1, 0:3], m2 * b[1, 7:10]) + I1 @ b[0, 10:13] + I2 @ b[1, 10:13]
+        return lin, ang
+
+    L0, A0 = momenta()
+    w0 = w.bodies_d()[0, 10:13].copy()
+    for _ in range(8):
+        w.fn("jor_world_iterate")(w.h, 1 if bias else 0)
+        L, A = momenta()
+        assert np.abs(L - L0).max() < 10 * tol * 10 and np.abs(A - A0).max() < 10 * tol * 10
+    c = w.contacts()[0]
+    assert c["accumulated"][0] > tol
+    assert abs(c["accumulated"][1]) + abs(c["accumulated"][2]) > tol
+    assert np.abs(w.bodies_d()[0, 10:13] - w0).max() > tol
+
+
+# ---- behaviour (Behavior/StackingTests.cs) ----------------------------------------------------
+def test_box_stack_stays_upright():
+    # StackingTests: a 12-box stack stays standing (StackingTests.cs:22-40)
+    n = 12
+    bodies = scenes._body(n + 1)
+    shapes = np.zeros(n + 1, abi.SHAPE_DTYPE)
+    scenes.ground(bodies, shapes, 0, 0)
+    shapes["kind"][1:] = abi.SHAPE_BOX
+    shapes["dims"][1:, :3] = 0.5
+    shapes["body"] = np.arange(n + 1)
+    bodies["position"][1:] = np.stack([np.zeros(n), 0.5 + np.arange(n) * 0.999, np.zeros(n)], 1)
+    scenes.set_mass(bodies, shapes, None, 1, 1)
+    bodies["inv_mass"][1:] = bodies["inv_mass"][1]
+    bodies["inv_inertia"][1:] = bodies["inv_inertia"][1]
+    scene = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                 triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[], params=dict(substeps=4, solver_iterations=8))
+    w = O.OracleWorld(scene)
+    top0 = w.bodies()["position"][n].copy()
+    for _ in range(600):
+        w.step(0.01)
+    top = w.bodies()["position"][n]
+    assert np.linalg.norm(top - top0) < 1.0
