@@ -1,0 +1,253 @@
+"""Throughput of the GB300 contact pipeline on the 100k-body mixed pile.
+
+Workload: 100,000 bodies drawn uniformly from box / sphere / capsule / cylinder / cone /
+32-point hull, uniform in a 120 x 200 x 120 volume over a static ground box and a
+64 x 64-cell heightfield (amplitude 2); dt = 1/100, 4 substeps, 8 + 4 iterations,
+float32.  Seeded synthetic scene (numpy PCG64), no dataset.  The scene is first stepped
+until the pile has formed (untimed), then K steps are timed.
+
+A "step" is one full World.Step: broadphase, narrowphase + manifold, contact cache,
+colouring, substepped solve + integration, contact and body update.
+
+  value   contacts/s = active contact points summed over the timed steps / device time
+          (CUDA events on the library's stream; state resident in HBM; L2 flushed
+          between steps by a 256 MiB write)
+  e2e     the same metric through jg_step_host: bodies copied from pinned host memory to
+          the device and back every step, copies inside the timed region
+  roofline  the substepped solve kernel against HBM bandwidth, bytes per step =
+          S * ((I + R) * 276 * C + 320 * C + 116 * N) + 52 * N
+  cpu_baseline  the oracle's multithreaded Regular-mode restatement of the reference
+          (C++ restatement of Jitter2, all host threads) on 2 steps of the same state
+
+--impl reference times that CPU restatement alone (the reference is C# and no .NET
+runtime exists on either machine) and prints the same line with "impl": "reference".
+Multi-GPU: the single world does not shard ("replicas only"); with N ranks each rank
+steps its own replica and value sums contacts over ranks / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_BODIES = 100000
+SETTLE_STEPS = 800
+SEED = 12347
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed loop runs."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_scene():
+    from jitterphysics2_gb300 import scenes
+    return scenes.mixed_pile(n=N_BODIES, box=(120.0, 200.0, 120.0), seed=SEED)
+
+
+def solver_bytes(counters, n_bodies, substeps=4, iters=8, relax=4):
+    c = counters["contacts"]
+    return substeps * ((iters + relax) * 276 * c + 320 * c + 116 * n_bodies) + 52 * n_bodies
+
+
+def cpu_baseline(scene, bodies, contacts, steps=2):
+    """The oracle's multithreaded Regular-mode step on the GPU's settled state."""
+    import oracle_lib as O
+    threads = os.cpu_count() or 1
+    sc = dict(scene)
+    sc["bodies"] = bodies
+    o = O.OracleWorld(sc)
+    o.set_contacts(contacts)
+    total_t, total_c = 0.0, 0
+    for _ in range(steps):
+        t = o.step_mt(scene["dt"], threads)
+        total_t += t
+        total_c += o.counters()["contacts"]
+    return {"value": total_c / total_t, "unit": "contacts/s", "cores": threads, "kind": "port",
+            "sample": "%d steps of the settled %d-body pile (C++ restatement of Jitter2, Regular mode)" % (steps, N_BODIES),
+            "seconds": total_t}
+
+
+def dist_setup(n_gpus):
+    if n_gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+    dist.init_process_group("nccl" if os.environ.get("JG_DIST_BACKEND", "nccl") == "nccl" else "gloo")
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def run_reference(args):
+    rank, ws, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    import oracle_lib as O
+    sc = make_scene()
+    o = O.OracleWorld(sc)
+    threads = os.cpu_count() or 1
+    # the CPU restatement settles the pile for a bounded number of steps (the full settle
+    # would take far longer than the run allows), then each timed step is one MT step
+    for _ in range(args.warmup):
+        o.step_mt(sc["dt"], threads)
+    total_t, total_c = 0.0, 0
+    for _ in range(args.steps):
+        total_t += o.step_mt(sc["dt"], threads)
+        total_c += o.counters()["contacts"]
+    v = total_c / total_t if total_t > 0 else 0.0
+    line = {"metric": "contacts/s @100k bodies", "value": v, "unit": "contacts/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "mixed pile, 100k bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations",
+                       "bodies": N_BODIES, "note": "C++ restatement of Jitter2 (Regular mode); the C# reference "
+                       "needs a .NET runtime, absent on both machines"},
+            "cpu_baseline": {"value": v, "unit": "contacts/s", "cores": threads, "kind": "port",
+                             "sample": "%d warm-up + %d timed multithreaded steps of the freshly dropped pile"
+                                       % (args.warmup, args.steps)},
+            "e2e": {"value": v, "unit": "contacts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--settle", type=int, default=SETTLE_STEPS)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, ws, dist = dist_setup(args.gpus)
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from jitterphysics2_gb300 import abi
+    from jitterphysics2_gb300.world import world_for_scene
+
+    sc = make_scene()
+    w = world_for_scene(sc)
+    for _ in range(args.settle):
+        w.step(sc["dt"])
+    for _ in range(max(3, args.warmup)):
+        w.step(sc["dt"])
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # device-timed steps (inputs resident)
+    clocks = ClockSampler()
+    clocks.start()
+    step_ms, solve_ms, contacts, sbytes, launches = [], [], 0, [], 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        w.step(sc["dt"])
+        t = w.timings()
+        c = w.counters()
+        step_ms.append(t["total"])
+        solve_ms.append(t["solve"])
+        contacts += c["contacts"]
+        sbytes.append(solver_bytes(c, len(sc["bodies"])))
+        launches += c["kernel_launches"]
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist is not None:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        cc = torch.tensor([float(contacts)], device="cuda")
+        dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+        total_ms, contacts_all = float(tt.item()), float(cc.item())
+    else:
+        contacts_all = float(contacts)
+    value = contacts_all / (total_ms / 1e3)
+
+    # end to end through the host-buffer call
+    host = np.ascontiguousarray(w.bodies())
+    pinned = torch.from_numpy(host.view(np.uint8)).pin_memory()
+    hb = pinned.numpy().view(abi.BODY_DTYPE)
+    e2e_c, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        w.step_host(sc["dt"], hb)
+        e2e_c += w.counters()["contacts"]
+    e2e_s = time.perf_counter() - t0
+    nbytes = hb.nbytes
+
+    peak, peak_kind = peaks()
+    achieved = float(np.mean([b / (s / 1e3) for b, s in zip(sbytes, solve_ms)])) / 1e9
+    line = {"metric": "contacts/s @100k bodies", "value": value, "unit": "contacts/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded mixed pile)",
+            "config": {"workload": "mixed pile, 100k bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations",
+                       "bodies": N_BODIES, "settle_steps": args.settle, "parallelism": "replicas only",
+                       "l2": "flushed between steps (256 MiB write)",
+                       "contacts_per_step": contacts / args.steps},
+            "e2e": {"value": e2e_c / e2e_s, "unit": "contacts/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "solve_ms_per_step": float(np.mean(solve_ms))},
+            "clocks": clk, "gpu_launches": launches,
+            "stage_ms": w.timings()}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(sc, w.bodies(), w.contacts())
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    w.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -165,6 +165,7 @@ typedef struct jg_counters {
     int64_t status;                     /* JG_ERR_* raised on the device, 0 if none      */
     int64_t created_arbiters;
     int64_t removed_arbiters;
+    int64_t kernel_launches;            /* device kernels launched by the last step       */
 } jg_counters;
 
 /* Stage timings in milliseconds (World.DebugTimings buckets, World.Step.cs:44-81). */

@@ -74,7 +74,8 @@ CONTACT_DTYPE = np.dtype([
     ("penalty_bias", "<f4"), ("friction", "<f4"), ("restitution", "<f4"),
 ])
 COUNTER_NAMES = ["pairs", "colliding", "manifold_points", "arbiters", "contacts", "new_contacts", "colors",
-                 "epa_calls", "epa_failures", "exact_fallbacks", "status", "created_arbiters", "removed_arbiters"]
+                 "epa_calls", "epa_failures", "exact_fallbacks", "status", "created_arbiters", "removed_arbiters",
+                 "kernel_launches"]
 TIMING_NAMES = ["broadphase", "narrowphase", "add_arbiter", "coloring", "solve", "update_contacts",
                 "update_bodies", "total"]
 

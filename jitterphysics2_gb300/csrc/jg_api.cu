@@ -41,6 +41,7 @@ struct jg_world {
     int nworlds = 1;
     std::vector<void*> allocs;
     bool mlp_ready = false;
+    int launches = 0;
 };
 
 namespace {
@@ -89,7 +90,7 @@ int allocate(jg_world* w) {
     int rs_blocks = (d.cap_shapes + 2047) / 2048;
     DA(d.hist, std::max(256 * rs_blocks + 1, 8192));
     DA(d.node, d.cap_shapes); DA(d.node_range, d.cap_shapes); DA(d.nmin, d.cap_shapes); DA(d.nmax, d.cap_shapes);
-    DA(d.leaf_parent, d.cap_shapes); DA(d.node_flag, d.cap_shapes);
+    DA(d.leaf_parent, d.cap_shapes); DA(d.node_parent, d.cap_shapes); DA(d.node_flag, d.cap_shapes);
     DA(d.scene_box, 2);
     DA(d.pairs, d.cap_pairs);
     DA(d.cs_key, d.cap_pairs); DA(d.cs_n, d.cap_pairs); DA(d.cs_pa, 4 * (size_t)d.cap_pairs); DA(d.cs_pb, 4 * (size_t)d.cap_pairs);
@@ -97,6 +98,7 @@ int allocate(jg_world* w) {
     if ((r = alloc_store(w, d.arb[0], d.cap_arb))) return r;
     if ((r = alloc_store(w, d.arb[1], d.cap_arb))) return r;
     d.cur = 0;
+    DA(d.col_pair, d.cap_arb); DA(d.col_res, 3 * (size_t)d.cap_arb); DA(d.col_portal, 12 * (size_t)d.cap_arb);
     d.hcap = next_pow2(2 * d.cap_arb);
     DA(d.hkeys, d.hcap); DA(d.hvals, d.hcap);
     DA(d.cstat, d.cap_arb + d.cap_joints);
@@ -198,7 +200,12 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
     if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 128, s);
     jg_launch_aabb(d, s);
-    jg_launch_broadphase(d, s, w->nsm);
+    int passes = jg_launch_broadphase(d, s, w->nsm);
+    // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
+    // narrowphase 2, merge 3 (+1 learned warm start), colour/permute 4, count 1, solve 1,
+    // contact update 1, body update 1
+    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 2 + 3 + 4 + 1 + 1 + 1 + 1 +
+                  ((sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) ? 1 : 0);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);
@@ -231,6 +238,7 @@ int finish_step(jg_world* w, bool timed) {
     o.contacts = c.contacts; o.new_contacts = c.new_contacts; o.colors = c.ncolors; o.epa_calls = c.nepa;
     o.epa_failures = c.epa_fail; o.exact_fallbacks = c.exact; o.status = c.status;
     o.created_arbiters = c.nnew; o.removed_arbiters = c.nremoved;
+    o.kernel_launches = w->launches;
     if (timed) {
         float t[8];
         for (int i = 0; i < 7; i++) cudaEventElapsedTime(&t[i], w->ev[i], w->ev[i + 1]);

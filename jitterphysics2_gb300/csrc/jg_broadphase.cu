@@ -197,15 +197,15 @@ __global__ void k_build(WorldDev w, int n) {
     int first = min(i, j), last = max(i, j);
     int left = (first == g) ? ~g : g;
     int right = (last == g + 1) ? ~(g + 1) : (g + 1);
-    w.node[i] = make_int4(left, right, w.node[i].z, 0);
+    w.node[i] = make_int4(left, right, 0, 0);
     w.node_range[i] = make_int2(first, last);
-    if (left < 0) w.leaf_parent[~left] = i; else w.node[left].z = i;
-    if (right < 0) w.leaf_parent[~right] = i; else w.node[right].z = i;
+    if (left < 0) w.leaf_parent[~left] = i; else w.node_parent[left] = i;
+    if (right < 0) w.leaf_parent[~right] = i; else w.node_parent[right] = i;
 }
 
 __global__ void k_build_init(WorldDev w, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n - 1) { w.node[i] = make_int4(0, 0, -1, 0); w.node_flag[i] = 0; }
+    if (i < n - 1) { w.node_parent[i] = -1; w.node_flag[i] = 0; }
 }
 
 __global__ void k_refit(WorldDev w, int n) {
@@ -223,7 +223,7 @@ __global__ void k_refit(WorldDev w, int n) {
         else { rmn = __ldcg(&w.nmin[nd.y]); rmx = __ldcg(&w.nmax[nd.y]); }
         __stcg(&w.nmin[p], make_float4(fminf(lmn.x, rmn.x), fminf(lmn.y, rmn.y), fminf(lmn.z, rmn.z), 0.f));
         __stcg(&w.nmax[p], make_float4(fmaxf(lmx.x, rmx.x), fmaxf(lmx.y, rmx.y), fmaxf(lmx.z, rmx.z), 0.f));
-        p = nd.z;
+        p = w.node_parent[p];
     }
 }
 

@@ -25,18 +25,24 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct MV { v3 V, A, B; };
 
-__device__ __forceinline__ void mk_support(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, v3 d, MV& v) {
+// MinkowskiDifference.Support (MinkowskiDifference.cs:57-69).  WARP: the 32 lanes of a
+// warp evaluate it together (point clouds split across lanes); otherwise one thread.
+template <bool WARP>
+__device__ __forceinline__ void mk_support_t(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, v3 d, MV& v) {
     v3 tmp = -d;
-    v.A = support(sa, d);
+    v.A = WARP ? support(sa, d) : support_lane(sa, d);
     v3 tmp2 = rotate_inv(tmp, qb);
-    v.B = support(sb, tmp2);
+    v.B = WARP ? support(sb, tmp2) : support_lane(sb, tmp2);
     v.B = rotate(v.B, qb);
     v.B = v.B + pb;
     v.V = v.A - v.B;
 }
+__device__ __forceinline__ void mk_support(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, v3 d, MV& v) {
+    mk_support_t<true>(sa, sb, qb, pb, d, v);
+}
 __device__ __forceinline__ void mk_center(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, MV& c) {
-    c.A = sa.center;
-    c.B = rotate(sb.center, qb);
+    c.A = shape_center(sa);
+    c.B = rotate(shape_center(sb), qb);
     c.B = pb + c.B;
     c.V = c.A - c.B;
 }
@@ -82,7 +88,7 @@ struct Exp {
         return addp(o, len, c, nc, d, nd, true, 16);
     }
     // ExpansionArithmetic.Side (ExactArithmetic/ExpansionArithmetic.cs:20-41)
-    __device__ static int side(v3 a, v3 b, v3 c, v3 p) {
+    __device__ __noinline__ static int side(v3 a, v3 b, v3 c, v3 p) {
         double ux[2], uy[2], uz[2], vx[2], vy[2], vz[2], dx[2], dy[2], dz[2];
         int nx = diff(a.x, b.x, ux), ny = diff(a.y, b.y, uy), nz = diff(a.z, b.z, uz);
         int mx = diff(a.x, c.x, vx), my = diff(a.y, c.y, vy), mz = diff(a.z, c.z, vz);
@@ -99,7 +105,7 @@ struct Exp {
         return t > 0 ? 1 : (t < 0 ? -1 : 0);
     }
     // ExpansionArithmetic.Normal (ExpansionArithmetic.cs:43-55)
-    __device__ static v3 normal(v3 a, v3 b, v3 c) {
+    __device__ __noinline__ static v3 normal(v3 a, v3 b, v3 c) {
         double ux[2], uy[2], uz[2], vx[2], vy[2], vz[2], cr[16];
         int nx = diff(a.x, b.x, ux), ny = diff(a.y, b.y, uy), nz = diff(a.z, b.z, uz);
         int mx = diff(a.x, c.x, vx), my = diff(a.y, c.y, vy), mz = diff(a.z, c.z, vz);
@@ -119,7 +125,7 @@ struct Exp {
 
 // PlaneFilter in double (ExactArithmetic/PlaneFilter.cs:29-70); the FP32 filter below
 // tries first.
-__device__ bool dfilter_side(v3 a, v3 b, v3 c, v3 p, int& sign) {
+__device__ __noinline__ bool dfilter_side(v3 a, v3 b, v3 c, v3 p, int& sign) {
     const double EF = 16 * 1.1102230246251565e-16;
     double ux = (double)a.x - b.x, uy = (double)a.y - b.y, uz = (double)a.z - b.z;
     double vx = (double)a.x - c.x, vy = (double)a.y - c.y, vz = (double)a.z - c.z;
@@ -219,7 +225,7 @@ __device__ bool calc_bary(v3 a, v3 b, v3 c, v3 n, float nscale, float nsq, v3& o
 }
 
 // ConvexPolytope.CreateTriangle (ConvexPolytope.cs:267-318), one lane per face.
-__device__ int create_tri(EpaSmem& E, int a, int b, int c, int slot, NpStats& st) {
+__device__ __noinline__ int create_tri(EpaSmem& E, int a, int b, int c, int slot, NpStats& st) {
     v3 va = mk3(E.vV[a]), vb = mk3(E.vV[b]), vc = mk3(E.vV[c]);
     int orient = 0;
     for (int i = 0; i < 4 && orient == 0; i++) {
@@ -301,7 +307,7 @@ __device__ int epa_closest(EpaSmem& E) {
 }
 
 // ConvexPolytope.AddVertexDetailed (ConvexPolytope.cs:199-265)
-__device__ int epa_add(EpaSmem& E, const MV& v, NpStats& st) {
+__device__ __noinline__ int epa_add(EpaSmem& E, const MV& v, NpStats& st) {
     const int lane = threadIdx.x & 31;
     if (E.nt == 0 || !is_safe(v.V)) return NUMERICAL;
     int nv = E.nv;
@@ -388,7 +394,7 @@ __device__ int epa_add(EpaSmem& E, const MV& v, NpStats& st) {
 }
 
 // MprEpaSolver.SolveMprEpa (NarrowPhase.cs:39-95).  Seed vertices are in E.v*[0..3].
-__device__ bool solve_epa(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb,
+__device__ __noinline__ bool solve_epa(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb,
                           v3& p1, v3& p2, v3& n, float& pen, NpStats& st) {
     const float eps = 1e-5f;
     const int maxIter = 85;
@@ -437,9 +443,13 @@ converged:
     return true;
 }
 
-// MprEpaSolver.SolveMpr (NarrowPhase.cs:98-347), all lanes redundantly.
-__device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, float epa_threshold,
-                          v3& pA, v3& pB, v3& normal, float& pen, NpStats& st, int& epa_calls, int& epa_fail) {
+// MprEpaSolver.SolveMpr (NarrowPhase.cs:98-347) up to the EPA hand-off.  Returns 0 (no
+// overlap), 1 (overlap, result final) or 2 (overlap deeper than epa_threshold: the MPR
+// result is in pA/pB/normal/pen as the fallback, and `portal` holds the tetrahedron EPA
+// starts from).  WARP: evaluated redundantly by a whole warp; otherwise one thread.
+template <bool WARP>
+__device__ int mpr_core(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, float epa_threshold,
+                        v3& pA, v3& pB, v3& normal, float& pen, MV* portal) {
     const float eps = 1e-5f;
     const int maxIter = 34;
     const float NumericEpsilon = 1e-16f;
@@ -449,19 +459,19 @@ __device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4
     mk_center(sa, sb, qb, pb, v0);
     if (fabsf(v0.V.x) < NumericEpsilon && fabsf(v0.V.y) < NumericEpsilon && fabsf(v0.V.z) < NumericEpsilon) v0.V.x = 1e-05f;
     normal = -v0.V;
-    mk_support(sa, sb, qb, pb, normal, v1);
+    mk_support_t<WARP>(sa, sb, qb, pb, normal, v1);
     pA = v1.A; pB = v1.B;
-    if (dot(v1.V, normal) <= 0.0f) return false;
+    if (dot(v1.V, normal) <= 0.0f) return 0;
     normal = cross(v1.V, v0.V);
     if (len2(normal) < 1e-12f) {
         normal = v1.V - v0.V;
         normal = normalize(normal);
         t1 = v1.A - v1.B;
         pen = dot(t1, normal);
-        return true;
+        return 1;
     }
-    mk_support(sa, sb, qb, pb, normal, v2);
-    if (dot(v2.V, normal) <= 0.0f) return false;
+    mk_support_t<WARP>(sa, sb, qb, pb, normal, v2);
+    if (dot(v2.V, normal) <= 0.0f) return 0;
     t1 = v1.V - v0.V;
     t2 = v2.V - v0.V;
     normal = cross(t1, t2);
@@ -474,10 +484,10 @@ __device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4
     int phase2 = 0, phase1 = 0;
     bool hit = false;
     while (true) {
-        if (phase1 > maxIter) return false;
+        if (phase1 > maxIter) return 0;
         phase1++;
-        mk_support(sa, sb, qb, pb, normal, v3v);
-        if (dot(v3v.V, normal) <= 0.0f) return false;
+        mk_support_t<WARP>(sa, sb, qb, pb, normal, v3v);
+        if (dot(v3v.V, normal) <= 0.0f) return 0;
         t1 = cross(v1.V, v3v.V);
         if (dot(t1, v0.V) < 0.0f) {
             v2 = v3v;
@@ -500,42 +510,33 @@ __device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4
         t2 = v3v.V - v1.V;
         normal = cross(t1, t2);
         float nsq = len2(normal);
-        if (nsq < NumericEpsilon) return false;
+        if (nsq < NumericEpsilon) return 0;
         if (!hit) {
             float d = dot(normal, v1.V);
             hit = d >= 0;
         }
-        mk_support(sa, sb, qb, pb, normal, v4);
+        mk_support_t<WARP>(sa, sb, qb, pb, normal, v4);
         t3 = v4.V - v3v.V;
         float delta = dot(t3, normal);
         pen = dot(v4.V, normal);
         if (delta * delta <= eps * eps * nsq || pen <= 0.0f || phase2 > maxIter) {
-            if (hit) {
-                float invn = 1.0f / sqrtf(nsq);
-                pen *= invn;
-                if (pen > epa_threshold) {
-                    const int lane = threadIdx.x & 31;
-                    if (lane == 0) {
-                        E.vV[0] = f4(v0.V, 0.f); E.vA[0] = f4(v0.A, 0.f); E.vB[0] = f4(v0.B, 0.f);
-                        E.vV[1] = f4(v1.V, 0.f); E.vA[1] = f4(v1.A, 0.f); E.vB[1] = f4(v1.B, 0.f);
-                        E.vV[2] = f4(v2.V, 0.f); E.vA[2] = f4(v2.A, 0.f); E.vB[2] = f4(v2.B, 0.f);
-                        E.vV[3] = f4(v3v.V, 0.f); E.vA[3] = f4(v3v.A, 0.f); E.vB[3] = f4(v3v.B, 0.f);
-                    }
-                    __syncwarp();
-                    epa_calls++;
-                    if (solve_epa(E, sa, sb, qb, pb, pA, pB, normal, pen, st)) return true;
-                    epa_fail++;
-                }
-                normal = normal * invn;
-                t3 = cross(v1.V, t1);
-                float gamma = dot(t3, normal) * invn;
-                t3 = cross(t2, v1.V);
-                float beta = dot(t3, normal) * invn;
-                float alpha = 1.0f - gamma - beta;
-                pA = alpha * v1.A + beta * v2.A + gamma * v3v.A;
-                pB = alpha * v1.B + beta * v2.B + gamma * v3v.B;
+            if (!hit) return 0;
+            float invn = 1.0f / sqrtf(nsq);
+            pen *= invn;
+            int code = 1;
+            if (pen > epa_threshold) {
+                portal[0] = v0; portal[1] = v1; portal[2] = v2; portal[3] = v3v;
+                code = 2;
             }
-            return hit;
+            normal = normal * invn;
+            t3 = cross(v1.V, t1);
+            float gamma = dot(t3, normal) * invn;
+            t3 = cross(t2, v1.V);
+            float beta = dot(t3, normal) * invn;
+            float alpha = 1.0f - gamma - beta;
+            pA = alpha * v1.A + beta * v2.A + gamma * v3v.A;
+            pB = alpha * v1.B + beta * v2.B + gamma * v3v.B;
+            return code;
         }
         t1 = cross(v4.V, v0.V);
         float d = dot(t1, v1.V);
@@ -547,6 +548,33 @@ __device__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4
             if (d >= 0.0f) v2 = v4; else v1 = v4;
         }
     }
+}
+
+// EPA from a saved MPR portal, by the whole warp; on failure the MPR result stands
+// (NarrowPhase.cs:287-298).
+__device__ void run_epa(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, const MV* portal,
+                        v3& pA, v3& pB, v3& normal, float& pen, NpStats& st, int& epa_calls, int& epa_fail) {
+    const int lane = threadIdx.x & 31;
+    if (lane < 4) {
+        E.vV[lane] = f4(portal[lane].V, 0.f);
+        E.vA[lane] = f4(portal[lane].A, 0.f);
+        E.vB[lane] = f4(portal[lane].B, 0.f);
+    }
+    __syncwarp();
+    epa_calls++;
+    v3 a, b, n;
+    float p;
+    if (solve_epa(E, sa, sb, qb, pb, a, b, n, p, st)) { pA = a; pB = b; normal = n; pen = p; }
+    else epa_fail++;
+}
+
+// MprEpaSolver.SolveMpr with its EPA refinement, whole warp (the edge filter's rerun).
+__device__ __noinline__ bool solve_mpr(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, float epa_threshold,
+                          v3& pA, v3& pB, v3& normal, float& pen, NpStats& st, int& epa_calls, int& epa_fail) {
+    MV portal[4];
+    int code = mpr_core<true>(sa, sb, qb, pb, epa_threshold, pA, pB, normal, pen, portal);
+    if (code == 2) run_epa(E, sa, sb, qb, pb, portal, pA, pB, normal, pen, st, epa_calls, epa_fail);
+    return code != 0;
 }
 
 // NarrowPhase.MprEpa world-space wrapper (NarrowPhase.cs:902-927)
@@ -563,7 +591,7 @@ __device__ bool mpr_epa_world(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb
 
 // ---- TriangleEdgeCollisionFilter (TriangleEdgeCollisionFilter.cs:183-420) ---------------
 enum { KEEP = 0, DISCARD = 1, EDGE = 2 };
-__device__ int edge_evaluate(const WorldDev& w, int tri, q4 tq, v3 tp, bool tri_is_b, v3 cp, v3 n, v3& tn, v3& nn) {
+__device__ __noinline__ int edge_evaluate(const WorldDev& w, int tri, q4 tq, v3 tp, bool tri_is_b, v3 cp, v3 n, v3& tn, v3& nn) {
     const TriDev& T = w.tris[tri];
     const float cosAngle = 0.999f, edgeThreshold = 0.01f;
     tn = rotate(mk3(T.n), tq);
@@ -713,7 +741,7 @@ struct MF {
     }
 };
 
-__device__ int build_manifold(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qa, q4 qb, v3 pa, v3 pb,
+__device__ __noinline__ int build_manifold(EpaSmem& E, const ShapeRef& sa, const ShapeRef& sb, q4 qa, q4 qb, v3 pa, v3 pb,
                               v3 pA, v3 pB, v3 n, v3* outA, v3* outB) {
     const int lane = threadIdx.x & 31;
     const float P = 0.01f, S = 0.86602540378f;
@@ -832,6 +860,65 @@ finalize:
 
 constexpr int NP_WARPS = 4;
 
+// Stage 1, one thread per broadphase pair: the MPR overlap test in A's frame
+// (NarrowPhase.MprEpa, NarrowPhase.cs:902-927, up to the EPA hand-off).  Overlapping pairs
+// are appended (warp-aggregated) to the colliding list with their MPR result and, when
+// deeper than the EPA threshold, the MPR portal EPA starts from.
+__global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
+    const int lane = threadIdx.x & 31;
+    const int npairs = min(w.ctr->npairs, w.cap_pairs);
+    const int cap = w.cap_arb;
+    for (int base = blockIdx.x * blockDim.x; base < npairs; base += gridDim.x * blockDim.x) {
+        int p = base + threadIdx.x;
+        int code = 0;
+        v3 pA, pB, n;
+        float pen = 0.f;
+        MV portal[4];
+        if (p < npairs) {
+            int2 pr = w.pairs[p];
+            int s1 = pr.x, s2 = pr.y;  // s1 < s2: ShapeId order (World.Detect.cs:141-144)
+            int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
+            int4 i1 = w.binfo[b1], i2 = w.binfo[b2];
+            bool skip = (!(i1.y & JG_BODY_ACTIVE) && !(i2.y & JG_BODY_ACTIVE)) ||
+                        (i1.x != JG_MOTION_DYNAMIC && i2.x != JG_MOTION_DYNAMIC);
+            if (!skip) {
+                ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
+                q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+                v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+                q4 q = qmul(qconj(qa), qb);
+                v3 pr_ = rotate_inv(pb - pa, qa);
+                code = mpr_core<false>(sa, sb, q, pr_, 0.02f, pA, pB, n, pen, portal);
+            }
+        }
+        unsigned m = __ballot_sync(FULL, code != 0);
+        if (!m) continue;
+        int leader = __ffs(m) - 1;
+        int baseidx = 0;
+        if (lane == leader) baseidx = atomicAdd(&w.ctr->ncol, __popc(m));
+        baseidx = __shfl_sync(FULL, baseidx, leader);
+        if (code) {
+            int c = baseidx + __popc(m & ((1u << lane) - 1u));
+            if (c < cap) {
+                w.col_pair[c] = make_int2(p, code);
+                w.col_res[3 * c + 0] = f4(pA, 0.f);
+                w.col_res[3 * c + 1] = f4(pB, 0.f);
+                w.col_res[3 * c + 2] = f4(n, pen);
+                if (code == 2) {
+                    for (int k = 0; k < 4; k++) {
+                        w.col_portal[12 * c + 3 * k + 0] = f4(portal[k].V, 0.f);
+                        w.col_portal[12 * c + 3 * k + 1] = f4(portal[k].A, 0.f);
+                        w.col_portal[12 * c + 3 * k + 2] = f4(portal[k].B, 0.f);
+                    }
+                }
+            } else {
+                atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY);
+            }
+        }
+    }
+}
+
+// Stage 2, one warp per overlapping pair: EPA from the saved portal when needed, the
+// triangle-edge filter and the one-shot manifold; appends the contact stream record.
 __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams sp) {
     __shared__ EpaSmem smem[NP_WARPS];
     const int lane = threadIdx.x & 31;
@@ -839,21 +926,35 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams
     EpaSmem& E = smem[wib];
     NpStats st; st.exact = 0;
     int epa_calls = 0, epa_fail = 0, written = 0, pts = 0;
-    int npairs = min(w.ctr->npairs, w.cap_pairs);
-    for (int p = blockIdx.x * NP_WARPS + wib; p < npairs; p += gridDim.x * NP_WARPS) {
-        int2 pr = w.pairs[p];
-        int s1 = pr.x, s2 = pr.y;  // s1 < s2: ShapeId order (World.Detect.cs:141-144)
+    int ncol = min(w.ctr->ncol, w.cap_arb);
+    for (int c = blockIdx.x * NP_WARPS + wib; c < ncol; c += gridDim.x * NP_WARPS) {
+        int2 cp = w.col_pair[c];
+        int2 pr = w.pairs[cp.x];
+        int s1 = pr.x, s2 = pr.y;
         ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
         int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
         int4 i1 = w.binfo[b1], i2 = w.binfo[b2];
-        if (!(i1.y & JG_BODY_ACTIVE) && !(i2.y & JG_BODY_ACTIVE)) continue;
-        if (i1.x != JG_MOTION_DYNAMIC && i2.x != JG_MOTION_DYNAMIC) continue;
         q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
         v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
-        v3 pA, pB, n;
-        float pen;
-        bool hit = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, n, pen, 0.02f, st, epa_calls, epa_fail);
-        if (!hit) continue;  // speculative contacts (off by default, RigidBody.cs:863) not handled
+        v3 pA = mk3(w.col_res[3 * c + 0]), pB = mk3(w.col_res[3 * c + 1]);
+        float4 nr = w.col_res[3 * c + 2];
+        v3 n = mk3(nr);
+        float pen = nr.w;
+        if (cp.y == 2) {
+            MV portal[4];
+            for (int k = 0; k < 4; k++) {
+                portal[k].V = mk3(w.col_portal[12 * c + 3 * k + 0]);
+                portal[k].A = mk3(w.col_portal[12 * c + 3 * k + 1]);
+                portal[k].B = mk3(w.col_portal[12 * c + 3 * k + 2]);
+            }
+            q4 q = qmul(qconj(qa), qb);
+            v3 prl = rotate_inv(pb - pa, qa);
+            run_epa(E, sa, sb, q, prl, portal, pA, pB, n, pen, st, epa_calls, epa_fail);
+        }
+        // back to world space (NarrowPhase.cs:920-924)
+        pA = rotate(pA, qa); pA = pA + pa;
+        pB = rotate(pB, qa); pB = pB + pa;
+        n = rotate(n, qa);
         if (sp.edge_filter) {
             bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
             bool tri_dyn = c1 ? i1.x == JG_MOTION_DYNAMIC : i2.x == JG_MOTION_DYNAMIC;
@@ -936,6 +1037,7 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams
 
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
     (void)tile;
+    k_mpr<<<nsm * 8, 256, 0, s>>>(w);
     int blocks = nsm * 8;
     k_narrow<<<blocks, NP_WARPS * 32, 0, s>>>(w, p);
 }

@@ -5,41 +5,48 @@
 #pragma once
 #include "jg_world.cuh"
 
+// Compact shape record (kept small: the MPR stage runs one pair per thread).
+//   analytic shapes: d = dims (box half extents; r, half length; r, height), b = centre
+//   point cloud:     d = shift, b = centre of mass, hull / nhull = vertices
+//   triangle:        d, b, c = mesh-local vertices, tri = triangle id
 struct ShapeRef {
     int kind;
-    v3 d;          // dims
-    v3 center;     // GetCenter
-    v3 shift;      // point cloud shift
+    v3 d, b, c;
     const float4* hull;
     int nhull;
-    v3 ta, tb, tc; // triangle vertices (mesh local)
-    int tri;       // triangle id
+    int tri;
 };
 
 __device__ __forceinline__ ShapeRef load_shape(const WorldDev& w, int s) {
     ShapeRef r;
     int4 info = w.sinfo[s];
-    float4 d = w.sdims[s];
-    float4 c = w.scenter[s];
     r.kind = info.x;
-    r.d = mk3(d.x, d.y, d.z);
-    r.center = mk3(c.x, c.y, c.z);
-    r.shift = mk3(0.f);
     r.hull = nullptr;
     r.nhull = 0;
     r.tri = -1;
-    r.ta = r.tb = r.tc = mk3(0.f);
-    if (r.kind == JG_SHAPE_POINTCLOUD) {
-        r.shift = r.d;
-        r.hull = w.hull + info.z;
-        r.nhull = info.w;
-    } else if (r.kind == JG_SHAPE_TRIANGLE) {
+    r.c = mk3(0.f);
+    if (r.kind == JG_SHAPE_TRIANGLE) {
         const TriDev& t = w.tris[info.z];
         r.tri = info.z;
-        r.ta = mk3(t.a); r.tb = mk3(t.b); r.tc = mk3(t.c);
-        r.center = (1.0f / 3.0f) * (r.ta + r.tb + r.tc);  // TriangleShape.GetCenter (TriangleShape.cs:158-165)
+        r.d = mk3(t.a); r.b = mk3(t.b); r.c = mk3(t.c);
+    } else {
+        float4 d = w.sdims[s];
+        float4 c = w.scenter[s];
+        r.d = mk3(d.x, d.y, d.z);
+        r.b = mk3(c.x, c.y, c.z);
+        if (r.kind == JG_SHAPE_POINTCLOUD) {
+            r.hull = w.hull + info.z;
+            r.nhull = info.w;
+        }
     }
     return r;
+}
+
+// GetCenter: the uploaded centre (zero for analytic shapes, the centre of mass for point
+// clouds) or the triangle centroid (TriangleShape.GetCenter, TriangleShape.cs:158-165).
+__device__ __forceinline__ v3 shape_center(const ShapeRef& s) {
+    if (s.kind == JG_SHAPE_TRIANGLE) return (1.0f / 3.0f) * (s.d + s.b + s.c);
+    return s.b;
 }
 
 // Warp-cooperative VertexSupportMap.SupportMapScalar (VertexSupportMap.cs:127-147):
@@ -94,14 +101,14 @@ __device__ __forceinline__ v3 support(const ShapeRef& s, v3 d) {
             return mk3(0.0f, 0.75f * s.d.y, 0.0f);
         }
         case JG_SHAPE_POINTCLOUD:
-            return hull_support_warp(s.hull, s.nhull, d) + s.shift;
+            return hull_support_warp(s.hull, s.nhull, d) + s.d;
         default: {
-            float mn = dot(s.ta, d);
-            float dt = dot(s.tb, d);
-            v3 r = s.ta;
-            if (dt > mn) { mn = dt; r = s.tb; }
-            dt = dot(s.tc, d);
-            if (dt > mn) r = s.tc;
+            float mn = dot(s.d, d);
+            float dt = dot(s.b, d);
+            v3 r = s.d;
+            if (dt > mn) { mn = dt; r = s.b; }
+            dt = dot(s.c, d);
+            if (dt > mn) r = s.c;
             return r;
         }
     }
@@ -121,7 +128,7 @@ __device__ __forceinline__ v3 support_lane(const ShapeRef& s, v3 d) {
             best = dp; bi = i;
         }
         float4 p = __ldg(s.hull + bi);
-        return mk3(p.x, p.y, p.z) + s.shift;
+        return mk3(p.x, p.y, p.z) + s.d;
     }
     switch (s.kind) {
         case JG_SHAPE_BOX:
@@ -146,12 +153,12 @@ __device__ __forceinline__ v3 support_lane(const ShapeRef& s, v3 d) {
             return mk3(0.0f, 0.75f * s.d.y, 0.0f);
         }
         default: {
-            float mn = dot(s.ta, d);
-            float dt = dot(s.tb, d);
-            v3 r = s.ta;
-            if (dt > mn) { mn = dt; r = s.tb; }
-            dt = dot(s.tc, d);
-            if (dt > mn) r = s.tc;
+            float mn = dot(s.d, d);
+            float dt = dot(s.b, d);
+            v3 r = s.d;
+            if (dt > mn) { mn = dt; r = s.b; }
+            dt = dot(s.c, d);
+            if (dt > mn) r = s.c;
             return r;
         }
     }
@@ -213,7 +220,7 @@ __device__ __forceinline__ void shape_aabb(const ShapeRef& s, q4 q, v3 p, v3& mn
             break;
         }
         default: {
-            v3 a = rotate(s.ta, q), b = rotate(s.tb, q), c = rotate(s.tc, q);
+            v3 a = rotate(s.d, q), b = rotate(s.b, q), c = rotate(s.c, q);
             mn = mk3(3.402823466e+38f);
             mx = mk3(-3.402823466e+38f);
             mx = vmax(mx, a); mn = vmin(mn, a);

@@ -78,7 +78,8 @@ struct DevCounters {
     int contacts;     // active contact points after the merge
     int new_contacts;
     int color_rounds;
-    int pad[2];
+    int ncol;         // overlapping pairs found by the MPR stage
+    int pad;
 };
 
 struct WorldDev {
@@ -102,18 +103,18 @@ struct WorldDev {
     int2* node_range;            // leaf range [first, last] per internal node
     float4 *nmin, *nmax;         // internal node AABBs
     int* leaf_parent;
+    int* node_parent;            // parent of each internal node (-1 for the root)
     int* node_flag;
     float4* scene_box;           // [0] min, [1] max (reduction)
     int2* pairs;
-    // narrowphase output (contact stream) and EPA queue
+    // narrowphase: overlapping pairs from the MPR stage, then the contact stream
+    int2* col_pair;              // [cap_arb] pair index, MPR code (1 final, 2 needs EPA)
+    float4* col_res;             // [3 * cap_arb] MPR result in A's frame: pA, pB, normal|depth
+    float4* col_portal;          // [12 * cap_arb] MPR portal (4 vertices: V, A, B)
     int2* cs_key;
     float4* cs_n;                // normal xyz, count
     float4* cs_pa;               // [4 * cap_pairs]
     float4* cs_pb;
-    int* epa_pair;               // pair index
-    float4* epa_seed;            // [4 * 3 * cap] MPR portal vertices V, A, B
-    float4* epa_mpr;             // MPR fallback: pA, pB, n|pen
-    int* epa_flag;               // bit0: threshold-zero rerun from the edge filter
     // arbiters
     ArbStore arb[2];
     int cur;                     // which ArbStore holds the live arbiters

