@@ -99,6 +99,7 @@ int allocate(jg_world* w) {
     if ((r = alloc_store(w, d.arb[1], d.cap_arb))) return r;
     d.cur = 0;
     DA(d.col_pair, d.cap_arb); DA(d.col_res, 3 * (size_t)d.cap_arb); DA(d.col_portal, 12 * (size_t)d.cap_arb);
+    DA(d.epa_list, d.cap_arb); DA(d.edge_list, d.cap_arb);
     d.hcap = next_pow2(2 * d.cap_arb);
     DA(d.hkeys, d.hcap); DA(d.hvals, d.hcap);
     DA(d.cstat, d.cap_arb + d.cap_joints);
@@ -202,9 +203,9 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     jg_launch_aabb(d, s);
     int passes = jg_launch_broadphase(d, s, w->nsm);
     // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
-    // narrowphase 2, merge 3 (+1 learned warm start), colour/permute 4, count 1, solve 1,
+    // narrowphase 4, merge 3 (+1 learned warm start), colour/permute 4, count 1, solve 1,
     // contact update 1, body update 1
-    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 2 + 3 + 4 + 1 + 1 + 1 + 1 +
+    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 4 + 3 + 4 + 1 + 1 + 1 + 1 +
                   ((sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) ? 1 : 0);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);

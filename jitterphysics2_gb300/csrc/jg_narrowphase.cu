@@ -858,14 +858,155 @@ finalize:
     return count;
 }
 
+// ---- one-shot manifold, one thread per pair ----------------------------------------------
+// The same steps as build_manifold (CollisionManifold.cs:393-566) with the candidate lists
+// in thread-local storage, for analytic shapes and point clouds alike.
+struct MFT {
+    float4 A[12], B[12];
+    int count;
+    __device__ void on_a(v3 p, v3 pB, v3 n) {
+        if (count == 12) return;
+        float diff = dot(p - pB, n);
+        if (diff < 0.0f) return;
+        if (is_dup(A, count, p)) return;
+        A[count] = f4(p, 0.f); B[count] = f4(p - diff * n, 0.f); count++;
+    }
+    __device__ void on_b(v3 p, v3 pA, v3 n) {
+        if (count == 12) return;
+        float diff = dot(p - pA, n);
+        if (diff > 0.0f) return;
+        if (is_dup(B, count, p)) return;
+        A[count] = f4(p - diff * n, 0.f); B[count] = f4(p, 0.f); count++;
+    }
+    __device__ void pair(v3 a, v3 b, v3 n) {
+        if (count == 12) return;
+        if (dot(a - b, n) < 0.0f) return;
+        if (is_dup(A, count, a)) return;
+        if (is_dup(B, count, b)) return;
+        A[count] = f4(a, 0.f); B[count] = f4(b, 0.f); count++;
+    }
+};
+__device__ __forceinline__ void push_local(float4* arr, int& cnt, v3 v) {
+    if (cnt > 0 && len2(mk3(arr[0]) - v) < 0.001f) return;
+    if (cnt > 1 && len2(mk3(arr[cnt - 1]) - v) < 0.001f) return;
+    arr[cnt++] = f4(v, 0.f);
+}
+
+__device__ __noinline__ int manifold_thread(const ShapeRef& sa, const ShapeRef& sb, q4 qa, q4 qb, v3 pa, v3 pb,
+                                            v3 pA, v3 pB, v3 n, float4* outA, float4* outB) {
+    const float P = 0.01f, S = 0.86602540378f;
+    const float hx[12] = {1.0f, 0.0f, 0.5f, S, -0.5f, S, -1.0f, 0.0f, -0.5f, -S, 0.5f, -S};
+    v3 c1 = create_orthonormal(n);
+    v3 c2 = cross(n, c1);
+    v3 relB = pb - pa, pAl = pA - pa, pBl = pB - pa;
+    float4 left[6], right[6];
+    int lc = 0, rc = 0;
+    for (int e = 0; e < 6; e++) {
+        v3 pn = n + hx[2 * e + 0] * P * c1 + hx[2 * e + 1] * P * c2;
+        push_local(left, lc, rotate(support_lane(sa, rotate_inv(pn, qa)), qa));
+        pn = -pn;
+        push_local(right, rc, rotate(support_lane(sb, rotate_inv(pn, qb)), qb) + relB);
+    }
+    float ls = 0.f, rs = 0.f;
+    bool lp = lc > 2 && polygon_sign(left, lc, n, ls);
+    bool rp = rc > 2 && polygon_sign(right, rc, n, rs);
+    MFT m;
+    m.count = 0;
+    if (lp) {
+        for (int e = 0; e < rc; e++) {
+            v3 p = mk3(right[e]);
+            if (!contains_pt(left, lc, p, n, ls)) continue;
+            m.on_b(p, pAl, n);
+            if (m.count == 12) goto finalize;
+        }
+        if (rc == 2) {
+            v3 cl[2];
+            int k = clip_segment(mk3(right[0]), mk3(right[1]), left, lc, n, ls, cl);
+            for (int i = 0; i < k; i++) { m.on_b(cl[i], pAl, n); if (m.count == 12) goto finalize; }
+        }
+    }
+    if (rp) {
+        for (int e = 0; e < lc; e++) {
+            v3 p = mk3(left[e]);
+            if (!contains_pt(right, rc, p, n, rs)) continue;
+            m.on_a(p, pBl, n);
+            if (m.count == 12) goto finalize;
+        }
+        if (lc == 2) {
+            v3 cl[2];
+            int k = clip_segment(mk3(left[0]), mk3(left[1]), right, rc, n, rs, cl);
+            for (int i = 0; i < k; i++) { m.on_a(cl[i], pBl, n); if (m.count == 12) goto finalize; }
+        }
+    }
+    if (lc == 2 && rc == 2) {
+        v3 cA[2], cB[2];
+        int k = intersect_seg(mk3(left[0]), mk3(left[1]), mk3(right[0]), mk3(right[1]), n, cA, cB);
+        for (int i = 0; i < k; i++) { m.pair(cA[i], cB[i], n); if (m.count == 12) goto finalize; }
+    }
+    if (lp && rp) {
+        for (int i = 0; i < lc; i++) {
+            v3 sA = mk3(left[i]), eA = mk3(left[(i + 1) % lc]);
+            for (int j = 0; j < rc; j++) {
+                v3 cA[2], cB[2];
+                int k = intersect_seg(sA, eA, mk3(right[j]), mk3(right[(j + 1) % rc]), n, cA, cB);
+                for (int q = 0; q < k; q++) { m.pair(cA[q], cB[q], n); if (m.count == 12) goto finalize; }
+            }
+        }
+    }
+    if (m.count <= 1) { m.A[0] = f4(pAl, 0.f); m.B[0] = f4(pBl, 0.f); m.count = 1; }
+    else if (m.count < 4) { m.A[m.count] = f4(pAl, 0.f); m.B[m.count] = f4(pBl, 0.f); m.count++; }
+finalize:
+    int count = m.count;
+    if (count > 4) {
+        // ReduceManifold (CollisionManifold.cs:321-375)
+        v3 c = mk3(0.f);
+        for (int i = 0; i < count; i++) c = c + mk3(m.A[i]);
+        c = c * (float)(1.0 / count);
+        v3 t1 = create_orthonormal(n);
+        v3 t2 = cross(n, t1);
+        float ang[12];
+        int order[12];
+        for (int i = 0; i < count; i++) {
+            v3 d = mk3(m.A[i]) - c;
+            ang[i] = StableMathF::atan2(dot(d, t2), dot(d, t1));
+            order[i] = i;
+        }
+        for (int i = 1; i < count; i++) {
+            int cur = order[i];
+            float ca = ang[cur];
+            int j = i - 1;
+            while (j >= 0 && ang[order[j]] > ca) { order[j + 1] = order[j]; j--; }
+            order[j + 1] = cur;
+        }
+        for (int i = 0; i < 4; i++) {
+            int sel = order[((2 * i + 1) * count) / 8];
+            outA[i] = f4(mk3(m.A[sel]) + pa, 0.f);
+            outB[i] = f4(mk3(m.B[sel]) + pa, 0.f);
+        }
+        return 4;
+    }
+    for (int i = 0; i < count; i++) { outA[i] = f4(mk3(m.A[i]) + pa, 0.f); outB[i] = f4(mk3(m.B[i]) + pa, 0.f); }
+    return count;
+}
+
 constexpr int NP_WARPS = 4;
+
+__device__ __forceinline__ int warp_append(int* counter, bool pred) {
+    const int lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(FULL, pred);
+    if (!m) return -1;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(FULL, base, leader);
+    return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
 
 // Stage 1, one thread per broadphase pair: the MPR overlap test in A's frame
 // (NarrowPhase.MprEpa, NarrowPhase.cs:902-927, up to the EPA hand-off).  Overlapping pairs
-// are appended (warp-aggregated) to the colliding list with their MPR result and, when
-// deeper than the EPA threshold, the MPR portal EPA starts from.
+// are appended to the colliding list with their MPR result; deeper than the EPA threshold,
+// also to the EPA list with the MPR portal EPA starts from.
 __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
-    const int lane = threadIdx.x & 31;
     const int npairs = min(w.ctr->npairs, w.cap_pairs);
     const int cap = w.cap_arb;
     for (int base = blockIdx.x * blockDim.x; base < npairs; base += gridDim.x * blockDim.x) {
@@ -890,115 +1031,194 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
                 code = mpr_core<false>(sa, sb, q, pr_, 0.02f, pA, pB, n, pen, portal);
             }
         }
-        unsigned m = __ballot_sync(FULL, code != 0);
-        if (!m) continue;
-        int leader = __ffs(m) - 1;
-        int baseidx = 0;
-        if (lane == leader) baseidx = atomicAdd(&w.ctr->ncol, __popc(m));
-        baseidx = __shfl_sync(FULL, baseidx, leader);
-        if (code) {
-            int c = baseidx + __popc(m & ((1u << lane) - 1u));
-            if (c < cap) {
-                w.col_pair[c] = make_int2(p, code);
-                w.col_res[3 * c + 0] = f4(pA, 0.f);
-                w.col_res[3 * c + 1] = f4(pB, 0.f);
-                w.col_res[3 * c + 2] = f4(n, pen);
-                if (code == 2) {
-                    for (int k = 0; k < 4; k++) {
-                        w.col_portal[12 * c + 3 * k + 0] = f4(portal[k].V, 0.f);
-                        w.col_portal[12 * c + 3 * k + 1] = f4(portal[k].A, 0.f);
-                        w.col_portal[12 * c + 3 * k + 2] = f4(portal[k].B, 0.f);
-                    }
-                }
-            } else {
-                atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY);
+        int c = warp_append(&w.ctr->ncol, code != 0);
+        if (c >= cap) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); c = -1; }
+        if (c >= 0) {
+            w.col_pair[c] = make_int2(p, code);
+            w.col_res[3 * c + 0] = f4(pA, 0.f);
+            w.col_res[3 * c + 1] = f4(pB, 0.f);
+            w.col_res[3 * c + 2] = f4(n, pen);
+        }
+        int e = warp_append(&w.ctr->nepa_list, code == 2 && c >= 0);
+        if (e >= 0) {
+            w.epa_list[e] = c;
+            for (int k = 0; k < 4; k++) {
+                w.col_portal[12 * e + 3 * k + 0] = f4(portal[k].V, 0.f);
+                w.col_portal[12 * e + 3 * k + 1] = f4(portal[k].A, 0.f);
+                w.col_portal[12 * e + 3 * k + 2] = f4(portal[k].B, 0.f);
             }
         }
     }
 }
 
-// Stage 2, one warp per overlapping pair: EPA from the saved portal when needed, the
-// triangle-edge filter and the one-shot manifold; appends the contact stream record.
-__global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams sp) {
+// Stage 2, one warp per deep pair: EPA from the saved portal (NarrowPhase.cs:39-95); on
+// success the colliding record takes the EPA result, otherwise the MPR result stands.
+__global__ void __launch_bounds__(NP_WARPS * 32) k_epa(WorldDev w) {
     __shared__ EpaSmem smem[NP_WARPS];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     EpaSmem& E = smem[wib];
     NpStats st; st.exact = 0;
-    int epa_calls = 0, epa_fail = 0, written = 0, pts = 0;
-    int ncol = min(w.ctr->ncol, w.cap_arb);
-    for (int c = blockIdx.x * NP_WARPS + wib; c < ncol; c += gridDim.x * NP_WARPS) {
-        int2 cp = w.col_pair[c];
-        int2 pr = w.pairs[cp.x];
+    int epa_calls = 0, epa_fail = 0;
+    const int ne = min(w.ctr->nepa_list, w.cap_arb);
+    for (int e = blockIdx.x * NP_WARPS + wib; e < ne; e += gridDim.x * NP_WARPS) {
+        int c = w.epa_list[e];
+        int2 pr = w.pairs[w.col_pair[c].x];
+        ShapeRef sa = load_shape(w, pr.x), sb = load_shape(w, pr.y);
+        int b1 = w.sinfo[pr.x].y, b2 = w.sinfo[pr.y].y;
+        q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+        v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+        MV portal[4];
+        for (int k = 0; k < 4; k++) {
+            portal[k].V = mk3(w.col_portal[12 * e + 3 * k + 0]);
+            portal[k].A = mk3(w.col_portal[12 * e + 3 * k + 1]);
+            portal[k].B = mk3(w.col_portal[12 * e + 3 * k + 2]);
+        }
+        v3 pA = mk3(w.col_res[3 * c + 0]), pB = mk3(w.col_res[3 * c + 1]);
+        float4 nr = w.col_res[3 * c + 2];
+        v3 n = mk3(nr);
+        float pen = nr.w;
+        q4 q = qmul(qconj(qa), qb);
+        v3 prl = rotate_inv(pb - pa, qa);
+        run_epa(E, sa, sb, q, prl, portal, pA, pB, n, pen, st, epa_calls, epa_fail);
+        if (lane == 0) {
+            w.col_res[3 * c + 0] = f4(pA, 0.f);
+            w.col_res[3 * c + 1] = f4(pB, 0.f);
+            w.col_res[3 * c + 2] = f4(n, pen);
+        }
+    }
+    if (lane == 0) {
+        if (epa_calls) atomicAdd(&w.ctr->nepa, epa_calls);
+        if (epa_fail) atomicAdd(&w.ctr->epa_fail, epa_fail);
+    }
+    int ex = st.exact;
+    for (int off = 16; off > 0; off >>= 1) ex += __shfl_xor_sync(FULL, ex, off);
+    if (lane == 0 && ex) atomicAdd(&w.ctr->exact, ex);
+}
+
+__device__ __forceinline__ void write_stream(WorldDev& w, int idx, int s1, int s2, v3 n, int cnt, const float4* oA,
+                                             const float4* oB) {
+    if (idx >= w.cap_pairs) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); return; }
+    w.cs_key[idx] = make_int2(s1, s2);
+    w.cs_n[idx] = f4(n, __int_as_float(cnt));
+    for (int k = 0; k < cnt; k++) { w.cs_pa[4 * idx + k] = oA[k]; w.cs_pb[4 * idx + k] = oB[k]; }
+}
+
+// Stage 3, one thread per overlapping pair: world transform, the first test of the
+// triangle-edge filter (TriangleEdgeCollisionFilter.cs:183-240; pairs near a mesh edge
+// move to stage 4) and the one-shot manifold; appends the contact stream record.
+__global__ void __launch_bounds__(128) k_manifold(WorldDev w, StepParams sp) {
+    const int ncol = min(w.ctr->ncol, w.cap_arb);
+    int pts = 0;
+    for (int base = blockIdx.x * blockDim.x; base < ncol; base += gridDim.x * blockDim.x) {
+        int c = base + threadIdx.x;
+        bool emit = false, to_edge = false;
+        int s1 = 0, s2 = 0, cnt = 0;
+        v3 n = mk3(0.f);
+        float4 oA[4], oB[4];
+        if (c < ncol) {
+            int2 pr = w.pairs[w.col_pair[c].x];
+            s1 = pr.x; s2 = pr.y;
+            ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
+            int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
+            q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+            v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+            v3 pA = mk3(w.col_res[3 * c + 0]), pB = mk3(w.col_res[3 * c + 1]);
+            float4 nr = w.col_res[3 * c + 2];
+            n = mk3(nr);
+            float pen = nr.w;
+            pA = rotate(pA, qa); pA = pA + pa;
+            pB = rotate(pB, qa); pB = pB + pa;
+            n = rotate(n, qa);
+            emit = true;
+            bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
+            if (sp.edge_filter && c1 != c2) {
+                int4 i1 = w.binfo[b1], i2 = w.binfo[b2];
+                bool tri_dyn = c1 ? i1.x == JG_MOTION_DYNAMIC : i2.x == JG_MOTION_DYNAMIC;
+                if (!tri_dyn) {
+                    v3 tn, nn;
+                    int ev = edge_evaluate(w, c1 ? sa.tri : sb.tri, c1 ? qa : qb, c1 ? pa : pb, c2, c1 ? pA : pB, n, tn, nn);
+                    if (ev == DISCARD) emit = false;
+                    else if (ev == EDGE) { emit = false; to_edge = true; }
+                }
+            }
+            (void)pen;
+            if (emit) {
+                if (sp.aux_contacts) cnt = manifold_thread(sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
+                else { cnt = 1; oA[0] = f4(pA, 0.f); oB[0] = f4(pB, 0.f); }
+            }
+        }
+        int idx = warp_append(&w.ctr->nstream, emit);
+        if (idx >= 0) { write_stream(w, idx, s1, s2, n, cnt, oA, oB); pts += cnt; }
+        int ei = warp_append(&w.ctr->nedge, to_edge);
+        if (ei >= 0) w.edge_list[ei] = c;
+    }
+    for (int off = 16; off > 0; off >>= 1) pts += __shfl_xor_sync(FULL, pts, off);
+    if ((threadIdx.x & 31) == 0 && pts) atomicAdd(&w.ctr->points, pts);
+}
+
+// Stage 4, one warp per pair near a mesh edge: the rest of the triangle-edge filter
+// (rerun of MPR/EPA with threshold zero, normal snapping; TriangleEdgeCollisionFilter.cs:
+// 294-420) and the manifold.
+__global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams sp) {
+    __shared__ EpaSmem smem[NP_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    EpaSmem& E = smem[wib];
+    NpStats st; st.exact = 0;
+    int epa_calls = 0, epa_fail = 0, pts = 0;
+    const int ne = min(w.ctr->nedge, w.cap_arb);
+    for (int e = blockIdx.x * NP_WARPS + wib; e < ne; e += gridDim.x * NP_WARPS) {
+        int c = w.edge_list[e];
+        int2 pr = w.pairs[w.col_pair[c].x];
         int s1 = pr.x, s2 = pr.y;
         ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
         int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
-        int4 i1 = w.binfo[b1], i2 = w.binfo[b2];
         q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
         v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
         v3 pA = mk3(w.col_res[3 * c + 0]), pB = mk3(w.col_res[3 * c + 1]);
         float4 nr = w.col_res[3 * c + 2];
         v3 n = mk3(nr);
         float pen = nr.w;
-        if (cp.y == 2) {
-            MV portal[4];
-            for (int k = 0; k < 4; k++) {
-                portal[k].V = mk3(w.col_portal[12 * c + 3 * k + 0]);
-                portal[k].A = mk3(w.col_portal[12 * c + 3 * k + 1]);
-                portal[k].B = mk3(w.col_portal[12 * c + 3 * k + 2]);
-            }
-            q4 q = qmul(qconj(qa), qb);
-            v3 prl = rotate_inv(pb - pa, qa);
-            run_epa(E, sa, sb, q, prl, portal, pA, pB, n, pen, st, epa_calls, epa_fail);
-        }
-        // back to world space (NarrowPhase.cs:920-924)
         pA = rotate(pA, qa); pA = pA + pa;
         pB = rotate(pB, qa); pB = pB + pa;
         n = rotate(n, qa);
-        if (sp.edge_filter) {
-            bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
-            bool tri_dyn = c1 ? i1.x == JG_MOTION_DYNAMIC : i2.x == JG_MOTION_DYNAMIC;
-            if (c1 != c2 && !tri_dyn) {
-                int tri = c1 ? sa.tri : sb.tri;
-                q4 tq = c1 ? qa : qb;
-                v3 tp = c1 ? pa : pb;
-                v3 tn, nn;
-                int ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
-                if (ev == DISCARD) continue;
-                if (ev == EDGE) {
-                    bool spec = pen < 0.0f;
-                    bool keep = true, done = false;
-                    if (!spec) {
-                        bool res = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, n, pen, 0.0f, st, epa_calls, epa_fail);
-                        if (!res) keep = false;
-                        else {
-                            ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
-                            if (ev == DISCARD) keep = false;
-                            else if (ev == KEEP) done = true;
-                        }
-                    }
-                    if (!keep) continue;
-                    if (!done) {
-                        v3 mid = 0.5f * (pA + pB);
-                        if (dot(tn, nn) > 0.999f) {
-                            float f5 = dot(n, nn), f6 = dot(n, tn);
-                            if (!spec) { pen = 0; pA = pB = mid; }
-                            n = f5 > f6 ? nn : tn;
-                        } else {
-                            v3 cr = cross(nn, tn);
-                            float crl = len2(cr);
-                            v3 proj = n - (dot(cr, n) / crl) * cr;
-                            if (len2(proj) < 0.5f * 0.5f) continue;
-                            float f1 = dot(cross(proj, nn), cr);
-                            float f2 = dot(cross(proj, tn), cr);
-                            bool between = f1 <= 0.0f && f2 >= 0.0f;
-                            if (!between) {
-                                float f3 = dot(n, nn), f4v = dot(n, tn);
-                                if (!spec) { pen = 0; pA = pB = mid; }
-                                n = f3 > f4v ? nn : tn;
-                            }
-                        }
-                    }
+        bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
+        int tri = c1 ? sa.tri : sb.tri;
+        q4 tq = c1 ? qa : qb;
+        v3 tp = c1 ? pa : pb;
+        v3 tn, nn;
+        int ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
+        bool spec = pen < 0.0f;
+        bool keep = true, done = false;
+        if (!spec) {
+            bool res = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, n, pen, 0.0f, st, epa_calls, epa_fail);
+            if (!res) keep = false;
+            else {
+                ev = edge_evaluate(w, tri, tq, tp, c2, c1 ? pA : pB, n, tn, nn);
+                if (ev == DISCARD) keep = false;
+                else if (ev == KEEP) done = true;
+            }
+        }
+        if (!keep) continue;
+        if (!done) {
+            v3 mid = 0.5f * (pA + pB);
+            if (dot(tn, nn) > 0.999f) {
+                float f5 = dot(n, nn), f6 = dot(n, tn);
+                if (!spec) { pen = 0; pA = pB = mid; }
+                n = f5 > f6 ? nn : tn;
+            } else {
+                v3 cr = cross(nn, tn);
+                float crl = len2(cr);
+                v3 proj = n - (dot(cr, n) / crl) * cr;
+                if (len2(proj) < 0.5f * 0.5f) continue;
+                float f1 = dot(cross(proj, nn), cr);
+                float f2 = dot(cross(proj, tn), cr);
+                bool between = f1 <= 0.0f && f2 >= 0.0f;
+                if (!between) {
+                    float f3 = dot(n, nn), f4v = dot(n, tn);
+                    if (!spec) { pen = 0; pA = pB = mid; }
+                    n = f3 > f4v ? nn : tn;
                 }
             }
         }
@@ -1008,18 +1228,10 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams
         else { cnt = 1; oA[0] = pA; oB[0] = pB; }
         if (lane == 0) {
             int idx = atomicAdd(&w.ctr->nstream, 1);
-            if (idx < w.cap_pairs) {
-                w.cs_key[idx] = make_int2(s1, s2);
-                w.cs_n[idx] = f4(n, __int_as_float(cnt));
-                for (int k = 0; k < cnt; k++) {
-                    w.cs_pa[4 * idx + k] = f4(oA[k], 0.f);
-                    w.cs_pb[4 * idx + k] = f4(oB[k], 0.f);
-                }
-            } else {
-                atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY);
-            }
+            float4 fa[4], fb[4];
+            for (int k = 0; k < cnt; k++) { fa[k] = f4(oA[k], 0.f); fb[k] = f4(oB[k], 0.f); }
+            write_stream(w, idx, s1, s2, n, cnt, fa, fb);
         }
-        written++;
         pts += cnt;
     }
     if (lane == 0) {
@@ -1030,7 +1242,6 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams
     int ex = st.exact;
     for (int off = 16; off > 0; off >>= 1) ex += __shfl_xor_sync(FULL, ex, off);
     if (lane == 0 && ex) atomicAdd(&w.ctr->exact, ex);
-    (void)written;
 }
 
 }  // namespace
@@ -1038,6 +1249,7 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_narrow(WorldDev w, StepParams
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
     (void)tile;
     k_mpr<<<nsm * 8, 256, 0, s>>>(w);
-    int blocks = nsm * 8;
-    k_narrow<<<blocks, NP_WARPS * 32, 0, s>>>(w, p);
+    k_epa<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w);
+    k_manifold<<<nsm * 16, 128, 0, s>>>(w, p);
+    k_edge<<<nsm * 2, NP_WARPS * 32, 0, s>>>(w, p);
 }

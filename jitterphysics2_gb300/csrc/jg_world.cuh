@@ -79,6 +79,8 @@ struct DevCounters {
     int new_contacts;
     int color_rounds;
     int ncol;         // overlapping pairs found by the MPR stage
+    int nepa_list;    // of those, deeper than the EPA threshold
+    int nedge;        // of those, near a mesh edge (triangle-edge filter)
     int pad;
 };
 
@@ -110,7 +112,9 @@ struct WorldDev {
     // narrowphase: overlapping pairs from the MPR stage, then the contact stream
     int2* col_pair;              // [cap_arb] pair index, MPR code (1 final, 2 needs EPA)
     float4* col_res;             // [3 * cap_arb] MPR result in A's frame: pA, pB, normal|depth
-    float4* col_portal;          // [12 * cap_arb] MPR portal (4 vertices: V, A, B)
+    float4* col_portal;          // [12 * cap_arb] MPR portal (4 vertices: V, A, B), by EPA-list slot
+    int* epa_list;               // [cap_arb] colliding-record index of each deep pair
+    int* edge_list;              // [cap_arb] colliding-record index of each pair near a mesh edge
     int2* cs_key;
     float4* cs_n;                // normal xyz, count
     float4* cs_pa;               // [4 * cap_pairs]

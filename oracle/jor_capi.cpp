@@ -95,6 +95,15 @@ template <class R> void get_bodies(const World<R>& w, jg_body_desc* d, int n) {
         s.delta_angular_velocity[0] = (float)b.dangvel.x; s.delta_angular_velocity[1] = (float)b.dangvel.y; s.delta_angular_velocity[2] = (float)b.dangvel.z;
         s.motion_type = b.motion;
         s.world = b.world;
+        const Sym3<R>& L = b.inv_inertia_local;
+        s.inv_inertia[0] = (float)L.m11; s.inv_inertia[1] = (float)L.m12; s.inv_inertia[2] = (float)L.m13;
+        s.inv_inertia[3] = (float)L.m22; s.inv_inertia[4] = (float)L.m23; s.inv_inertia[5] = (float)L.m33;
+        s.inv_mass = (float)b.inv_mass;
+        s.friction = (float)b.friction; s.restitution = (float)b.restitution;
+        s.linear_damping = (float)b.lin_damp; s.angular_damping = (float)b.ang_damp;
+        s.force[0] = (float)b.force.x; s.force[1] = (float)b.force.y; s.force[2] = (float)b.force.z;
+        s.torque[0] = (float)b.torque.x; s.torque[1] = (float)b.torque.y; s.torque[2] = (float)b.torque.z;
+        s.flags = b.flags | (b.gravity ? 0 : JG_BODY_NO_GRAVITY);
     }
 }
 
