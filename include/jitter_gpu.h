@@ -222,6 +222,14 @@ int jg_step_host(jg_world* world, float dt, jg_body_desc* bodies, int32_t count)
 
 /* ---- inspection ------------------------------------------------------------------------ */
 
+/* Batched NarrowPhase.MprEpa (NarrowPhase.cs:902-927) on the world's shapes at the
+ * bodies' current poses: shape_pairs holds 2*count shape indices; results receives 10
+ * floats per pair (pointA xyz, pointB xyz, normal xyz, penetration, world frame, the
+ * reference's out parameters) and hits the method's return value (1 colliding, 0 not).
+ * Host buffers; synchronous.  Device scratch grows on demand with the largest count. */
+int jg_collide_pairs(jg_world* world, const int32_t* shape_pairs, int32_t count,
+                     float* results, int32_t* hits);
+
 /* Arbiter/ContactData view (World.RawData, World.cs:95-141).  Writes up to capacity
  * entries; *out_count receives the number of active contact points. */
 int jg_get_contacts(jg_world* world, jg_contact_view* out, int32_t capacity, int32_t* out_count);

@@ -97,6 +97,7 @@ SIGNATURES = {
     "jg_add_constraint": (_I, [_P, _I, _I, _I, _P, _PI]),
     "jg_step": (_I, [_P, _F]),
     "jg_step_host": (_I, [_P, _F, _P, _I]),
+    "jg_collide_pairs": (_I, [_P, _P, _I, _P, _P]),
     "jg_get_contacts": (_I, [_P, _P, _I, _PI]),
     "jg_get_arbiter_events": (_I, [_P, _P, _I, _PI, _P, _I, _PI]),
     "jg_get_counters": (_I, [_P, _P]),

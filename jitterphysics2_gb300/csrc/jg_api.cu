@@ -18,6 +18,8 @@ void jg_launch_update_contacts(WorldDev& w, cudaStream_t s, int nsm);
 void jg_solver_reset_launch_cache();
 int jg_mlp_alloc(WorldDev& w);
 int jg_mlp_launch_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
+                             cudaStream_t s, int nsm);
 
 static thread_local std::string g_err;
 
@@ -42,6 +44,11 @@ struct jg_world {
     std::vector<void*> allocs;
     bool mlp_ready = false;
     int launches = 0;
+    // jg_collide_pairs scratch, grown on demand: pairs, 10 floats and a hit flag per pair
+    int2* q_pairs = nullptr;
+    float* q_out = nullptr;
+    int* q_hit = nullptr;
+    int q_cap = 0;
 };
 
 namespace {
@@ -317,6 +324,7 @@ int jg_destroy(jg_world* w) {
     for (int i = 0; i < 2; i++) if (w->graph[i]) cudaGraphExecDestroy(w->graph[i]);
     if (w->stream) cudaStreamSynchronize(w->stream);
     for (void* p : w->allocs) cudaFree(p);
+    cudaFree(w->q_pairs); cudaFree(w->q_out); cudaFree(w->q_hit);
     if (w->h_ctr) cudaFreeHost(w->h_ctr);
     for (int i = 0; i < 9; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -605,6 +613,47 @@ int jg_get_residuals(jg_world* w, float* out, int32_t cap, int32_t* n) {
     *n = k;
     for (int i = 0; i < k && i < cap; i++) out[i] = (float)(std::sqrt((double)h[2 * i]) / std::max(std::sqrt((double)h[2 * i + 1]), 1e-12));
     return JG_OK;
+}
+
+static int check_query_args(const char* fn, jg_world* w, const int32_t* pairs, int32_t n, float* out, int32_t* hit) {
+    if (!w || n < 0 || (n > 0 && (!pairs || !out || !hit))) {
+        g_err = std::string(fn) + ": null buffer or negative count";
+        return JG_ERR_INVALID_ARG;
+    }
+    for (int32_t i = 0; i < 2 * n; i++)
+        if (pairs[i] < 0 || pairs[i] >= w->d.ns) {
+            g_err = std::string(fn) + ": shape index " + std::to_string(pairs[i]) + " out of range";
+            return JG_ERR_INVALID_ARG;
+        }
+    return JG_OK;
+}
+
+// Pairs in, results out through the world's stream; synchronous.
+static int run_query(jg_world* w, const int32_t* pairs, int32_t n, float* out, int32_t* hit, int2* d_pairs,
+                     float* d_out, int* d_hit) {
+    cudaStream_t s = w->stream;
+    CK(cudaMemcpyAsync(d_pairs, pairs, sizeof(int2) * n, cudaMemcpyHostToDevice, s));
+    jg_launch_collide_query(w->d, d_pairs, n, 0.02f, d_out, d_hit, s, w->nsm);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d_out, sizeof(float) * 10 * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hit, d_hit, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return JG_OK;
+}
+
+int jg_collide_pairs(jg_world* w, const int32_t* pairs, int32_t n, float* out, int32_t* hit) {
+    int r = check_query_args("jg_collide_pairs", w, pairs, n, out, hit);
+    if (r || n == 0) return r;
+    if (n > w->q_cap) {
+        CK(cudaStreamSynchronize(w->stream));
+        cudaFree(w->q_pairs); cudaFree(w->q_out); cudaFree(w->q_hit);
+        w->q_pairs = nullptr; w->q_out = nullptr; w->q_hit = nullptr; w->q_cap = 0;
+        CK(cudaMalloc((void**)&w->q_pairs, sizeof(int2) * n));
+        CK(cudaMalloc((void**)&w->q_out, sizeof(float) * 10 * n));
+        CK(cudaMalloc((void**)&w->q_hit, sizeof(int) * n));
+        w->q_cap = n;
+    }
+    return run_query(w, pairs, n, out, hit, w->q_pairs, w->q_out, w->q_hit);
 }
 
 int jg_get_contacts(jg_world* w, jg_contact_view* out, int32_t cap, int32_t* count) {

@@ -1244,7 +1244,47 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
     if (lane == 0 && ex) atomicAdd(&w.ctr->exact, ex);
 }
 
+// Batched NarrowPhase.MprEpa query (NarrowPhase.cs:902-927), one warp per shape pair, on
+// the world's shapes and body poses.  out holds 10 floats per pair (pointA, pointB,
+// normal, penetration, world frame) and hit the method's return value; every slot is
+// written, so neither buffer needs clearing.
+__global__ void __launch_bounds__(NP_WARPS * 32) k_collide_query(WorldDev w, const int2* pairs, int n, float threshold,
+                                                                 float* out, int* hit) {
+    __shared__ EpaSmem smem[NP_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    EpaSmem& E = smem[wib];
+    NpStats st; st.exact = 0;
+    int ec = 0, ef = 0;
+    for (int i = blockIdx.x * NP_WARPS + wib; i < n; i += gridDim.x * NP_WARPS) {
+        int2 pr = pairs[i];
+        ShapeRef sa = load_shape(w, pr.x), sb = load_shape(w, pr.y);
+        int b1 = w.sinfo[pr.x].y, b2 = w.sinfo[pr.y].y;
+        q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+        v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+        v3 pA = mk3(0.f), pB = mk3(0.f), nn = mk3(0.f);
+        float pen = 0.f;
+        bool h = mpr_epa_world(E, sa, sb, qa, qb, pa, pb, pA, pB, nn, pen, threshold, st, ec, ef);
+        if (lane == 0) {
+            float* o = out + 10 * (size_t)i;
+            o[0] = pA.x; o[1] = pA.y; o[2] = pA.z;
+            o[3] = pB.x; o[4] = pB.y; o[5] = pB.z;
+            o[6] = nn.x; o[7] = nn.y; o[8] = nn.z;
+            o[9] = pen;
+            hit[i] = h ? 1 : 0;
+        }
+    }
+}
+
 }  // namespace
+
+void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
+                             cudaStream_t s, int nsm) {
+    if (n <= 0) return;
+    int blocks = (n + NP_WARPS - 1) / NP_WARPS;
+    if (blocks > nsm * 4) blocks = nsm * 4;
+    k_collide_query<<<blocks, NP_WARPS * 32, 0, s>>>(w, pairs, n, threshold, out, hit);
+}
 
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
     (void)tile;

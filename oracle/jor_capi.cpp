@@ -284,6 +284,17 @@ template <class R> struct Handle {
         out[28] = (double)r.pen; put3d(out + 29, r.pA); put3d(out + 32, r.pB);                                     \
         return 1;                                                                                                  \
     }                                                                                                              \
+    /* NarrowPhase.MprEpa (NarrowPhase.cs:902-927) on two shapes of the world at their     \
+       bodies' poses: out = pA, pB, n, pen */                                                                      \
+    extern "C" int jor_world_collide_##SUF(void* h, int s1, int s2, double* out) {                                \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        const Body<R>& b1 = w.bodies[w.shape_body[s1]];                                                            \
+        const Body<R>& b2 = w.bodies[w.shape_body[s2]];                                                            \
+        MprEpa<R> sol; V3<R> pA, pB, n; R pen = 0;                                                                 \
+        bool hit = sol.mpr_epa_world(w.shapes[s1], w.shapes[s2], b1.q, b2.q, b1.pos, b2.pos, pA, pB, n, pen);      \
+        put3d(out, pA); put3d(out + 3, pB); put3d(out + 6, n); out[9] = (double)pen;                              \
+        return hit ? 1 : 0;                                                                                        \
+    }                                                                                                              \
     extern "C" void jor_support_##SUF(const jg_shape_desc* d, const float* verts, const double* dir, double* out) { \
         Shape<R> s; std::vector<R> st; desc_to_shape<R>(d, verts, s, st);                                          \
         put3d(out, support(s, get3d<R>(dir)));                                                                     \

@@ -44,6 +44,7 @@ def load():
             "jor_world_step": (None, [P, F, I]), "jor_world_step_mt": (D, [P, F, I]),
             "jor_world_counters": (None, [P, P]), "jor_world_pairs": (I, [P, P, I]),
             "jor_world_residuals": (I, [P, P, I]), "jor_world_detect": (I, [P, I, I, P]),
+            "jor_world_collide": (I, [P, I, I, P]),
             "jor_support": (None, [P, P, P, P]), "jor_aabb": (None, [P, P, P, P, P]),
             "jor_collide": (I, [P, P, P, P, P, P, P, P, D, I, P]),
             "jor_manifold": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
@@ -235,6 +236,12 @@ class OracleWorld:
         out = np.zeros(64, np.float32)
         n = self.fn("jor_world_residuals")(self.h, p(out), 64)
         return out[:n].copy()
+
+    def collide(self, s1, s2):
+        """NarrowPhase.MprEpa on two of the world's shapes: (hit, pA, pB, n, pen)."""
+        out = np.zeros(10, np.float64)
+        hit = self.fn("jor_world_collide")(self.h, s1, s2, p(out))
+        return bool(hit), out[0:3], out[3:6], out[6:9], out[9]
 
     def detect(self, s1, s2):
         out = np.zeros(40, np.float64)
