@@ -230,6 +230,23 @@ int jg_step_host(jg_world* world, float dt, jg_body_desc* bodies, int32_t count)
 int jg_collide_pairs(jg_world* world, const int32_t* shape_pairs, int32_t count,
                      float* results, int32_t* hits);
 
+/* No counterpart in the reference.  jg_collide_pairs without any allocation in the call:
+ * its device scratch is a fixed array of JG_COLLIDE_NOALLOC_MAX_PAIRS pairs (52 B per
+ * pair, 832 KiB per device) built into the library, instead of buffers that
+ * jg_collide_pairs grows with cudaMalloc.  For hosts that may not allocate device memory
+ * once running: a frame loop under a fixed memory budget, or a thread that must not take
+ * cudaMalloc's implicit device-wide synchronisation while other streams work.  Same
+ * arguments, results and errors as jg_collide_pairs, plus JG_ERR_CAPACITY when count
+ * exceeds JG_COLLIDE_NOALLOC_MAX_PAIRS (split the batch).  Every world of a device shares
+ * the one scratch array: calls that overlap on the GPU (from several host threads) race
+ * on it, so the caller serialises them.  Nothing in the scratch has to start at zero; the
+ * kernel writes every slot of the batch.  The first call on a device looks up the
+ * array's address (which loads the library's device code there): make it before any
+ * stream capture.  The current device must be the world's. */
+#define JG_COLLIDE_NOALLOC_MAX_PAIRS 16384
+int jg_collide_pairs_noalloc(jg_world* world, const int32_t* shape_pairs, int32_t count,
+                             float* results, int32_t* hits);
+
 /* Arbiter/ContactData view (World.RawData, World.cs:95-141).  Writes up to capacity
  * entries; *out_count receives the number of active contact points. */
 int jg_get_contacts(jg_world* world, jg_contact_view* out, int32_t capacity, int32_t* out_count);

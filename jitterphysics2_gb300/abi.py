@@ -27,6 +27,7 @@ BODY_ACTIVE = 1 << 2
 BODY_GYROSCOPIC = 1 << 3
 BODY_LOCKS_SHIFT = 4
 BODY_NO_GRAVITY = 1 << 12
+COLLIDE_NOALLOC_MAX_PAIRS = 16384  # JG_COLLIDE_NOALLOC_MAX_PAIRS
 WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
 CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE = 1, 2
 
@@ -98,6 +99,7 @@ SIGNATURES = {
     "jg_step": (_I, [_P, _F]),
     "jg_step_host": (_I, [_P, _F, _P, _I]),
     "jg_collide_pairs": (_I, [_P, _P, _I, _P, _P]),
+    "jg_collide_pairs_noalloc": (_I, [_P, _P, _I, _P, _P]),
     "jg_get_contacts": (_I, [_P, _P, _I, _PI]),
     "jg_get_arbiter_events": (_I, [_P, _P, _I, _PI, _P, _I, _PI]),
     "jg_get_counters": (_I, [_P, _P]),

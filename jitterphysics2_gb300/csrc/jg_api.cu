@@ -10,6 +10,7 @@
 #include <string>
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 
 void jg_contacts_set_scratch(int2* created, int2* removed, int* remaining, int* dst_index);
 void jg_flip_store(WorldDev& w);
@@ -654,6 +655,51 @@ int jg_collide_pairs(jg_world* w, const int32_t* pairs, int32_t n, float* out, i
         w->q_cap = n;
     }
     return run_query(w, pairs, n, out, hit, w->q_pairs, w->q_out, w->q_hit);
+}
+
+// jg_collide_pairs_noalloc: the same query with its scratch in a fixed device array of
+// JG_COLLIDE_NOALLOC_MAX_PAIRS pairs instead of buffers grown with cudaMalloc.  Layout:
+// pairs (int2), results (10 floats), hit flags (int), each region 256-byte aligned.  The
+// kernel writes every result and hit slot of the batch, so nothing in the array has to
+// start at zero.  The array is shared by every world of a device: calls that overlap on
+// the GPU race on it.
+namespace {
+constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kNaPairs = 0;
+constexpr size_t kNaOut = kNaPairs + align256(sizeof(int2) * JG_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaHit = kNaOut + align256(sizeof(float) * 10 * JG_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaBytes = kNaHit + align256(sizeof(int) * JG_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr int kNaMaxDevices = 64;
+}  // namespace
+static __device__ __align__(256) unsigned char g_collide_scratch[kNaBytes];
+static std::mutex g_collide_scratch_mu;
+static void* g_collide_scratch_addr[kNaMaxDevices];  // per device, looked up on first use
+
+int jg_collide_pairs_noalloc(jg_world* w, const int32_t* pairs, int32_t n, float* out, int32_t* hit) {
+    int r = check_query_args("jg_collide_pairs_noalloc", w, pairs, n, out, hit);
+    if (r || n == 0) return r;
+    if (n > JG_COLLIDE_NOALLOC_MAX_PAIRS) {
+        g_err = "jg_collide_pairs_noalloc: " + std::to_string(n) + " pairs exceed the fixed scratch of " +
+                std::to_string(JG_COLLIDE_NOALLOC_MAX_PAIRS) + "; split the batch or call jg_collide_pairs";
+        return JG_ERR_CAPACITY;
+    }
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev != w->device || dev < 0 || dev >= kNaMaxDevices) {
+        g_err = "jg_collide_pairs_noalloc: the current device is not the world's device (or above 63)";
+        return JG_ERR_INVALID_ARG;
+    }
+    unsigned char* base;
+    {
+        std::lock_guard<std::mutex> lock(g_collide_scratch_mu);
+        if (!g_collide_scratch_addr[dev]) {
+            void* p = nullptr;
+            CK(cudaGetSymbolAddress(&p, g_collide_scratch));
+            g_collide_scratch_addr[dev] = p;
+        }
+        base = (unsigned char*)g_collide_scratch_addr[dev];
+    }
+    return run_query(w, pairs, n, out, hit, (int2*)(base + kNaPairs), (float*)(base + kNaOut), (int*)(base + kNaHit));
 }
 
 int jg_get_contacts(jg_world* w, jg_contact_view* out, int32_t cap, int32_t* count) {

@@ -114,14 +114,17 @@ class World:
         check(self._lib.jg_download_bodies(self._h, ptr(out), self.n_bodies), "jg_download_bodies")
         return out
 
-    def collide_pairs(self, pairs):
+    def collide_pairs(self, pairs, noalloc=False):
         """Batched NarrowPhase.MprEpa on shape-index pairs at the current poses.
-        Returns (hit[n] bool, pointA[n,3], pointB[n,3], normal[n,3], penetration[n])."""
+        Returns (hit[n] bool, pointA[n,3], pointB[n,3], normal[n,3], penetration[n]).
+        noalloc=True calls jg_collide_pairs_noalloc (fixed device scratch, at most
+        abi.COLLIDE_NOALLOC_MAX_PAIRS pairs per call)."""
         pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
         n = len(pr)
         out = np.zeros((max(n, 1), 10), np.float32)
         hit = np.zeros(max(n, 1), np.int32)
-        check(self._lib.jg_collide_pairs(self._h, ptr(pr), n, ptr(out), ptr(hit)), "jg_collide_pairs")
+        name = "jg_collide_pairs_noalloc" if noalloc else "jg_collide_pairs"
+        check(getattr(self._lib, name)(self._h, ptr(pr), n, ptr(out), ptr(hit)), name)
         return hit[:n] != 0, out[:n, 0:3], out[:n, 3:6], out[:n, 6:9], out[:n, 9]
 
     def contacts(self):
