@@ -87,6 +87,7 @@ typedef struct jg_world_params {
     int32_t use_graph;                  /* capture the step in a CUDA graph             */
     int32_t record_residual;            /* record the per-iteration residual (metric)   */
     int32_t deterministic;              /* sort new arbiters by key every step          */
+    int32_t partitioned_solve;          /* 1 (default): spatial tasks in shared memory   */
 } jg_world_params;
 
 /* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the
@@ -166,6 +167,9 @@ typedef struct jg_counters {
     int64_t created_arbiters;
     int64_t removed_arbiters;
     int64_t kernel_launches;            /* device kernels launched by the last step       */
+    int64_t solver_tasks;               /* partitioned solve: tasks (cells) of the step   */
+    int64_t task_arbiters;              /* arbiters solved in tasks (rest: global colours) */
+    int64_t task_colors;                /* most local colours of one task                 */
 } jg_counters;
 
 /* Stage timings in milliseconds (World.DebugTimings buckets, World.Step.cs:44-81). */

@@ -46,6 +46,7 @@ PARAMS_FIELDS = [
     ("max_constraints", ctypes.c_int32), ("solver_block", ctypes.c_int32), ("solver_ctas_per_sm", ctypes.c_int32),
     ("narrow_tile", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_residual", ctypes.c_int32),
     ("deterministic", ctypes.c_int32),
+    ("partitioned_solve", ctypes.c_int32),
 ]
 
 
@@ -76,7 +77,7 @@ CONTACT_DTYPE = np.dtype([
 ])
 COUNTER_NAMES = ["pairs", "colliding", "manifold_points", "arbiters", "contacts", "new_contacts", "colors",
                  "epa_calls", "epa_failures", "exact_fallbacks", "status", "created_arbiters", "removed_arbiters",
-                 "kernel_launches"]
+                 "kernel_launches", "solver_tasks", "task_arbiters", "task_colors"]
 TIMING_NAMES = ["broadphase", "narrowphase", "add_arbiter", "coloring", "solve", "update_contacts",
                 "update_bodies", "total"]
 

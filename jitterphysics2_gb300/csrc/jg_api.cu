@@ -21,6 +21,7 @@ int jg_mlp_alloc(WorldDev& w);
 int jg_mlp_launch_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
                              cudaStream_t s, int nsm);
+int jg_schedule_launches(const StepParams& p);
 
 static thread_local std::string g_err;
 
@@ -72,6 +73,7 @@ template <class T> int dalloc(jg_world* w, T** p, size_t count) {
 
 int alloc_store(jg_world* w, ArbStore& A, int cap) {
     DA(A.key, cap); DA(A.body, cap); DA(A.info, cap); DA(A.mat, cap);
+    DA(A.lslot, cap); DA(A.sv, 2 * (size_t)cap);
     DA(A.cn, 4 * cap); DA(A.ct1, 4 * cap); DA(A.ct2, 4 * cap); DA(A.cr1, 4 * cap);
     DA(A.cr2, 4 * cap); DA(A.cacc, 4 * cap); DA(A.cp1, 4 * cap); DA(A.cp2, 4 * cap);
     return JG_OK;
@@ -122,6 +124,15 @@ int allocate(jg_world* w) {
     DA(d.bar_count, 2); d.bar_gen = d.bar_count + 1;
     DA(d.resid, 2 * 64);
     DA(d.ctr, 1);
+    // partitioned solve schedule
+    DA(d.sc, 1);
+    DA(d.sc_cell, 3 * (size_t)d.cap_bodies); DA(d.sc_stamp, 3 * (size_t)d.cap_bodies);
+    DA(d.sc_bslot, 3 * (size_t)d.cap_bodies); DA(d.sc_tbody, 3 * (size_t)d.cap_bodies);
+    DA(d.sc_arb, d.cap_arb); DA(d.sc_tlist, d.cap_arb); DA(d.sc_dst, d.cap_arb); DA(d.sc_lcol, d.cap_arb);
+    DA(d.sc_ls, d.cap_arb);
+    DA(d.sc_acount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_bcount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_task_of, 3 * JG_SCHED_MAXCELLS);
+    DA(d.sc_task, JG_SCHED_MAXTASKS); DA(d.sc_cursor, JG_SCHED_MAXTASKS); DA(d.sc_tnc, JG_SCHED_MAXTASKS);
+    DA(d.sc_tcol, (size_t)JG_SCHED_MAXTASKS * (JG_TASK_MAXC + 1));
     DA(w->ev_created, d.cap_arb); DA(w->ev_removed, d.cap_arb); DA(w->remaining, 2); DA(w->dst_index, d.cap_arb);
     CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));
     memset(w->h_ctr, 0, sizeof(DevCounters));
@@ -197,6 +208,10 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.spec_relax = p.speculative_relaxation;
     sp.warm_start = p.warm_start_mode;
     sp.record_residual = p.record_residual;
+    sp.partition = p.partitioned_solve ? 1 : 0;
+    sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : 64,
+                                       p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : 2);
+    if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
     return sp;
 }
 
@@ -214,13 +229,14 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     // narrowphase 4, merge 3 (+1 learned warm start), colour/permute 4, count 1, solve 1,
     // contact update 1, body update 1
     w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 4 + 3 + 4 + 1 + 1 + 1 + 1 +
-                  ((sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) ? 1 : 0);
+                  ((sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) ? 1 : 0) + jg_schedule_launches(sp);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);
     jg_launch_merge(d, sp, s, w->nsm);
     if (sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) jg_mlp_launch_warmstart(d, sp, s, w->nsm);
     if (timed) cudaEventRecord(w->ev[3], s);
+    jg_launch_schedule(d, sp, s, w->nsm);
     jg_launch_color(d, s, w->nsm);
     jg_flip_store(d);
     if (timed) cudaEventRecord(w->ev[4], s);
@@ -248,6 +264,7 @@ int finish_step(jg_world* w, bool timed) {
     o.epa_failures = c.epa_fail; o.exact_fallbacks = c.exact; o.status = c.status;
     o.created_arbiters = c.nnew; o.removed_arbiters = c.nremoved;
     o.kernel_launches = w->launches;
+    o.solver_tasks = c.ntasks; o.task_arbiters = c.narb_task; o.task_colors = c.task_colors;
     if (timed) {
         float t[8];
         for (int i = 0; i < 7; i++) cudaEventElapsedTime(&t[i], w->ev[i], w->ev[i + 1]);
@@ -283,6 +300,7 @@ int jg_default_params(jg_world_params* p) {
     p->edge_filter = 1;
     p->warm_start_mode = JG_WARMSTART_CACHED;
     p->narrow_tile = 32;
+    p->partitioned_solve = 1;
     return JG_OK;
 }
 
@@ -839,13 +857,20 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     if (r) return r;
     std::vector<char> snap(size);
     if ((r = jg_export_state(w, snap.data(), size, &size))) return r;
-    const int blocks[] = {128, 256, 512};
-    const int ctas[] = {1, 2, 4};
+    // partitioned solve: threads per task CTA (one CTA per SM, shared memory bound);
+    // global-colour solve: threads per CTA x CTAs per SM
+    const bool part = w->prm.partitioned_solve != 0;
+    const int pblocks[] = {64, 96, 128}, gblocks[] = {128, 256, 512};
+    const int pctas[] = {1, 2}, gctas[] = {1, 2, 4};
+    const int* blocks = part ? pblocks : gblocks;
+    const int* ctas = part ? pctas : gctas;
+    const int nbk = 3, nct = part ? 2 : 3;
     float best = 1e30f;
-    int bb = 256, bc = 2;
+    int bb = part ? 64 : 256, bc = 2;
     jg_world_params saved = w->prm;
-    for (int b : blocks)
-        for (int c : ctas) {
+    for (int ib = 0; ib < nbk; ib++)
+        for (int ic = 0; ic < nct; ic++) {
+            const int b = blocks[ib], c = ctas[ic];
             w->prm.solver_block = b;
             w->prm.solver_ctas_per_sm = c;
             w->prm.use_graph = 0;

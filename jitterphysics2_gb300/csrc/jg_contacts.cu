@@ -225,8 +225,10 @@ __global__ void k_color(WorldDev w, int* remaining) {
     for (int c = tid; c < JG_MAX_COLORS + 1; c += nth) { w.color_count[c] = 0; w.color_cursor[c] = 0; }
     if (tid < 2) remaining[tid] = 0;
     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
+    const bool tasks = w.sc->ntasks > 0;
     for (int c = tid; c < ncons; c += nth) {
         if (c < narb && (A.info[c].x & 15) == 0) { w.cstat[c] = -2; continue; }
+        if (c < narb && tasks && w.sc_dst[c] >= 0) { w.cstat[c] = -4; continue; }  // solved in a task
         int b1, b2; unsigned long long key;
         cons_bodies(w, A, c, narb, b1, b2, key);
         w.cstat[c] = -1;
@@ -277,7 +279,7 @@ __global__ void k_color(WorldDev w, int* remaining) {
     }
     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
     for (int c = tid; c < ncons; c += nth) {
-        if (w.cstat[c] == -2) continue;
+        if (w.cstat[c] < -1) continue;
         int b1, b2; unsigned long long key;
         cons_bodies(w, A, c, narb, b1, b2, key);
         if (b1 >= 0) { int s = atomicAdd(&w.deg[b1], 1); w.adj[w.adj_off[b1] + s] = c; }
@@ -342,7 +344,7 @@ __global__ void k_color(WorldDev w, int* remaining) {
     }
     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int acc = 0, jacc = 0, nc = 0;
+        int acc = tasks ? w.sc->narb_task : 0, jacc = 0, nc = 0;  // the remainder follows the tasks
         for (int c = 0; c < JG_MAX_COLORS; c++) {
             int t = w.color_count[c], jt = w.color_cursor[c];
             if (t || jt) nc = c + 1;
@@ -365,19 +367,34 @@ __global__ void k_permute(WorldDev w, int2* ev_removed, int* dst_index) {
     const int cap = w.cap_arb;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < narb; a += gridDim.x * blockDim.x) {
         int st = w.cstat[a];
-        if (st < 0) {
+        int d, key;
+        int4 ls;
+        if (st == -4) {  // task arbiter: slot, order key and body slots from the schedule
+            d = w.sc_dst[a];
+            key = w.sc_lcol[a];
+            ls = w.sc_ls[a];
+        } else if (st < 0) {
             int e = atomicAdd(&w.ctr->nremoved, 1);
             if (e < cap) ev_removed[e] = S.key[a];
             dst_index[a] = -1;
             continue;
+        } else {
+            int col = st & 255;
+            d = w.color_start[col] + atomicAdd(&w.color_cursor[col], 1);
+            key = JG_ORDER_REMAINDER + col;
+            ls = make_int4(-1, -1, 3, 0);
         }
-        int col = st & 255;
-        int d = w.color_start[col] + atomicAdd(&w.color_cursor[col], 1);
         dst_index[a] = d;
         int4 info = S.info[a];
+        int2 bb = S.body[a];
         D.key[d] = S.key[a];
-        D.body[d] = S.body[a];
-        D.info[d] = make_int4(info.x, info.y, col, info.w);
+        D.body[d] = bb;
+        D.info[d] = make_int4(info.x, info.y, key, info.w);
+        D.lslot[d] = ls;
+        // velocities of a non-dynamic body stay constant through the solve
+        int nd = w.binfo[bb.x].x != JG_MOTION_DYNAMIC ? bb.x : (w.binfo[bb.y].x != JG_MOTION_DYNAMIC ? bb.y : -1);
+        D.sv[d] = nd >= 0 ? w.body[nd].v : make_float4(0.f, 0.f, 0.f, 0.f);
+        D.sv[cap + d] = nd >= 0 ? w.body[nd].w : make_float4(0.f, 0.f, 0.f, 0.f);
         D.mat[d] = S.mat[a];
         for (int k = 0; k < 4; k++) {
             if (!(info.x & (1 << k))) continue;
@@ -392,7 +409,7 @@ __global__ void k_permute(WorldDev w, int2* ev_removed, int* dst_index) {
         int col = st >= 0 ? (st & 255) : 0;
         int d = w.jcolor_start[col] + atomicAdd(&w.jorder[w.cap_joints + col], 1);
         w.jorder[d] = j;
-        w.joints[j].hdr.w = col;
+        w.joints[j].hdr.w = JG_ORDER_REMAINDER + col;
     }
 }
 

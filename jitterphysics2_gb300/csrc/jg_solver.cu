@@ -11,6 +11,7 @@
 // records.  The per-step body update (RigidBody.Update, RigidBody.cs:716-764) is a
 // separate kernel.
 #include "jg_sync.cuh"
+#include <algorithm>
 
 namespace {
 
@@ -107,11 +108,11 @@ __device__ __forceinline__ void prepare_contact(const ArbStore& A, int i, int mo
     A.cacc[i] = make_float4(ca.x, ca.y, ca.z, mT2);
 }
 
-// Contact.Iterate (Contact.cs:931-1018).  Returns the squared impulse change for the
-// residual metric.
-__device__ __forceinline__ void iterate_contact(const ArbStore& A, int i, int mode, float friction, LBody& b1, LBody& b2,
-                                                bool apply_bias, float& d2, float& l2) {
-    float4 cn = A.cn[i], ct1 = A.ct1[i], ct2 = A.ct2[i], cr1 = A.cr1[i], cr2 = A.cr2[i], ca = A.cacc[i];
+// Contact.Iterate (Contact.cs:931-1018) on one contact row held in registers; returns the
+// new accumulated impulses (with the tangent-2 mass) and adds the squared impulse change
+// and squared impulse to d2, l2 for the residual metric.
+__device__ __forceinline__ float4 iterate_row(float4 cn, float4 ct1, float4 ct2, float4 cr1, float4 cr2, float4 ca, int mode,
+                                              float friction, LBody& b1, LBody& b2, bool apply_bias, float& d2, float& l2) {
     float mN = cr1.w, mT1 = cr2.w, mT2 = ca.w;
     float aN = ca.x, aT1 = ca.y, aT2 = ca.z;
     v3 n = mk3(cn), t1 = mk3(ct1), t2 = mk3(ct2), rel1 = mk3(cr1), rel2 = mk3(cr2);
@@ -139,7 +140,6 @@ __device__ __forceinline__ void iterate_contact(const ArbStore& A, int i, int mo
     aT2 = oldT2 + ti2;
     aT2 = fminf(fmaxf(aT2, -maxT), maxT);
     ti2 = aT2 - oldT2;
-    A.cacc[i] = make_float4(aN, aT1, aT2, mT2);
     d2 += ni * ni + ti1 * ti1 + ti2 * ti2;
     l2 += aN * aN + aT1 * aT1 + aT2 * aT2;
     v3 imp = ni * n;
@@ -149,6 +149,13 @@ __device__ __forceinline__ void iterate_contact(const ArbStore& A, int i, int mo
     if (mode & 2) b1.w = b1.w - sym_mul(b1.I, cross(rel1, imp));
     if (mode & 4) b2.v = b2.v + cmul(imp, b2.im);
     if (mode & 8) b2.w = b2.w + sym_mul(b2.I, cross(rel2, imp));
+    return make_float4(aN, aT1, aT2, mT2);
+}
+
+__device__ __forceinline__ void iterate_contact(const ArbStore& A, int i, int mode, float friction, LBody& b1, LBody& b2,
+                                                bool apply_bias, float& d2, float& l2) {
+    A.cacc[i] = iterate_row(A.cn[i], A.ct1[i], A.ct2[i], A.cr1[i], A.cr2[i], A.cacc[i], mode, friction, b1, b2, apply_bias,
+                            d2, l2);
 }
 
 #include "jg_joints.cuh"
@@ -188,99 +195,285 @@ __device__ __forceinline__ void block_reduce_add(float a, float b, float* out) {
     }
 }
 
+// IntegrateForces (World.Step.cs:1060-1072): v += dv, w += dw for dynamic bodies.
+__device__ __forceinline__ void integrate_forces_all(const WorldDev& w, int tid, int nth) {
+    for (int i = tid; i < w.nb; i += nth) {
+        if (w.binfo[i].x != JG_MOTION_DYNAMIC) continue;
+        SBody b = w.body[i];
+        float4 dv = w.dv[i], dw = w.dw[i];
+        b.w = make_float4(b.w.x + dw.x, b.w.y + dw.y, b.w.z + dw.z, b.w.w);
+        b.v = make_float4(b.v.x + dv.x, b.v.y + dv.y, b.v.z + dv.z, b.v.w);
+        w.body[i].v = b.v;
+        w.body[i].w = b.w;
+    }
+}
+
+// IntegrateVelocities (World.Step.cs:1106-1133) with SolveGyroscopic (World.Step.cs:1075-1104).
+__device__ __forceinline__ void integrate_velocities_all(const WorldDev& w, const StepParams& sp, int tid, int nth) {
+    for (int i = tid; i < w.nb; i += nth) {
+        int4 bi = w.binfo[i];
+        if (bi.x == JG_MOTION_STATIC) continue;
+        SBody b = w.body[i];
+        v3 lv = mk3(b.v), av = mk3(b.w);
+        float4 p = w.pos[i];
+        w.pos[i] = make_float4(p.x + lv.x * sp.sub_dt, p.y + lv.y * sp.sub_dt, p.z + lv.z * sp.sub_dt, p.w);
+        q4 rq = rotation_quaternion(av, sp.sub_dt);
+        q4 q = qnormalize(qmul(rq, mkq(w.q[i])));
+        w.q[i] = f4(q);
+        if ((bi.y & JG_BODY_GYROSCOPIC) && ((bi.y >> 4) & 63) == 0) {
+            // one implicit Newton step on the gyroscopic term
+            sym6 Ii;
+            Ii.m11 = b.i0.x; Ii.m12 = b.i0.y; Ii.m13 = b.i0.z; Ii.m22 = b.i0.w; Ii.m23 = b.i1.x; Ii.m33 = b.i1.y;
+            float det = Ii.m11 * (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) + Ii.m12 * (Ii.m23 * Ii.m13 - Ii.m12 * Ii.m33) +
+                        Ii.m13 * (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13);
+            float id = 1.0f / det;
+            if (isfinite(id) && id != 0.f) {
+                sym6 I;
+                I.m11 = (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) * id; I.m12 = (Ii.m13 * Ii.m23 - Ii.m12 * Ii.m33) * id;
+                I.m13 = (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13) * id; I.m22 = (Ii.m11 * Ii.m33 - Ii.m13 * Ii.m13) * id;
+                I.m23 = (Ii.m13 * Ii.m12 - Ii.m23 * Ii.m11) * id; I.m33 = (Ii.m11 * Ii.m22 - Ii.m12 * Ii.m12) * id;
+                v3 Iw = sym_mul(I, av);
+                v3 f = sp.sub_dt * cross(av, Iw);
+                float M[3][3] = {{I.m11, I.m12, I.m13}, {I.m12, I.m22, I.m23}, {I.m13, I.m23, I.m33}};
+                float W[3][3] = {{0, -av.z, av.y}, {av.z, 0, -av.x}, {-av.y, av.x, 0}};
+                float L[3][3] = {{0, -Iw.z, Iw.y}, {Iw.z, 0, -Iw.x}, {-Iw.y, Iw.x, 0}};
+                float J[3][3];
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        J[r][c] = M[r][c] + sp.sub_dt * ((W[r][0] * M[0][c] + W[r][1] * M[1][c] + W[r][2] * M[2][c]) - L[r][c]);
+                float jd = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                if (jd != 0.f && isfinite(jd)) {
+                    float ij = 1.0f / jd;
+                    float inv[3][3];
+                    inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * ij;
+                    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * ij;
+                    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * ij;
+                    inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * ij;
+                    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * ij;
+                    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * ij;
+                    inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * ij;
+                    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * ij;
+                    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * ij;
+                    v3 d = mk3(f.x * inv[0][0] + f.y * inv[0][1] + f.z * inv[0][2], f.x * inv[1][0] + f.y * inv[1][1] + f.z * inv[1][2],
+                               f.x * inv[2][0] + f.y * inv[2][1] + f.z * inv[2][2]);
+                    v3 nw = av - d;
+                    w.body[i].w = f4(nw, b.w.w);
+                }
+            }
+        }
+    }
+}
+
+// Global-colour passes (all constraints when the solve is not partitioned, else the
+// remainder): one grid barrier per non-empty colour.
+__device__ __forceinline__ bool remainder_pass(const WorldDev& w, const ArbStore& A, const StepParams& sp, int phase,
+                                               bool bias, bool joints, int tid, int nth, float& d2, float& l2) {
+    const int ncol = w.ctr->ncolors;
+    int* status = &w.ctr->status;
+    for (int c = 0; c < ncol; c++) {
+        int beg = w.color_start[c], end = w.color_start[c + 1];
+        int jb = joints ? w.jcolor_start[c] : 0, je = joints ? w.jcolor_start[c + 1] : 0;
+        if (beg == end && jb == je) continue;
+        for (int a = beg + tid; a < end; a += nth) solve_arbiter(w, A, a, phase, sp, bias, d2, l2);
+        for (int j = jb + tid; j < je; j += nth) {
+            if (phase == 0) joint_prepare(w, w.jorder[j], sp);
+            else joint_iterate(w, w.jorder[j], sp);
+        }
+        if (!grid_sync(w.bar_count, w.bar_gen, status)) return false;
+    }
+    return true;
+}
+
 __global__ void k_solve(WorldDev w, StepParams sp) {
     const ArbStore& A = w.arb[w.cur];
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    const int ncol = w.ctr->ncolors;
     int* status = &w.ctr->status;
-    const int nb = w.nb;
     for (int s = 0; s < sp.substeps; s++) {
-        // IntegrateForces
-        for (int i = tid; i < nb; i += nth) {
-            if (w.binfo[i].x != JG_MOTION_DYNAMIC) continue;
-            SBody b = w.body[i];
-            float4 dv = w.dv[i], dw = w.dw[i];
-            b.w = make_float4(b.w.x + dw.x, b.w.y + dw.y, b.w.z + dw.z, b.w.w);
-            b.v = make_float4(b.v.x + dv.x, b.v.y + dv.y, b.v.z + dv.z, b.v.w);
-            w.body[i].v = b.v;
-            w.body[i].w = b.w;
-        }
+        integrate_forces_all(w, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
-        const int total_iters = 1 + sp.iterations;
-        for (int it = 0; it < total_iters; it++) {
+        for (int it = 0; it < 1 + sp.iterations; it++) {
             float d2 = 0.f, l2 = 0.f;
-            for (int c = 0; c < ncol; c++) {
-                int beg = w.color_start[c], end = w.color_start[c + 1];
-                for (int a = beg + tid; a < end; a += nth) solve_arbiter(w, A, a, it == 0 ? 0 : 1, sp, true, d2, l2);
-                int jb = w.jcolor_start[c], je = w.jcolor_start[c + 1];
-                for (int j = jb + tid; j < je; j += nth) {
-                    if (it == 0) joint_prepare(w, w.jorder[j], sp);
-                    else joint_iterate(w, w.jorder[j], sp);
-                }
-                if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
-            }
+            if (!remainder_pass(w, A, sp, it == 0 ? 0 : 1, true, true, tid, nth, d2, l2)) return;
             if (sp.record_residual && s == 0 && it > 0 && it <= 64) block_reduce_add(d2, l2, w.resid + 2 * (it - 1));
         }
-        // IntegrateVelocities
-        for (int i = tid; i < nb; i += nth) {
-            int4 bi = w.binfo[i];
-            if (bi.x == JG_MOTION_STATIC) continue;
-            SBody b = w.body[i];
-            v3 lv = mk3(b.v), av = mk3(b.w);
-            float4 p = w.pos[i];
-            w.pos[i] = make_float4(p.x + lv.x * sp.sub_dt, p.y + lv.y * sp.sub_dt, p.z + lv.z * sp.sub_dt, p.w);
-            q4 rq = rotation_quaternion(av, sp.sub_dt);
-            q4 q = qnormalize(qmul(rq, mkq(w.q[i])));
-            w.q[i] = f4(q);
-            if ((bi.y & JG_BODY_GYROSCOPIC) && ((bi.y >> 4) & 63) == 0) {
-                // SolveGyroscopic (World.Step.cs:1075-1104): one implicit Newton step
-                sym6 Ii;
-                Ii.m11 = b.i0.x; Ii.m12 = b.i0.y; Ii.m13 = b.i0.z; Ii.m22 = b.i0.w; Ii.m23 = b.i1.x; Ii.m33 = b.i1.y;
-                float det = Ii.m11 * (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) + Ii.m12 * (Ii.m23 * Ii.m13 - Ii.m12 * Ii.m33) +
-                            Ii.m13 * (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13);
-                float id = 1.0f / det;
-                if (isfinite(id) && id != 0.f) {
-                    sym6 I;
-                    I.m11 = (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) * id; I.m12 = (Ii.m13 * Ii.m23 - Ii.m12 * Ii.m33) * id;
-                    I.m13 = (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13) * id; I.m22 = (Ii.m11 * Ii.m33 - Ii.m13 * Ii.m13) * id;
-                    I.m23 = (Ii.m13 * Ii.m12 - Ii.m23 * Ii.m11) * id; I.m33 = (Ii.m11 * Ii.m22 - Ii.m12 * Ii.m12) * id;
-                    v3 Iw = sym_mul(I, av);
-                    v3 f = sp.sub_dt * cross(av, Iw);
-                    float M[3][3] = {{I.m11, I.m12, I.m13}, {I.m12, I.m22, I.m23}, {I.m13, I.m23, I.m33}};
-                    float W[3][3] = {{0, -av.z, av.y}, {av.z, 0, -av.x}, {-av.y, av.x, 0}};
-                    float L[3][3] = {{0, -Iw.z, Iw.y}, {Iw.z, 0, -Iw.x}, {-Iw.y, Iw.x, 0}};
-                    float J[3][3];
-                    for (int r = 0; r < 3; r++)
-                        for (int c = 0; c < 3; c++)
-                            J[r][c] = M[r][c] + sp.sub_dt * ((W[r][0] * M[0][c] + W[r][1] * M[1][c] + W[r][2] * M[2][c]) - L[r][c]);
-                    float jd = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-                    if (jd != 0.f && isfinite(jd)) {
-                        float ij = 1.0f / jd;
-                        float inv[3][3];
-                        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * ij;
-                        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * ij;
-                        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * ij;
-                        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * ij;
-                        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * ij;
-                        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * ij;
-                        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * ij;
-                        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * ij;
-                        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * ij;
-                        v3 d = mk3(f.x * inv[0][0] + f.y * inv[0][1] + f.z * inv[0][2], f.x * inv[1][0] + f.y * inv[1][1] + f.z * inv[1][2],
-                                   f.x * inv[2][0] + f.y * inv[2][1] + f.z * inv[2][2]);
-                        v3 nw = av - d;
-                        w.body[i].w = f4(nw, b.w.w);
-                    }
-                }
-            }
-        }
+        integrate_velocities_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int it = 0; it < sp.relax; it++) {
             float d2 = 0.f, l2 = 0.f;
-            for (int c = 0; c < ncol; c++) {
-                int beg = w.color_start[c], end = w.color_start[c + 1];
-                for (int a = beg + tid; a < end; a += nth) solve_arbiter(w, A, a, 1, sp, false, d2, l2);
+            if (!remainder_pass(w, A, sp, 1, false, false, tid, nth, d2, l2)) return;
+        }
+    }
+}
+
+// ---- partitioned solve ---------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// the oldest of the JG_TASK_RING groups in flight has landed
+__device__ __forceinline__ void cp_async_wait_ring() { asm volatile("cp.async.wait_group %0;" :: "n"(JG_TASK_RING - 1) : "memory"); }
+
+// Staged arbiter (JG_TASK_STAGE_F4 float4): info, body slots, material, the non-dynamic
+// body's v and w, then 6 rows per contact slot (cn, ct1, ct2, cr1, cr2, cacc).
+__device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap) {
+    cp_async16(dst + 0, &A.info[d]);
+    cp_async16(dst + 1, &A.lslot[d]);
+    cp_async16(dst + 2, &A.mat[d]);
+    cp_async16(dst + 3, &A.sv[d]);
+    cp_async16(dst + 4, &A.sv[cap + d]);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        int i = k * cap + d;
+        float4* q = dst + 5 + 6 * k;
+        cp_async16(q + 0, &A.cn[i]); cp_async16(q + 1, &A.ct1[i]); cp_async16(q + 2, &A.ct2[i]);
+        cp_async16(q + 3, &A.cr1[i]); cp_async16(q + 4, &A.cr2[i]); cp_async16(q + 5, &A.cacc[i]);
+    }
+}
+
+__device__ __forceinline__ LBody sbody_load(const float4* sb, int slot) {
+    float4 v = sb[4 * slot], wv = sb[4 * slot + 1], i0 = sb[4 * slot + 2], i1 = sb[4 * slot + 3];
+    LBody b;
+    b.v = mk3(v); b.w = mk3(wv);
+    b.im = mk3(v.w, wv.w, i1.z);
+    b.I.m11 = i0.x; b.I.m12 = i0.y; b.I.m13 = i0.z; b.I.m22 = i0.w; b.I.m23 = i1.x; b.I.m33 = i1.y;
+    b.flags = __float_as_int(i1.w);
+    return b;
+}
+__device__ __forceinline__ void sbody_store(float4* sb, int slot, const LBody& b) {
+    sb[4 * slot] = f4(b.v, b.im.x);
+    sb[4 * slot + 1] = f4(b.w, b.im.y);
+}
+// A non-dynamic body: velocities only (zero inverse mass and inertia, as its SBody holds).
+__device__ __forceinline__ LBody fixed_body(float4 v, float4 wv) {
+    LBody b;
+    b.v = mk3(v); b.w = mk3(wv);
+    b.im = mk3(v.w, wv.w, 0.f);
+    b.I.m11 = b.I.m12 = b.I.m13 = b.I.m22 = b.I.m23 = b.I.m33 = 0.f;
+    b.flags = 0;
+    return b;
+}
+
+enum { PASS_PREPARE = 0, PASS_ITERATE = 1, PASS_RELAX = 2 };
+
+// One task in one pass: bodies staged into shared memory, colours in order with a block
+// barrier between them, bodies written back.  Iterations stage each (colour, chunk) step's
+// rows with cp.async while the previous step computes.
+__device__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind, float4* sbody,
+                         float4* ring, float& d2, float& l2) {
+    const int4 T = w.sc_task[t];
+    const int nc = w.sc_tnc[t];
+    const int* tc = w.sc_tcol + t * (JG_TASK_MAXC + 1);
+    const int cap = w.cap_arb;
+    const int bs = blockDim.x, tid = threadIdx.x;
+    for (int i = tid; i < T.w; i += bs) {
+        const float4* src = (const float4*)&w.body[w.sc_tbody[T.z + i]];
+        sbody[4 * i] = src[0]; sbody[4 * i + 1] = src[1]; sbody[4 * i + 2] = src[2]; sbody[4 * i + 3] = src[3];
+    }
+    __syncthreads();
+    if (kind == PASS_PREPARE) {
+        for (int c = 0; c < nc; c++) {
+            for (int j = tc[c] + tid; j < tc[c + 1]; j += bs) {
+                int d = T.x + j;
+                int4 info = A.info[d];
+                int usage = info.x & 15, mode = info.y;
+                int4 ls = A.lslot[d];
+                int2 bb = A.body[d];
+                LBody b1 = ls.x >= 0 ? sbody_load(sbody, ls.x) : fixed_body(A.sv[d], A.sv[cap + d]);
+                LBody b2 = ls.y >= 0 ? sbody_load(sbody, ls.y) : fixed_body(A.sv[d], A.sv[cap + d]);
+                float spec = A.mat[d].z;
+                v3 pos1 = mk3(w.pos[bb.x]), pos2 = mk3(w.pos[bb.y]);
+                q4 q1 = mkq(w.q[bb.x]), q2 = mkq(w.q[bb.y]);
+                for (int k = 0; k < 4; k++)
+                    if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
+                if ((mode & 3) && ls.x >= 0) sbody_store(sbody, ls.x, b1);
+                if ((mode & 12) && ls.y >= 0) sbody_store(sbody, ls.y, b2);
+            }
+            __syncthreads();
+        }
+    } else if (nc > 0) {
+        const bool bias = kind == PASS_ITERATE;
+        // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order),
+        // so consecutive colours are spread over different threads.  Each thread keeps
+        // its next JG_TASK_RING arbiters in flight (one cp.async group per arbiter, empty
+        // groups past the end keep the count uniform): the ring holds bs * JG_TASK_RING
+        // arbiters, several colours ahead of the one being solved.
+        const int n = T.y;
+        for (int m = 0; m < JG_TASK_RING; m++) {
+            int j = m * bs + tid;
+            if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap);
+            cp_async_commit();
+        }
+        int m = 0;  // next owned arbiter: j = m * bs + tid
+        for (int c = 0; c < nc; c++) {
+            const int cend = tc[c + 1];
+            for (; m * bs + tid < cend; m++) {
+                const int j = m * bs + tid, d = T.x + j;
+                float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
+                cp_async_wait_ring();
+                float4 r0 = r[0], r1 = r[1];
+                int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
+                int l1 = __float_as_int(r1.x), l2s = __float_as_int(r1.y);
+                float fr = r[2].x;
+                LBody b1 = l1 >= 0 ? sbody_load(sbody, l1) : fixed_body(r[3], r[4]);
+                LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s) : fixed_body(r[3], r[4]);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (!(usage & (1 << k))) continue;
+                    const float4* q = r + 5 + 6 * k;
+                    A.cacc[k * cap + d] = iterate_row(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
+                }
+                if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, b1);
+                if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, b2);
+                // refill the slot just consumed (its values are in registers by now)
+                const int jn = j + JG_TASK_RING * bs;
+                if (jn < n) stage_arbiter(r, A, T.x + jn, cap);
+                cp_async_commit();
+            }
+            __syncthreads();
+        }
+        cp_async_wait_0();
+    }
+    __syncthreads();
+    for (int i = tid; i < T.w; i += bs) {
+        float4* dst = (float4*)&w.body[w.sc_tbody[T.z + i]];
+        dst[0] = sbody[4 * i];
+        dst[1] = sbody[4 * i + 1];
+    }
+    __syncthreads();
+}
+
+// Partitioned solve: the schedule's three grids run as three phases of tasks per pass,
+// then the remainder in global colours; integration phases are grid-stride.
+__global__ void k_solve_tasks(WorldDev w, StepParams sp) {
+    extern __shared__ float4 solve_smem[];
+    float4* sbody = solve_smem;
+    float4* ring = solve_smem + 4 * sp.task_maxb;
+    const ArbStore& A = w.arb[w.cur];
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    int* status = &w.ctr->status;
+    int ntask[JG_SCHED_GRIDS], tbase[JG_SCHED_GRIDS];
+    for (int g = 0; g < JG_SCHED_GRIDS; g++) { ntask[g] = w.sc->ntask[g]; tbase[g] = w.sc->task_base[g]; }
+    for (int s = 0; s < sp.substeps; s++) {
+        integrate_forces_all(w, tid, nth);
+        if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
+        const int npass = 1 + sp.iterations + sp.relax;
+        for (int pass = 0; pass < npass; pass++) {
+            const bool relax = pass > sp.iterations;
+            const int kind = pass == 0 ? PASS_PREPARE : (relax ? PASS_RELAX : PASS_ITERATE);
+            float d2 = 0.f, l2 = 0.f;
+            for (int g = 0; g < JG_SCHED_GRIDS; g++) {
+                if (ntask[g] == 0) continue;
+                for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x)
+                    run_task(w, A, sp, t, kind, sbody, ring, d2, l2);
+                if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
+            }
+            if (!remainder_pass(w, A, sp, pass == 0 ? 0 : 1, !relax, !relax, tid, nth, d2, l2)) return;
+            if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= 64) block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
+            if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
+                integrate_velocities_all(w, sp, tid, nth);
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }
         }
@@ -353,8 +546,58 @@ __global__ void k_update_bodies(WorldDev w, StepParams sp) {
 
 }  // namespace
 
-static int g_solve_grid = 0, g_solve_block = 0;
+static void smem_limits(int& per_block, int& per_sm) {
+    static int b = 0, m = 0;
+    if (!b) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&b, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (b <= 0) b = 48 * 1024;
+        if (m <= 0) m = b;
+    }
+    per_block = b; per_sm = m;
+}
+
+// Bodies a task can stage next to the arbiter ring of `block` threads when
+// `ctas_per_sm` task CTAs share an SM (1 KB per CTA is reserved by the runtime).
+int jg_solver_task_maxb(int block, int ctas_per_sm) {
+    int pb, psm;
+    smem_limits(pb, psm);
+    if (ctas_per_sm < 1) ctas_per_sm = 1;
+    long long avail = std::min<long long>(pb, psm / ctas_per_sm - 1024);
+    long long ring = (long long)JG_TASK_RING * block * JG_TASK_STAGE_F4 * 16;
+    long long m = (avail - ring - 256) / 64;
+    if (m > 4096) m = 4096;
+    return m > 0 ? (int)m : 0;
+}
+
+static size_t task_smem(const StepParams& p, int block) {
+    return ((size_t)4 * p.task_maxb + (size_t)JG_TASK_RING * block * JG_TASK_STAGE_F4) * 16;
+}
+
+static int g_solve_grid = 0, g_solve_block = 0, g_tasks_grid = 0, g_tasks_block = 0;
+static size_t g_tasks_smem = 0;
 int jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm) {
+    if (p.partition) {
+        if (block <= 0) block = 64;
+        size_t smem = task_smem(p, block);
+        if (g_tasks_block != block || g_tasks_smem != smem || g_tasks_grid == 0) {
+            cudaFuncSetAttribute(k_solve_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int occ = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve_tasks, block, smem);
+            if (occ < 1) return -1;
+            if (ctas_per_sm > 0 && occ > ctas_per_sm) occ = ctas_per_sm;
+            g_tasks_grid = nsm * occ;
+            g_tasks_block = block;
+            g_tasks_smem = smem;
+        }
+        cudaMemsetAsync(w.bar_count, 0, sizeof(unsigned) * 2, s);
+        StepParams sp = p;
+        void* args[] = {(void*)&w, (void*)&sp};
+        cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_solve_tasks, dim3(g_tasks_grid), dim3(block), args, smem, s);
+        return e == cudaSuccess ? g_tasks_grid : -1;
+    }
     if (block <= 0) block = 256;
     if (ctas_per_sm <= 0) ctas_per_sm = 2;
     if (g_solve_block != block || g_solve_grid == 0) {
@@ -376,4 +619,4 @@ void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm)
     k_update_bodies<<<nsm * 4, 256, 0, s>>>(w, p);
 }
 
-void jg_solver_reset_launch_cache() { g_solve_grid = 0; }
+void jg_solver_reset_launch_cache() { g_solve_grid = 0; g_tasks_grid = 0; }

@@ -16,33 +16,37 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 // Returns false when the barrier timed out or another block reported a failure.
+// The counter only grows (it is zeroed before each cooperative launch): barrier k of
+// the launch is passed when it reaches (k + 1) * gridDim.x, so an arrival is one
+// release atomic and the wait one acquire load per poll.
 __device__ __forceinline__ bool grid_sync(unsigned* count, unsigned* gen, int* status) {
+    (void)gen;
     __shared__ int ok_flag;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        unsigned g = ld_acquire(gen);
         __threadfence();
-        unsigned arrived = atomicAdd(count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            // about 2^22 polls with back-off (about a second), far above any legitimate wait
-            unsigned spins = 0;
-            while (ld_acquire(gen) == g) {
-                if (ld_relaxed_int(status) == JG_ERR_TIMEOUT) { ok = 0; break; }
-                if (++spins > (1u << 22)) {
-                    atomicCAS(status, 0, JG_ERR_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(spins < 64 ? 0 : 64);
+        unsigned old = atom_add_release(count, 1u);
+        unsigned target = (old / gridDim.x + 1) * gridDim.x;
+        // about 2^21 polls (well over a second), far above any legitimate wait
+        unsigned spins = 0;
+        while ((int)(ld_acquire(count) - target) < 0) {
+            ++spins;
+            if ((spins & 63) == 0 && ld_relaxed_int(status) == JG_ERR_TIMEOUT) { ok = 0; break; }
+            if (spins > (1u << 21)) {
+                atomicCAS(status, 0, JG_ERR_TIMEOUT);
+                ok = 0;
+                break;
             }
+            if (spins > 4096) __nanosleep(64);
         }
-        __threadfence();
         ok_flag = ok;
     }
     __syncthreads();

@@ -32,10 +32,41 @@ struct __align__(16) TriDev {
     float4 nb[3];      // neighbour normals across edges A, B, C; w = 1 when the neighbour exists
 };
 
+// Partitioned solve schedule.  Three staggered column grids in x-z (offsets 0, h/3, 2h/3
+// of the cell size h, with h above three times the largest horizontal distance between
+// two dynamic bodies sharing an arbiter): every such arbiter lies inside one cell of at
+// least one grid.  A cell's arbiters form a task, solved by one CTA with the cell's
+// bodies in shared memory; the three grids are three phases per solver pass, so a pass
+// needs three grid barriers instead of one per colour.  Arbiters that fit no task
+// (and all joints) form the remainder, solved in global colours as before.
+#define JG_SCHED_GRIDS 3
+#define JG_SCHED_MAXCELLS 65536      // cells per grid
+#define JG_SCHED_MAXTASKS 32768
+#define JG_TASK_MAXC 64              // local colours per task
+#define JG_TASK_MAXA 6144            // arbiters per task (local colouring in shared memory)
+#define JG_ORDER_REMAINDER 768       // order keys: task arbiters grid * 256 + colour, remainder 768 + colour
+
+struct SchedInfo {
+    unsigned span_bits;              // largest |dx|, |dz| between two dynamic bodies of an arbiter
+    unsigned bbox[4];                // dynamic body x min, z min, x max, z max (order-preserving bits)
+    float h, x0, z0;                 // cell size and grid origin
+    int ncx, ncz, ncells;            // cells per grid (ncells = worlds * ncx * ncz, or worlds)
+    int ntask[JG_SCHED_GRIDS];       // tasks per grid
+    int task_base[JG_SCHED_GRIDS];   // first task of each grid
+    int ntasks;
+    int narb_task;                   // arbiters placed in tasks (the remainder starts there)
+    int tag;                         // step counter for the body claim stamps
+    int overflow;                    // cells pushed to the remainder (too large)
+    int maxc;                        // most local colours of any task
+    int pad[3];
+};
+
 struct ArbStore {
     int2* key;      // shape ids (ArbiterKey)
     int2* body;     // body indices
-    int4* info;     // usage mask, solve mode, colour, created-this-step flag
+    int4* info;     // usage mask, solve mode, order key, created-this-step flag
+    int4* lslot;    // task body slots of body 1 and 2 (-1: not in the task's bodies)
+    float4* sv;     // [2 * cap] velocity, angular velocity of a non-dynamic body (constant in the solve)
     float4* mat;    // friction, restitution, speculative relaxation, 0
     float4* cn;     // normal xyz, Bias
     float4* ct1;    // tangent1 xyz, PenaltyBias
@@ -81,6 +112,9 @@ struct DevCounters {
     int ncol;         // overlapping pairs found by the MPR stage
     int nepa_list;    // of those, deeper than the EPA threshold
     int nedge;        // of those, near a mesh edge (triangle-edge filter)
+    int ntasks;       // partitioned solve: tasks, arbiters in tasks, most local colours
+    int narb_task;
+    int task_colors;
     int pad;
 };
 
@@ -144,6 +178,24 @@ struct WorldDev {
     float* resid;                // per iteration: sum dlambda^2, sum lambda^2 [2 * 64]
     float* mlp_w;                // MLP parameters (device)
     DevCounters* ctr;
+    // partitioned solve schedule (see SchedInfo)
+    SchedInfo* sc;
+    int* sc_cell;                // [3 * cap_bodies] cell of each dynamic body per grid, -1 otherwise
+    int* sc_stamp;               // [3 * cap_bodies] step tag of the body's claim per grid
+    int* sc_bslot;               // [3 * cap_bodies] body slot in its cell's task
+    int2* sc_arb;                // [cap_arb] grid (3 = remainder, -1 = dead) and cell of each arbiter
+    int* sc_acount;              // [3 * MAXCELLS] arbiters per cell
+    int* sc_bcount;              // [3 * MAXCELLS] bodies claimed per cell
+    int* sc_task_of;             // [3 * MAXCELLS] task of each cell, -1 if none
+    int4* sc_task;               // [MAXTASKS] arbiter offset, count, body offset, count
+    int* sc_cursor;              // [MAXTASKS]
+    int* sc_tnc;                 // [MAXTASKS] local colours of the task
+    int* sc_tcol;                // [MAXTASKS * (MAXC + 1)] colour offsets inside the task
+    int* sc_tlist;               // [cap_arb] arbiters of each task (pre-permute ids)
+    int* sc_tbody;               // [3 * cap_bodies] bodies of each task
+    int* sc_dst;                 // [cap_arb] final slot of a task arbiter, -1 for the remainder
+    int* sc_lcol;                // [cap_arb] local colour of a task arbiter
+    int4* sc_ls;                 // [cap_arb] body slots of a task arbiter
 };
 
 struct StepParams {
@@ -154,7 +206,15 @@ struct StepParams {
     float spec_relax;
     int warm_start;
     int record_residual;
+    int partition;               // 1: partitioned solve (tasks + remainder), 0: global colours only
+    int task_maxb;               // bodies a task may hold in the solver's shared memory
 };
+
+// Partitioned-solve launch shape: threads per CTA and bytes of shared memory per
+// staged arbiter (4 contact slots x 6 float4 rows + info, slots, material, 2 x static body).
+#define JG_TASK_STAGE_F4 29
+#define JG_TASK_RING 2           // staged arbiters per thread
+int jg_solver_task_maxb(int block, int ctas_per_sm);
 
 // ---- stage launchers (each defined in its own translation unit) ------------------------
 void jg_launch_aabb(WorldDev& w, cudaStream_t s);
@@ -162,6 +222,7 @@ int  jg_launch_broadphase(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile);
 void jg_launch_merge(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 void jg_launch_color(WorldDev& w, cudaStream_t s, int nsm);
+void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 int  jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm);
 void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 void jg_launch_mlp_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);

@@ -120,15 +120,37 @@ def _one_step_velocity_errors(sc, w):
     return np.maximum(dv, dw)
 
 
-def test_one_step_solve_matches_oracle_on_resting_boxes():
+@pytest.mark.parametrize("partitioned", [1, 0])
+def test_one_step_solve_matches_oracle_on_resting_boxes(partitioned):
     # resting boxes: shallow contacts, MPR only, so both sides hold identical contacts and
-    # the colour-ordered solve must agree to float rounding
+    # the solve in the GPU's order must agree to float rounding; partitioned=1 solves in
+    # spatial tasks, 0 in global colours only
     sc = scenes.box_grid(n_side=6)
-    w = world_for_scene(sc)
+    w = world_for_scene(sc, partitioned_solve=partitioned)
     for _ in range(350):
         w.step(sc["dt"])
+    c = w.counters()
+    if partitioned:
+        assert c["solver_tasks"] >= 1 and c["task_arbiters"] == c["arbiters"]
+    else:
+        assert c["solver_tasks"] == 0
     err = _one_step_velocity_errors(sc, w)
     assert err.max() < 1e-3, err.max()
+
+
+def test_partitioned_schedule_covers_a_wide_pile():
+    # a pile wider than a cell: several tasks per grid, nearly every arbiter in a task
+    sc = scenes.mixed_pile(n=3000, box=(60.0, 4.0, 60.0), y0=0.0, cells=8, seed=9, lattice=2.0)
+    w = world_for_scene(sc)
+    for _ in range(60):
+        w.step(sc["dt"])
+    c = w.counters()
+    assert c["status"] == 0
+    assert c["solver_tasks"] > 10, c
+    assert c["task_arbiters"] >= 0.95 * c["arbiters"], c
+    b = w.bodies()
+    dyn = b["motion_type"] == abi.MOTION_DYNAMIC
+    assert np.isfinite(b["velocity"]).all() and np.abs(b["velocity"][dyn]).max() < 20.0
 
 
 def test_one_step_solve_matches_oracle_on_a_pile():
@@ -164,7 +186,10 @@ def test_box_grid_settles_without_explosion():
         w.step(sc["dt"])
     b = w.bodies()
     dyn = b["motion_type"] == abi.MOTION_DYNAMIC
-    assert np.abs(b["velocity"][dyn]).max() < 5.0
+    # ten-high columns sway and may shed a top box, which then falls freely from about 10 m
+    # (under 15 m/s); nothing tunnels through the ground and nothing blows up
+    assert np.abs(b["velocity"][dyn]).max() < 15.0
+    assert np.sum(np.abs(b["velocity"][dyn]).max(axis=1) > 3.0) <= 5
     assert b["position"][dyn, 1].min() > 0.3
     c = w.counters()
     assert c["status"] == 0 and c["contacts"] > 1000
