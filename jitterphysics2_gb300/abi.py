@@ -28,6 +28,9 @@ BODY_GYROSCOPIC = 1 << 3
 BODY_LOCKS_SHIFT = 4
 BODY_NO_GRAVITY = 1 << 12
 COLLIDE_NOALLOC_MAX_PAIRS = 16384  # JG_COLLIDE_NOALLOC_MAX_PAIRS
+MLP_IN, MLP_HID, MLP_OUT = 24, 64, 3
+MLP_NW = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_OUT * MLP_HID + MLP_OUT  # trainable
+MLP_NPARAM = MLP_NW + MLP_IN + MLP_IN + MLP_OUT  # + feature mean, feature scale, output scale
 WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
 CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE = 1, 2
 

@@ -17,8 +17,8 @@ void jg_flip_store(WorldDev& w);
 void jg_launch_count_contacts(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_update_contacts(WorldDev& w, cudaStream_t s, int nsm);
 void jg_solver_reset_launch_cache();
-int jg_mlp_alloc(WorldDev& w);
-int jg_mlp_launch_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+int jg_mlp_step_hook(jg_world* w, const StepParams& p);
+void jg_mlp_free(void* mlp);
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
                              cudaStream_t s, int nsm);
 int jg_schedule_launches(const StepParams& p);
@@ -51,6 +51,7 @@ struct jg_world {
     float* q_out = nullptr;
     int* q_hit = nullptr;
     int q_cap = 0;
+    void* mlp = nullptr;              // learned warm start state (jg_mlp.cu)
 };
 
 namespace {
@@ -226,15 +227,14 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     jg_launch_aabb(d, s);
     int passes = jg_launch_broadphase(d, s, w->nsm);
     // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
-    // narrowphase 4, merge 3 (+1 learned warm start), colour/permute 4, count 1, solve 1,
-    // contact update 1, body update 1
-    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 4 + 3 + 4 + 1 + 1 + 1 + 1 +
-                  ((sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) ? 1 : 0) + jg_schedule_launches(sp);
+    // narrowphase 4, merge 3 (+ warm-start hook), schedule, colour/permute 4, count 1,
+    // solve 1, contact update 1, body update 1
+    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 4 + 3 + 4 + 1 + 1 + 1 + 1 + jg_schedule_launches(sp);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);
     jg_launch_merge(d, sp, s, w->nsm);
-    if (sp.warm_start == JG_WARMSTART_MLP && w->mlp_ready) jg_mlp_launch_warmstart(d, sp, s, w->nsm);
+    w->launches += jg_mlp_step_hook(w, sp);
     if (timed) cudaEventRecord(w->ev[3], s);
     jg_launch_schedule(d, sp, s, w->nsm);
     jg_launch_color(d, s, w->nsm);
@@ -344,6 +344,7 @@ int jg_destroy(jg_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     for (void* p : w->allocs) cudaFree(p);
     cudaFree(w->q_pairs); cudaFree(w->q_out); cudaFree(w->q_hit);
+    jg_mlp_free(w->mlp);
     if (w->h_ctr) cudaFreeHost(w->h_ctr);
     for (int i = 0; i < 9; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -902,6 +903,10 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
 }  // extern "C"
 
 // accessors for the MLP translation unit
+void*& jg_world_mlp(jg_world* w) { return w->mlp; }
+void jg_world_invalidate_graphs(jg_world* w) { invalidate_graphs(w); }
+int* jg_world_dst_index(jg_world* w) { return w->dst_index; }
+void jg_set_error(const char* msg) { g_err = msg; }
 WorldDev& jg_world_dev(jg_world* w) { return w->d; }
 cudaStream_t jg_world_stream(jg_world* w) { return w->stream; }
 int jg_world_nsm(jg_world* w) { return w->nsm; }

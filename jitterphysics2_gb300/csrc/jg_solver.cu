@@ -285,6 +285,19 @@ __device__ __forceinline__ bool remainder_pass(const WorldDev& w, const ArbStore
     return true;
 }
 
+// Training targets of the learned warm start: the accumulated impulses of this step's
+// new contacts once the first substep's iterations have converged them (the impulse a
+// warm start of that substep should have supplied).
+__device__ __forceinline__ void record_targets(const WorldDev& w, const ArbStore& A, int tid, int nth) {
+    const int n = min(*w.rec_count, w.rec_cap), cap = w.cap_arb;
+    for (int e = tid; e < n; e += nth) {
+        int2 ak = w.rec_fidx[e];
+        int d = w.rec_dst[ak.x];
+        float4 c = d >= 0 ? A.cacc[ak.y * cap + d] : make_float4(0.f, 0.f, 0.f, 0.f);
+        w.rec_tgt[3 * e] = c.x; w.rec_tgt[3 * e + 1] = c.y; w.rec_tgt[3 * e + 2] = c.z;
+    }
+}
+
 __global__ void k_solve(WorldDev w, StepParams sp) {
     const ArbStore& A = w.arb[w.cur];
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -297,6 +310,7 @@ __global__ void k_solve(WorldDev w, StepParams sp) {
             if (!remainder_pass(w, A, sp, it == 0 ? 0 : 1, true, true, tid, nth, d2, l2)) return;
             if (sp.record_residual && s == 0 && it > 0 && it <= 64) block_reduce_add(d2, l2, w.resid + 2 * (it - 1));
         }
+        if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
         integrate_velocities_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int it = 0; it < sp.relax; it++) {
@@ -473,6 +487,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
             if (!remainder_pass(w, A, sp, pass == 0 ? 0 : 1, !relax, !relax, tid, nth, d2, l2)) return;
             if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= 64) block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
             if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
+                if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
                 integrate_velocities_all(w, sp, tid, nth);
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }

@@ -196,6 +196,15 @@ struct WorldDev {
     int* sc_dst;                 // [cap_arb] final slot of a task arbiter, -1 for the remainder
     int* sc_lcol;                // [cap_arb] local colour of a task arbiter
     int4* sc_ls;                 // [cap_arb] body slots of a task arbiter
+    // learned warm start: for the contacts created this step (arbiter before the colouring
+    // permutation, slot), the accumulated impulse after the first substep's iterations
+    // is copied to rec_tgt (training targets); rec_on enables it
+    int rec_on;
+    int rec_cap;
+    const int2* rec_fidx;
+    const int* rec_count;
+    const int* rec_dst;
+    float* rec_tgt;
 };
 
 struct StepParams {

@@ -175,6 +175,50 @@ class World:
         check(self._lib.jg_autotune(self._h, ctypes.c_float(dt), steps, ctypes.byref(chosen)), "jg_autotune")
         return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile")}
 
+    # -- learned warm start (no reference counterpart) ------------------------------------
+    def mlp_load(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        check(self._lib.jg_mlp_load(self._h, ptr(p), len(p)), "jg_mlp_load")
+
+    def mlp_export(self):
+        n = ctypes.c_int32()
+        check(self._lib.jg_mlp_export(self._h, None, 0, ctypes.byref(n)), "jg_mlp_export")
+        out = np.zeros(n.value, np.float32)
+        check(self._lib.jg_mlp_export(self._h, ptr(out), len(out), ctypes.byref(n)), "jg_mlp_export")
+        return out
+
+    def mlp_predict(self, features):
+        x = np.ascontiguousarray(features, np.float32).reshape(-1, abi.MLP_IN)
+        out = np.zeros((len(x), abi.MLP_OUT), np.float32)
+        check(self._lib.jg_mlp_predict(self._h, ptr(x), len(x), ptr(out)), "jg_mlp_predict")
+        return out
+
+    def mlp_gradients(self, features, targets):
+        x = np.ascontiguousarray(features, np.float32).reshape(-1, abi.MLP_IN)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, abi.MLP_OUT)
+        g = np.zeros(abi.MLP_NW, np.float32)
+        loss = ctypes.c_float()
+        check(self._lib.jg_mlp_gradients(self._h, ptr(x), ptr(t), len(x), ptr(g), len(g), ctypes.byref(loss)),
+              "jg_mlp_gradients")
+        return g, loss.value
+
+    def mlp_train_step(self, features, targets, lr):
+        x = np.ascontiguousarray(features, np.float32).reshape(-1, abi.MLP_IN)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, abi.MLP_OUT)
+        loss = ctypes.c_float()
+        check(self._lib.jg_mlp_train_step(self._h, ptr(x), ptr(t), len(x), ctypes.c_float(lr), ctypes.byref(loss)),
+              "jg_mlp_train_step")
+        return loss.value
+
+    def collect_training(self, capacity=1 << 20):
+        """(features [n,24], converged impulses [n,3]) of the contacts the last step created.
+        The first call arms the recording and returns empty arrays."""
+        f = np.zeros((capacity, abi.MLP_IN), np.float32)
+        t = np.zeros((capacity, abi.MLP_OUT), np.float32)
+        n = ctypes.c_int32()
+        check(self._lib.jg_collect_training(self._h, ptr(f), ptr(t), capacity, ctypes.byref(n)), "jg_collect_training")
+        return f[:n.value].copy(), t[:n.value].copy()
+
     @property
     def handle(self):
         return self._h

@@ -1,0 +1,110 @@
+"""Learned warm start on the GPU: tensor-core forward and backward kernels against the
+CPU oracle (oracle/mlp_ref.py), training, data collection, and what the trained network
+gains over the plain (cached) warm start."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from jitterphysics2_gb300 import abi, learned, scenes
+from jitterphysics2_gb300.world import World, world_for_scene
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "oracle"))
+import mlp_ref as M  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def model(seed=1):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(0, 2, (4096, M.IN)).astype(np.float32)
+    T = rng.normal(0, 3, (4096, M.OUT)).astype(np.float32)
+    p = learned.init_params(X, T, seed=seed)
+    p[M.NW - M.OUT:M.NW] = rng.normal(0, 0.1, M.OUT)  # non-zero output bias
+    return p, X, T
+
+
+def test_forward_matches_oracle():
+    p, X, _ = model()
+    w = World(max_bodies=16)
+    w.mlp_load(p)
+    for n in (1, 100, 128, 1000):  # partial and several tiles
+        got = w.mlp_predict(X[:n])
+        want, _, _ = M.forward_backward(p.astype(np.float64), X[:n])
+        osc = M.unpack(p)["oscale"]
+        err = np.abs(got - want) / osc
+        # FP32 accumulation order differs from the oracle; a BF16 activation that lands on
+        # the other side of a rounding boundary moves an output by far less than 1e-2
+        assert err.max() < 1e-2 and err.mean() < 1e-4, (n, err.max(), err.mean())
+
+
+def test_gradients_match_oracle():
+    p, X, T = model(2)
+    w = World(max_bodies=16)
+    w.mlp_load(p)
+    n = 1000
+    g, loss = w.mlp_gradients(X[:n], T[:n])
+    _, oloss, og = M.forward_backward(p.astype(np.float64), X[:n], T[:n])
+    assert abs(loss - oloss) <= 1e-4 * abs(oloss) + 1e-6, (loss, oloss)
+    o = 0
+    for name, shp in M.SIZES[:6]:
+        k = int(np.prod(shp))
+        a, b = g[o:o + k], og[o:o + k]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert rel < 1e-3, (name, rel)
+        o += k
+
+
+def test_training_reduces_the_loss():
+    rng = np.random.default_rng(4)
+    X = rng.normal(0, 1, (8192, M.IN)).astype(np.float32)
+    T = np.stack([np.maximum(X[:, 0] + 0.5 * X[:, 1], 0), 0.3 * X[:, 2] * X[:, 3], np.tanh(X[:, 4])], 1).astype(np.float32)
+    p = learned.init_params(X, T, seed=4)
+    w = World(max_bodies=16)
+    w.mlp_load(p)
+    losses = learned.train(w, X, T, epochs=12, batch=1024, lr=3e-3)
+    assert losses[-1] < 0.25 * losses[0], losses
+    # the exported parameters predict what the device predicts
+    q = w.mlp_export()
+    want, _, _ = M.forward_backward(q.astype(np.float64), X[:256])
+    got = w.mlp_predict(X[:256])
+    assert np.abs(got - want).max() < 1e-2 * np.abs(want).max()
+
+
+def rubble_scene(seed):
+    return scenes.towers_rubble(n_towers=4, height=10, n_rubble=1500, seed=seed)
+
+
+def test_collect_training_pairs():
+    X, T = learned.collect(rubble_scene(5), steps=60, start=10)
+    assert len(X) > 200
+    assert X.shape[1] == abi.MLP_IN and T.shape[1] == abi.MLP_OUT
+    assert np.isfinite(X).all() and np.isfinite(T).all()
+    assert (T[:, 0] >= 0).all()               # accumulated normal impulses are non-negative
+    assert np.abs(np.linalg.norm(X[:, 0:3], axis=1) - 1).max() < 1e-3  # unit normals
+
+
+def test_learned_warm_start_needs_fewer_iterations():
+    Xs, Ts = [], []
+    for seed in (11, 12, 13):
+        X, T = learned.collect(rubble_scene(seed), steps=160, start=20)
+        Xs.append(X)
+        Ts.append(T)
+    X, T = np.concatenate(Xs), np.concatenate(Ts)
+    p = learned.init_params(X, T, seed=0)
+    w = World(max_bodies=16)
+    w.mlp_load(p)
+    losses = learned.train(w, X, T, epochs=30, batch=2048, lr=2e-3)
+    print("training pairs %d, loss %.3f -> %.3f" % (len(X), losses[0], losses[-1]))
+    assert losses[-1] < 0.8 * losses[0], losses
+    params = w.mlp_export()
+    it_plain, it_learned, rp, rl = learned.paired_residuals(rubble_scene(21), params, steps=12, settle=60)
+    print("iterations to 1e-4: plain %.2f learned %.2f" % (it_plain.mean(), it_learned.mean()))
+    print("residual after 8 iterations: plain %.3g learned %.3g" % (np.exp(np.log(rp[:, 7]).mean()),
+                                                                   np.exp(np.log(rl[:, 7]).mean())))
+    # what the trained network gains: a lower residual after the reference's 8 iterations
+    # and no more iterations to reach 1e-4
+    g_plain, g_learned = np.exp(np.log(rp[:, 7]).mean()), np.exp(np.log(rl[:, 7]).mean())
+    assert g_learned < 0.9 * g_plain, (g_plain, g_learned)
+    assert it_learned.mean() <= it_plain.mean(), (it_plain, it_learned)
