@@ -326,3 +326,33 @@ def batched_worlds(n_worlds=4096, lo=8, hi=512, seed=12348):
     bodies["inv_inertia"][static] = 0
     return dict(bodies=bodies, shapes=shapes, hull=hull, triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=joints,
                 n_worlds=n_worlds, params=dict(substeps=4, solver_iterations=8, relax_iterations=4), dt=1.0 / 120.0)
+
+
+def free_cluster(n=300, spacing=3.2, speed=2.0, seed=12350):
+    """n mixed bodies in free space (no gravity, no damping, no static body) thrown toward
+    a common centre: contacts are the only forces, so linear and angular momentum are
+    conserved and kinetic energy can only fall (restitution 0)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    bodies = _body(n)
+    bodies["linear_damping"] = 1.0
+    bodies["angular_damping"] = 1.0
+    bodies["flags"] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY
+    hull_list = []
+    shapes = _mixed_shapes(rng, n, hull_list, 0)
+    shapes["body"] = np.arange(n)
+    hull = np.concatenate(hull_list) if hull_list else np.zeros((0, 3), np.float32)
+    # jittered lattice inside a sphere; the spacing exceeds every body's extent (no initial overlap)
+    side = int(np.ceil(np.cbrt(n * 6.0 / np.pi))) + 1
+    g = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3) - (side - 1) / 2.0
+    g = g[np.argsort(np.linalg.norm(g, axis=1), kind="stable")][:n] * spacing
+    pos = g + rng.uniform(-0.05, 0.05, g.shape)
+    bodies["position"] = pos.astype(np.float32)
+    bodies["orientation"] = random_quaternions(rng, n)
+    d = -pos / np.maximum(np.linalg.norm(pos, axis=1, keepdims=True), 1e-3)
+    bodies["velocity"] = (d * speed + rng.normal(0, 0.3 * speed, pos.shape)).astype(np.float32)
+    bodies["angular_velocity"] = rng.normal(0, 1.0, pos.shape).astype(np.float32)
+    _finish_mass(bodies, shapes, hull, 0, 0, n)
+    bodies["friction"] = 0.5
+    return dict(bodies=bodies, shapes=shapes, hull=hull, triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[],
+                params=dict(substeps=4, solver_iterations=8, relax_iterations=4, gravity=(0.0, 0.0, 0.0)),
+                dt=1.0 / 100.0)

@@ -181,8 +181,23 @@ class OracleWorld:
         return out
 
     def bodies_d(self):
-        out = np.zeros((self.n, 13), np.float64)
-        self.fn("jor_world_get_bodies_d")(self.h, p(out), self.n)
+        """Body state at full precision: position, orientation, velocity, angular velocity
+        as float64 fields, the other fields as bodies() gives them."""
+        raw = np.zeros((self.n, 13), np.float64)
+        self.fn("jor_world_get_bodies_d")(self.h, p(raw), self.n)
+        base = self.bodies()
+        fields = [(name, base.dtype.fields[name][0]) for name in base.dtype.names]
+        dt = np.dtype([(name, np.float64, (k,)) if name in ("position", "orientation", "velocity", "angular_velocity")
+                       else (name, t) for name, t in fields
+                       for k in [{"position": 3, "orientation": 4, "velocity": 3, "angular_velocity": 3}.get(name, 0)]])
+        out = np.zeros(self.n, dt)
+        for name in base.dtype.names:
+            if name not in ("position", "orientation", "velocity", "angular_velocity"):
+                out[name] = base[name]
+        out["position"] = raw[:, 0:3]
+        out["orientation"] = raw[:, 3:7]
+        out["velocity"] = raw[:, 7:10]
+        out["angular_velocity"] = raw[:, 10:13]
         return out
 
     def set_bodies(self, b):

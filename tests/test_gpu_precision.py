@@ -1,0 +1,105 @@
+"""FP32 GPU path against the FP64 oracle (the reference built with double precision):
+one-step errors from identical states, and momentum / energy drift over 1000 steps.
+
+Graph colouring reorders the Gauss-Seidel sweep, so trajectories cannot be compared
+bitwise over many steps; conserved quantities can.  In a free cluster (no gravity, no
+damping, no static body) contacts are the only forces: normal impulses conserve linear
+and angular momentum exactly, friction impulses conserve linear momentum; the step
+without the gyroscopic term keeps angular velocity, not angular momentum, between
+contacts, so angular momentum and rotational energy drift on both sides alike.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi, scenes
+from jitterphysics2_gb300.world import world_for_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def quat_mat(q):
+    x, y, z, w = [np.asarray(q[:, i], np.float64) for i in range(4)]
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+                     np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+                     np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], -2)
+
+
+def sym_full(s):
+    m = np.zeros((len(s), 3, 3))
+    idx = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    for k, (i, j) in enumerate(idx):
+        m[:, i, j] = s[:, k]
+        m[:, j, i] = s[:, k]
+    return m
+
+
+def invariants(b, inv_inertia_local):
+    m = 1.0 / np.asarray(b["inv_mass"], np.float64)
+    v = np.asarray(b["velocity"], np.float64)
+    w = np.asarray(b["angular_velocity"], np.float64)
+    x = np.asarray(b["position"], np.float64)
+    R = quat_mat(np.asarray(b["orientation"], np.float64))
+    I_local = np.linalg.inv(sym_full(inv_inertia_local))
+    I_world = R @ I_local @ np.transpose(R, (0, 2, 1))
+    Iw = np.einsum("nij,nj->ni", I_world, w)
+    P = (m[:, None] * v).sum(0)
+    L = (np.cross(x, m[:, None] * v) + Iw).sum(0)
+    E_lin = 0.5 * (m * (v * v).sum(1)).sum()
+    E_rot = 0.5 * (w * Iw).sum()
+    return P, L, E_lin, E_rot, (m * np.linalg.norm(v, axis=1)).sum()
+
+
+def test_momentum_and_energy_over_1000_steps_against_fp64():
+    sc = scenes.free_cluster(n=300)
+    inv_local = np.asarray(sc["bodies"]["inv_inertia"], np.float64)
+    g = world_for_scene(sc)
+    o = O.OracleWorld(sc, real="d")
+    P0, L0, El0, Er0, scale = invariants(sc["bodies"], inv_local)
+    for _ in range(1000):
+        g.step(sc["dt"])
+        o.step(sc["dt"])
+    assert g.counters()["status"] == 0
+    gb, ob = g.bodies(), o.bodies_d()
+    Pg, Lg, Elg, Erg, _ = invariants(gb, inv_local)
+    Po, Lo, Elo, Ero, _ = invariants(ob, inv_local)
+    dP_g = np.linalg.norm(Pg - P0) / scale
+    dP_o = np.linalg.norm(Po - P0) / scale
+    print("linear momentum drift / sum m|v|: fp32 GPU %.3g, fp64 oracle %.3g" % (dP_g, dP_o))
+    print("linear kinetic energy: start %.4g, fp32 GPU %.4g, fp64 oracle %.4g" % (El0, Elg, Elo))
+    print("angular momentum |L|: start %.4g, fp32 GPU %.4g, fp64 oracle %.4g" % (np.linalg.norm(L0), np.linalg.norm(Lg),
+                                                                                 np.linalg.norm(Lo)))
+    # contact impulses are equal and opposite: only FP32 rounding moves the momentum
+    assert dP_o < 1e-9
+    assert dP_g < 1e-4
+    # the cluster collapses and loses most of its linear kinetic energy on both sides
+    assert Elg < 0.6 * El0 and Elo < 0.6 * El0
+    assert abs(Elg - Elo) < 0.25 * El0
+
+
+def test_one_step_error_against_fp64():
+    sc = scenes.mixed_pile(n=400, box=(20.0, 3.0, 20.0), y0=0.0, cells=8, seed=17, lattice=3.0)
+    w = world_for_scene(sc)
+    for _ in range(200):
+        w.step(sc["dt"])
+    b0, c0 = w.bodies(), w.contacts()
+    w.step(sc["dt"])
+    b1, c1 = w.bodies(), w.contacts()
+    o = O.OracleWorld(sc, real="d", external_order=True)
+    o.set_bodies(b0)
+    o.set_contacts(c0)
+    o.narrowphase()
+    for c in c1:
+        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
+    o.step(sc["dt"], narrow=False)
+    ob = o.bodies_d()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    dv = np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1)
+    dw = np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1)
+    dx = np.abs(b1["position"][dyn] - ob["position"][dyn]).max(axis=1)
+    err = np.maximum(dv, dw)
+    print("one step vs fp64: velocity error max %.3g mean %.3g median %.3g; position max %.3g"
+          % (err.max(), err.mean(), np.median(err), dx.max()))
+    assert np.median(err) < 1e-4
+    assert np.mean(err < 1e-3) > 0.9
+    assert dx.max() < 1e-3
