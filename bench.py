@@ -94,9 +94,9 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def make_scene():
+def make_scene(n=N_BODIES):
     from jitterphysics2_gb300 import scenes
-    return scenes.mixed_pile(n=N_BODIES, box=(120.0, 200.0, 120.0), seed=SEED)
+    return scenes.mixed_pile(n=n, box=(120.0, 200.0, 120.0), seed=SEED)
 
 
 def solver_bytes(counters, n_bodies, substeps=4, iters=8, relax=4):
@@ -120,6 +120,81 @@ def cpu_baseline(scene, bodies, contacts, steps=2):
     return {"value": total_c / total_t, "unit": "contacts/s", "cores": threads, "kind": "port",
             "sample": "%d steps of the settled %d-body pile (C++ restatement of Jitter2, Regular mode)" % (steps, N_BODIES),
             "seconds": total_t}
+
+
+def learned_section(eval_steps=10):
+    """Learned against plain warm start on the towers-and-rubble workload (50 towers of
+    20 unit boxes + 49k mixed rubble): training pairs collected from two seeds, the
+    network trained on the device, then from identical states one step each way with 64
+    iterations (iterations to residual 1e-4, residual after the 8 iterations the
+    workload uses) and the contact throughput of both at 8 iterations."""
+    from jitterphysics2_gb300 import abi, learned, scenes
+    from jitterphysics2_gb300.world import World, world_for_scene
+    t0 = time.perf_counter()
+    xs, ts = [], []
+    for seed in (101, 102):
+        x, t = learned.collect(scenes.towers_rubble(seed=seed), steps=100, start=10)
+        xs.append(x)
+        ts.append(t)
+    X, T = np.concatenate(xs), np.concatenate(ts)
+    params = learned.init_params(X, T, seed=0)
+    trainer = World(max_bodies=16)
+    trainer.mlp_load(params)
+    losses = learned.train(trainer, X, T, epochs=20, batch=4096, lr=2e-3)
+    params = trainer.mlp_export()
+    trainer.close()
+    sc = scenes.towers_rubble(seed=12349)
+    ip, il, rp, rl = learned.paired_residuals(sc, params, steps=eval_steps, settle=60, iterations=64)
+    # contacts/s at the workload's 8 iterations, plain and learned, from the same state
+    rates = {}
+    plain = world_for_scene(sc)
+    for _ in range(60):
+        plain.step(sc["dt"])
+    state = plain.export_state()
+    for mode in ("plain", "learned"):
+        w = world_for_scene(sc, warm_start_mode=abi.WARMSTART_MLP if mode == "learned" else abi.WARMSTART_CACHED)
+        if mode == "learned":
+            w.mlp_load(params)
+        w.import_state(state)
+        ms, cnt = 0.0, 0
+        for _ in range(eval_steps):
+            w.step(sc["dt"])
+            ms += w.timings()["total"]
+            cnt += w.counters()["contacts"]
+        rates[mode] = cnt / (ms / 1e3)
+        w.close()
+    plain.close()
+    gm = lambda a: float(np.exp(np.mean(np.log(np.maximum(a, 1e-30)))))
+    return {"workload": "50 towers x 20 unit boxes + 49k mixed rubble, dt 1/100, 4 substeps",
+            "training_pairs": int(len(X)), "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+            "iters_to_1e-4_plain": float(ip.mean()), "iters_to_1e-4_learned": float(il.mean()),
+            "iteration_cap": 64, "residual_after_8_plain": gm(rp[:, 7]), "residual_after_8_learned": gm(rl[:, 7]),
+            "contacts_per_s_plain": rates["plain"], "contacts_per_s_learned": rates["learned"],
+            "steps_compared": eval_steps, "seconds": time.perf_counter() - t0}
+
+
+def fp64_section(scene, bodies, contacts_before, contacts_after, gpu_after):
+    """One step from the GPU's state replayed by the FP64 oracle in the GPU's solve
+    order: velocity and position error of the FP32 path against double precision."""
+    import oracle_lib as O
+    from jitterphysics2_gb300 import abi
+    t0 = time.perf_counter()
+    o = O.OracleWorld(scene, real="d", external_order=True)
+    o.set_bodies(bodies)
+    o.set_contacts(contacts_before)
+    o.narrowphase()
+    for c in contacts_after:
+        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
+    o.step(scene["dt"], narrow=False)
+    ob = o.bodies_d()
+    dyn = gpu_after["motion_type"] == abi.MOTION_DYNAMIC
+    dv = np.maximum(np.abs(gpu_after["velocity"][dyn] - ob["velocity"][dyn]).max(1),
+                    np.abs(gpu_after["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(1))
+    dx = np.abs(gpu_after["position"][dyn] - ob["position"][dyn]).max(1)
+    return {"velocity_err_max": float(dv.max()), "velocity_err_mean": float(dv.mean()),
+            "velocity_err_median": float(np.median(dv)), "velocity_within_1e-3": float(np.mean(dv < 1e-3)),
+            "position_err_max": float(dx.max()), "seconds": time.perf_counter() - t0,
+            "sample": "one step of the settled pile from identical state, FP64 oracle in the GPU's order"}
 
 
 def dist_setup(n_gpus):
@@ -168,7 +243,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--settle", type=int, default=SETTLE_STEPS)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--bodies", type=int, default=N_BODIES, help="smaller piles for profiling captures")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 and learned warm start sections")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -179,7 +256,7 @@ def main():
     from jitterphysics2_gb300 import abi
     from jitterphysics2_gb300.world import world_for_scene
 
-    sc = make_scene()
+    sc = make_scene(args.bodies)
     w = world_for_scene(sc)
     for _ in range(args.settle):
         w.step(sc["dt"])
@@ -227,26 +304,37 @@ def main():
 
     peak, peak_kind = peaks()
     achieved = float(np.mean([b / (s / 1e3) for b, s in zip(sbytes, solve_ms)])) / 1e9
+    nb = len(sc["bodies"])
+    cnt = w.counters()
     line = {"metric": "contacts/s @100k bodies", "value": value, "unit": "contacts/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded mixed pile)",
-            "config": {"workload": "mixed pile, 100k bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations",
-                       "bodies": N_BODIES, "settle_steps": args.settle, "parallelism": "replicas only",
+            "config": {"workload": "mixed pile, %d bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations" % nb,
+                       "bodies": nb, "settle_steps": args.settle, "parallelism": "replicas only",
                        "l2": "flushed between steps (256 MiB write)",
-                       "contacts_per_step": contacts / args.steps},
+                       "contacts_per_step": contacts / args.steps, "arbiters": cnt["arbiters"],
+                       "solver_tasks": cnt["solver_tasks"], "task_colors": cnt["task_colors"]},
+            "body_steps_per_s": nb * args.steps * ws / (total_ms / 1e3),
             "e2e": {"value": e2e_c / e2e_s, "unit": "contacts/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
-            "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "k_solve_tasks", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "solve_ms_per_step": float(np.mean(solve_ms))},
+                         "solve_ms_per_step": float(np.mean(solve_ms)),
+                         "bytes_model": "S*((I+R)*276*C + 320*C + 116*N) + 52*N"},
             "clocks": clk, "gpu_launches": launches,
             "stage_ms": w.timings()}
+    if rank == 0 and not args.no_extras:
+        b0, c0 = w.bodies(), w.contacts()
+        w.step(sc["dt"])
+        line["fp64_error"] = fp64_section(sc, b0, c0, w.contacts(), w.bodies())
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(sc, w.bodies(), w.contacts())
+    w.close()
+    if rank == 0 and not args.no_extras:
+        line["learned_warm_start"] = learned_section()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    w.close()
 
 
 if __name__ == "__main__":
