@@ -275,7 +275,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
     const int maxb = sp.task_maxb;
     unsigned long long* s_mask = tc_smem;                          // [maxb]
     unsigned long long* s_own = s_mask + maxb;                      // [maxb]
-    int* s_l1 = (int*)(s_own + maxb);                               // [MAXA]
+    int* s_deg = (int*)(s_own + maxb);                              // [maxb] arbiters per body
+    int* s_l1 = s_deg + ((maxb + 1) & ~1);                          // [MAXA]
     int* s_l2 = s_l1 + JG_TASK_MAXA;                                // [MAXA]
     int* s_a = s_l2 + JG_TASK_MAXA;                                 // [MAXA]
     unsigned char* s_col = (unsigned char*)(s_a + JG_TASK_MAXA);    // [MAXA]
@@ -288,18 +289,31 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
         const int4 T = w.sc_task[t];
         const int n = T.y, nb = T.w;
         const int g = t >= S->task_base[2] && S->ntask[2] ? 2 : (t >= S->task_base[1] && S->ntask[1] ? 1 : 0);
-        for (int i = threadIdx.x; i < nb; i += blockDim.x) { s_mask[i] = 0ull; s_own[i] = 0ull; }
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) { s_mask[i] = 0ull; s_own[i] = 0ull; s_deg[i] = 0; }
         for (int i = threadIdx.x; i <= JG_TASK_MAXC; i += blockDim.x) { s_cnt[i] = 0; s_cur[i] = 0; }
+        __syncthreads();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             int a = w.sc_tlist[T.x + i];
             int2 b = A.body[a];
             s_a[i] = a;
-            s_l1[i] = dyn(w, b.x) ? w.sc_bslot[g * cb + b.x] : -1;
-            s_l2[i] = dyn(w, b.y) ? w.sc_bslot[g * cb + b.y] : -1;
+            int l1 = dyn(w, b.x) ? w.sc_bslot[g * cb + b.x] : -1;
+            int l2 = dyn(w, b.y) ? w.sc_bslot[g * cb + b.y] : -1;
+            s_l1[i] = l1;
+            s_l2[i] = l2;
             s_col[i] = 0xff;
+            if (l1 >= 0) atomicAdd(&s_deg[l1], 1);
+            if (l2 >= 0) atomicAdd(&s_deg[l2], 1);
         }
         __syncthreads();
-        // priorities: a hash of the arbiter key (deterministic), the list position breaks ties
+        // priorities, largest degree first (an arbiter's degree: the arbiters sharing one of
+        // its bodies), then a hash of the arbiter key (deterministic), then the list position
+        auto prio = [&](int i) -> unsigned long long {
+            int l1 = s_l1[i], l2 = s_l2[i];
+            unsigned long long deg = (unsigned long long)min((l1 >= 0 ? s_deg[l1] : 0) + (l2 >= 0 ? s_deg[l2] : 0), 8191);
+            int2 key = A.key[s_a[i]];
+            unsigned long long h = mix64(((unsigned long long)(unsigned)key.x << 32) | (unsigned)key.y) & ((1ull << 37) - 1);
+            return (1ull << 63) | (deg << 50) | (h << 13) | (unsigned long long)i;
+        };
         unsigned todo = 0;  // bit k: element threadIdx.x + k * blockDim.x still uncoloured
         for (int k = 0; k * (int)blockDim.x + (int)threadIdx.x < n; k++) todo |= 1u << k;
         // every round colours at least the highest-priority uncoloured arbiter, so n rounds
@@ -309,8 +323,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
             for (unsigned m = todo; m; m &= m - 1) {
                 int i = __ffs(m) - 1;
                 i = threadIdx.x + i * blockDim.x;
-                int2 key = A.key[s_a[i]];
-                unsigned long long p = (mix64(((unsigned long long)(unsigned)key.x << 32) | (unsigned)key.y) << 13) | (unsigned)i | 1ull << 63;
+                unsigned long long p = prio(i);
                 if (s_l1[i] >= 0) atomicMax(&s_own[s_l1[i]], p);
                 if (s_l2[i] >= 0) atomicMax(&s_own[s_l2[i]], p);
             }
@@ -319,8 +332,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
             for (unsigned m = todo; m; m &= m - 1) {
                 int k = __ffs(m) - 1;
                 int i = threadIdx.x + k * blockDim.x;
-                int2 key = A.key[s_a[i]];
-                unsigned long long p = (mix64(((unsigned long long)(unsigned)key.x << 32) | (unsigned)key.y) << 13) | (unsigned)i | 1ull << 63;
+                unsigned long long p = prio(i);
                 int l1 = s_l1[i], l2 = s_l2[i];
                 if ((l1 < 0 || s_own[l1] == p) && (l2 < 0 || s_own[l2] == p)) won |= 1u << k;
             }
@@ -380,7 +392,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
 }  // namespace
 
 size_t jg_task_color_smem(int maxb) {
-    return (size_t)maxb * 16 + (size_t)JG_TASK_MAXA * 13;
+    return (size_t)maxb * 16 + (size_t)((maxb + 1) & ~1) * 4 + (size_t)JG_TASK_MAXA * 13;
 }
 
 void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm) {

@@ -329,10 +329,14 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 // the oldest of the JG_TASK_RING groups in flight has landed
 __device__ __forceinline__ void cp_async_wait_ring() { asm volatile("cp.async.wait_group %0;" :: "n"(JG_TASK_RING - 1) : "memory"); }
+// everything but the JG_TASK_RING most recent groups (the ring prologue) has landed
+__device__ __forceinline__ void cp_async_wait_bodies() { asm volatile("cp.async.wait_group %0;" :: "n"(JG_TASK_RING) : "memory"); }
 
 // Staged arbiter (JG_TASK_STAGE_F4 float4): info, body slots, material, the non-dynamic
 // body's v and w, then 6 rows per contact slot (cn, ct1, ct2, cr1, cr2, cacc).
-__device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap) {
+// Only the contact slots in `usage` are copied; the others keep stale data that the
+// staged usage mask tells the consumer to skip.
+__device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap, int usage) {
     cp_async16(dst + 0, &A.info[d]);
     cp_async16(dst + 1, &A.lslot[d]);
     cp_async16(dst + 2, &A.mat[d]);
@@ -340,6 +344,7 @@ __device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, in
     cp_async16(dst + 4, &A.sv[cap + d]);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
+        if (!(usage & (1 << k))) continue;
         int i = k * cap + d;
         float4* q = dst + 5 + 6 * k;
         cp_async16(q + 0, &A.cn[i]); cp_async16(q + 1, &A.ct1[i]); cp_async16(q + 2, &A.ct2[i]);
@@ -382,12 +387,17 @@ __device__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams&
     const int* tc = w.sc_tcol + t * (JG_TASK_MAXC + 1);
     const int cap = w.cap_arb;
     const int bs = blockDim.x, tid = threadIdx.x;
+    // the task's bodies, one cp.async group per thread (the arbiter ring, in iterations,
+    // follows as later groups so that both loads are in flight together)
     for (int i = tid; i < T.w; i += bs) {
         const float4* src = (const float4*)&w.body[w.sc_tbody[T.z + i]];
-        sbody[4 * i] = src[0]; sbody[4 * i + 1] = src[1]; sbody[4 * i + 2] = src[2]; sbody[4 * i + 3] = src[3];
+        cp_async16(&sbody[4 * i], src); cp_async16(&sbody[4 * i + 1], src + 1);
+        cp_async16(&sbody[4 * i + 2], src + 2); cp_async16(&sbody[4 * i + 3], src + 3);
     }
-    __syncthreads();
+    cp_async_commit();
     if (kind == PASS_PREPARE) {
+        cp_async_wait_0();
+        __syncthreads();
         for (int c = 0; c < nc; c++) {
             for (int j = tc[c] + tid; j < tc[c + 1]; j += bs) {
                 int d = T.x + j;
@@ -417,15 +427,21 @@ __device__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams&
         const int n = T.y;
         for (int m = 0; m < JG_TASK_RING; m++) {
             int j = m * bs + tid;
-            if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap);
+            if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap, A.info[T.x + j].x);
             cp_async_commit();
         }
+        cp_async_wait_bodies();  // this thread's body copies have landed
+        __syncthreads();         // ... and everyone's
         int m = 0;  // next owned arbiter: j = m * bs + tid
         for (int c = 0; c < nc; c++) {
             const int cend = tc[c + 1];
             for (; m * bs + tid < cend; m++) {
                 const int j = m * bs + tid, d = T.x + j;
                 float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
+                // usage of the arbiter this slot is refilled with, loaded now and used after
+                // the compute below, so its latency stays off the critical path
+                const int jn = j + JG_TASK_RING * bs;
+                const int un = jn < n ? __ldg(&A.info[T.x + jn].x) : 0;
                 cp_async_wait_ring();
                 float4 r0 = r[0], r1 = r[1];
                 int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
@@ -442,14 +458,13 @@ __device__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams&
                 if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, b1);
                 if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, b2);
                 // refill the slot just consumed (its values are in registers by now)
-                const int jn = j + JG_TASK_RING * bs;
-                if (jn < n) stage_arbiter(r, A, T.x + jn, cap);
+                if (jn < n) stage_arbiter(r, A, T.x + jn, cap, un);
                 cp_async_commit();
             }
             __syncthreads();
         }
-        cp_async_wait_0();
     }
+    cp_async_wait_0();  // no copy into shared memory outlives the task
     __syncthreads();
     for (int i = tid; i < T.w; i += bs) {
         float4* dst = (float4*)&w.body[w.sc_tbody[T.z + i]];
