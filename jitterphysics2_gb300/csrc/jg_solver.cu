@@ -380,8 +380,8 @@ enum { PASS_PREPARE = 0, PASS_ITERATE = 1, PASS_RELAX = 2 };
 // One task in one pass: bodies staged into shared memory, colours in order with a block
 // barrier between them, bodies written back.  Iterations stage each (colour, chunk) step's
 // rows with cp.async while the previous step computes.
-__device__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind, float4* sbody,
-                         float4* ring, float& d2, float& l2) {
+__device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind,
+                                         float4* sbody, float4* ring, float& d2, float& l2) {
     const int4 T = w.sc_task[t];
     const int nc = w.sc_tnc[t];
     const int* tc = w.sc_tcol + t * (JG_TASK_MAXC + 1);

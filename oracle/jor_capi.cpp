@@ -269,6 +269,11 @@ template <class R> struct Handle {
         for (int i = 0; i < (int)p.size() && i < cap; i++) { out[2 * i] = p[i].first; out[2 * i + 1] = p[i].second; } \
         return (int)p.size();                                                                                      \
     }                                                                                                              \
+    extern "C" int jor_world_pairs_sweep_##SUF(void* h, int* out, int cap) {                                      \
+        auto p = ((Handle<R>*)h)->w.find_pairs_sweep();                                                            \
+        for (int i = 0; i < (int)p.size() && i < cap; i++) { out[2 * i] = p[i].first; out[2 * i + 1] = p[i].second; } \
+        return (int)p.size();                                                                                      \
+    }                                                                                                              \
     extern "C" int jor_world_residuals_##SUF(void* h, float* out, int cap) {                                      \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         for (int i = 0; i < (int)w.residuals.size() && i < cap; i++) out[i] = (float)w.residuals[i];              \

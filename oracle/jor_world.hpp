@@ -1,7 +1,7 @@
 // Oracle (test infrastructure only): a CPU world that strings the restated stages
 // together the way World.StepInternal does (World.Step.cs:153-296) with deactivation
 // disabled.  Pairs are every shape pair with non-disjoint exact world AABBs on different
-// bodies (DynamicTree.cs:266-286 + World.cs:447-455), found by sort-and-sweep.  Solve
+// bodies (DynamicTree.cs:266-286 + World.cs:447-455), found with a uniform grid.  Solve
 // order: the reference's deterministic order (contacts sorted by arbiter key, then
 // constraints by id; World.Deterministic.cs:142-203) or an external colour order
 // (colour by colour; inside a colour rows share no dynamic body, so their order does
@@ -13,6 +13,10 @@
 #include <algorithm>
 #include <numeric>
 #include <condition_variable>
+#include <mutex>
+#include <atomic>
+#include <thread>
+#include <functional>
 
 namespace jor {
 
@@ -69,8 +73,16 @@ template <class R> struct World {
         }
         return out;
     }
-    // The reference's pair contract, evaluated by sort-and-sweep on x.
-    std::vector<std::pair<int, int>> find_pairs() {
+    // The reference's pair contract (DynamicTree.EnumerateOverlapsCallback with the
+    // default filter, DynamicTree.cs:266-286, World.cs:447-455): every shape pair with
+    // non-disjoint world AABBs, on different bodies of one world, at least one active and
+    // one dynamic.  Evaluated with a uniform grid (the reference's tree gives the same
+    // set): shapes spanning more than 8 cells on an axis are tested against all others,
+    // the rest are binned by the cells their AABB covers and each pair is reported by the
+    // cell that holds the lower corner of the two AABBs' intersection.
+    // The same contract by sort-and-sweep on x: quadratic in dense scenes, kept to check
+    // the grid against.
+    std::vector<std::pair<int, int>> find_pairs_sweep() {
         auto box = aabbs();
         std::vector<int> ord(shapes.size());
         std::iota(ord.begin(), ord.end(), 0);
@@ -81,16 +93,99 @@ template <class R> struct World {
             for (size_t jj = ii + 1; jj < ord.size(); jj++) {
                 int j = ord[jj];
                 if (box[j].mn.x > box[i].mx.x) break;
-                if (disjoint(box[i], box[j])) continue;
-                int bi = shape_body[i], bj = shape_body[j];
-                if (bi == bj) continue;
-                if (bodies[bi].world != bodies[bj].world) continue;
-                if (!bodies[bi].active() && !bodies[bj].active()) continue;
-                if (bodies[bi].motion != DYNAMIC && bodies[bj].motion != DYNAMIC) continue;
+                if (disjoint(box[i], box[j]) || !pair_ok(i, j)) continue;
                 pairs.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
             }
         }
         std::sort(pairs.begin(), pairs.end());
+        return pairs;
+    }
+    bool pair_ok(int i, int j) const {
+        int bi = shape_body[i], bj = shape_body[j];
+        if (bi == bj) return false;
+        if (bodies[bi].world != bodies[bj].world) return false;
+        if (!bodies[bi].active() && !bodies[bj].active()) return false;
+        if (bodies[bi].motion != DYNAMIC && bodies[bj].motion != DYNAMIC) return false;
+        return true;
+    }
+    std::vector<std::pair<int, int>> find_pairs() {
+        auto box = aabbs();
+        const int n = (int)shapes.size();
+        std::vector<std::pair<int, int>> pairs;
+        if (n < 2) return pairs;
+        // cell size: twice the median largest AABB extent
+        std::vector<double> ext(n);
+        for (int i = 0; i < n; i++) {
+            V3<R> d = box[i].mx - box[i].mn;
+            ext[i] = std::max((double)d.x, std::max((double)d.y, (double)d.z));
+        }
+        std::vector<double> tmp(ext);
+        std::nth_element(tmp.begin(), tmp.begin() + n / 2, tmp.end());
+        const double cell = std::max(2.0 * tmp[n / 2], 1e-3);
+        auto cidx = [&](double v) { return (long long)std::floor(v / cell); };
+        std::vector<int> big;
+        std::vector<std::pair<unsigned long long, int>> ent;
+        ent.reserve((size_t)n * 4);
+        auto key = [](long long x, long long y, long long z) {
+            return ((unsigned long long)(x & 0x1FFFFF) << 42) | ((unsigned long long)(y & 0x1FFFFF) << 21) |
+                   (unsigned long long)(z & 0x1FFFFF);
+        };
+        for (int i = 0; i < n; i++) {
+            long long x0 = cidx(box[i].mn.x), x1 = cidx(box[i].mx.x), y0 = cidx(box[i].mn.y), y1 = cidx(box[i].mx.y),
+                      z0 = cidx(box[i].mn.z), z1 = cidx(box[i].mx.z);
+            if (x1 - x0 > 8 || y1 - y0 > 8 || z1 - z0 > 8 || !(box[i].mx.x - box[i].mn.x < 1e30)) {
+                big.push_back(i);
+                continue;
+            }
+            for (long long x = x0; x <= x1; x++)
+                for (long long y = y0; y <= y1; y++)
+                    for (long long z = z0; z <= z1; z++) ent.push_back({key(x, y, z), i});
+        }
+        std::sort(ent.begin(), ent.end());
+        std::vector<std::pair<size_t, size_t>> runs;
+        for (size_t s = 0; s < ent.size();) {
+            size_t e = s + 1;
+            while (e < ent.size() && ent[e].first == ent[s].first) e++;
+            if (e - s > 1) runs.push_back({s, e});
+            s = e;
+        }
+        const int nt = std::max(1, nthreads);
+        std::vector<std::vector<std::pair<int, int>>> part(nt);
+        std::atomic<int> slot{0};
+        parallel_for((int)runs.size(), 64, [&](int b, int e) {
+            thread_local std::vector<std::pair<int, int>> local;
+            local.clear();
+            for (int r = b; r < e; r++) {
+                auto [s0, s1] = runs[r];
+                unsigned long long ck = ent[s0].first;
+                for (size_t a = s0; a < s1; a++)
+                    for (size_t c = a + 1; c < s1; c++) {
+                        int i = ent[a].second, j = ent[c].second;
+                        if (disjoint(box[i], box[j]) || !pair_ok(i, j)) continue;
+                        // report once: the cell of the intersection's lower corner
+                        double lx = std::max((double)box[i].mn.x, (double)box[j].mn.x);
+                        double ly = std::max((double)box[i].mn.y, (double)box[j].mn.y);
+                        double lz = std::max((double)box[i].mn.z, (double)box[j].mn.z);
+                        if (key(cidx(lx), cidx(ly), cidx(lz)) != ck) continue;
+                        local.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
+                    }
+            }
+            int k = slot.fetch_add(1);
+            std::vector<std::pair<int, int>>& dst = part[k % nt];
+            static std::mutex mu;
+            std::lock_guard<std::mutex> lock(mu);
+            dst.insert(dst.end(), local.begin(), local.end());
+        });
+        for (auto& p : part) pairs.insert(pairs.end(), p.begin(), p.end());
+        // large shapes against everything
+        for (int i : big)
+            for (int j = 0; j < n; j++) {
+                if (j == i || (std::binary_search(big.begin(), big.end(), j) && j < i)) continue;
+                if (disjoint(box[i], box[j]) || !pair_ok(i, j)) continue;
+                pairs.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
+            }
+        std::sort(pairs.begin(), pairs.end());
+        pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
         return pairs;
     }
 

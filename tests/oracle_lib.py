@@ -43,6 +43,7 @@ def load():
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
             "jor_world_step": (None, [P, F, I]), "jor_world_step_mt": (D, [P, F, I]),
             "jor_world_counters": (None, [P, P]), "jor_world_pairs": (I, [P, P, I]),
+            "jor_world_pairs_sweep": (I, [P, P, I]),
             "jor_world_residuals": (I, [P, P, I]), "jor_world_detect": (I, [P, I, I, P]),
             "jor_world_collide": (I, [P, I, I, P]),
             "jor_support": (None, [P, P, P, P]), "jor_aabb": (None, [P, P, P, P, P]),
@@ -241,10 +242,11 @@ class OracleWorld:
         self.fn("jor_world_counters")(self.h, p(out))
         return dict(zip(["pairs", "colliding", "points", "arbiters", "contacts", "epa_calls", "epa_failures"], out.tolist()))
 
-    def pairs(self):
-        n = self.fn("jor_world_pairs")(self.h, None, 0)
+    def pairs(self, sweep=False):
+        name = "jor_world_pairs_sweep" if sweep else "jor_world_pairs"
+        n = self.fn(name)(self.h, None, 0)
         out = np.zeros((max(n, 1), 2), np.int32)
-        self.fn("jor_world_pairs")(self.h, p(out), n)
+        self.fn(name)(self.h, p(out), n)
         return out[:n]
 
     def residuals(self):
