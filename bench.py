@@ -18,9 +18,15 @@ colouring, substepped solve + integration, contact and body update.
           S * ((I + R) * 276 * C + 320 * C + 116 * N) + 52 * N
   cpu_baseline  the oracle's multithreaded Regular-mode restatement of the reference
           (C++ restatement of Jitter2, all host threads) on 2 steps of the same state
+  fp64_error  one step from the timed state replayed by the FP64 oracle in the GPU's order
+  learned_warm_start  the learned against the plain warm start on 50 towers + 49k rubble:
+          residual after 8 iterations, iterations to 1e-4 (cap 64), contacts/s of both
 
---impl reference times that CPU restatement alone (the reference is C# and no .NET
-runtime exists on either machine) and prints the same line with "impl": "reference".
+--config c1 | c2 | c4 | c5 runs the workload's other configurations (1000-box grid, 20k
+pile, 4096 batched worlds, towers + rubble) and prints their line; the default (c3, the
+100k pile) is the headline.  --impl reference times the CPU restatement alone (the
+reference is C# and no .NET runtime exists on either machine) and prints the same line
+with "impl": "reference".
 Multi-GPU: the single world does not shard ("replicas only"); with N ranks each rank
 steps its own replica and value sums contacts over ranks / max time.
 """
@@ -97,6 +103,28 @@ class ClockSampler:
 def make_scene(n=N_BODIES):
     from jitterphysics2_gb300 import scenes
     return scenes.mixed_pile(n=n, box=(120.0, 200.0, 120.0), seed=SEED)
+
+
+# The workload's configurations; c3 (the 100k pile) is the headline line, the others
+# are run with --config for the results table.  Settle steps before timing:
+CONFIG_SETTLE = {"c3": SETTLE_STEPS, "c1": 300, "c2": 600, "c4": 200, "c5": 100}
+
+
+def config_scene(name, n):
+    from jitterphysics2_gb300 import scenes
+    if name == "c3":
+        return make_scene(n), None, "mixed pile, %d bodies, 120x200x120 over ground + heightfield"
+    if name == "c1":
+        return scenes.box_grid(n_side=10), None, "1000 unit boxes in a 10x10x10 grid on a ground box"
+    if name == "c2":
+        return (scenes.mixed_pile(n=20000, box=(60.0, 120.0, 60.0), seed=12346), None,
+                "mixed pile, 20k bodies, 60x120x60 over ground + heightfield")
+    if name == "c4":
+        return (scenes.batched_worlds(), None,
+                "4096 batched worlds, 8-512 bodies each, capsule chains (BallSocket + HingeAngle)")
+    if name == "c5":
+        return scenes.towers_rubble(), None, "50 towers x 20 unit boxes + 49k mixed rubble"
+    raise SystemExit("unknown config " + name)
 
 
 def solver_bytes(counters, n_bodies, substeps=4, iters=8, relax=4):
@@ -254,11 +282,14 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--settle", type=int, default=SETTLE_STEPS)
+    ap.add_argument("--settle", type=int, default=None, help="settle steps (default: the config's)")
     ap.add_argument("--bodies", type=int, default=N_BODIES, help="smaller piles for profiling captures")
+    ap.add_argument("--config", default="c3", help="c3 (headline, default), c1, c2, c4, c5")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 and learned warm start sections")
     args = ap.parse_args()
+    if args.settle is None:
+        args.settle = CONFIG_SETTLE.get(args.config, SETTLE_STEPS)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -268,7 +299,9 @@ def main():
     from jitterphysics2_gb300 import abi
     from jitterphysics2_gb300.world import world_for_scene
 
-    sc = make_scene(args.bodies)
+    sc, _, workload = config_scene(args.config, args.bodies)
+    prm = sc["params"]
+    S, I, R = prm.get("substeps", 1), prm.get("solver_iterations", 6), prm.get("relax_iterations", 4)
     w = world_for_scene(sc)
     for _ in range(args.settle):
         w.step(sc["dt"])
@@ -279,7 +312,7 @@ def main():
     # device-timed steps (inputs resident)
     clocks = ClockSampler()
     clocks.start()
-    step_ms, solve_ms, contacts, sbytes, launches = [], [], 0, [], 0
+    step_ms, solve_ms, contacts, sbytes, launches, stages = [], [], 0, [], 0, []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -288,9 +321,11 @@ def main():
         c = w.counters()
         step_ms.append(t["total"])
         solve_ms.append(t["solve"])
+        stages.append(t)
         contacts += c["contacts"]
-        sbytes.append(solver_bytes(c, len(sc["bodies"])))
+        sbytes.append(solver_bytes(c, len(sc["bodies"]), S, I, R))
         launches += c["kernel_launches"]
+    stage_ms = {k: float(np.mean([s[k] for s in stages])) for k in stages[0]}
     clk = clocks.stop()
     total_ms = float(np.sum(step_ms))
     if dist is not None:
@@ -318,11 +353,14 @@ def main():
     achieved = float(np.mean([b / (s / 1e3) for b, s in zip(sbytes, solve_ms)])) / 1e9
     nb = len(sc["bodies"])
     cnt = w.counters()
-    line = {"metric": "contacts/s @100k bodies", "value": value, "unit": "contacts/s", "n_gpus": ws,
+    metric = "contacts/s @100k bodies" if args.config == "c3" else "contacts/s"
+    line = {"metric": metric, "value": value, "unit": "contacts/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded mixed pile)",
-            "config": {"workload": "mixed pile, %d bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations" % nb,
+            "data": "synthetic (seeded scene)",
+            "config": {"name": args.config,
+                       "workload": "%s; dt %.5g, %d substeps, (%d,%d) iterations" % (workload % nb if "%d" in workload
+                                                                                    else workload, sc["dt"], S, I, R),
                        "bodies": nb, "settle_steps": args.settle, "parallelism": "replicas only",
                        "l2": "flushed between steps (256 MiB write)",
                        "contacts_per_step": contacts / args.steps, "arbiters": cnt["arbiters"],
@@ -335,15 +373,16 @@ def main():
                          "solve_ms_per_step": float(np.mean(solve_ms)),
                          "bytes_model": "S*((I+R)*276*C + 320*C + 116*N) + 52*N"},
             "clocks": clk, "gpu_launches": launches,
-            "stage_ms": w.timings()}
-    if rank == 0 and not args.no_extras:
+            "stage_ms": stage_ms}
+    extras = rank == 0 and not args.no_extras and args.config == "c3"
+    if extras:
         b0, c0 = w.bodies(), w.contacts()
         w.step(sc["dt"])
         line["fp64_error"] = fp64_section(sc, b0, c0, w.contacts(), w.bodies())
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(sc, w.bodies(), w.contacts())
     w.close()
-    if rank == 0 and not args.no_extras:
+    if extras:
         line["learned_warm_start"] = learned_section()
     if rank == 0:
         print(json.dumps(line), flush=True)
