@@ -35,8 +35,10 @@ struct jg_world {
     int* remaining = nullptr;
     int* dst_index = nullptr;
     std::vector<jg_body_desc> host_bodies;
+    bool host_current = false;         // host_bodies equals the device state (no step since the upload)
     std::vector<jg_shape_desc> host_shapes;
     int nj_host = 0;
+    std::vector<JointDev> pending_joints;  // added since the last step, uploaded in one copy
     cudaEvent_t ev[9]{};
     jg_timings timings{};
     jg_counters counters{};
@@ -412,6 +414,7 @@ int jg_upload_bodies(jg_world* w, const jg_body_desc* b, int32_t n) {
     if (D.nb != n) invalidate_graphs(w);
     D.nb = n;
     w->host_bodies.assign(b, b + n);
+    w->host_current = true;
     return JG_OK;
 }
 
@@ -537,18 +540,28 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
     if (kind != JG_CONSTRAINT_BALLSOCKET && kind != JG_CONSTRAINT_HINGEANGLE) return JG_ERR_INVALID_ARG;
     if (b1 < 0 || b2 < 0 || b1 >= w->d.nb || b2 >= w->d.nb || b1 == b2) return JG_ERR_INVALID_ARG;
     if (w->nj_host >= w->d.cap_joints) return JG_ERR_CAPACITY;
-    jg_body_desc bd[2];
-    int r;
-    std::vector<jg_body_desc> all(w->d.nb);
-    if ((r = jg_download_bodies(w, all.data(), w->d.nb))) return r;
-    bd[0] = all[b1]; bd[1] = all[b2];
+    // the two bodies' current poses: from the host copy while it is current, else from the device
+    float4 pq[4];
+    if (w->host_current) {
+        const jg_body_desc& d1 = w->host_bodies[b1];
+        const jg_body_desc& d2 = w->host_bodies[b2];
+        pq[0] = make_float4(d1.position[0], d1.position[1], d1.position[2], 0.f);
+        pq[1] = make_float4(d1.orientation[0], d1.orientation[1], d1.orientation[2], d1.orientation[3]);
+        pq[2] = make_float4(d2.position[0], d2.position[1], d2.position[2], 0.f);
+        pq[3] = make_float4(d2.orientation[0], d2.orientation[1], d2.orientation[2], d2.orientation[3]);
+    } else {
+        CK(cudaMemcpy(&pq[0], w->d.pos + b1, sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&pq[1], w->d.q + b1, sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&pq[2], w->d.pos + b2, sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&pq[3], w->d.q + b2, sizeof(float4), cudaMemcpyDeviceToHost));
+    }
     JointDev J;
     memset(&J, 0, sizeof(J));
     J.hdr = make_int4(kind, b1, b2, 0);
-    q4 q1{bd[0].orientation[0], bd[0].orientation[1], bd[0].orientation[2], bd[0].orientation[3]};
-    q4 q2{bd[1].orientation[0], bd[1].orientation[1], bd[1].orientation[2], bd[1].orientation[3]};
-    v3 p1 = mk3(bd[0].position[0], bd[0].position[1], bd[0].position[2]);
-    v3 p2 = mk3(bd[1].position[0], bd[1].position[1], bd[1].position[2]);
+    q4 q1{pq[1].x, pq[1].y, pq[1].z, pq[1].w};
+    q4 q2{pq[3].x, pq[3].y, pq[3].z, pq[3].w};
+    v3 p1 = mk3(pq[0]);
+    v3 p2 = mk3(pq[2]);
     if (kind == JG_CONSTRAINT_BALLSOCKET) {
         // BallSocket.Initialize (BallSocket.cs:120-138)
         v3 anchor = mk3(init[0], init[1], init[2]);
@@ -564,11 +577,20 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         J.axis = f4(rotate_inv(axis, q2), 0.f);
         J.q0 = f4(qmul(qconj(q2), q1));
     }
-    CK(cudaMemcpy(w->d.joints + w->nj_host, &J, sizeof(J), cudaMemcpyHostToDevice));
+    w->pending_joints.push_back(J);
     if (out_id) *out_id = w->nj_host;
     w->nj_host++;
     w->d.nj = w->nj_host;
     invalidate_graphs(w);
+    return JG_OK;
+}
+
+// Uploads the constraints added since the last flush in one copy.
+static int flush_joints(jg_world* w) {
+    if (w->pending_joints.empty()) return JG_OK;
+    size_t k = w->pending_joints.size();
+    CK(cudaMemcpy(w->d.joints + (w->nj_host - k), w->pending_joints.data(), sizeof(JointDev) * k, cudaMemcpyHostToDevice));
+    w->pending_joints.clear();
     return JG_OK;
 }
 
@@ -577,6 +599,9 @@ int jg_step(jg_world* w, float dt) {
     if (!std::isfinite(dt)) return JG_ERR_NONFINITE;
     if (dt < 0) return JG_ERR_INVALID_ARG;
     if (dt < 1.401298e-45f) return JG_OK;
+    int fr = flush_joints(w);
+    if (fr) return fr;
+    w->host_current = false;
     StepParams sp = make_params(w, dt);
     if (w->d.ns == 0 && w->d.nb == 0) return JG_OK;
     int parity = w->d.cur;
@@ -783,6 +808,8 @@ struct StateHeader { int magic, version, nb, narb, nj, cap_arb; };
 
 int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
     if (!w || !size) return JG_ERR_INVALID_ARG;
+    int fr = flush_joints(w);
+    if (fr) return fr;
     WorldDev& D = w->d;
     int narb = 0;
     CK(cudaMemcpy(&narb, &D.ctr->narb, sizeof(int), cudaMemcpyDeviceToHost));
@@ -818,6 +845,9 @@ int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
 
 int jg_import_state(jg_world* w, const void* buf, int64_t size) {
     if (!w || !buf || size < (int64_t)sizeof(StateHeader)) return JG_ERR_INVALID_ARG;
+    int fr = flush_joints(w);
+    if (fr) return fr;
+    w->host_current = false;
     const char* p = (const char*)buf;
     StateHeader h;
     memcpy(&h, p, sizeof(h)); p += sizeof(h);
