@@ -258,6 +258,12 @@ int jg_get_contacts(jg_world* world, jg_contact_view* out, int32_t capacity, int
 int jg_get_arbiter_events(jg_world* world, int32_t* created_pairs, int32_t created_capacity,
                           int32_t* n_created, int32_t* removed_pairs, int32_t removed_capacity,
                           int32_t* n_removed);
+/* Constraint state in creation order: the accumulated impulse (BallSocket.Impulse,
+ * BallSocket.cs:221; HingeAngle.Impulse, HingeAngle.cs:311) as 3 floats each, and
+ * the order key of the last step's solve (768 + global colour: constraints sharing a key
+ * share no dynamic body). */
+int jg_get_constraints(jg_world* world, int32_t* order_keys, float* impulses, int32_t capacity,
+                       int32_t* out_count);
 int jg_get_counters(jg_world* world, jg_counters* out);
 int jg_get_timings(jg_world* world, jg_timings* out);
 /* Per-iteration residual of the first substep of the last step (record_residual=1):

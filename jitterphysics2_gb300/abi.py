@@ -106,6 +106,7 @@ SIGNATURES = {
     "jg_collide_pairs_noalloc": (_I, [_P, _P, _I, _P, _P]),
     "jg_get_contacts": (_I, [_P, _P, _I, _PI]),
     "jg_get_arbiter_events": (_I, [_P, _P, _I, _PI, _P, _I, _PI]),
+    "jg_get_constraints": (_I, [_P, _P, _P, _I, _PI]),
     "jg_get_counters": (_I, [_P, _P]),
     "jg_get_timings": (_I, [_P, _P]),
     "jg_get_residuals": (_I, [_P, _P, _I, _PI]),

@@ -639,6 +639,23 @@ int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
     return jg_download_bodies(w, bodies, n);
 }
 
+int jg_get_constraints(jg_world* w, int32_t* keys, float* imp, int32_t cap, int32_t* count) {
+    if (!w || !count || cap < 0) return JG_ERR_INVALID_ARG;
+    int r = flush_joints(w);
+    if (r) return r;
+    const int n = w->nj_host;
+    *count = n;
+    const int k = std::min(n, cap);
+    if (k == 0 || (!keys && !imp)) return JG_OK;
+    std::vector<JointDev> J(k);
+    CK(cudaMemcpy(J.data(), w->d.joints, sizeof(JointDev) * k, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < k; i++) {
+        if (keys) keys[i] = J[i].hdr.w;
+        if (imp) { imp[3 * i] = J[i].acc.x; imp[3 * i + 1] = J[i].acc.y; imp[3 * i + 2] = J[i].acc.z; }
+    }
+    return JG_OK;
+}
+
 int jg_get_counters(jg_world* w, jg_counters* out) {
     if (!w || !out) return JG_ERR_INVALID_ARG;
     *out = w->counters;

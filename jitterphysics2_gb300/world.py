@@ -134,6 +134,15 @@ class World:
         check(self._lib.jg_get_contacts(self._h, ptr(out), len(out), ctypes.byref(n)), "jg_get_contacts")
         return out[:n.value]
 
+    def constraints(self):
+        """(order keys [n], accumulated impulses [n,3]) of the constraints, creation order."""
+        n = ctypes.c_int32()
+        check(self._lib.jg_get_constraints(self._h, None, None, 0, ctypes.byref(n)), "jg_get_constraints")
+        keys = np.zeros(max(n.value, 1), np.int32)
+        imp = np.zeros((max(n.value, 1), 3), np.float32)
+        check(self._lib.jg_get_constraints(self._h, ptr(keys), ptr(imp), n.value, ctypes.byref(n)), "jg_get_constraints")
+        return keys[:n.value], imp[:n.value]
+
     def counters(self):
         buf = np.zeros(len(abi.COUNTER_NAMES), np.int64)
         check(self._lib.jg_get_counters(self._h, ptr(buf)), "jg_get_counters")

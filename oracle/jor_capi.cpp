@@ -211,6 +211,11 @@ template <class R> struct Handle {
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         for (int i = 0; i < n && i < (int)w.joints.size(); i++) put3(out + 3 * i, w.joints[i].acc);                \
     }                                                                                                              \
+    extern "C" void jor_world_set_joint_impulses_##SUF(void* h, const float* in, int n) {                          \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        for (int i = 0; i < n && i < (int)w.joints.size(); i++)                                                    \
+            w.joints[i].acc = V3<R>((R)in[3 * i], (R)in[3 * i + 1], (R)in[3 * i + 2]);                             \
+    }                                                                                                              \
     extern "C" void jor_world_external_order_##SUF(void* h, int on) { ((Handle<R>*)h)->w.external_order = on != 0; } \
     extern "C" void jor_world_set_contacts_##SUF(void* h, const jg_contact_view* v, int n) { set_contacts(((Handle<R>*)h)->w, v, n); } \
     extern "C" int jor_world_get_contacts_##SUF(void* h, jg_contact_view* v, int cap) { return get_contacts(((Handle<R>*)h)->w, v, cap); } \

@@ -35,6 +35,7 @@ def load():
             "jor_world_get_bodies_d": (None, [P, P, I]),
             "jor_world_set_shapes": (None, [P, P, I, P, I, P, I]), "jor_world_add_joint": (I, [P, I, I, I, P]),
             "jor_world_set_joint_colors": (None, [P, P, I]), "jor_world_get_joint_impulses": (None, [P, P, I]),
+            "jor_world_set_joint_impulses": (None, [P, P, I]),
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
@@ -226,6 +227,10 @@ class OracleWorld:
         out = np.zeros((n, 3), np.float32)
         self.fn("jor_world_get_joint_impulses")(self.h, p(out), n)
         return out
+
+    def set_joint_impulses(self, imp):
+        v = np.ascontiguousarray(imp, np.float32).reshape(-1, 3)
+        self.fn("jor_world_set_joint_impulses")(self.h, p(v), len(v))
 
     def external_order(self, on):
         self.fn("jor_world_external_order")(self.h, 1 if on else 0)

@@ -161,6 +161,39 @@ def test_one_step_solve_matches_oracle_on_a_pile():
     assert np.mean(err < 1e-3) > 0.9, (np.mean(err < 1e-3), np.sort(err)[-5:])
 
 
+def test_one_step_solve_with_joints_matches_oracle():
+    # capsule chains linked by BallSocket + HingeAngle over a small pile: joints are solved
+    # in global colours after the contact tasks; the oracle replays contacts and joints
+    # in the GPU's order keys, warm-started with the GPU's joint impulses
+    sc = scenes.batched_worlds(n_worlds=1, lo=24, hi=48, seed=5)
+    assert len(sc["joints"]) >= 8
+    w = world_for_scene(sc)
+    for _ in range(80):
+        w.step(sc["dt"])
+    b0, c0 = w.bodies(), w.contacts()
+    _, j0 = w.constraints()
+    w.step(sc["dt"])
+    b1, c1 = w.bodies(), w.contacts()
+    k1, j1 = w.constraints()
+    assert (k1 >= 768).all() and np.abs(j1).max() > 0
+    o = O.OracleWorld(sc, external_order=True)
+    o.set_bodies(b0)
+    o.set_contacts(c0)
+    o.set_joint_impulses(j0)
+    o.narrowphase()
+    for c in c1:
+        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
+    o.set_joint_colors(k1)
+    o.step(sc["dt"], narrow=False)
+    ob = o.bodies()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    err = np.maximum(np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1),
+                     np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1))
+    jerr = np.abs(j1 - o.joint_impulses(len(j1))).max(axis=1) / np.maximum(1.0, np.abs(j1).max(axis=1))
+    assert np.mean(err < 1e-3) > 0.95, (np.mean(err < 1e-3), np.sort(err)[-5:])
+    assert np.mean(jerr < 1e-3) > 0.95, np.sort(jerr)[-5:]
+
+
 def test_colours_are_conflict_free():
     sc, w = _settled_pile(n=300, steps=30, seed=5)
     c = w.contacts()
