@@ -212,8 +212,8 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.warm_start = p.warm_start_mode;
     sp.record_residual = p.record_residual;
     sp.partition = p.partitioned_solve ? 1 : 0;
-    sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : 64,
-                                       p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : 2);
+    sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : JG_TASK_BLOCK,
+                                       p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
     return sp;
 }
@@ -914,7 +914,7 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     const int* ctas = part ? pctas : gctas;
     const int nbk = 3, nct = part ? 2 : 3;
     float best = 1e30f;
-    int bb = part ? 64 : 256, bc = 2;
+    int bb = part ? JG_TASK_BLOCK : 256, bc = part ? JG_TASK_CTAS : 2;
     jg_world_params saved = w->prm;
     for (int ib = 0; ib < nbk; ib++)
         for (int ic = 0; ic < nct; ic++) {

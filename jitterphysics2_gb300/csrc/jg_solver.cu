@@ -610,7 +610,8 @@ static int g_solve_grid = 0, g_solve_block = 0, g_tasks_grid = 0, g_tasks_block 
 static size_t g_tasks_smem = 0;
 int jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm) {
     if (p.partition) {
-        if (block <= 0) block = 64;
+        if (block <= 0) block = JG_TASK_BLOCK;
+        if (ctas_per_sm <= 0) ctas_per_sm = JG_TASK_CTAS;
         size_t smem = task_smem(p, block);
         if (g_tasks_block != block || g_tasks_smem != smem || g_tasks_grid == 0) {
             cudaFuncSetAttribute(k_solve_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

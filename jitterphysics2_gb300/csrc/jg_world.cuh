@@ -222,7 +222,12 @@ struct StepParams {
 // Partitioned-solve launch shape: threads per CTA and bytes of shared memory per
 // staged arbiter (4 contact slots x 6 float4 rows + info, slots, material, 2 x static body).
 #define JG_TASK_STAGE_F4 29
-#define JG_TASK_RING 2           // staged arbiters per thread
+// Staged arbiters per thread.  Thread t owns every blockDim-th arbiter of its task, so its
+// next arbiter lies blockDim positions (several colours) ahead: one slot in flight is
+// enough, and the small ring lets two 128-thread task CTAs share an SM.
+#define JG_TASK_RING 1
+#define JG_TASK_BLOCK 128        // default threads per task CTA
+#define JG_TASK_CTAS 2           // default task CTAs per SM
 int jg_solver_task_maxb(int block, int ctas_per_sm);
 
 // ---- stage launchers (each defined in its own translation unit) ------------------------
