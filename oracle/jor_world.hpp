@@ -126,10 +126,13 @@ template <class R> struct World {
         std::vector<int> big;
         std::vector<std::pair<unsigned long long, int>> ent;
         ent.reserve((size_t)n * 4);
-        auto key = [](long long x, long long y, long long z) {
-            return ((unsigned long long)(x & 0x1FFFFF) << 42) | ((unsigned long long)(y & 0x1FFFFF) << 21) |
-                   (unsigned long long)(z & 0x1FFFFF);
+        // cell key: world id and cell coordinates (different worlds never share a cell;
+        // coordinates wrap at 2^14 cells, which only adds candidate pairs)
+        auto key = [](int world, long long x, long long y, long long z) {
+            return ((unsigned long long)(x & 0x3FFF) << 50) | ((unsigned long long)(y & 0x3FFF) << 36) |
+                   ((unsigned long long)(z & 0x3FFF) << 22) | (unsigned long long)(world & 0x3FFFFF);
         };
+        auto wld = [&](int i) { return bodies[shape_body[i]].world; };
         for (int i = 0; i < n; i++) {
             long long x0 = cidx(box[i].mn.x), x1 = cidx(box[i].mx.x), y0 = cidx(box[i].mn.y), y1 = cidx(box[i].mx.y),
                       z0 = cidx(box[i].mn.z), z1 = cidx(box[i].mx.z);
@@ -139,7 +142,7 @@ template <class R> struct World {
             }
             for (long long x = x0; x <= x1; x++)
                 for (long long y = y0; y <= y1; y++)
-                    for (long long z = z0; z <= z1; z++) ent.push_back({key(x, y, z), i});
+                    for (long long z = z0; z <= z1; z++) ent.push_back({key(wld(i), x, y, z), i});
         }
         std::sort(ent.begin(), ent.end());
         std::vector<std::pair<size_t, size_t>> runs;
@@ -166,7 +169,7 @@ template <class R> struct World {
                         double lx = std::max((double)box[i].mn.x, (double)box[j].mn.x);
                         double ly = std::max((double)box[i].mn.y, (double)box[j].mn.y);
                         double lz = std::max((double)box[i].mn.z, (double)box[j].mn.z);
-                        if (key(cidx(lx), cidx(ly), cidx(lz)) != ck) continue;
+                        if (key(wld(i), cidx(lx), cidx(ly), cidx(lz)) != ck) continue;
                         local.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
                     }
             }
@@ -177,13 +180,21 @@ template <class R> struct World {
             dst.insert(dst.end(), local.begin(), local.end());
         });
         for (auto& p : part) pairs.insert(pairs.end(), p.begin(), p.end());
-        // large shapes against everything
-        for (int i : big)
-            for (int j = 0; j < n; j++) {
-                if (j == i || (std::binary_search(big.begin(), big.end(), j) && j < i)) continue;
-                if (disjoint(box[i], box[j]) || !pair_ok(i, j)) continue;
-                pairs.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
+        // large shapes against every shape of their world
+        if (!big.empty()) {
+            std::vector<int> by_world(n);
+            std::iota(by_world.begin(), by_world.end(), 0);
+            std::stable_sort(by_world.begin(), by_world.end(), [&](int a, int b) { return wld(a) < wld(b); });
+            for (int i : big) {
+                auto lo = std::lower_bound(by_world.begin(), by_world.end(), wld(i), [&](int s, int w) { return wld(s) < w; });
+                for (auto it = lo; it != by_world.end() && wld(*it) == wld(i); ++it) {
+                    int j = *it;
+                    if (j == i || (std::binary_search(big.begin(), big.end(), j) && j < i)) continue;
+                    if (disjoint(box[i], box[j]) || !pair_ok(i, j)) continue;
+                    pairs.push_back(i < j ? std::make_pair(i, j) : std::make_pair(j, i));
+                }
             }
+        }
         std::sort(pairs.begin(), pairs.end());
         pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
         return pairs;
