@@ -106,6 +106,7 @@ int allocate(jg_world* w) {
     DA(d.leaf_parent, d.cap_shapes); DA(d.node_parent, d.cap_shapes); DA(d.node_flag, d.cap_shapes);
     DA(d.scene_box, 2);
     DA(d.pairs, d.cap_pairs);
+    DA(d.pair_order, d.cap_pairs); DA(d.pair_kind, 2 * 64);
     DA(d.cs_key, d.cap_pairs); DA(d.cs_n, d.cap_pairs); DA(d.cs_pa, 4 * (size_t)d.cap_pairs); DA(d.cs_pb, 4 * (size_t)d.cap_pairs);
     int r;
     if ((r = alloc_store(w, d.arb[0], d.cap_arb))) return r;
@@ -229,9 +230,9 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     jg_launch_aabb(d, s);
     int passes = jg_launch_broadphase(d, s, w->nsm);
     // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
-    // narrowphase 4, merge 3 (+ warm-start hook), schedule, colour/permute 4, count 1,
+    // narrowphase 3 + 4, merge 3 (+ warm-start hook), schedule, colour/permute 4, count 1,
     // solve 1, contact update 1, body update 1
-    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 4 + 3 + 4 + 1 + 1 + 1 + 1 + jg_schedule_launches(sp);
+    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 7 + 3 + 4 + 1 + 1 + 1 + 1 + jg_schedule_launches(sp);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);

@@ -282,9 +282,11 @@ __global__ void k_traverse(WorldDev w, int n) {
                 buf[nbuf++] = make_int2(min(sa, sb), max(sa, sb));
                 if (nbuf == PAIR_BUF) flush_pairs(w, buf, nbuf);
             } else {
-                int2 rg = w.node_range[cidx];
-                int wf = (int)(w.mkey[rg.x] >> 32), wl = (int)(w.mkey[rg.y] >> 32);
-                if (world < wf || world > wl) continue;
+                if (w.nworlds > 1) {  // subtrees hold one world range (the world id leads the Morton key)
+                    int2 rg = w.node_range[cidx];
+                    int wf = (int)(w.mkey[rg.x] >> 32), wl = (int)(w.mkey[rg.y] >> 32);
+                    if (world < wf || world > wl) continue;
+                }
                 if (!overlap(qmn, qmx, w.nmin[cidx], w.nmax[cidx])) continue;
                 next_nodes[push_cnt++] = cidx;
             }

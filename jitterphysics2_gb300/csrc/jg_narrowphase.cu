@@ -1002,6 +1002,42 @@ __device__ __forceinline__ int warp_append(int* counter, bool pred) {
     return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
+// Pairs grouped by the kinds of their two shapes (a counting sort over the 64 kind
+// combinations), so that the threads of a warp run the same support maps in MPR.  The
+// order inside a group does not matter: results do not depend on the pair order.
+__device__ __forceinline__ int pair_kind_key(const WorldDev& w, int p) {
+    int2 pr = w.pairs[p];
+    return ((w.sinfo[pr.x].x & 7) << 3) | (w.sinfo[pr.y].x & 7);
+}
+__global__ void k_pair_hist(WorldDev w) {
+    __shared__ int h[64];
+    if (threadIdx.x < 64) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int n = min(w.ctr->npairs, w.cap_pairs);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        atomicAdd(&h[pair_kind_key(w, p)], 1);
+    __syncthreads();
+    if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(&w.pair_kind[threadIdx.x], h[threadIdx.x]);
+}
+__global__ void k_pair_offsets(WorldDev w) {
+    int acc = 0;
+    for (int k = 0; k < 64; k++) { w.pair_kind[64 + k] = acc; acc += w.pair_kind[k]; }
+}
+__global__ void k_pair_scatter(WorldDev w) {
+    const int n = min(w.ctr->npairs, w.cap_pairs);
+    const int lane = threadIdx.x & 31;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int key = pair_kind_key(w, p);
+        const unsigned act = __activemask();
+        const unsigned same = __match_any_sync(act, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&w.pair_kind[64 + key], __popc(same));
+        base = __shfl_sync(act, base, leader);
+        w.pair_order[base + __popc(same & ((1u << lane) - 1u))] = p;
+    }
+}
+
 // Stage 1, one thread per broadphase pair: the MPR overlap test in A's frame
 // (NarrowPhase.MprEpa, NarrowPhase.cs:902-927, up to the EPA hand-off).  Overlapping pairs
 // are appended to the colliding list with their MPR result; deeper than the EPA threshold,
@@ -1010,7 +1046,8 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
     const int npairs = min(w.ctr->npairs, w.cap_pairs);
     const int cap = w.cap_arb;
     for (int base = blockIdx.x * blockDim.x; base < npairs; base += gridDim.x * blockDim.x) {
-        int p = base + threadIdx.x;
+        const int q = base + threadIdx.x;
+        const int p = q < npairs ? w.pair_order[q] : npairs;
         int code = 0;
         v3 pA, pB, n;
         float pen = 0.f;
@@ -1288,6 +1325,10 @@ void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float thresh
 
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
     (void)tile;
+    cudaMemsetAsync(w.pair_kind, 0, sizeof(int) * 64, s);
+    k_pair_hist<<<nsm * 4, 256, 0, s>>>(w);
+    k_pair_offsets<<<1, 1, 0, s>>>(w);
+    k_pair_scatter<<<nsm * 4, 256, 0, s>>>(w);
     k_mpr<<<nsm * 8, 256, 0, s>>>(w);
     k_epa<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w);
     k_manifold<<<nsm * 16, 128, 0, s>>>(w, p);

@@ -143,6 +143,8 @@ struct WorldDev {
     int* node_flag;
     float4* scene_box;           // [0] min, [1] max (reduction)
     int2* pairs;
+    int* pair_order;             // [cap_pairs] pair indices grouped by the two shapes' kinds
+    int* pair_kind;              // [2 * 64] counts, then cursors, per kind combination
     // narrowphase: overlapping pairs from the MPR stage, then the contact stream
     int2* col_pair;              // [cap_arb] pair index, MPR code (1 final, 2 needs EPA)
     float4* col_res;             // [3 * cap_arb] MPR result in A's frame: pA, pB, normal|depth
