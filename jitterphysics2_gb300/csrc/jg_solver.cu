@@ -109,8 +109,9 @@ __device__ __forceinline__ void prepare_contact(const ArbStore& A, int i, int mo
 }
 
 // Contact.Iterate (Contact.cs:931-1018) on one contact row held in registers; returns the
-// new accumulated impulses (with the tangent-2 mass) and adds the squared impulse change
-// and squared impulse to d2, l2 for the residual metric.
+// new accumulated impulses (with the tangent-2 mass) and, with kResid, adds the squared
+// impulse change and squared impulse to d2, l2 for the residual metric.
+template <bool kResid = true>
 __device__ __forceinline__ float4 iterate_row(float4 cn, float4 ct1, float4 ct2, float4 cr1, float4 cr2, float4 ca, int mode,
                                               float friction, LBody& b1, LBody& b2, bool apply_bias, float& d2, float& l2) {
     float mN = cr1.w, mT1 = cr2.w, mT2 = ca.w;
@@ -140,8 +141,10 @@ __device__ __forceinline__ float4 iterate_row(float4 cn, float4 ct1, float4 ct2,
     aT2 = oldT2 + ti2;
     aT2 = fminf(fmaxf(aT2, -maxT), maxT);
     ti2 = aT2 - oldT2;
-    d2 += ni * ni + ti1 * ti1 + ti2 * ti2;
-    l2 += aN * aN + aT1 * aT1 + aT2 * aT2;
+    if (kResid) {
+        d2 += ni * ni + ti1 * ti1 + ti2 * ti2;
+        l2 += aN * aN + aT1 * aT1 + aT2 * aT2;
+    }
     v3 imp = ni * n;
     imp = imp + ti1 * t1;
     imp = imp + ti2 * t2;
@@ -377,16 +380,69 @@ __device__ __forceinline__ LBody fixed_body(float4 v, float4 wv) {
 
 enum { PASS_PREPARE = 0, PASS_ITERATE = 1, PASS_RELAX = 2 };
 
+// Iterate / relax colours of one task (its bodies already staged or in flight).
+template <bool kResid>
+__device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStore& A, int4 T, int nc, const int* tc,
+                                                bool bias, float4* sbody, float4* ring, float& d2, float& l2) {
+    const int cap = w.cap_arb, bs = blockDim.x, tid = threadIdx.x;
+    // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order),
+    // so consecutive colours are spread over different threads.  Each thread keeps
+    // its next JG_TASK_RING arbiters in flight (one cp.async group per arbiter, empty
+    // groups past the end keep the count uniform): the ring holds bs * JG_TASK_RING
+    // arbiters, several colours ahead of the one being solved.
+    const int n = T.y;
+    for (int m = 0; m < JG_TASK_RING; m++) {
+        int j = m * bs + tid;
+        if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap, A.info[T.x + j].x);
+        cp_async_commit();
+    }
+    cp_async_wait_bodies();  // this thread's body copies have landed
+    __syncthreads();         // ... and everyone's
+    int m = 0;  // next owned arbiter: j = m * bs + tid
+    for (int c = 0; c < nc; c++) {
+        const int cend = tc[c + 1];
+        for (; m * bs + tid < cend; m++) {
+            const int j = m * bs + tid, d = T.x + j;
+            float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
+            // usage of the arbiter this slot is refilled with, loaded now and used after
+            // the compute below, so its latency stays off the critical path
+            const int jn = j + JG_TASK_RING * bs;
+            const int un = jn < n ? __ldg(&A.info[T.x + jn].x) : 0;
+            cp_async_wait_ring();
+            float4 r0 = r[0], r1 = r[1];
+            int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
+            int l1 = __float_as_int(r1.x), l2s = __float_as_int(r1.y);
+            float fr = r[2].x;
+            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1) : fixed_body(r[3], r[4]);
+            LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s) : fixed_body(r[3], r[4]);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (!(usage & (1 << k))) continue;
+                const float4* q = r + 5 + 6 * k;
+                A.cacc[k * cap + d] = iterate_row<kResid>(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
+            }
+            if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, b1);
+            if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, b2);
+            // refill the slot just consumed (its values are in registers by now)
+            if (jn < n) stage_arbiter(r, A, T.x + jn, cap, un);
+            cp_async_commit();
+        }
+        __syncthreads();
+    }
+}
+
 // One task in one pass: bodies staged into shared memory, colours in order with a block
 // barrier between them, bodies written back.  Iterations stage each (colour, chunk) step's
 // rows with cp.async while the previous step computes.
 __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind,
-                                         float4* sbody, float4* ring, float& d2, float& l2) {
+                                         float4* sbody, float4* ring, int* tc, float& d2, float& l2) {
     const int4 T = w.sc_task[t];
     const int nc = w.sc_tnc[t];
-    const int* tc = w.sc_tcol + t * (JG_TASK_MAXC + 1);
     const int cap = w.cap_arb;
     const int bs = blockDim.x, tid = threadIdx.x;
+    // the task's colour boundaries, read once into shared memory (visible after the
+    // barrier that follows the body staging)
+    for (int c = tid; c <= nc; c += bs) tc[c] = w.sc_tcol[t * (JG_TASK_MAXC + 1) + c];
     // the task's bodies, one cp.async group per thread (the arbiter ring, in iterations,
     // follows as later groups so that both loads are in flight together)
     for (int i = tid; i < T.w; i += bs) {
@@ -418,51 +474,10 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
             __syncthreads();
         }
     } else if (nc > 0) {
-        const bool bias = kind == PASS_ITERATE;
-        // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order),
-        // so consecutive colours are spread over different threads.  Each thread keeps
-        // its next JG_TASK_RING arbiters in flight (one cp.async group per arbiter, empty
-        // groups past the end keep the count uniform): the ring holds bs * JG_TASK_RING
-        // arbiters, several colours ahead of the one being solved.
-        const int n = T.y;
-        for (int m = 0; m < JG_TASK_RING; m++) {
-            int j = m * bs + tid;
-            if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap, A.info[T.x + j].x);
-            cp_async_commit();
-        }
-        cp_async_wait_bodies();  // this thread's body copies have landed
-        __syncthreads();         // ... and everyone's
-        int m = 0;  // next owned arbiter: j = m * bs + tid
-        for (int c = 0; c < nc; c++) {
-            const int cend = tc[c + 1];
-            for (; m * bs + tid < cend; m++) {
-                const int j = m * bs + tid, d = T.x + j;
-                float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
-                // usage of the arbiter this slot is refilled with, loaded now and used after
-                // the compute below, so its latency stays off the critical path
-                const int jn = j + JG_TASK_RING * bs;
-                const int un = jn < n ? __ldg(&A.info[T.x + jn].x) : 0;
-                cp_async_wait_ring();
-                float4 r0 = r[0], r1 = r[1];
-                int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
-                int l1 = __float_as_int(r1.x), l2s = __float_as_int(r1.y);
-                float fr = r[2].x;
-                LBody b1 = l1 >= 0 ? sbody_load(sbody, l1) : fixed_body(r[3], r[4]);
-                LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s) : fixed_body(r[3], r[4]);
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (!(usage & (1 << k))) continue;
-                    const float4* q = r + 5 + 6 * k;
-                    A.cacc[k * cap + d] = iterate_row(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
-                }
-                if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, b1);
-                if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, b2);
-                // refill the slot just consumed (its values are in registers by now)
-                if (jn < n) stage_arbiter(r, A, T.x + jn, cap, un);
-                cp_async_commit();
-            }
-            __syncthreads();
-        }
+        if (sp.record_residual)
+            iterate_colours<true>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, ring, d2, l2);
+        else
+            iterate_colours<false>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, ring, d2, l2);
     }
     cp_async_wait_0();  // no copy into shared memory outlives the task
     __syncthreads();
@@ -480,6 +495,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     extern __shared__ float4 solve_smem[];
     float4* sbody = solve_smem;
     float4* ring = solve_smem + 4 * sp.task_maxb;
+    __shared__ int s_tc[JG_TASK_MAXC + 1];
     const ArbStore& A = w.arb[w.cur];
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int* status = &w.ctr->status;
@@ -496,7 +512,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
             for (int g = 0; g < JG_SCHED_GRIDS; g++) {
                 if (ntask[g] == 0) continue;
                 for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x)
-                    run_task(w, A, sp, t, kind, sbody, ring, d2, l2);
+                    run_task(w, A, sp, t, kind, sbody, ring, s_tc, d2, l2);
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }
             if (!remainder_pass(w, A, sp, pass == 0 ? 0 : 1, !relax, !relax, tid, nth, d2, l2)) return;
@@ -597,7 +613,7 @@ int jg_solver_task_maxb(int block, int ctas_per_sm) {
     if (ctas_per_sm < 1) ctas_per_sm = 1;
     long long avail = std::min<long long>(pb, psm / ctas_per_sm - 1024);
     long long ring = (long long)JG_TASK_RING * block * JG_TASK_STAGE_F4 * 16;
-    long long m = (avail - ring - 256) / 64;
+    long long m = (avail - ring - (JG_TASK_MAXC + 1) * 4 - 256) / 64;  // minus the static shared memory
     if (m > 4096) m = 4096;
     return m > 0 ? (int)m : 0;
 }

@@ -16,6 +16,12 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v) {
     unsigned old;
     asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
@@ -35,17 +41,23 @@ __device__ __forceinline__ bool grid_sync(unsigned* count, unsigned* gen, int* s
         __threadfence();
         unsigned old = atom_add_release(count, 1u);
         unsigned target = (old / gridDim.x + 1) * gridDim.x;
-        // about 2^21 polls (well over a second), far above any legitimate wait
+        // Polls are spaced by a short sleep: back-to-back polls from every block saturate
+        // the L2 slice that holds the counter, which delays the arrivals and every other
+        // access that maps to that slice.  The wait gives up after one second (or 2^22
+        // polls), far above any legitimate wait.
+        const unsigned long long t0 = globaltimer_ns();
         unsigned spins = 0;
         while ((int)(ld_acquire(count) - target) < 0) {
             ++spins;
-            if ((spins & 63) == 0 && ld_relaxed_int(status) == JG_ERR_TIMEOUT) { ok = 0; break; }
-            if (spins > (1u << 21)) {
-                atomicCAS(status, 0, JG_ERR_TIMEOUT);
-                ok = 0;
-                break;
+            if ((spins & 63) == 0) {
+                if (ld_relaxed_int(status) == JG_ERR_TIMEOUT) { ok = 0; break; }
+                if (globaltimer_ns() - t0 > 1000000000ull || spins > (1u << 22)) {
+                    atomicCAS(status, 0, JG_ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
             }
-            if (spins > 4096) __nanosleep(64);
+            __nanosleep(spins < 4 ? 20 : 80);
         }
         ok_flag = ok;
     }
