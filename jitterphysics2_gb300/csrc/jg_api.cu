@@ -103,6 +103,7 @@ int allocate(jg_world* w) {
     int rs_blocks = (d.cap_shapes + 2047) / 2048;
     DA(d.hist, std::max(256 * rs_blocks + 1, 8192));
     DA(d.node, d.cap_shapes); DA(d.node_range, d.cap_shapes); DA(d.nmin, d.cap_shapes); DA(d.nmax, d.cap_shapes);
+    DA(d.cbox, 4 * (size_t)d.cap_shapes);
     DA(d.leaf_parent, d.cap_shapes); DA(d.node_parent, d.cap_shapes); DA(d.node_flag, d.cap_shapes);
     DA(d.scene_box, 2);
     DA(d.pairs, d.cap_pairs);

@@ -217,12 +217,24 @@ __global__ void k_refit(WorldDev w, int n) {
         if (atomicAdd(&w.node_flag[p], 1) == 0) return;
         int4 nd = w.node[p];
         float4 lmn, lmx, rmn, rmx;
-        if (nd.x < 0) { int s = w.midx[~nd.x]; lmn = w.amin[s]; lmx = w.amax[s]; }
-        else { lmn = __ldcg(&w.nmin[nd.x]); lmx = __ldcg(&w.nmax[nd.x]); }
-        if (nd.y < 0) { int s = w.midx[~nd.y]; rmn = w.amin[s]; rmx = w.amax[s]; }
-        else { rmn = __ldcg(&w.nmin[nd.y]); rmx = __ldcg(&w.nmax[nd.y]); }
+        int lcode, rcode;
+        if (nd.x < 0) { int s = w.midx[~nd.x]; lmn = w.amin[s]; lmx = w.amax[s]; lcode = ~s; }
+        else { lmn = __ldcg(&w.nmin[nd.x]); lmx = __ldcg(&w.nmax[nd.x]); lcode = nd.x; }
+        if (nd.y < 0) { int s = w.midx[~nd.y]; rmn = w.amin[s]; rmx = w.amax[s]; rcode = ~s; }
+        else { rmn = __ldcg(&w.nmin[nd.y]); rmx = __ldcg(&w.nmax[nd.y]); rcode = nd.y; }
         __stcg(&w.nmin[p], make_float4(fminf(lmn.x, rmn.x), fminf(lmn.y, rmn.y), fminf(lmn.z, rmn.z), 0.f));
         __stcg(&w.nmax[p], make_float4(fmaxf(lmx.x, rmx.x), fmaxf(lmx.y, rmx.y), fmaxf(lmx.z, rmx.z), 0.f));
+        // both children's boxes in the parent, for the traversal (one 64-byte read per node)
+        int lw = 0, rw = 0;
+        if (w.nworlds > 1 && w.nworlds <= 65536) {
+            if (nd.x >= 0) { int2 rg = w.node_range[nd.x]; lw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16); }
+            if (nd.y >= 0) { int2 rg = w.node_range[nd.y]; rw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16); }
+        }
+        float4* cb = w.cbox + 4 * (size_t)p;
+        cb[0] = make_float4(lmn.x, lmn.y, lmn.z, __int_as_float(lcode));
+        cb[1] = make_float4(lmx.x, lmx.y, lmx.z, __int_as_float(lw));
+        cb[2] = make_float4(rmn.x, rmn.y, rmn.z, __int_as_float(rcode));
+        cb[3] = make_float4(rmx.x, rmx.y, rmx.z, __int_as_float(rw));
         p = w.node_parent[p];
     }
 }
@@ -260,18 +272,20 @@ __global__ void k_traverse(WorldDev w, int n) {
     int sp = 0;
     int node = 0;
     if (n == 1) return;
+    const bool packed_worlds = w.nworlds <= 65536;
     while (true) {
-        int4 nd = w.node[node];
-        int ch[2] = {nd.x, nd.y};
+        // both children's boxes, stored in the node by k_refit
+        const float4* cb = w.cbox + 4 * (size_t)node;
+        const float4 box[4] = {__ldg(cb), __ldg(cb + 1), __ldg(cb + 2), __ldg(cb + 3)};
         int push_cnt = 0;
         int next_nodes[2];
         for (int c = 0; c < 2; c++) {
-            int cidx = ch[c];
+            const float4 bmn = box[2 * c], bmx = box[2 * c + 1];
+            const int cidx = __float_as_int(bmn.w);
+            if (!overlap(qmn, qmx, bmn, bmx)) continue;
             if (cidx < 0) {
-                int lj = ~cidx;
-                int sb = w.midx[lj];
+                int sb = ~cidx;
                 if (sb == sa) continue;
-                if (!overlap(qmn, qmx, w.amin[sb], w.amax[sb])) continue;
                 int4 sib = w.sinfo[sb];
                 if (sib.y == sia.y) continue;
                 int4 bib = w.binfo[sib.y];
@@ -283,11 +297,16 @@ __global__ void k_traverse(WorldDev w, int n) {
                 if (nbuf == PAIR_BUF) flush_pairs(w, buf, nbuf);
             } else {
                 if (w.nworlds > 1) {  // subtrees hold one world range (the world id leads the Morton key)
-                    int2 rg = w.node_range[cidx];
-                    int wf = (int)(w.mkey[rg.x] >> 32), wl = (int)(w.mkey[rg.y] >> 32);
+                    int wf, wl;
+                    if (packed_worlds) {
+                        const int wr = __float_as_int(bmx.w);
+                        wf = wr & 0xffff; wl = (wr >> 16) & 0xffff;
+                    } else {
+                        int2 rg = w.node_range[cidx];
+                        wf = (int)(w.mkey[rg.x] >> 32); wl = (int)(w.mkey[rg.y] >> 32);
+                    }
                     if (world < wf || world > wl) continue;
                 }
-                if (!overlap(qmn, qmx, w.nmin[cidx], w.nmax[cidx])) continue;
                 next_nodes[push_cnt++] = cidx;
             }
         }

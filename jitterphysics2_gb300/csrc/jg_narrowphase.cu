@@ -1332,5 +1332,5 @@ void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int
     k_mpr<<<nsm * 8, 256, 0, s>>>(w);
     k_epa<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w);
     k_manifold<<<nsm * 16, 128, 0, s>>>(w, p);
-    k_edge<<<nsm * 2, NP_WARPS * 32, 0, s>>>(w, p);
+    k_edge<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w, p);
 }

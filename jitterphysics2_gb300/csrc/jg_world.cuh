@@ -138,6 +138,10 @@ struct WorldDev {
     int4* node;                  // internal nodes: left, right, parent, first|last packed
     int2* node_range;            // leaf range [first, last] per internal node
     float4 *nmin, *nmax;         // internal node AABBs
+    float4* cbox;                // [4 * cap_shapes] per internal node, both children's boxes:
+                                 // left min|code, left max|worlds, right min|code, right max|worlds
+                                 // (code: internal child index, or ~shape for a leaf; worlds:
+                                 // first | last << 16 of an internal child's subtree)
     int* leaf_parent;
     int* node_parent;            // parent of each internal node (-1 for the root)
     int* node_flag;
