@@ -87,6 +87,10 @@ int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
 int allocate(jg_world* w) {
     WorldDev& d = w->d;
     const jg_world_params& p = w->prm;
+    if (p.max_bodies >= (1 << 29)) {  // the broadphase packs a body id into 29 bits
+        g_err = "max_bodies must be below 2^29";
+        return JG_ERR_INVALID_ARG;
+    }
     d.cap_bodies = std::max(p.max_bodies, 16);
     d.cap_shapes = std::max(p.max_shapes, 16);
     d.cap_pairs = std::max(p.max_pairs, 1024);

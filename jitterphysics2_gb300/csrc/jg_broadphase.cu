@@ -208,6 +208,15 @@ __global__ void k_build_init(WorldDev w, int n) {
     if (i < n - 1) { w.node_parent[i] = -1; w.node_flag[i] = 0; }
 }
 
+// A leaf's body id with its motion and activity, stored beside the leaf's box:
+// body | dynamic << 30 | active << 29.
+constexpr int LEAF_DYN = 1 << 30, LEAF_ACTIVE = 1 << 29, LEAF_BODY = (1 << 29) - 1;
+__device__ __forceinline__ int leaf_word(const WorldDev& w, int shape) {
+    const int body = w.sinfo[shape].y;
+    const int4 bi = w.binfo[body];
+    return body | (bi.x == JG_MOTION_DYNAMIC ? LEAF_DYN : 0) | ((bi.y & JG_BODY_ACTIVE) ? LEAF_ACTIVE : 0);
+}
+
 __global__ void k_refit(WorldDev w, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -226,9 +235,15 @@ __global__ void k_refit(WorldDev w, int n) {
         __stcg(&w.nmax[p], make_float4(fmaxf(lmx.x, rmx.x), fmaxf(lmx.y, rmx.y), fmaxf(lmx.z, rmx.z), 0.f));
         // both children's boxes in the parent, for the traversal (one 64-byte read per node)
         int lw = 0, rw = 0;
-        if (w.nworlds > 1 && w.nworlds <= 65536) {
-            if (nd.x >= 0) { int2 rg = w.node_range[nd.x]; lw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16); }
-            if (nd.y >= 0) { int2 rg = w.node_range[nd.y]; rw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16); }
+        if (nd.x < 0) lw = leaf_word(w, ~lcode);
+        else if (w.nworlds > 1 && w.nworlds <= 65536) {
+            int2 rg = w.node_range[nd.x];
+            lw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16);
+        }
+        if (nd.y < 0) rw = leaf_word(w, ~rcode);
+        else if (w.nworlds > 1 && w.nworlds <= 65536) {
+            int2 rg = w.node_range[nd.y];
+            rw = (int)(w.mkey[rg.x] >> 32) | ((int)(w.mkey[rg.y] >> 32) << 16);
         }
         float4* cb = w.cbox + 4 * (size_t)p;
         cb[0] = make_float4(lmn.x, lmn.y, lmn.z, __int_as_float(lcode));
@@ -286,13 +301,13 @@ __global__ void k_traverse(WorldDev w, int n) {
             if (cidx < 0) {
                 int sb = ~cidx;
                 if (sb == sa) continue;
-                int4 sib = w.sinfo[sb];
-                if (sib.y == sia.y) continue;
-                int4 bib = w.binfo[sib.y];
-                if (bib.z != world) continue;
-                bool dyn_b = bib.x == JG_MOTION_DYNAMIC;
+                const int lf = __float_as_int(bmx.w);  // body, dynamic, active of the leaf
+                const int body_b = lf & LEAF_BODY;
+                if (body_b == sia.y) continue;
+                if (w.nworlds > 1 && w.binfo[body_b].z != world) continue;
+                const bool dyn_b = (lf & LEAF_DYN) != 0;
                 if (dyn_b && sb < sa) continue;            // each dynamic pair once
-                if (!act_a && (bib.y & JG_BODY_ACTIVE) == 0) continue;
+                if (!act_a && (lf & LEAF_ACTIVE) == 0) continue;
                 buf[nbuf++] = make_int2(min(sa, sb), max(sa, sb));
                 if (nbuf == PAIR_BUF) flush_pairs(w, buf, nbuf);
             } else {
