@@ -224,6 +224,8 @@ __global__ void __launch_bounds__(1024) k_sched_tasks(WorldDev w, StepParams sp)
                 if (ok2) {
                     w.sc_task[t + idx.x] = make_int4(aoff + offs.x, ac, boff + offs.y, bc);
                     w.sc_cursor[t + idx.x] = 0;
+                    w.sc_tcell[t + idx.x] = cell;
+                    w.sc_done[t + idx.x] = 0u;
                 }
             }
             over += __syncthreads_count(ac > 0 && !ok2);
@@ -252,6 +254,34 @@ __global__ void k_sched_scatter(WorldDev w) {
         if (t < 0) { w.sc_arb[a] = make_int2(3, -1); continue; }
         int p = atomicAdd(&w.sc_cursor[t], 1);
         w.sc_tlist[w.sc_task[t].x + p] = a;
+    }
+    // Dependencies of each task on the two grid phases before it (grids g - 1 and g - 2,
+    // wrapping to the previous pass): the tasks of those grids that may share a body with
+    // it.  A body in cell ix of grid g (offset g/3) lies in cell ix - 1 or ix of a grid with
+    // a smaller offset and in ix or ix + 1 of one with a larger offset, in each axis, so at
+    // most four tasks per grid.  Both grids are needed: a body's cell in the phase just
+    // before may hold no task, and then only the direct wait orders the accesses.
+    const SchedInfo& S = *w.sc;
+    for (int t = tid; t < S.ntasks; t += nth) {
+        int g = 0;
+        while (g + 1 < JG_SCHED_GRIDS && t >= S.task_base[g + 1]) g++;
+        for (int back = 1; back <= 2; back++) {
+            int4 dep = make_int4(-1, -1, -1, -1);
+            if (w.nworlds <= 1) {
+                const int gp = (g + JG_SCHED_GRIDS - back) % JG_SCHED_GRIDS;
+                const int c = w.sc_tcell[t], ix = c % S.ncx, iz = c / S.ncx;
+                const int d0 = gp > g ? 0 : -1;
+                int k = 0;
+                for (int dz = d0; dz <= d0 + 1; dz++)
+                    for (int dx = d0; dx <= d0 + 1; dx++) {
+                        const int jx = min(max(ix + dx, 0), S.ncx - 1), jz = min(max(iz + dz, 0), S.ncz - 1);
+                        const int n = w.sc_task_of[gp * JG_SCHED_MAXCELLS + jz * S.ncx + jx];
+                        if (n < 0 || n == dep.x || n == dep.y || n == dep.z) continue;
+                        (&dep.x)[k++] = n;
+                    }
+            }
+            w.sc_tdep[2 * t + back - 1] = dep;
+        }
     }
     for (int b = tid; b < w.nb; b += nth) {
         for (int g = 0; g < JG_SCHED_GRIDS; g++) {

@@ -489,6 +489,53 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
     __syncthreads();
 }
 
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// Waits until the tasks of the two grid phases before this one that may share a body with
+// task t have completed them (phase level - 1, counter >= level; phase level - 2, counter
+// >= level - 1) and task t its previous pass (counter >= level - 2); with these the last
+// earlier access to each of t's bodies is finished.  False after about a second
+// (JG_ERR_TIMEOUT recorded), or when another block has recorded a timeout.
+__device__ __forceinline__ bool wait_deps(const WorldDev& w, int t, unsigned level, int* status) {
+    __shared__ int dep_ok;
+    if (threadIdx.x < 32) {  // warp 0: one dependency per lane, polled together
+        const int lane = threadIdx.x;
+        // lanes 0-3: grid phase level - 1; 4-7: level - 2; 8: the task itself, whose
+        // previous pass (level - 3) another block may have run
+        int n = -1;
+        unsigned need = 0;
+        if (lane < 8) {
+            const int4 dep = w.sc_tdep[2 * t + (lane >> 2)];
+            n = (&dep.x)[lane & 3];
+            need = lane < 4 ? level : level - 1;
+            if (lane >= 4 && level < 2) n = -1;
+        } else if (lane == 8 && level >= 3) {
+            n = t;
+            need = level - 2;
+        }
+        const unsigned long long t0 = globaltimer_ns();
+        int ok = 1;
+        for (unsigned spins = 0;; ++spins) {
+            const bool ready = n < 0 || (int)(ld_acquire(&w.sc_done[n]) - need) >= 0;
+            if (__all_sync(0xffffffffu, ready)) break;
+            if ((spins & 63) == 63) {
+                int bad = 0;
+                if (lane == 0) {
+                    if (ld_relaxed_int(status) == JG_ERR_TIMEOUT) bad = 1;
+                    else if (globaltimer_ns() - t0 > 1000000000ull) { atomicCAS(status, 0, JG_ERR_TIMEOUT); bad = 1; }
+                }
+                if (__shfl_sync(0xffffffffu, bad, 0)) { ok = 0; break; }
+            }
+            __nanosleep(spins < 4 ? 20 : 80);
+        }
+        if (lane == 0) dep_ok = ok;
+    }
+    __syncthreads();
+    return dep_ok != 0;
+}
+
 // Partitioned solve: the schedule's three grids run as three phases of tasks per pass,
 // then the remainder in global colours; integration phases are grid-stride.
 __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
@@ -501,10 +548,51 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     int* status = &w.ctr->status;
     int ntask[JG_SCHED_GRIDS], tbase[JG_SCHED_GRIDS];
     for (int g = 0; g < JG_SCHED_GRIDS; g++) { ntask[g] = w.sc->ntask[g]; tbase[g] = w.sc->task_base[g]; }
+    const int ntasks = ntask[0] + ntask[1] + ntask[2];
+    const int npass = 1 + sp.iterations + sp.relax;
+    // With no remainder, consecutive grid phases hand off task by task instead of waiting at
+    // a grid barrier: a task waits only for the tasks of the two phases before it that may
+    // share its bodies (their completion counters), so a slow task delays its neighbours,
+    // not the whole pass.  Grid barriers stay around the whole-body integration steps.
+    // Every block runs its tasks in phase order and each awaited task belongs to an earlier
+    // phase, so the waits end.
+    if (w.ctr->ncolors == 0) {
+        unsigned level = 0;  // grid phases started so far in this launch
+        for (int s = 0; s < sp.substeps; s++) {
+            integrate_forces_all(w, tid, nth);
+            if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
+            for (int pass = 0; pass < npass; pass++) {
+                const bool relax = pass > sp.iterations;
+                const int kind = pass == 0 ? PASS_PREPARE : (relax ? PASS_RELAX : PASS_ITERATE);
+                float d2 = 0.f, l2 = 0.f;
+                for (int g = 0; g < JG_SCHED_GRIDS; g++, level++) {
+                    for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x) {
+                        if (!wait_deps(w, t, level, status)) return;
+                        run_task(w, A, sp, t, kind, sbody, ring, s_tc, d2, l2);
+                        if (threadIdx.x == 0) {  // run_task ended with a block barrier
+                            __threadfence();
+                            st_release_u32(&w.sc_done[t], level + 1);
+                        }
+                    }
+                }
+                if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= 64)
+                    block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
+                if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
+                    if (!grid_sync(w.bar_count, w.bar_gen, status)) return;  // every task of the pass
+                    if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
+                    integrate_velocities_all(w, sp, tid, nth);
+                    if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
+                }
+            }
+            if (!grid_sync(w.bar_count, w.bar_gen, status)) return;  // before the next IntegrateForces
+        }
+        return;
+    }
+    // With a remainder: the three grids as three phases per pass with a grid barrier after
+    // each, then the remainder in global colours.
     for (int s = 0; s < sp.substeps; s++) {
         integrate_forces_all(w, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
-        const int npass = 1 + sp.iterations + sp.relax;
         for (int pass = 0; pass < npass; pass++) {
             const bool relax = pass > sp.iterations;
             const int kind = pass == 0 ? PASS_PREPARE : (relax ? PASS_RELAX : PASS_ITERATE);

@@ -196,6 +196,9 @@ struct WorldDev {
     int4* sc_task;               // [MAXTASKS] arbiter offset, count, body offset, count
     int* sc_cursor;              // [MAXTASKS]
     int* sc_tnc;                 // [MAXTASKS] local colours of the task
+    int* sc_tcell;               // [MAXTASKS] cell of the task (in its grid)
+    int4* sc_tdep;               // [2 * MAXTASKS] tasks of the previous two grid phases sharing bodies (-1: none)
+    unsigned* sc_done;           // [MAXTASKS] levels (grid phases) the task has completed in the solve
     int* sc_tcol;                // [MAXTASKS * (MAXC + 1)] colour offsets inside the task
     int* sc_tlist;               // [cap_arb] arbiters of each task (pre-permute ids)
     int* sc_tbody;               // [3 * cap_bodies] bodies of each task
