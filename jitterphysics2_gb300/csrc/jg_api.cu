@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <chrono>
 #include <mutex>
+#include <climits>
 
 void jg_contacts_set_scratch(int2* created, int2* removed, int* remaining, int* dst_index);
 void jg_flip_store(WorldDev& w);
@@ -31,6 +32,10 @@ struct jg_world {
     cudaStream_t stream = nullptr;
     int device = 0, nsm = 0;
     DevCounters* h_ctr = nullptr;     // pinned
+    jg_body_desc* d_desc = nullptr;   // device copy of the body descriptors (last upload, updated by downloads)
+    jg_body_desc* d_stage = nullptr;  // an upload lands here and becomes d_desc once it is valid
+    int* d_bad = nullptr;             // first invalid body of an upload: index * 4 + reason
+    int* h_bad = nullptr;             // pinned
     int2 *ev_created = nullptr, *ev_removed = nullptr;
     int* remaining = nullptr;
     int* dst_index = nullptr;
@@ -146,6 +151,8 @@ int allocate(jg_world* w) {
     DA(w->ev_created, d.cap_arb); DA(w->ev_removed, d.cap_arb); DA(w->remaining, 2); DA(w->dst_index, d.cap_arb);
     CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));
     memset(w->h_ctr, 0, sizeof(DevCounters));
+    DA(w->d_desc, d.cap_bodies); DA(w->d_stage, d.cap_bodies); DA(w->d_bad, 1);
+    CK(cudaMallocHost((void**)&w->h_bad, sizeof(int)));
     return JG_OK;
 }
 
@@ -162,12 +169,12 @@ int ensure_tris(jg_world* w, int n) {
     return JG_OK;
 }
 
-bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+JG_HD bool finite3(const float* v) { return isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]); }
 float host_int_as_float(int i) { float f; memcpy(&f, &i, 4); return f; }
 int host_float_as_int(float f) { int i; memcpy(&i, &f, 4); return i; }
 
 // RigidBody.UpdateWorldInertia (RigidBody.cs:903-923) on the host, for uploads.
-void host_world_inertia(const jg_body_desc& b, float* i0, float* i1, float* imv) {
+JG_HD void body_world_inertia(const jg_body_desc& b, float* i0, float* i1, float* imv) {
     float x = b.orientation[0], y = b.orientation[1], z = b.orientation[2], ww = b.orientation[3];
     m33 R;
     R.m[0][0] = 1.0f - 2.0f * (y * y + z * z); R.m[0][1] = 2.0f * (x * y - z * ww); R.m[0][2] = 2.0f * (x * z + y * ww);
@@ -355,6 +362,7 @@ int jg_destroy(jg_world* w) {
     cudaFree(w->q_pairs); cudaFree(w->q_out); cudaFree(w->q_hit);
     jg_mlp_free(w->mlp);
     if (w->h_ctr) cudaFreeHost(w->h_ctr);
+    if (w->h_bad) cudaFreeHost(w->h_bad);
     for (int i = 0; i < 9; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
@@ -369,57 +377,111 @@ static void invalidate_graphs(jg_world* w) {
     }
 }
 
+}  // extern "C"
+
+namespace {
+
+// Body descriptors in and out through the device: one copy of the caller's array each
+// way, validation, conversion to the solver layout and the write-back of the state a step
+// changes run as kernels.  Reasons recorded in d_bad: 1 non-finite, 2 invalid argument;
+// the body with the smallest index wins, as a sequential check would report it.
+__global__ void k_bodies_check(const jg_body_desc* d, int n, int nworlds, int* bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const jg_body_desc& b = d[i];
+        int why = 0;
+        if (!finite3(b.position) || !finite3(b.velocity) || !finite3(b.angular_velocity) ||
+            !isfinite(b.orientation[3]) || !finite3(b.orientation) || !isfinite(b.inv_mass))
+            why = 1;
+        else if (b.motion_type < 0 || b.motion_type > 2 || b.world < 0 || b.world >= nworlds)
+            why = 2;
+        if (why) atomicMin(bad, i * 4 + why);
+    }
+}
+
+__global__ void k_bodies_in(const jg_body_desc* d, int n, WorldDev D, const int* bad) {
+    if (*bad != INT_MAX) return;  // an invalid body: the state stays as it was
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const jg_body_desc& b = d[i];
+        float i0[4], i1[2], imv[3];
+        body_world_inertia(b, i0, i1, imv);
+        int fl = 0;
+        if (b.motion_type == JG_MOTION_DYNAMIC) fl |= SB_DYNAMIC;
+        if (b.motion_type == JG_MOTION_DYNAMIC && ((b.flags >> 4) & 7)) fl |= SB_LINLOCK;
+        SBody sb;
+        sb.v = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], imv[0]);
+        sb.w = make_float4(b.angular_velocity[0], b.angular_velocity[1], b.angular_velocity[2], imv[1]);
+        sb.i0 = make_float4(i0[0], i0[1], i0[2], i0[3]);
+        sb.i1 = make_float4(i1[0], i1[1], imv[2], __int_as_float(fl));
+        D.body[i] = sb;
+        D.pos[i] = make_float4(b.position[0], b.position[1], b.position[2], 0.f);
+        D.q[i] = make_float4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
+        D.dv[i] = make_float4(b.delta_velocity[0], b.delta_velocity[1], b.delta_velocity[2], 0.f);
+        D.dw[i] = make_float4(b.delta_angular_velocity[0], b.delta_angular_velocity[1], b.delta_angular_velocity[2], 0.f);
+        D.il0[i] = make_float4(b.inv_inertia[0], b.inv_inertia[1], b.inv_inertia[2], b.inv_inertia[3]);
+        D.il1[i] = make_float4(b.inv_inertia[4], b.inv_inertia[5], b.inv_mass, 0.f);
+        D.force[i] = make_float4(b.force[0], b.force[1], b.force[2], 0.f);
+        D.torque[i] = make_float4(b.torque[0], b.torque[1], b.torque[2], 0.f);
+        D.mat[i] = make_float4(b.friction, b.restitution, b.linear_damping, b.angular_damping);
+        D.binfo[i] = make_int4(b.motion_type, b.flags, b.world, 0);
+    }
+}
+
+// The state a step changes, written over the stored descriptors (forces are cleared after
+// each step, RigidBody.cs:760).
+__global__ void k_bodies_out(jg_body_desc* d, int n, WorldDev D) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        jg_body_desc& o = d[i];
+        const float4 p = D.pos[i], q = D.q[i], v = D.body[i].v, av = D.body[i].w, dv = D.dv[i], dw = D.dw[i];
+        o.position[0] = p.x; o.position[1] = p.y; o.position[2] = p.z;
+        o.orientation[0] = q.x; o.orientation[1] = q.y; o.orientation[2] = q.z; o.orientation[3] = q.w;
+        o.velocity[0] = v.x; o.velocity[1] = v.y; o.velocity[2] = v.z;
+        o.angular_velocity[0] = av.x; o.angular_velocity[1] = av.y; o.angular_velocity[2] = av.z;
+        o.delta_velocity[0] = dv.x; o.delta_velocity[1] = dv.y; o.delta_velocity[2] = dv.z;
+        o.delta_angular_velocity[0] = dw.x; o.delta_angular_velocity[1] = dw.y; o.delta_angular_velocity[2] = dw.z;
+        o.force[0] = o.force[1] = o.force[2] = 0.f;
+        o.torque[0] = o.torque[1] = o.torque[2] = 0.f;
+    }
+}
+
+int upload_bodies_device(jg_world* w, const jg_body_desc* b, int32_t n) {
+    WorldDev& D = w->d;
+    cudaStream_t s = w->stream;
+    const int blocks = std::max(1, std::min((n + 255) / 256, w->nsm * 8));
+    const int none = INT_MAX;
+    CK(cudaMemcpyAsync(w->d_bad, &none, sizeof(int), cudaMemcpyHostToDevice, s));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(w->d_stage, b, sizeof(jg_body_desc) * n, cudaMemcpyHostToDevice, s));
+        k_bodies_check<<<blocks, 256, 0, s>>>(w->d_stage, n, w->nworlds, w->d_bad);
+        k_bodies_in<<<blocks, 256, 0, s>>>(w->d_stage, n, D, w->d_bad);
+    }
+    CK(cudaMemcpyAsync(w->h_bad, w->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (*w->h_bad != INT_MAX) return (*w->h_bad & 3) == 1 ? JG_ERR_NONFINITE : JG_ERR_INVALID_ARG;
+    std::swap(w->d_desc, w->d_stage);  // the accepted descriptors
+    if (D.nb != n) invalidate_graphs(w);
+    D.nb = n;
+    return JG_OK;
+}
+
+int download_bodies_device(jg_world* w, jg_body_desc* b, int32_t n) {
+    cudaStream_t s = w->stream;
+    if (n > 0) {
+        k_bodies_out<<<std::max(1, std::min((n + 255) / 256, w->nsm * 8)), 256, 0, s>>>(w->d_desc, n, w->d);
+        CK(cudaMemcpyAsync(b, w->d_desc, sizeof(jg_body_desc) * n, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return JG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int jg_upload_bodies(jg_world* w, const jg_body_desc* b, int32_t n) {
     if (!w || (!b && n > 0) || n < 0) return JG_ERR_INVALID_ARG;
     if (n > w->d.cap_bodies) return JG_ERR_CAPACITY;
-    std::vector<SBody> sb(n);
-    std::vector<float4> pos(n), q(n), dv(n), dw(n), il0(n), il1(n), force(n), torque(n), mat(n);
-    std::vector<int4> info(n);
-    int maxworld = 0;
-    for (int i = 0; i < n; i++) {
-        const jg_body_desc& d = b[i];
-        if (!finite3(d.position) || !finite3(d.velocity) || !finite3(d.angular_velocity) ||
-            !std::isfinite(d.orientation[3]) || !finite3(d.orientation) || !std::isfinite(d.inv_mass))
-            return JG_ERR_NONFINITE;
-        if (d.motion_type < 0 || d.motion_type > 2) return JG_ERR_INVALID_ARG;
-        if (d.world < 0 || d.world >= w->nworlds) return JG_ERR_INVALID_ARG;
-        maxworld = std::max(maxworld, d.world);
-        float i0[4], i1[2], imv[3];
-        host_world_inertia(d, i0, i1, imv);
-        int fl = 0;
-        if (d.motion_type == JG_MOTION_DYNAMIC) fl |= SB_DYNAMIC;
-        if (d.motion_type == JG_MOTION_DYNAMIC && ((d.flags >> 4) & 7)) fl |= SB_LINLOCK;
-        sb[i].v = make_float4(d.velocity[0], d.velocity[1], d.velocity[2], imv[0]);
-        sb[i].w = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], imv[1]);
-        sb[i].i0 = make_float4(i0[0], i0[1], i0[2], i0[3]);
-        sb[i].i1 = make_float4(i1[0], i1[1], imv[2], host_int_as_float(fl));
-        pos[i] = make_float4(d.position[0], d.position[1], d.position[2], 0.f);
-        q[i] = make_float4(d.orientation[0], d.orientation[1], d.orientation[2], d.orientation[3]);
-        dv[i] = make_float4(d.delta_velocity[0], d.delta_velocity[1], d.delta_velocity[2], 0.f);
-        dw[i] = make_float4(d.delta_angular_velocity[0], d.delta_angular_velocity[1], d.delta_angular_velocity[2], 0.f);
-        il0[i] = make_float4(d.inv_inertia[0], d.inv_inertia[1], d.inv_inertia[2], d.inv_inertia[3]);
-        il1[i] = make_float4(d.inv_inertia[4], d.inv_inertia[5], d.inv_mass, 0.f);
-        force[i] = make_float4(d.force[0], d.force[1], d.force[2], 0.f);
-        torque[i] = make_float4(d.torque[0], d.torque[1], d.torque[2], 0.f);
-        mat[i] = make_float4(d.friction, d.restitution, d.linear_damping, d.angular_damping);
-        info[i] = make_int4(d.motion_type, d.flags, d.world, 0);
-    }
-    WorldDev& D = w->d;
-    cudaStream_t s = w->stream;
-    CK(cudaMemcpyAsync(D.body, sb.data(), sizeof(SBody) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.pos, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.q, q.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.dv, dv.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.dw, dw.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.il0, il0.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.il1, il1.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.force, force.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.torque, torque.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.mat, mat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(D.binfo, info.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
-    if (D.nb != n) invalidate_graphs(w);
-    D.nb = n;
+    int r = upload_bodies_device(w, b, n);
+    if (r) return r;
     w->host_bodies.assign(b, b + n);
     w->host_current = true;
     return JG_OK;
@@ -427,29 +489,7 @@ int jg_upload_bodies(jg_world* w, const jg_body_desc* b, int32_t n) {
 
 int jg_download_bodies(jg_world* w, jg_body_desc* b, int32_t n) {
     if (!w || (!b && n > 0) || n < 0 || n > w->d.nb) return JG_ERR_INVALID_ARG;
-    WorldDev& D = w->d;
-    std::vector<SBody> sb(n);
-    std::vector<float4> pos(n), q(n), dv(n), dw(n);
-    cudaStream_t s = w->stream;
-    CK(cudaMemcpyAsync(sb.data(), D.body, sizeof(SBody) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(pos.data(), D.pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(q.data(), D.q, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(dv.data(), D.dv, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(dw.data(), D.dw, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    for (int i = 0; i < n; i++) {
-        jg_body_desc& o = b[i];
-        if (i < (int)w->host_bodies.size()) o = w->host_bodies[i];
-        o.position[0] = pos[i].x; o.position[1] = pos[i].y; o.position[2] = pos[i].z;
-        o.orientation[0] = q[i].x; o.orientation[1] = q[i].y; o.orientation[2] = q[i].z; o.orientation[3] = q[i].w;
-        o.velocity[0] = sb[i].v.x; o.velocity[1] = sb[i].v.y; o.velocity[2] = sb[i].v.z;
-        o.angular_velocity[0] = sb[i].w.x; o.angular_velocity[1] = sb[i].w.y; o.angular_velocity[2] = sb[i].w.z;
-        o.delta_velocity[0] = dv[i].x; o.delta_velocity[1] = dv[i].y; o.delta_velocity[2] = dv[i].z;
-        o.delta_angular_velocity[0] = dw[i].x; o.delta_angular_velocity[1] = dw[i].y; o.delta_angular_velocity[2] = dw[i].z;
-        o.force[0] = o.force[1] = o.force[2] = 0;
-        o.torque[0] = o.torque[1] = o.torque[2] = 0;
-    }
-    return JG_OK;
+    return download_bodies_device(w, b, n);
 }
 
 int jg_upload_shapes(jg_world* w, const jg_shape_desc* sh, int32_t n, const float* hull, int32_t nh,
@@ -639,11 +679,13 @@ int jg_batch_step(jg_world* w, float dt) { return jg_step(w, dt); }
 
 int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
     if (!w || !bodies || n != w->d.nb) return JG_ERR_INVALID_ARG;
-    int r = jg_upload_bodies(w, bodies, n);
+    // one copy of the caller's array each way; validation and conversion on the device
+    int r = upload_bodies_device(w, bodies, n);
     if (r) return r;
+    w->host_current = false;
     r = jg_step(w, dt);
     if (r) return r;
-    return jg_download_bodies(w, bodies, n);
+    return download_bodies_device(w, bodies, n);
 }
 
 int jg_get_constraints(jg_world* w, int32_t* keys, float* imp, int32_t cap, int32_t* count) {
