@@ -450,8 +450,22 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
         cp_async16(&sbody[4 * i], src); cp_async16(&sbody[4 * i + 1], src + 1);
         cp_async16(&sbody[4 * i + 2], src + 2); cp_async16(&sbody[4 * i + 3], src + 3);
     }
-    cp_async_commit();
+    // (the bodies' group: committed with the positions below in Prepare, here otherwise,
+    // so that the arbiter ring of the iterations follows as later groups)
+    if (kind != PASS_PREPARE) cp_async_commit();
     if (kind == PASS_PREPARE) {
+        // Prepare also needs the bodies' positions and orientations: staged into the
+        // arbiter ring, which Prepare does not use, when they fit
+        float4* spos = ring;
+        float4* sq = ring + T.w;
+        const bool staged = 2 * T.w <= JG_TASK_RING * bs * JG_TASK_STAGE_F4;
+        if (staged)
+            for (int i = tid; i < T.w; i += bs) {
+                const int b = w.sc_tbody[T.z + i];
+                cp_async16(&spos[i], &w.pos[b]);
+                cp_async16(&sq[i], &w.q[b]);
+            }
+        cp_async_commit();
         cp_async_wait_0();
         __syncthreads();
         for (int c = 0; c < nc; c++) {
@@ -464,8 +478,9 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
                 LBody b1 = ls.x >= 0 ? sbody_load(sbody, ls.x) : fixed_body(A.sv[d], A.sv[cap + d]);
                 LBody b2 = ls.y >= 0 ? sbody_load(sbody, ls.y) : fixed_body(A.sv[d], A.sv[cap + d]);
                 float spec = A.mat[d].z;
-                v3 pos1 = mk3(w.pos[bb.x]), pos2 = mk3(w.pos[bb.y]);
-                q4 q1 = mkq(w.q[bb.x]), q2 = mkq(w.q[bb.y]);
+                const bool s1 = staged && ls.x >= 0, s2 = staged && ls.y >= 0;
+                v3 pos1 = mk3(s1 ? spos[ls.x] : w.pos[bb.x]), pos2 = mk3(s2 ? spos[ls.y] : w.pos[bb.y]);
+                q4 q1 = mkq(s1 ? sq[ls.x] : w.q[bb.x]), q2 = mkq(s2 ? sq[ls.y] : w.q[bb.y]);
                 for (int k = 0; k < 4; k++)
                     if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
                 if ((mode & 3) && ls.x >= 0) sbody_store(sbody, ls.x, b1);
