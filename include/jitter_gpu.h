@@ -193,7 +193,11 @@ int jg_destroy(jg_world* world);
 
 /* ---- state upload / download -------------------------------------------------------- */
 
-/* World.CreateRigidBody + RigidBody setters (World.cs:930-965, RigidBody.cs:503-760). */
+/* World.CreateRigidBody + RigidBody setters (World.cs:930-965, RigidBody.cs:503-760).
+ * An upload with a non-finite body returns JG_ERR_NONFINITE, one with an invalid motion type
+ * or world JG_ERR_INVALID_ARG (the lowest-indexed invalid body decides), and leaves the
+ * world's state unchanged.  A download returns the last uploaded descriptors with the state a
+ * step changes (position, orientation, velocities, delta velocities; force and torque 0). */
 int jg_upload_bodies(jg_world* world, const jg_body_desc* bodies, int32_t count);
 int jg_download_bodies(jg_world* world, jg_body_desc* bodies, int32_t count);
 
@@ -221,7 +225,8 @@ int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body
 int jg_step(jg_world* world, float dt);
 
 /* Like jg_step but with the body state taken from and returned to host buffers
- * (copies included), the call a host that keeps its own bodies makes. */
+ * (copies included), the call a host that keeps its own bodies makes: one copy of the array
+ * each way (pinned memory copies fastest), validated as jg_upload_bodies does. */
 int jg_step_host(jg_world* world, float dt, jg_body_desc* bodies, int32_t count);
 
 /* ---- inspection ------------------------------------------------------------------------ */
