@@ -50,7 +50,7 @@ SETTLE_STEPS = 800
 SEED = 12347
 
 
-SOLVE_DRAM_BYTES = 1.234e9
+SOLVE_DRAM_BYTES = 0.645e9
 
 
 def peaks():
