@@ -20,7 +20,8 @@ colouring, substepped solve + integration, contact and body update.
           (C++ restatement of Jitter2, all host threads) on 2 steps of the same state
   fp64_error  one step from the timed state replayed by the FP64 oracle in the GPU's order
   learned_warm_start  the learned against the plain warm start on 50 towers + 49k rubble:
-          residual after 8 iterations, iterations to 1e-4 (cap 64), contacts/s of both
+          residual after 8 and 64 iterations, iterations to 1e-4 and 1e-3 (cap 2048),
+          contacts/s of both
 
 --config c1 | c2 | c4 | c5 runs the workload's other configurations (1000-box grid, 20k
 pile, 4096 batched worlds, towers + rubble) and prints their line; the default (c3, the
@@ -157,9 +158,9 @@ def cpu_baseline(scene, bodies, contacts, steps=2):
 def learned_section(eval_steps=10):
     """Learned against plain warm start on the towers-and-rubble workload (50 towers of
     20 unit boxes + 49k mixed rubble): training pairs collected from two seeds, the
-    network trained on the device, then from identical states one step each way with 64
-    iterations (iterations to residual 1e-4, residual after the 8 iterations the
-    workload uses) and the contact throughput of both at 8 iterations."""
+    network trained on the device, then from identical states one step each way with 2048
+    iterations (iterations to residual 1e-4 and 1e-3, residual after the 8 iterations the
+    workload uses and after 64) and the contact throughput of both at 8 iterations."""
     from jitterphysics2_gb300 import abi, learned, scenes
     from jitterphysics2_gb300.world import World, world_for_scene
     t0 = time.perf_counter()
@@ -176,7 +177,9 @@ def learned_section(eval_steps=10):
     params = trainer.mlp_export()
     trainer.close()
     sc = scenes.towers_rubble(seed=12349)
-    ip, il, rp, rl = learned.paired_residuals(sc, params, steps=eval_steps, settle=60, iterations=64)
+    cap = abi.RESID_MAX
+    ip, il, rp, rl = learned.paired_residuals(sc, params, steps=eval_steps, settle=60, iterations=cap)
+    to3 = lambda r: float(np.mean([learned.iterations_to(x, 1e-3) for x in r]))
     # contacts/s at the workload's 8 iterations, plain and learned, from the same state
     rates = {}
     plain = world_for_scene(sc)
@@ -200,7 +203,10 @@ def learned_section(eval_steps=10):
     return {"workload": "50 towers x 20 unit boxes + 49k mixed rubble, dt 1/100, 4 substeps",
             "training_pairs": int(len(X)), "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
             "iters_to_1e-4_plain": float(ip.mean()), "iters_to_1e-4_learned": float(il.mean()),
-            "iteration_cap": 64, "residual_after_8_plain": gm(rp[:, 7]), "residual_after_8_learned": gm(rl[:, 7]),
+            "iters_to_1e-3_plain": to3(rp), "iters_to_1e-3_learned": to3(rl),
+            "iteration_cap": cap, "residual_after_8_plain": gm(rp[:, 7]), "residual_after_8_learned": gm(rl[:, 7]),
+            "residual_after_64_plain": gm(rp[:, 63]), "residual_after_64_learned": gm(rl[:, 63]),
+            "residual_after_cap_plain": gm(rp[:, -1]), "residual_after_cap_learned": gm(rl[:, -1]),
             "contacts_per_s_plain": rates["plain"], "contacts_per_s_learned": rates["learned"],
             "steps_compared": eval_steps, "seconds": time.perf_counter() - t0}
 

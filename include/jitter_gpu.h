@@ -69,7 +69,7 @@ extern "C" {
 typedef struct jg_world_params {
     float   gravity[3];                 /* default (0,-9.81,0), World.cs:389           */
     int32_t substeps;                   /* SubstepCount, default 1                      */
-    int32_t solver_iterations;          /* SolverIterations.solver, default 6           */
+    int32_t solver_iterations;          /* SolverIterations.solver, default 6, at most 4096 */
     int32_t relax_iterations;           /* SolverIterations.relaxation, default 4       */
     int32_t enable_auxiliary_contacts;  /* EnableAuxiliaryContactPoints, default 1      */
     int32_t persistent_manifold;        /* PersistentContactManifold, default 1         */
@@ -271,7 +271,8 @@ int jg_get_constraints(jg_world* world, int32_t* order_keys, float* impulses, in
                        int32_t* out_count);
 int jg_get_counters(jg_world* world, jg_counters* out);
 int jg_get_timings(jg_world* world, jg_timings* out);
-/* Per-iteration residual of the first substep of the last step (record_residual=1):
+/* Per-iteration residual of the first substep of the last step (record_residual=1), for up
+ * to the first 2048 iterations:
  * r_k = |lambda_k - lambda_{k-1}| / max(|lambda_k|, 1e-12) over all contact rows. */
 int jg_get_residuals(jg_world* world, float* out, int32_t capacity, int32_t* out_count);
 

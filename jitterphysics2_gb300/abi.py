@@ -27,6 +27,7 @@ BODY_ACTIVE = 1 << 2
 BODY_GYROSCOPIC = 1 << 3
 BODY_LOCKS_SHIFT = 4
 BODY_NO_GRAVITY = 1 << 12
+RESID_MAX = 2048                # iterations whose residual a step records (jg_get_residuals)
 COLLIDE_NOALLOC_MAX_PAIRS = 16384  # JG_COLLIDE_NOALLOC_MAX_PAIRS
 MLP_IN, MLP_HID, MLP_OUT = 24, 64, 3
 MLP_NW = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_OUT * MLP_HID + MLP_OUT  # trainable

@@ -136,7 +136,7 @@ int allocate(jg_world* w) {
     DA(d.jorder, d.cap_joints + JG_MAX_COLORS);
     DA(d.joints, d.cap_joints);
     DA(d.bar_count, 2); d.bar_gen = d.bar_count + 1;
-    DA(d.resid, 2 * 64);
+    DA(d.resid, 2 * JG_RESID_MAX);
     DA(d.ctr, 1);
     // partitioned solve schedule
     DA(d.sc, 1);
@@ -239,7 +239,7 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     jg_contacts_set_scratch(w->ev_created, w->ev_removed, w->remaining, w->dst_index);
     if (timed) cudaEventRecord(w->ev[0], s);
     k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
-    if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 128, s);
+    if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 2 * JG_RESID_MAX, s);
     jg_launch_aabb(d, s);
     int passes = jg_launch_broadphase(d, s, w->nsm);
     // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
@@ -324,7 +324,7 @@ int jg_create(const jg_world_params* params, jg_world** out) {
     if (!params || !out) return JG_ERR_INVALID_ARG;
     *out = nullptr;
     if (params->substeps < 1 || params->solver_iterations < 1 || params->relax_iterations < 0) return JG_ERR_INVALID_ARG;
-    if (params->solver_iterations > 64) return JG_ERR_INVALID_ARG;
+    if (params->solver_iterations > 4096) return JG_ERR_INVALID_ARG;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) { g_err = "no CUDA device"; return JG_ERR_NOT_SUPPORTED; }
@@ -718,9 +718,9 @@ int jg_get_timings(jg_world* w, jg_timings* out) {
 
 int jg_get_residuals(jg_world* w, float* out, int32_t cap, int32_t* n) {
     if (!w || !out || !n) return JG_ERR_INVALID_ARG;
-    float h[128];
-    CK(cudaMemcpy(h, w->d.resid, sizeof(h), cudaMemcpyDeviceToHost));
-    int k = std::min(w->prm.solver_iterations, 64);
+    std::vector<float> h(2 * JG_RESID_MAX);
+    CK(cudaMemcpy(h.data(), w->d.resid, sizeof(float) * h.size(), cudaMemcpyDeviceToHost));
+    int k = std::min(w->prm.solver_iterations, JG_RESID_MAX);
     *n = k;
     for (int i = 0; i < k && i < cap; i++) out[i] = (float)(std::sqrt((double)h[2 * i]) / std::max(std::sqrt((double)h[2 * i + 1]), 1e-12));
     return JG_OK;

@@ -311,7 +311,7 @@ __global__ void k_solve(WorldDev w, StepParams sp) {
         for (int it = 0; it < 1 + sp.iterations; it++) {
             float d2 = 0.f, l2 = 0.f;
             if (!remainder_pass(w, A, sp, it == 0 ? 0 : 1, true, true, tid, nth, d2, l2)) return;
-            if (sp.record_residual && s == 0 && it > 0 && it <= 64) block_reduce_add(d2, l2, w.resid + 2 * (it - 1));
+            if (sp.record_residual && s == 0 && it > 0 && it <= JG_RESID_MAX) block_reduce_add(d2, l2, w.resid + 2 * (it - 1));
         }
         if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
         integrate_velocities_all(w, sp, tid, nth);
@@ -590,7 +590,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
                         }
                     }
                 }
-                if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= 64)
+                if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= JG_RESID_MAX)
                     block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
                 if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
                     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;  // every task of the pass
@@ -619,7 +619,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }
             if (!remainder_pass(w, A, sp, pass == 0 ? 0 : 1, !relax, !relax, tid, nth, d2, l2)) return;
-            if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= 64) block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
+            if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= JG_RESID_MAX) block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
             if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
                 if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
                 integrate_velocities_all(w, sp, tid, nth);

@@ -13,6 +13,7 @@
 #include "../../include/jitter_gpu.h"
 
 #define JG_MAX_COLORS 128
+#define JG_RESID_MAX 2048       // iterations whose residual a step records (record_residual)
 #define JG_HULL_MAX 64          // point-cloud vertices per shape handled on the device
 #define JG_EPA_MAXV 64          // EPA polytope capacity on the device (reference: 128/256)
 #define JG_EPA_MAXT 128

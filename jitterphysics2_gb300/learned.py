@@ -73,14 +73,18 @@ def iterations_to(resid, tol=1e-4):
 
 def paired_residuals(scene, params, steps, settle, iterations=32, tol=1e-4):
     """From the same state at each of `steps` steps (after `settle` steps of the plain
-    solver), one step with the plain (cached) warm start and one with the learned warm
-    start; returns the iterations to `tol` and the residual curves of both."""
+    solver at the scene's own iteration count), one step with the plain (cached) warm
+    start and one with the learned warm start, both with `iterations` iterations; returns
+    the iterations to `tol` and the residual curves of both."""
     kw = dict(record_residual=1, solver_iterations=iterations)
+    settler = world_for_scene(scene, warm_start_mode=abi.WARMSTART_CACHED)
+    for _ in range(settle):
+        settler.step(scene["dt"])
     plain = world_for_scene(scene, warm_start_mode=abi.WARMSTART_CACHED, **kw)
+    plain.import_state(settler.export_state())
+    settler.close()
     learned = world_for_scene(scene, warm_start_mode=abi.WARMSTART_MLP, **kw)
     learned.mlp_load(params)
-    for _ in range(settle):
-        plain.step(scene["dt"])
     it_plain, it_learned, r_plain, r_learned = [], [], [], []
     for _ in range(steps):
         state = plain.export_state()

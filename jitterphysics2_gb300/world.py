@@ -154,9 +154,9 @@ class World:
         return dict(zip(abi.TIMING_NAMES, buf.tolist()))
 
     def residuals(self):
-        buf = np.zeros(64, np.float32)
+        buf = np.zeros(abi.RESID_MAX, np.float32)
         n = ctypes.c_int32()
-        check(self._lib.jg_get_residuals(self._h, ptr(buf), 64, ctypes.byref(n)), "jg_get_residuals")
+        check(self._lib.jg_get_residuals(self._h, ptr(buf), abi.RESID_MAX, ctypes.byref(n)), "jg_get_residuals")
         return buf[:n.value].copy()
 
     def arbiter_events(self):
