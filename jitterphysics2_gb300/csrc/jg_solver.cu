@@ -355,8 +355,10 @@ __device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, in
     }
 }
 
-__device__ __forceinline__ LBody sbody_load(const float4* sb, int slot) {
-    float4 v = sb[4 * slot], wv = sb[4 * slot + 1], i0 = sb[4 * slot + 2], i1 = sb[4 * slot + 3];
+// Staged task bodies in shared memory as four arrays of `stride` float4 (v, w, i0, i1 of
+// SBody): random slots spread over all banks, where 64-byte records would meet in two.
+__device__ __forceinline__ LBody sbody_load(const float4* sb, int slot, int stride) {
+    float4 v = sb[slot], wv = sb[stride + slot], i0 = sb[2 * stride + slot], i1 = sb[3 * stride + slot];
     LBody b;
     b.v = mk3(v); b.w = mk3(wv);
     b.im = mk3(v.w, wv.w, i1.z);
@@ -364,9 +366,9 @@ __device__ __forceinline__ LBody sbody_load(const float4* sb, int slot) {
     b.flags = __float_as_int(i1.w);
     return b;
 }
-__device__ __forceinline__ void sbody_store(float4* sb, int slot, const LBody& b) {
-    sb[4 * slot] = f4(b.v, b.im.x);
-    sb[4 * slot + 1] = f4(b.w, b.im.y);
+__device__ __forceinline__ void sbody_store(float4* sb, int slot, int stride, const LBody& b) {
+    sb[slot] = f4(b.v, b.im.x);
+    sb[stride + slot] = f4(b.w, b.im.y);
 }
 // A non-dynamic body: velocities only (zero inverse mass and inertia, as its SBody holds).
 __device__ __forceinline__ LBody fixed_body(float4 v, float4 wv) {
@@ -383,7 +385,7 @@ enum { PASS_PREPARE = 0, PASS_ITERATE = 1, PASS_RELAX = 2 };
 // Iterate / relax colours of one task (its bodies already staged or in flight).
 template <bool kResid>
 __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStore& A, int4 T, int nc, const int* tc,
-                                                bool bias, float4* sbody, float4* ring, float& d2, float& l2) {
+                                                bool bias, float4* sbody, int sst, float4* ring, float& d2, float& l2) {
     const int cap = w.cap_arb, bs = blockDim.x, tid = threadIdx.x;
     // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order),
     // so consecutive colours are spread over different threads.  Each thread keeps
@@ -413,16 +415,16 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
             int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
             int l1 = __float_as_int(r1.x), l2s = __float_as_int(r1.y);
             float fr = r[2].x;
-            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1) : fixed_body(r[3], r[4]);
-            LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s) : fixed_body(r[3], r[4]);
+            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[3], r[4]);
+            LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s, sst) : fixed_body(r[3], r[4]);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 if (!(usage & (1 << k))) continue;
                 const float4* q = r + 5 + 6 * k;
                 A.cacc[k * cap + d] = iterate_row<kResid>(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
             }
-            if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, b1);
-            if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, b2);
+            if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);
+            if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, sst, b2);
             // refill the slot just consumed (its values are in registers by now)
             if (jn < n) stage_arbiter(r, A, T.x + jn, cap, un);
             cp_async_commit();
@@ -440,6 +442,7 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
     const int nc = w.sc_tnc[t];
     const int cap = w.cap_arb;
     const int bs = blockDim.x, tid = threadIdx.x;
+    const int sst = sp.task_maxb;  // stride of the staged body arrays
     // the task's colour boundaries, read once into shared memory (visible after the
     // barrier that follows the body staging)
     for (int c = tid; c <= nc; c += bs) tc[c] = w.sc_tcol[t * (JG_TASK_MAXC + 1) + c];
@@ -447,8 +450,8 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
     // follows as later groups so that both loads are in flight together)
     for (int i = tid; i < T.w; i += bs) {
         const float4* src = (const float4*)&w.body[w.sc_tbody[T.z + i]];
-        cp_async16(&sbody[4 * i], src); cp_async16(&sbody[4 * i + 1], src + 1);
-        cp_async16(&sbody[4 * i + 2], src + 2); cp_async16(&sbody[4 * i + 3], src + 3);
+        cp_async16(&sbody[i], src); cp_async16(&sbody[sst + i], src + 1);
+        cp_async16(&sbody[2 * sst + i], src + 2); cp_async16(&sbody[3 * sst + i], src + 3);
     }
     // (the bodies' group: committed with the positions below in Prepare, here otherwise,
     // so that the arbiter ring of the iterations follows as later groups)
@@ -475,31 +478,31 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
                 int usage = info.x & 15, mode = info.y;
                 int4 ls = A.lslot[d];
                 int2 bb = A.body[d];
-                LBody b1 = ls.x >= 0 ? sbody_load(sbody, ls.x) : fixed_body(A.sv[d], A.sv[cap + d]);
-                LBody b2 = ls.y >= 0 ? sbody_load(sbody, ls.y) : fixed_body(A.sv[d], A.sv[cap + d]);
+                LBody b1 = ls.x >= 0 ? sbody_load(sbody, ls.x, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
+                LBody b2 = ls.y >= 0 ? sbody_load(sbody, ls.y, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
                 float spec = A.mat[d].z;
                 const bool s1 = staged && ls.x >= 0, s2 = staged && ls.y >= 0;
                 v3 pos1 = mk3(s1 ? spos[ls.x] : w.pos[bb.x]), pos2 = mk3(s2 ? spos[ls.y] : w.pos[bb.y]);
                 q4 q1 = mkq(s1 ? sq[ls.x] : w.q[bb.x]), q2 = mkq(s2 ? sq[ls.y] : w.q[bb.y]);
                 for (int k = 0; k < 4; k++)
                     if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
-                if ((mode & 3) && ls.x >= 0) sbody_store(sbody, ls.x, b1);
-                if ((mode & 12) && ls.y >= 0) sbody_store(sbody, ls.y, b2);
+                if ((mode & 3) && ls.x >= 0) sbody_store(sbody, ls.x, sst, b1);
+                if ((mode & 12) && ls.y >= 0) sbody_store(sbody, ls.y, sst, b2);
             }
             __syncthreads();
         }
     } else if (nc > 0) {
         if (sp.record_residual)
-            iterate_colours<true>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, ring, d2, l2);
+            iterate_colours<true>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, sst, ring, d2, l2);
         else
-            iterate_colours<false>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, ring, d2, l2);
+            iterate_colours<false>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, sst, ring, d2, l2);
     }
     cp_async_wait_0();  // no copy into shared memory outlives the task
     __syncthreads();
     for (int i = tid; i < T.w; i += bs) {
         float4* dst = (float4*)&w.body[w.sc_tbody[T.z + i]];
-        dst[0] = sbody[4 * i];
-        dst[1] = sbody[4 * i + 1];
+        dst[0] = sbody[i];
+        dst[1] = sbody[sst + i];
     }
     __syncthreads();
 }
