@@ -390,9 +390,12 @@ __global__ void k_permute(WorldDev w, int2* ev_removed, int* dst_index) {
         D.key[d] = S.key[a];
         D.body[d] = bb;
         D.info[d] = make_int4(info.x, info.y, key, info.w);
-        D.lslot[d] = ls;
         // velocities of a non-dynamic body stay constant through the solve
         int nd = w.binfo[bb.x].x != JG_MOTION_DYNAMIC ? bb.x : (w.binfo[bb.y].x != JG_MOTION_DYNAMIC ? bb.y : -1);
+        // task arbiters: what the iterations read besides the rows, in one record
+        if (st == -4) ls = make_int4(ls.x, ls.y, (info.x & 15) | ((info.y & 15) << 4) | (nd >= 0 ? 256 : 0),
+                                     __float_as_int(S.mat[a].x));
+        D.lslot[d] = ls;
         D.sv[d] = nd >= 0 ? w.body[nd].v : make_float4(0.f, 0.f, 0.f, 0.f);
         D.sv[cap + d] = nd >= 0 ? w.body[nd].w : make_float4(0.f, 0.f, 0.f, 0.f);
         D.mat[d] = S.mat[a];

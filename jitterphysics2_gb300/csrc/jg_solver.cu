@@ -335,21 +335,22 @@ __device__ __forceinline__ void cp_async_wait_ring() { asm volatile("cp.async.wa
 // everything but the JG_TASK_RING most recent groups (the ring prologue) has landed
 __device__ __forceinline__ void cp_async_wait_bodies() { asm volatile("cp.async.wait_group %0;" :: "n"(JG_TASK_RING) : "memory"); }
 
-// Staged arbiter (JG_TASK_STAGE_F4 float4): info, body slots, material, the non-dynamic
-// body's v and w, then 6 rows per contact slot (cn, ct1, ct2, cr1, cr2, cacc).
-// Only the contact slots in `usage` are copied; the others keep stale data that the
-// staged usage mask tells the consumer to skip.
-__device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap, int usage) {
-    cp_async16(dst + 0, &A.info[d]);
-    cp_async16(dst + 1, &A.lslot[d]);
-    cp_async16(dst + 2, &A.mat[d]);
-    cp_async16(dst + 3, &A.sv[d]);
-    cp_async16(dst + 4, &A.sv[cap + d]);
+// Staged arbiter (JG_TASK_STAGE_F4 float4): the header (body slots, usage | mode << 4 |
+// non-dynamic << 8, friction), the non-dynamic body's v and w (copied only when there is
+// one), then 6 rows per contact slot (cn, ct1, ct2, cr1, cr2, cacc).  Only the contact
+// slots in the usage mask are copied; the others keep stale data that the staged mask
+// tells the consumer to skip.  `hz` is the header's third word.
+__device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap, int hz) {
+    cp_async16(dst + 0, &A.lslot[d]);
+    if (hz & 256) {
+        cp_async16(dst + 1, &A.sv[d]);
+        cp_async16(dst + 2, &A.sv[cap + d]);
+    }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        if (!(usage & (1 << k))) continue;
+        if (!(hz & (1 << k))) continue;
         int i = k * cap + d;
-        float4* q = dst + 5 + 6 * k;
+        float4* q = dst + 3 + 6 * k;
         cp_async16(q + 0, &A.cn[i]); cp_async16(q + 1, &A.ct1[i]); cp_async16(q + 2, &A.ct2[i]);
         cp_async16(q + 3, &A.cr1[i]); cp_async16(q + 4, &A.cr2[i]); cp_async16(q + 5, &A.cacc[i]);
     }
@@ -395,7 +396,7 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
     const int n = T.y;
     for (int m = 0; m < JG_TASK_RING; m++) {
         int j = m * bs + tid;
-        if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap, A.info[T.x + j].x);
+        if (j < n) stage_arbiter(ring + ((size_t)m * bs + tid) * JG_TASK_STAGE_F4, A, T.x + j, cap, A.lslot[T.x + j].z);
         cp_async_commit();
     }
     cp_async_wait_bodies();  // this thread's body copies have landed
@@ -406,21 +407,21 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
         for (; m * bs + tid < cend; m++) {
             const int j = m * bs + tid, d = T.x + j;
             float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
-            // usage of the arbiter this slot is refilled with, loaded now and used after
-            // the compute below, so its latency stays off the critical path
+            // header word of the arbiter this slot is refilled with, loaded now and used
+            // after the compute below, so its latency stays off the critical path
             const int jn = j + JG_TASK_RING * bs;
-            const int un = jn < n ? __ldg(&A.info[T.x + jn].x) : 0;
+            const int un = jn < n ? __ldg(&A.lslot[T.x + jn].z) : 0;
             cp_async_wait_ring();
-            float4 r0 = r[0], r1 = r[1];
-            int usage = __float_as_int(r0.x) & 15, mode = __float_as_int(r0.y);
-            int l1 = __float_as_int(r1.x), l2s = __float_as_int(r1.y);
-            float fr = r[2].x;
-            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[3], r[4]);
-            LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s, sst) : fixed_body(r[3], r[4]);
+            const float4 r0 = r[0];
+            const int l1 = __float_as_int(r0.x), l2s = __float_as_int(r0.y), hz = __float_as_int(r0.z);
+            const int usage = hz & 15, mode = (hz >> 4) & 15;
+            const float fr = r0.w;
+            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[1], r[2]);
+            LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s, sst) : fixed_body(r[1], r[2]);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 if (!(usage & (1 << k))) continue;
-                const float4* q = r + 5 + 6 * k;
+                const float4* q = r + 3 + 6 * k;
                 A.cacc[k * cap + d] = iterate_row<kResid>(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
             }
             if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);

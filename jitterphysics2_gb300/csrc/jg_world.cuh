@@ -66,7 +66,8 @@ struct ArbStore {
     int2* key;      // shape ids (ArbiterKey)
     int2* body;     // body indices
     int4* info;     // usage mask, solve mode, order key, created-this-step flag
-    int4* lslot;    // task body slots of body 1 and 2 (-1: not in the task's bodies)
+    int4* lslot;    // task arbiters: body slots of body 1 and 2 in the task (-1: not a task body),
+                    // usage | mode << 4 | (a non-dynamic body) << 8, friction bits
     float4* sv;     // [2 * cap] velocity, angular velocity of a non-dynamic body (constant in the solve)
     float4* mat;    // friction, restitution, speculative relaxation, 0
     float4* cn;     // normal xyz, Bias
@@ -230,8 +231,8 @@ struct StepParams {
 };
 
 // Partitioned-solve launch shape: threads per CTA and bytes of shared memory per
-// staged arbiter (4 contact slots x 6 float4 rows + info, slots, material, 2 x static body).
-#define JG_TASK_STAGE_F4 29
+// staged arbiter (4 contact slots x 6 float4 rows + header, 2 x non-dynamic body velocity).
+#define JG_TASK_STAGE_F4 27
 // Staged arbiters per thread.  Thread t owns every blockDim-th arbiter of its task, so its
 // next arbiter lies blockDim positions (several colours) ahead: one slot in flight is
 // enough, and the small ring lets two 128-thread task CTAs share an SM.
