@@ -337,7 +337,8 @@ __device__ __forceinline__ void cp_async_wait_bodies() { asm volatile("cp.async.
 
 // Staged arbiter (JG_TASK_STAGE_F4 float4): the header (body slots, usage | mode << 4 |
 // non-dynamic << 8, friction), the non-dynamic body's v and w (copied only when there is
-// one), then 6 rows per contact slot (cn, ct1, ct2, cr1, cr2, cacc).  Only the contact
+// one), then 5 rows per contact slot (cn, ct1, cr1, cr2, cacc; tangent 2 is cross(t1, n),
+// as the contact was created with, recomputed by the consumer).  Only the contact
 // slots in the usage mask are copied; the others keep stale data that the staged mask
 // tells the consumer to skip.  `hz` is the header's third word.
 __device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, int d, int cap, int hz) {
@@ -350,9 +351,9 @@ __device__ __forceinline__ void stage_arbiter(float4* dst, const ArbStore& A, in
     for (int k = 0; k < 4; k++) {
         if (!(hz & (1 << k))) continue;
         int i = k * cap + d;
-        float4* q = dst + 3 + 6 * k;
-        cp_async16(q + 0, &A.cn[i]); cp_async16(q + 1, &A.ct1[i]); cp_async16(q + 2, &A.ct2[i]);
-        cp_async16(q + 3, &A.cr1[i]); cp_async16(q + 4, &A.cr2[i]); cp_async16(q + 5, &A.cacc[i]);
+        float4* q = dst + 3 + 5 * k;
+        cp_async16(q + 0, &A.cn[i]); cp_async16(q + 1, &A.ct1[i]);
+        cp_async16(q + 2, &A.cr1[i]); cp_async16(q + 3, &A.cr2[i]); cp_async16(q + 4, &A.cacc[i]);
     }
 }
 
@@ -421,8 +422,10 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 if (!(usage & (1 << k))) continue;
-                const float4* q = r + 3 + 6 * k;
-                A.cacc[k * cap + d] = iterate_row<kResid>(q[0], q[1], q[2], q[3], q[4], q[5], mode, fr, b1, b2, bias, d2, l2);
+                const float4* q = r + 3 + 5 * k;
+                const float4 cn = q[0], ct1 = q[1];
+                const float4 ct2 = f4(cross(mk3(ct1), mk3(cn)), 0.f);  // bit-identical to the stored tangent 2
+                A.cacc[k * cap + d] = iterate_row<kResid>(cn, ct1, ct2, q[2], q[3], q[4], mode, fr, b1, b2, bias, d2, l2);
             }
             if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);
             if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, sst, b2);

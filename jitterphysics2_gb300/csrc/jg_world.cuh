@@ -231,8 +231,8 @@ struct StepParams {
 };
 
 // Partitioned-solve launch shape: threads per CTA and bytes of shared memory per
-// staged arbiter (4 contact slots x 6 float4 rows + header, 2 x non-dynamic body velocity).
-#define JG_TASK_STAGE_F4 27
+// staged arbiter (4 contact slots x 5 float4 rows + header, 2 x non-dynamic body velocity).
+#define JG_TASK_STAGE_F4 23
 // Staged arbiters per thread.  Thread t owns every blockDim-th arbiter of its task, so its
 // next arbiter lies blockDim positions (several colours) ahead: one slot in flight is
 // enough, and the small ring lets two 128-thread task CTAs share an SM.
