@@ -1090,6 +1090,13 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
 
 // Stage 2, one warp per deep pair: EPA from the saved portal (NarrowPhase.cs:39-95); on
 // success the colliding record takes the EPA result, otherwise the MPR result stands.
+// Next work item of a warp: lane 0 takes it from the cursor, every lane gets it.
+__device__ __forceinline__ int next_item(int* cursor, int lane) {
+    int e = 0;
+    if (lane == 0) e = atomicAdd(cursor, 1);
+    return __shfl_sync(0xffffffffu, e, 0);
+}
+
 __global__ void __launch_bounds__(NP_WARPS * 32) k_epa(WorldDev w) {
     __shared__ EpaSmem smem[NP_WARPS];
     const int lane = threadIdx.x & 31;
@@ -1098,7 +1105,9 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_epa(WorldDev w) {
     NpStats st; st.exact = 0;
     int epa_calls = 0, epa_fail = 0;
     const int ne = min(w.ctr->nepa_list, w.cap_arb);
-    for (int e = blockIdx.x * NP_WARPS + wib; e < ne; e += gridDim.x * NP_WARPS) {
+    // pairs handed out one at a time: EPA's cost varies by an order of magnitude between
+    // pairs, so a fixed share per warp would leave most warps idle behind a few
+    for (int e = next_item(&w.ctr->epa_next, lane); e < ne; e = next_item(&w.ctr->epa_next, lane)) {
         int c = w.epa_list[e];
         int2 pr = w.pairs[w.col_pair[c].x];
         ShapeRef sa = load_shape(w, pr.x), sb = load_shape(w, pr.y);
@@ -1205,7 +1214,7 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
     NpStats st; st.exact = 0;
     int epa_calls = 0, epa_fail = 0, pts = 0;
     const int ne = min(w.ctr->nedge, w.cap_arb);
-    for (int e = blockIdx.x * NP_WARPS + wib; e < ne; e += gridDim.x * NP_WARPS) {
+    for (int e = next_item(&w.ctr->edge_next, lane); e < ne; e = next_item(&w.ctr->edge_next, lane)) {
         int c = w.edge_list[e];
         int2 pr = w.pairs[w.col_pair[c].x];
         int s1 = pr.x, s2 = pr.y;

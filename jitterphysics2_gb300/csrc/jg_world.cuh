@@ -117,7 +117,9 @@ struct DevCounters {
     int ntasks;       // partitioned solve: tasks, arbiters in tasks, most local colours
     int narb_task;
     int task_colors;
-    int pad;
+    int epa_next;     // work cursors of the warp-per-pair narrowphase stages
+    int edge_next;
+    int pad[3];
 };
 
 struct WorldDev {
