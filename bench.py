@@ -51,7 +51,7 @@ SETTLE_STEPS = 800
 SEED = 12347
 
 
-SOLVE_DRAM_BYTES = 0.645e9
+SOLVE_DRAM_BYTES = 0.371e9
 
 
 def peaks():
