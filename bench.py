@@ -52,6 +52,7 @@ SEED = 12347
 
 
 SOLVE_DRAM_BYTES = 0.371e9
+MPR_FMA_PIPE_PCT = 33.5
 
 
 def peaks():
@@ -386,6 +387,11 @@ def main():
                          "traffic": SOLVE_DRAM_BYTES if args.config == "c3" and nb == N_BODIES + 2 else None,
                          "solve_ms_per_step": float(np.mean(solve_ms)),
                          "bytes_model": "S*((I+R)*276*C + 320*C + 116*N) + 52*N"},
+            # the narrowphase is bound by the FP32 pipe, not HBM: FMA-pipe cycles active of the
+            # MPR kernel from an ncu capture of this workload
+            "narrowphase": {"bound": "fp32 pipe", "kernel": "k_mpr", "fma_pipe_active_pct": MPR_FMA_PIPE_PCT,
+                            "ms_per_step": stage_ms["narrowphase"]}
+            if args.config == "c3" and nb == N_BODIES + 2 else None,
             "clocks": clk, "gpu_launches": launches,
             "stage_ms": stage_ms}
     extras = rank == 0 and not args.no_extras and args.config == "c3"
