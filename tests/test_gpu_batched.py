@@ -70,3 +70,19 @@ def test_autotune_picks_a_working_launch_shape():
     for _ in range(5):
         w.step(sc["dt"])
     assert w.counters()["status"] == 0
+
+
+def test_batched_worlds_without_joints_hand_off_and_match_the_oracle():
+    # without joints there is no remainder, so the task solve runs without grid barriers
+    # between its phases (each world is one task and waits only on its own previous pass);
+    # one step from identical state must match the oracle replaying the GPU's order
+    from test_gpu_parity import _one_step_velocity_errors
+    sc = dict(scenes.batched_worlds(n_worlds=48, lo=8, hi=96, seed=5))
+    sc["joints"] = []
+    w = world_for_scene(sc)
+    for _ in range(120):
+        w.step(sc["dt"])
+    c = w.counters()
+    assert c["status"] == 0 and c["colors"] == 0 and c["task_arbiters"] == c["arbiters"], c
+    err = _one_step_velocity_errors(sc, w)
+    assert np.mean(err < 1e-3) > 0.9, (np.mean(err < 1e-3), np.sort(err)[-5:])
