@@ -13,7 +13,9 @@
 //      touch, which no other task of the same grid touches;
 //   3. inside a task, arbiters get local colours (Jones-Plassmann in shared memory) and
 //      are ordered by colour; the solver runs a task in one CTA with the bodies in shared
-//      memory and a block barrier between colours, and the three grids one after another;
+//      memory and a block barrier between colours, and the three grids one after another
+//      (without a remainder a task waits only for the tasks of the two previous grid
+//      phases that may share its bodies; their list is built here);
 //   4. arbiters of cells too large for shared memory form the remainder, coloured
 //      globally and solved as before.
 // The resulting order key of an arbiter (grid * 256 + local colour, or 768 + global

@@ -6,10 +6,12 @@
 //     IntegrateVelocities (World.Step.cs:1106-1133)                   bodies, grid-stride
 //     relaxation x colours: Iterate without bias (World.Step.cs:1135-1153)
 // Rows of one colour share no dynamic body, so a colour is solved in parallel with no
-// atomics; a grid barrier separates colours.  Arbiters are stored colour-sorted, so each
-// colour is a contiguous range: row loads are coalesced float4s, body loads are 64-byte
-// records.  The per-step body update (RigidBody.Update, RigidBody.cs:716-764) is a
-// separate kernel.
+// atomics.  Two kernels: k_solve runs global colours with a grid barrier between them;
+// k_solve_tasks runs the partitioned schedule (spatial tasks with their bodies in shared
+// memory and a block barrier between local colours, the three grid phases handed off task
+// by task, and the remainder in global colours).  Arbiters are stored colour-sorted, so each
+// colour is a contiguous range of coalesced float4 rows.  The per-step body update
+// (RigidBody.Update, RigidBody.cs:716-764) is a separate kernel.
 #include "jg_sync.cuh"
 #include <algorithm>
 

@@ -38,7 +38,8 @@ struct __align__(16) TriDev {
 // two dynamic bodies sharing an arbiter): every such arbiter lies inside one cell of at
 // least one grid.  A cell's arbiters form a task, solved by one CTA with the cell's
 // bodies in shared memory; the three grids are three phases per solver pass, so a pass
-// needs three grid barriers instead of one per colour.  Arbiters that fit no task
+// needs at most three grid barriers instead of one per colour (none between phases when
+// tasks hand off through completion counters).  Arbiters that fit no task
 // (and all joints) form the remainder, solved in global colours as before.
 #define JG_SCHED_GRIDS 3
 #define JG_SCHED_MAXCELLS 65536      // cells per grid
