@@ -244,6 +244,19 @@ def dist_setup(n_gpus):
     return dist.get_rank(), dist.get_world_size(), dist
 
 
+def reduce_over_ranks(total_ms, contacts, dist, device="cuda"):
+    """Replicas only (the world does not shard): the job's time is the slowest rank's, its
+    contact count the sum over ranks.  No collective when running alone."""
+    if dist is None:
+        return float(total_ms), float(contacts)
+    import torch
+    tt = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    cc = torch.tensor([float(contacts)], dtype=torch.float64, device=device)
+    dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(cc.item())
+
+
 def run_reference(args):
     rank, ws, dist = dist_setup(args.gpus)
     if rank != 0:
@@ -320,7 +333,10 @@ def main():
         w.step(sc["dt"])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    # device-timed steps (inputs resident)
+    # device-timed steps (inputs resident), bracketed by a barrier when several ranks run
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
     clocks = ClockSampler()
     clocks.start()
     step_ms, solve_ms, contacts, sbytes, launches, stages = [], [], 0, [], 0, []
@@ -336,17 +352,12 @@ def main():
         contacts += c["contacts"]
         sbytes.append(solver_bytes(c, len(sc["bodies"]), S, I, R))
         launches += c["kernel_launches"]
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     stage_ms = {k: float(np.mean([s[k] for s in stages])) for k in stages[0]}
     clk = clocks.stop()
-    total_ms = float(np.sum(step_ms))
-    if dist is not None:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        cc = torch.tensor([float(contacts)], device="cuda")
-        dist.all_reduce(cc, op=dist.ReduceOp.SUM)
-        total_ms, contacts_all = float(tt.item()), float(cc.item())
-    else:
-        contacts_all = float(contacts)
+    total_ms, contacts_all = reduce_over_ranks(float(np.sum(step_ms)), contacts, dist)
     value = contacts_all / (total_ms / 1e3)
 
     # end to end through the host-buffer call
