@@ -52,6 +52,7 @@ extern "C" {
 #define JG_BODY_GYROSCOPIC        (1 << 3)
 #define JG_BODY_LOCKS_SHIFT       4       /* 6 bits: locked motion axes (MotionAxes ^ All) */
 #define JG_BODY_NO_GRAVITY        (1 << 12)
+#define JG_BODY_SPECULATIVE       (1 << 13) /* RigidBody.EnableSpeculativeContacts (RigidBody.cs:877-892) */
 
 /* Warm start of newly created contacts (no counterpart in the reference, which
  * always starts new contacts from zero: Contact.cs:727) */
@@ -88,6 +89,7 @@ typedef struct jg_world_params {
     int32_t record_residual;            /* record the per-iteration residual (metric)   */
     int32_t deterministic;              /* sort new arbiters by key every step          */
     int32_t partitioned_solve;          /* 1 (default): spatial tasks in shared memory   */
+    float   speculative_threshold;      /* SpeculativeVelocityThreshold, default 10      */
 } jg_world_params;
 
 /* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the
@@ -170,6 +172,7 @@ typedef struct jg_counters {
     int64_t solver_tasks;               /* partitioned solve: tasks (cells) of the step   */
     int64_t task_arbiters;              /* arbiters solved in tasks (rest: global colours) */
     int64_t task_colors;                /* most local colours of one task                 */
+    int64_t speculative_contacts;       /* pairs registered by the sweep (World.Detect.cs:168-196) */
 } jg_counters;
 
 /* Stage timings in milliseconds (World.DebugTimings buckets, World.Step.cs:44-81). */

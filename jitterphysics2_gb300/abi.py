@@ -27,6 +27,7 @@ BODY_ACTIVE = 1 << 2
 BODY_GYROSCOPIC = 1 << 3
 BODY_LOCKS_SHIFT = 4
 BODY_NO_GRAVITY = 1 << 12
+BODY_SPECULATIVE = 1 << 13   # RigidBody.EnableSpeculativeContacts
 RESID_MAX = 2048                # iterations whose residual a step records (jg_get_residuals)
 COLLIDE_NOALLOC_MAX_PAIRS = 16384  # JG_COLLIDE_NOALLOC_MAX_PAIRS
 MLP_IN, MLP_HID, MLP_OUT = 24, 64, 3
@@ -50,7 +51,7 @@ PARAMS_FIELDS = [
     ("max_constraints", ctypes.c_int32), ("solver_block", ctypes.c_int32), ("solver_ctas_per_sm", ctypes.c_int32),
     ("narrow_tile", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_residual", ctypes.c_int32),
     ("deterministic", ctypes.c_int32),
-    ("partitioned_solve", ctypes.c_int32),
+    ("partitioned_solve", ctypes.c_int32), ("speculative_threshold", ctypes.c_float),
 ]
 
 
@@ -81,7 +82,7 @@ CONTACT_DTYPE = np.dtype([
 ])
 COUNTER_NAMES = ["pairs", "colliding", "manifold_points", "arbiters", "contacts", "new_contacts", "colors",
                  "epa_calls", "epa_failures", "exact_fallbacks", "status", "created_arbiters", "removed_arbiters",
-                 "kernel_launches", "solver_tasks", "task_arbiters", "task_colors"]
+                 "kernel_launches", "solver_tasks", "task_arbiters", "task_colors", "speculative_contacts"]
 TIMING_NAMES = ["broadphase", "narrowphase", "add_arbiter", "coloring", "solve", "update_contacts",
                 "update_bodies", "total"]
 

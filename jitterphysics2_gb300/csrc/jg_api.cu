@@ -123,7 +123,7 @@ int allocate(jg_world* w) {
     if ((r = alloc_store(w, d.arb[1], d.cap_arb))) return r;
     d.cur = 0;
     DA(d.col_pair, d.cap_arb); DA(d.col_res, 3 * (size_t)d.cap_arb); DA(d.col_portal, 12 * (size_t)d.cap_arb);
-    DA(d.epa_list, d.cap_arb); DA(d.edge_list, d.cap_arb);
+    DA(d.epa_list, d.cap_arb); DA(d.edge_list, d.cap_arb); DA(d.spec_list, d.cap_pairs);
     d.hcap = next_pow2(2 * d.cap_arb);
     DA(d.hkeys, d.hcap); DA(d.hvals, d.hcap);
     DA(d.cstat, d.cap_arb + d.cap_joints);
@@ -223,6 +223,7 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.persistent = p.persistent_manifold;
     sp.edge_filter = p.edge_filter;
     sp.spec_relax = p.speculative_relaxation;
+    sp.spec_threshold = p.speculative_threshold;
     sp.warm_start = p.warm_start_mode;
     sp.record_residual = p.record_residual;
     sp.partition = p.partitioned_solve ? 1 : 0;
@@ -240,12 +241,12 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     if (timed) cudaEventRecord(w->ev[0], s);
     k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
     if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 2 * JG_RESID_MAX, s);
-    jg_launch_aabb(d, s);
+    jg_launch_aabb(d, sp.dt, s);
     int passes = jg_launch_broadphase(d, s, w->nsm);
     // kernels of this sequence: reset 1, aabb 2, broadphase 1 + 3 per radix pass + 4,
-    // narrowphase 3 + 4, merge 3 (+ warm-start hook), schedule, colour/permute 4, count 1,
+    // narrowphase 3 + 5, merge 3 (+ warm-start hook), schedule, colour/permute 4, count 1,
     // solve 1, contact update 1, body update 1
-    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 7 + 3 + 4 + 1 + 1 + 1 + 1 + jg_schedule_launches(sp);
+    w->launches = 1 + 2 + (d.ns >= 2 ? 5 + 3 * passes : 0) + 8 + 3 + 4 + 1 + 1 + 1 + 1 + jg_schedule_launches(sp);
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);
@@ -281,6 +282,7 @@ int finish_step(jg_world* w, bool timed) {
     o.created_arbiters = c.nnew; o.removed_arbiters = c.nremoved;
     o.kernel_launches = w->launches;
     o.solver_tasks = c.ntasks; o.task_arbiters = c.narb_task; o.task_colors = c.task_colors;
+    o.speculative_contacts = c.nspec_hit;
     if (timed) {
         float t[8];
         for (int i = 0; i < 7; i++) cudaEventElapsedTime(&t[i], w->ev[i], w->ev[i + 1]);
@@ -313,6 +315,7 @@ int jg_default_params(jg_world_params* p) {
     p->enable_auxiliary_contacts = 1;
     p->persistent_manifold = 1;
     p->speculative_relaxation = 0.9f;
+    p->speculative_threshold = 10.0f;
     p->edge_filter = 1;
     p->warm_start_mode = JG_WARMSTART_CACHED;
     p->narrow_tile = 32;

@@ -22,7 +22,7 @@ __device__ __forceinline__ float ord2f(unsigned u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-__global__ void k_aabb(WorldDev w, unsigned* scene) {
+__global__ void k_aabb(WorldDev w, unsigned* scene, float dt) {
     __shared__ unsigned smin[3], smax[3];
     if (threadIdx.x < 3) { smin[threadIdx.x] = 0xffffffffu; smax[threadIdx.x] = 0u; }
     __syncthreads();
@@ -32,6 +32,13 @@ __global__ void k_aabb(WorldDev w, unsigned* scene) {
         float4 p4 = w.pos[b], q4v = w.q[b];
         v3 mn, mx;
         shape_aabb(s, mkq(q4v), mk3(p4), mn, mx);
+        if (w.binfo[b].y & JG_BODY_SPECULATIVE) {
+            // RigidBodyShape.UpdateWorldBoundingBox (RigidBodyShape.cs:37-57): a speculative
+            // body's box grows by the distance its linear velocity covers in one step
+            float swept = dt * sqrtf(len2(mk3(w.body[b].v)));
+            mn = mn - mk3(swept);
+            mx = mx + mk3(swept);
+        }
         w.amin[i] = f4(mn, 0.f);
         w.amax[i] = f4(mx, 0.f);
         v3 c = 0.5f * (mn + mx);
@@ -341,12 +348,12 @@ __global__ void k_traverse(WorldDev w, int n) {
 
 }  // namespace
 
-void jg_launch_aabb(WorldDev& w, cudaStream_t s) {
+void jg_launch_aabb(WorldDev& w, float dt, cudaStream_t s) {
     if (w.ns == 0) return;
     k_scene_init<<<1, 32, 0, s>>>((unsigned*)w.scene_box);
     int blocks = (w.ns + 255) / 256;
     if (blocks > 1024) blocks = 1024;
-    k_aabb<<<blocks, 256, 0, s>>>(w, (unsigned*)w.scene_box);
+    k_aabb<<<blocks, 256, 0, s>>>(w, (unsigned*)w.scene_box, dt);
 }
 
 int jg_launch_broadphase(WorldDev& w, cudaStream_t s, int nsm) {

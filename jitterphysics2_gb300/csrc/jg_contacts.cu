@@ -155,7 +155,7 @@ __device__ void add_contact(const WorldDev& w, const ArbStore& A, int a, int& us
 __global__ void k_merge(WorldDev w, StepParams sp, int2* ev_created) {
     const ArbStore& A = w.arb[w.cur];
     int ns = min(w.ctr->nstream, w.cap_pairs);
-    int created_pts = 0, contacts = 0;
+    int created_pts = 0, contacts = 0, spec = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
         int2 key = w.cs_key[i];
         unsigned long long k64 = akey(key);
@@ -180,7 +180,10 @@ __global__ void k_merge(WorldDev w, StepParams sp, int2* ev_created) {
         int mode = (w.binfo[b1].x == JG_MOTION_DYNAMIC ? 3 : 0) | (w.binfo[b2].x == JG_MOTION_DYNAMIC ? 12 : 0);
         float4 nc = w.cs_n[i];
         v3 n = mk3(nc);
-        int cnt = __float_as_int(nc.w);
+        int cnt = __float_as_int(nc.w) & 0xff;
+        // a speculative contact updates linear velocities only: ResetMode(SolveMode.Angular)
+        // (World.Detect.cs:193-194)
+        if (__float_as_int(nc.w) & JG_STREAM_SPECULATIVE) { mode &= ~(2 | 8); spec++; }
         // ResetMode before AddContact: Initialize reads the mode
         for (int k = 0; k < cnt; k++)
             add_contact(w, A, a, usage, b1, b2, mode, restitution, mk3(w.cs_pa[4 * i + k]), mk3(w.cs_pb[4 * i + k]), n, created_pts);
@@ -188,6 +191,7 @@ __global__ void k_merge(WorldDev w, StepParams sp, int2* ev_created) {
         contacts += __popc(usage & 15);
     }
     if (created_pts) atomicAdd(&w.ctr->new_contacts, created_pts);
+    if (spec) atomicAdd(&w.ctr->nspec_hit, spec);
     (void)contacts;
 }
 

@@ -1041,7 +1041,8 @@ __global__ void k_pair_scatter(WorldDev w) {
 // Stage 1, one thread per broadphase pair: the MPR overlap test in A's frame
 // (NarrowPhase.MprEpa, NarrowPhase.cs:902-927, up to the EPA hand-off).  Overlapping pairs
 // are appended to the colliding list with their MPR result; deeper than the EPA threshold,
-// also to the EPA list with the MPR portal EPA starts from.
+// also to the EPA list with the MPR portal EPA starts from.  Separated pairs with a
+// speculative body go to the sweep list (World.Detect.cs:162-170).
 __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
     const int npairs = min(w.ctr->npairs, w.cap_pairs);
     const int cap = w.cap_arb;
@@ -1049,6 +1050,7 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
         const int q = base + threadIdx.x;
         const int p = q < npairs ? w.pair_order[q] : npairs;
         int code = 0;
+        bool sweep = false;
         v3 pA, pB, n;
         float pen = 0.f;
         MV portal[4];
@@ -1065,9 +1067,13 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
                 v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
                 q4 q = qmul(qconj(qa), qb);
                 v3 pr_ = rotate_inv(pb - pa, qa);
+                const bool spec_body = ((i1.y | i2.y) & JG_BODY_SPECULATIVE) != 0;
                 code = mpr_core<false>(sa, sb, q, pr_, 0.02f, pA, pB, n, pen, portal);
+                sweep = code == 0 && spec_body;
             }
         }
+        int si = warp_append(&w.ctr->nspec, sweep);
+        if (si >= 0) w.spec_list[si] = p;
         int c = warp_append(&w.ctr->ncol, code != 0);
         if (c >= cap) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); c = -1; }
         if (c >= 0) {
@@ -1084,6 +1090,204 @@ __global__ void __launch_bounds__(256, 2) k_mpr(WorldDev w) {
                 w.col_portal[12 * e + 3 * k + 1] = f4(portal[k].A, 0.f);
                 w.col_portal[12 * e + 3 * k + 2] = f4(portal[k].B, 0.f);
             }
+        }
+    }
+}
+
+// ---- speculative contacts: time of impact by conservative advancement --------------------
+// GJK simplex with witness points (SimplexSolverAB.cs:28-359), one thread: up to four
+// Minkowski vertices with their support points on A and B, the barycentric weights of the
+// point nearest the origin, and the mask of the vertices spanning it.
+struct SimplexAB {
+    MV v[4];
+    float bc[4];
+    unsigned mask;
+
+    // ClosestSegment (SimplexSolverAB.cs:60-100)
+    __device__ v3 segment(int i0, int i1, float* w, unsigned& m) const {
+        v3 a = v[i0].V, b = v[i1].V;
+        v3 d = b - a;
+        float dd = len2(d);
+        if (dd < 1e-8f) { m = 1u << i1; w[i0] = 0.f; w[i1] = 1.f; return b; }
+        float t = -dot(a, d) / dd;
+        if (t > 1.0f) { m = 1u << i1; w[i0] = 0.f; w[i1] = 1.f; return b; }
+        if (t < 0.0f) { m = 1u << i0; w[i0] = 1.f; w[i1] = 0.f; return a; }
+        w[i0] = 1.0f - t; w[i1] = t;
+        m = (1u << i0) | (1u << i1);
+        return cross(d, cross(a, d)) * (1.0f / dd);
+    }
+    // ClosestTriangle (SimplexSolverAB.cs:102-176): the interior when every weight is
+    // non-negative and the triangle is not degenerate, else the nearest edge among those
+    // opposite a negative weight (all three edges when degenerate).
+    __device__ v3 triangle(int i0, int i1, int i2, float* w, unsigned& m) const {
+        m = 0;
+        v3 a = v[i0].V, b = v[i1].V, c = v[i2].V;
+        v3 u = a - b, e = a - c;
+        v3 nrm = cross(u, e);
+        float t = len2(nrm);
+        float it = 1.0f / t;
+        bool degenerate = t < 1e-8f;
+        float l2 = dot(cross(u, a), nrm) * it;
+        float l1 = dot(cross(a, e), nrm) * it;
+        float l0 = 1.0f - l2 - l1;
+        const int ea[3] = {i1, i0, i0}, eb[3] = {i2, i2, i1};
+        const float lam[3] = {l0, l1, l2};
+        float best = 3.402823466e+38f;
+        v3 cp = mk3(0.f);
+        float tmp[4];
+        for (int k = 0; k < 3; k++) {
+            if (!(lam[k] < 0.0f || degenerate)) continue;
+            unsigned mk;
+            v3 q = segment(ea[k], eb[k], tmp, mk);
+            float dist = len2(q);
+            if (dist < best) {
+                for (int j = 0; j < 4; j++) w[j] = tmp[j];
+                m = mk; cp = q; best = dist;
+            }
+        }
+        if (m != 0) return cp;
+        w[i0] = l0; w[i1] = l1; w[i2] = l2;
+        m = (1u << i0) | (1u << i1) | (1u << i2);
+        return nrm * (dot(nrm, a) * it);
+    }
+    __device__ static float det(v3 a, v3 b, v3 c, v3 d) { return dot(b - a, cross(c - a, d - a)); }
+    // ClosestTetrahedron (SimplexSolverAB.cs:178-276)
+    __device__ v3 tetra(float* w, unsigned& m) const {
+        float dt = det(v[0].V, v[1].V, v[2].V, v[3].V);
+        float idt = 1.0f / dt;
+        bool degenerate = dt * dt < 1e-8f;
+        v3 z = mk3(0.f);
+        float l0 = det(z, v[1].V, v[2].V, v[3].V) * idt;
+        float l1 = det(v[0].V, z, v[2].V, v[3].V) * idt;
+        float l2 = det(v[0].V, v[1].V, z, v[3].V) * idt;
+        float l3 = 1.0f - l0 - l1 - l2;
+        const int fa[4] = {1, 0, 0, 0}, fb[4] = {2, 2, 1, 1}, fc[4] = {3, 3, 3, 2};
+        const float lam[4] = {l0, l1, l2, l3};
+        float best = 3.402823466e+38f;
+        v3 cp = mk3(0.f);
+        float tmp[4];
+        m = 0;
+        for (int k = 0; k < 4; k++) {
+            if (!(lam[k] < 0.0f || degenerate)) continue;
+            unsigned mk;
+            v3 q = triangle(fa[k], fb[k], fc[k], tmp, mk);
+            float dist = len2(q);
+            if (dist < best) {
+                for (int j = 0; j < 4; j++) w[j] = tmp[j];
+                m = mk; cp = q; best = dist;
+            }
+        }
+        if (m != 0) return cp;
+        w[0] = l0; w[1] = l1; w[2] = l2; w[3] = l3;
+        m = 15u;
+        return mk3(0.f);
+    }
+    // AddVertex (SimplexSolverAB.cs:300-357): false when the tetrahedron encloses the origin.
+    __device__ bool add(const MV& x, v3& closest) {
+        int ix[4], used = 0, free_slot = 0;
+        for (int i = 0; i < 4; i++) {
+            if (mask & (1u << i)) ix[used++] = i;
+            else free_slot = i;
+        }
+        ix[used++] = free_slot;
+        v[free_slot] = x;
+        if (used == 1) { closest = v[ix[0]].V; mask = 1u << ix[0]; bc[ix[0]] = 1.0f; return true; }
+        if (used == 2) { closest = segment(ix[0], ix[1], bc, mask); return true; }
+        if (used == 3) { closest = triangle(ix[0], ix[1], ix[2], bc, mask); return true; }
+        closest = tetra(bc, mask);
+        return mask != 15u;
+    }
+    // GetClosest (SimplexSolverAB.cs:278-293)
+    __device__ void closest_points(v3& pA, v3& pB) const {
+        pA = mk3(0.f); pB = mk3(0.f);
+        for (int i = 0; i < 4; i++) {
+            if (!(mask & (1u << i))) continue;
+            pA = pA + bc[i] * v[i].A;
+            pB = pB + bc[i] * v[i].B;
+        }
+    }
+};
+
+// NarrowPhase.Sweep with A at the origin (NarrowPhase.cs:1155-1222): B moves along `sweep`;
+// a support point in front of the search direction advances the time of impact to the
+// plane it spans.  False when B moves away from that plane (no hit); lambda = 0 when the
+// shapes already overlap.  At most 34 support evaluations.
+__device__ bool sweep_local(const ShapeRef& sa, const ShapeRef& sb, q4 qb, v3 pb, v3 sweep, v3& pA, v3& pB,
+                            v3& normal, float& lambda) {
+    SimplexAB sx;
+    sx.mask = 0;
+    MV c;
+    mk_center(sa, sb, qb, pb, c);
+    v3 pos = pb;
+    lambda = 0.0f;
+    v3 v = -c.V;
+    normal = mk3(0.f);
+    int iter = 34;
+    float d2 = len2(v);
+    while (d2 > 1e-4f * 1e-4f && iter-- != 0) {
+        MV x;
+        mk_support_t<false>(sa, sb, qb, pos, v, x);
+        float vw = -dot(v, x.V);
+        if (vw > 0.0f) {
+            float vr = dot(v, sweep);
+            if (vr >= -1e-12f) { lambda = __int_as_float(0x7f800000); return false; }
+            lambda -= vw / vr;
+            pos = pb + lambda * sweep;
+            normal = v;
+        }
+        if (!sx.add(x, v)) break;
+        v = -v;
+        d2 = len2(v);
+    }
+    sx.closest_points(pA, pB);
+    normal = normalize_safe(normal, 1e-16f);
+    return true;
+}
+
+// Stage 1b, one thread per pair the MPR stage found separated with a speculative body
+// (World.Detect.cs:168-196): pairs closing slower than the threshold speed are dropped; the
+// rest run the sweep in A's frame (NarrowPhase.cs:1100-1136) and are kept when it hits
+// within the step (0 < toi <= dt).  The record goes to the colliding list in world space
+// with kind 3, penetration n . (pA - pB) * SpeculativeRelaxationFactor.
+__global__ void __launch_bounds__(128) k_sweep(WorldDev w, StepParams sp) {
+    const int ns = min(w.ctr->nspec, w.cap_pairs);
+    const int cap = w.cap_arb;
+    for (int base = blockIdx.x * blockDim.x; base < ns; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool hit = false;
+        int p = 0;
+        v3 pA = mk3(0.f), pB = mk3(0.f), n = mk3(0.f);
+        float pen = 0.f;
+        if (i < ns) {
+            p = w.spec_list[i];
+            int2 pr = w.pairs[p];
+            int b1 = w.sinfo[pr.x].y, b2 = w.sinfo[pr.y].y;
+            ShapeRef sa = load_shape(w, pr.x), sb = load_shape(w, pr.y);
+            q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+            v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+            v3 va = mk3(w.body[b1].v), vb = mk3(w.body[b2].v);
+            v3 dv = vb - va;
+            q4 q = qmul(qconj(qa), qb);
+            v3 prl = rotate_inv(pb - pa, qa);
+            v3 swl = rotate_inv(dv, qa);
+            float toi;
+            if (!(len2(dv) < sp.spec_threshold * sp.spec_threshold) &&
+                sweep_local(sa, sb, q, prl, swl, pA, pB, n, toi)) {
+                pA = rotate(pA, qa); pA = pA + pa;
+                pB = rotate(pB, qa); pB = pB + pa;
+                n = rotate(n, qa);
+                pB = pB + toi * (va - vb);
+                hit = !(toi > sp.dt) && toi != 0.0f;
+                pen = dot(n, pA - pB) * sp.spec_relax;
+            }
+        }
+        int c = warp_append(&w.ctr->ncol, hit);
+        if (c >= cap) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); c = -1; }
+        if (c >= 0) {
+            w.col_pair[c] = make_int2(p, 3);
+            w.col_res[3 * c + 0] = f4(pA, 0.f);
+            w.col_res[3 * c + 1] = f4(pB, 0.f);
+            w.col_res[3 * c + 2] = f4(n, pen);
         }
     }
 }
@@ -1142,28 +1346,34 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_epa(WorldDev w) {
     if (lane == 0 && ex) atomicAdd(&w.ctr->exact, ex);
 }
 
-__device__ __forceinline__ void write_stream(WorldDev& w, int idx, int s1, int s2, v3 n, int cnt, const float4* oA,
-                                             const float4* oB) {
+// Contact stream record: shape pair, normal with the point count (low byte) and
+// JG_STREAM_SPECULATIVE, and the points.
+__device__ __forceinline__ void write_stream(WorldDev& w, int idx, int s1, int s2, v3 n, int cnt, bool spec,
+                                             const float4* oA, const float4* oB) {
     if (idx >= w.cap_pairs) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); return; }
     w.cs_key[idx] = make_int2(s1, s2);
-    w.cs_n[idx] = f4(n, __int_as_float(cnt));
+    w.cs_n[idx] = f4(n, __int_as_float(cnt | (spec ? JG_STREAM_SPECULATIVE : 0)));
     for (int k = 0; k < cnt; k++) { w.cs_pa[4 * idx + k] = oA[k]; w.cs_pb[4 * idx + k] = oB[k]; }
 }
 
-// Stage 3, one thread per overlapping pair: world transform, the first test of the
+// Stage 3, one thread per colliding record: world transform, the first test of the
 // triangle-edge filter (TriangleEdgeCollisionFilter.cs:183-240; pairs near a mesh edge
-// move to stage 4) and the one-shot manifold; appends the contact stream record.
+// move to stage 4) and the one-shot manifold; appends the contact stream record.  A
+// speculative record (kind 3, already in world space) registers its one point
+// (World.Detect.cs:185-196).
 __global__ void __launch_bounds__(128) k_manifold(WorldDev w, StepParams sp) {
     const int ncol = min(w.ctr->ncol, w.cap_arb);
     int pts = 0;
     for (int base = blockIdx.x * blockDim.x; base < ncol; base += gridDim.x * blockDim.x) {
         int c = base + threadIdx.x;
-        bool emit = false, to_edge = false;
+        bool emit = false, to_edge = false, spec = false;
         int s1 = 0, s2 = 0, cnt = 0;
         v3 n = mk3(0.f);
         float4 oA[4], oB[4];
         if (c < ncol) {
-            int2 pr = w.pairs[w.col_pair[c].x];
+            int2 cp = w.col_pair[c];
+            spec = cp.y == 3;
+            int2 pr = w.pairs[cp.x];
             s1 = pr.x; s2 = pr.y;
             ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
             int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
@@ -1173,9 +1383,11 @@ __global__ void __launch_bounds__(128) k_manifold(WorldDev w, StepParams sp) {
             float4 nr = w.col_res[3 * c + 2];
             n = mk3(nr);
             float pen = nr.w;
-            pA = rotate(pA, qa); pA = pA + pa;
-            pB = rotate(pB, qa); pB = pB + pa;
-            n = rotate(n, qa);
+            if (!spec) {
+                pA = rotate(pA, qa); pA = pA + pa;
+                pB = rotate(pB, qa); pB = pB + pa;
+                n = rotate(n, qa);
+            }
             emit = true;
             bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
             if (sp.edge_filter && c1 != c2) {
@@ -1190,12 +1402,12 @@ __global__ void __launch_bounds__(128) k_manifold(WorldDev w, StepParams sp) {
             }
             (void)pen;
             if (emit) {
-                if (sp.aux_contacts) cnt = manifold_thread(sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
+                if (sp.aux_contacts && !spec) cnt = manifold_thread(sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
                 else { cnt = 1; oA[0] = f4(pA, 0.f); oB[0] = f4(pB, 0.f); }
             }
         }
         int idx = warp_append(&w.ctr->nstream, emit);
-        if (idx >= 0) { write_stream(w, idx, s1, s2, n, cnt, oA, oB); pts += cnt; }
+        if (idx >= 0) { write_stream(w, idx, s1, s2, n, cnt, spec, oA, oB); pts += cnt; }
         int ei = warp_append(&w.ctr->nedge, to_edge);
         if (ei >= 0) w.edge_list[ei] = c;
     }
@@ -1216,7 +1428,9 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
     const int ne = min(w.ctr->nedge, w.cap_arb);
     for (int e = next_item(&w.ctr->edge_next, lane); e < ne; e = next_item(&w.ctr->edge_next, lane)) {
         int c = w.edge_list[e];
-        int2 pr = w.pairs[w.col_pair[c].x];
+        int2 cp = w.col_pair[c];
+        const bool from_sweep = cp.y == 3;
+        int2 pr = w.pairs[cp.x];
         int s1 = pr.x, s2 = pr.y;
         ShapeRef sa = load_shape(w, s1), sb = load_shape(w, s2);
         int b1 = w.sinfo[s1].y, b2 = w.sinfo[s2].y;
@@ -1226,9 +1440,11 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
         float4 nr = w.col_res[3 * c + 2];
         v3 n = mk3(nr);
         float pen = nr.w;
-        pA = rotate(pA, qa); pA = pA + pa;
-        pB = rotate(pB, qa); pB = pB + pa;
-        n = rotate(n, qa);
+        if (!from_sweep) {
+            pA = rotate(pA, qa); pA = pA + pa;
+            pB = rotate(pB, qa); pB = pB + pa;
+            n = rotate(n, qa);
+        }
         bool c1 = sa.kind == JG_SHAPE_TRIANGLE, c2 = sb.kind == JG_SHAPE_TRIANGLE;
         int tri = c1 ? sa.tri : sb.tri;
         q4 tq = c1 ? qa : qb;
@@ -1270,13 +1486,13 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
         }
         v3 oA[4], oB[4];
         int cnt;
-        if (sp.aux_contacts) cnt = build_manifold(E, sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
+        if (sp.aux_contacts && !from_sweep) cnt = build_manifold(E, sa, sb, qa, qb, pa, pb, pA, pB, n, oA, oB);
         else { cnt = 1; oA[0] = pA; oB[0] = pB; }
         if (lane == 0) {
             int idx = atomicAdd(&w.ctr->nstream, 1);
             float4 fa[4], fb[4];
             for (int k = 0; k < cnt; k++) { fa[k] = f4(oA[k], 0.f); fb[k] = f4(oB[k], 0.f); }
-            write_stream(w, idx, s1, s2, n, cnt, fa, fb);
+            write_stream(w, idx, s1, s2, n, cnt, from_sweep, fa, fb);
         }
         pts += cnt;
     }
@@ -1339,6 +1555,7 @@ void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int
     k_pair_offsets<<<1, 1, 0, s>>>(w);
     k_pair_scatter<<<nsm * 4, 256, 0, s>>>(w);
     k_mpr<<<nsm * 8, 256, 0, s>>>(w);
+    k_sweep<<<nsm * 2, 128, 0, s>>>(w, p);
     k_epa<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w);
     k_manifold<<<nsm * 16, 128, 0, s>>>(w, p);
     k_edge<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w, p);

@@ -120,7 +120,9 @@ struct DevCounters {
     int task_colors;
     int epa_next;     // work cursors of the warp-per-pair narrowphase stages
     int edge_next;
-    int pad[3];
+    int nspec;        // speculative sweep candidates, and of those the pairs registered
+    int nspec_hit;
+    int pad[1];
 };
 
 struct WorldDev {
@@ -160,6 +162,7 @@ struct WorldDev {
     float4* col_portal;          // [12 * cap_arb] MPR portal (4 vertices: V, A, B), by EPA-list slot
     int* epa_list;               // [cap_arb] colliding-record index of each deep pair
     int* edge_list;              // [cap_arb] colliding-record index of each pair near a mesh edge
+    int* spec_list;              // [cap_pairs] pairs without overlap that qualify for the sweep
     int2* cs_key;
     float4* cs_n;                // normal xyz, count
     float4* cs_pa;               // [4 * cap_pairs]
@@ -221,12 +224,17 @@ struct WorldDev {
     float* rec_tgt;
 };
 
+// Contact stream record flag (bits above the point count in the normal's w): the pair came
+// from the speculative sweep and is solved without angular terms (SolveMode.Angular removed).
+#define JG_STREAM_SPECULATIVE 0x100
+
 struct StepParams {
     float dt, sub_dt, inv_dt, inv_sub_dt;
     float3 gravity;
     int substeps, iterations, relax;
     int aux_contacts, persistent, edge_filter;
     float spec_relax;
+    float spec_threshold;        // SpeculativeVelocityThreshold
     int warm_start;
     int record_residual;
     int partition;               // 1: partitioned solve (tasks + remainder), 0: global colours only
@@ -245,7 +253,7 @@ struct StepParams {
 int jg_solver_task_maxb(int block, int ctas_per_sm);
 
 // ---- stage launchers (each defined in its own translation unit) ------------------------
-void jg_launch_aabb(WorldDev& w, cudaStream_t s);
+void jg_launch_aabb(WorldDev& w, float dt, cudaStream_t s);
 int  jg_launch_broadphase(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile);
 void jg_launch_merge(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);

@@ -356,3 +356,41 @@ def free_cluster(n=300, spacing=3.2, speed=2.0, seed=12350):
     return dict(bodies=bodies, shapes=shapes, hull=hull, triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[],
                 params=dict(substeps=4, solver_iterations=8, relax_iterations=4, gravity=(0.0, 0.0, 0.0)),
                 dt=1.0 / 100.0)
+
+
+def bullets(n=256, speed=(60.0, 150.0), speculative=True, seed=12351, spacing=1.2):
+    """Fast small bodies (spheres, boxes, capsules) fired down at a thin static slab
+    (0.1 thick), the case speculative contacts exist for: in one step of 1/60 s each body
+    covers 1 to 2.5 m, so without a sweep most pass through the slab between two steps
+    (World.Detect.cs:98-122).  Body 0 is the slab."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    side = int(np.ceil(np.sqrt(n)))
+    bodies = _body(n + 1)
+    shapes = np.zeros(n + 1, abi.SHAPE_DTYPE)
+    half = side * spacing / 2 + 1.0
+    ground(bodies, shapes, 0, 0, size=(2 * half, 0.1, 2 * half), y=0.0)
+    k = np.arange(n)
+    kinds = np.array([abi.SHAPE_SPHERE, abi.SHAPE_BOX, abi.SHAPE_CAPSULE])[k % 3]
+    shapes["kind"][1:] = kinds
+    shapes["body"][1:] = k + 1
+    shapes["dims"][1:][kinds == abi.SHAPE_SPHERE, 0] = 0.15
+    shapes["dims"][1:][kinds == abi.SHAPE_BOX, :3] = 0.12
+    shapes["dims"][1:][kinds == abi.SHAPE_CAPSULE, 0] = 0.1
+    shapes["dims"][1:][kinds == abi.SHAPE_CAPSULE, 1] = 0.1
+    gx, gz = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
+    xz = (np.stack([gx.ravel(), gz.ravel()], 1)[:n] - (side - 1) / 2.0) * spacing
+    pos = np.zeros((n, 3))
+    pos[:, 0], pos[:, 2] = xz[:, 0], xz[:, 1]
+    pos[:, 1] = rng.uniform(1.0, 3.0, n)
+    bodies["position"][1:] = pos.astype(np.float32)
+    bodies["orientation"][1:] = random_quaternions(rng, n)
+    vel = np.zeros((n, 3))
+    vel[:, 1] = -rng.uniform(speed[0], speed[1], n)
+    vel[:, [0, 2]] = rng.normal(0.0, 0.5, (n, 2))
+    bodies["velocity"][1:] = vel.astype(np.float32)
+    if speculative:
+        bodies["flags"][1:] |= abi.BODY_SPECULATIVE
+    _finish_mass(bodies, shapes, np.zeros((0, 3), np.float32), 1, 1, n)
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[],
+                params=dict(substeps=2, solver_iterations=8, relax_iterations=4), dt=1.0 / 60.0)

@@ -74,6 +74,7 @@ template <class R> void set_bodies(World<R>& w, const jg_body_desc* d, int n) {
         b.motion = s.motion_type;
         b.flags = (s.flags & 0x3f0) | (s.flags & JG_BODY_ACTIVE) | (s.flags & JG_BODY_GYROSCOPIC);
         b.gravity = (s.flags & JG_BODY_NO_GRAVITY) == 0;
+        b.speculative = (s.flags & JG_BODY_SPECULATIVE) != 0;
         b.world = s.world;
         // DeltaVelocity/DeltaAngularVelocity: the velocity change queued by the last
         // RigidBody.Update (zero for a body that has not been stepped yet).
@@ -103,7 +104,7 @@ template <class R> void get_bodies(const World<R>& w, jg_body_desc* d, int n) {
         s.linear_damping = (float)b.lin_damp; s.angular_damping = (float)b.ang_damp;
         s.force[0] = (float)b.force.x; s.force[1] = (float)b.force.y; s.force[2] = (float)b.force.z;
         s.torque[0] = (float)b.torque.x; s.torque[1] = (float)b.torque.y; s.torque[2] = (float)b.torque.z;
-        s.flags = b.flags | (b.gravity ? 0 : JG_BODY_NO_GRAVITY);
+        s.flags = b.flags | (b.gravity ? 0 : JG_BODY_NO_GRAVITY) | (b.speculative ? JG_BODY_SPECULATIVE : 0);
     }
 }
 
@@ -180,6 +181,7 @@ template <class R> struct Handle {
         w.substeps = p->substeps; w.iterations = p->solver_iterations; w.relax = p->relax_iterations;             \
         w.aux_contacts = p->enable_auxiliary_contacts != 0; w.persistent = p->persistent_manifold != 0;           \
         w.spec_relax = p->speculative_relaxation; w.edge_filter = p->edge_filter != 0;                             \
+        w.spec_threshold = p->speculative_threshold;                                                               \
         w.record_residual = p->record_residual != 0;                                                               \
     }                                                                                                              \
     extern "C" void jor_world_set_bodies_##SUF(void* h, const jg_body_desc* d, int n) { set_bodies(((Handle<R>*)h)->w, d, n); } \
@@ -232,6 +234,7 @@ template <class R> struct Handle {
         w.register_contact(s1, s2, r);                                                                             \
     }                                                                                                              \
     extern "C" void jor_world_narrowphase_##SUF(void* h) { ((Handle<R>*)h)->w.narrowphase(); }                    \
+    extern "C" void jor_world_set_step_dt_##SUF(void* h, float dt) { ((Handle<R>*)h)->w.step_dt = (R)dt; }        \
     /* ContactData.PrepareForIteration / Iterate on every arbiter, key order (tests) */                            \
     extern "C" void jor_world_prepare_##SUF(void* h, float dt, int substeps) {                                    \
         World<R>& w = ((Handle<R>*)h)->w; TimeStep<R> ts((R)dt, substeps);                                         \
@@ -267,7 +270,7 @@ template <class R> struct Handle {
         long long pts = 0;                                                                                         \
         for (auto& a : w.arbiters) pts += __builtin_popcount(a.usage & 15u);                                       \
         out[0] = w.n_pairs; out[1] = w.n_colliding; out[2] = w.n_points; out[3] = (long long)w.arbiters.size();    \
-        out[4] = pts; out[5] = w.solver.epa_calls; out[6] = w.solver.epa_failures;                                 \
+        out[4] = pts; out[5] = w.solver.epa_calls; out[6] = w.solver.epa_failures; out[7] = w.n_speculative;      \
     }                                                                                                              \
     extern "C" int jor_world_pairs_##SUF(void* h, int* out, int cap) {                                            \
         auto p = ((Handle<R>*)h)->w.find_pairs();                                                                  \
@@ -323,6 +326,17 @@ template <class R> struct Handle {
                              : sol.collision_world(sa, sb, get4d<R>(qa), get4d<R>(qb), get3d<R>(pa), get3d<R>(pb), pA, pB, n, pen); \
         put3d(out, pA); put3d(out + 3, pB); put3d(out + 6, n); out[9] = (double)pen;                             \
         out[10] = sol.epa_calls; out[11] = sol.epa_failures;                                                       \
+        return hit ? 1 : 0;                                                                                        \
+    }                                                                                                              \
+    /* NarrowPhase.Sweep (NarrowPhase.cs:1100-1136): out = pA, pB, n, toi */                                     \
+    extern "C" int jor_sweep_##SUF(const jg_shape_desc* da, const float* va, const jg_shape_desc* db,            \
+                                   const float* vb, const double* qa, const double* qb, const double* pa,         \
+                                   const double* pb, const double* sa_, const double* sb_, double* out) {          \
+        Shape<R> sa, sb; std::vector<R> s1, s2; desc_to_shape<R>(da, va, sa, s1); desc_to_shape<R>(db, vb, sb, s2); \
+        V3<R> pA, pB, n; R toi = 0;                                                                                \
+        bool hit = sweep_world(sa, sb, get4d<R>(qa), get4d<R>(qb), get3d<R>(pa), get3d<R>(pb), get3d<R>(sa_),     \
+                               get3d<R>(sb_), pA, pB, n, toi);                                                     \
+        put3d(out, pA); put3d(out + 3, pB); put3d(out + 6, n); out[9] = (double)toi;                              \
         return hit ? 1 : 0;                                                                                        \
     }                                                                                                              \
     extern "C" int jor_manifold_##SUF(const jg_shape_desc* da, const float* va, const jg_shape_desc* db,         \

@@ -696,6 +696,179 @@ template <class R> struct MprEpa {
     }
 };
 
+// ---- GJK simplex with witness points (Collision/NarrowPhase/SimplexSolverAB.cs:28-359) ---
+// The simplex keeps up to four Minkowski vertices with their support points on A and B,
+// the barycentric weights of the point closest to the origin, and a mask of the vertices
+// that span it.  Each sub-simplex test reduces to the feature nearest the origin; the
+// returned search point is computed directly (not from the weights) as the reference does.
+template <class R> struct SimplexAB {
+    static constexpr R Eps = (R)1e-8;
+    Vertex<R> v[4];
+    R bc[4];
+    unsigned mask = 0;
+
+    // ClosestSegment (SimplexSolverAB.cs:60-100)
+    V3<R> segment(int i0, int i1, R* w, unsigned& m) const {
+        V3<R> a = v[i0].V, b = v[i1].V;
+        V3<R> d = b - a;
+        R dd = len2(d);
+        if (dd < Eps) { m = 1u << i1; w[i0] = 0; w[i1] = 1; return b; }
+        R t = -dot(a, d) / dd;
+        if (t > (R)1.0) { m = 1u << i1; w[i0] = 0; w[i1] = 1; return b; }
+        if (t < (R)0.0) { m = 1u << i0; w[i0] = 1; w[i1] = 0; return a; }
+        w[i0] = (R)1.0 - t; w[i1] = t;
+        m = (1u << i0) | (1u << i1);
+        return cross(d, cross(a, d)) * ((R)1.0 / dd);
+    }
+    // ClosestTriangle (SimplexSolverAB.cs:102-176): the interior when all three weights are
+    // non-negative and the triangle is not degenerate, else the nearest of the edges whose
+    // opposite weight is negative (all three when degenerate).
+    V3<R> triangle(int i0, int i1, int i2, R* w, unsigned& m) const {
+        m = 0;
+        V3<R> a = v[i0].V, b = v[i1].V, c = v[i2].V;
+        V3<R> u = a - b, e = a - c;
+        V3<R> nrm = cross(u, e);
+        R t = len2(nrm);
+        R it = (R)1.0 / t;
+        bool degenerate = t < Eps;
+        R l2 = dot(cross(u, a), nrm) * it;
+        R l1 = dot(cross(a, e), nrm) * it;
+        R l0 = (R)1.0 - l2 - l1;
+        R best = std::numeric_limits<R>::max();
+        V3<R> cp;
+        R tmp[4];
+        const int edges[3][2] = {{i1, i2}, {i0, i2}, {i0, i1}};
+        const R lam[3] = {l0, l1, l2};
+        for (int k = 0; k < 3; k++) {
+            if (!(lam[k] < (R)0.0 || degenerate)) continue;
+            unsigned mk;
+            V3<R> q = segment(edges[k][0], edges[k][1], tmp, mk);
+            R dist = len2(q);
+            if (dist < best) {
+                for (int j = 0; j < 4; j++) w[j] = tmp[j];
+                m = mk; cp = q;
+                best = dist;
+            }
+        }
+        if (m != 0) return cp;
+        w[i0] = l0; w[i1] = l1; w[i2] = l2;
+        m = (1u << i0) | (1u << i1) | (1u << i2);
+        return nrm * (dot(nrm, a) * it);
+    }
+    static R det(V3<R> a, V3<R> b, V3<R> c, V3<R> d) { return dot(b - a, cross(c - a, d - a)); }
+    // ClosestTetrahedron (SimplexSolverAB.cs:178-276)
+    V3<R> tetra(R* w, unsigned& m) const {
+        R dt = det(v[0].V, v[1].V, v[2].V, v[3].V);
+        R idt = (R)1.0 / dt;
+        bool degenerate = dt * dt < Eps;
+        V3<R> z;
+        R l0 = det(z, v[1].V, v[2].V, v[3].V) * idt;
+        R l1 = det(v[0].V, z, v[2].V, v[3].V) * idt;
+        R l2 = det(v[0].V, v[1].V, z, v[3].V) * idt;
+        R l3 = (R)1.0 - l0 - l1 - l2;
+        R best = std::numeric_limits<R>::max();
+        V3<R> cp;
+        R tmp[4];
+        m = 0;
+        const int faces[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+        const R lam[4] = {l0, l1, l2, l3};
+        for (int k = 0; k < 4; k++) {
+            if (!(lam[k] < (R)0.0 || degenerate)) continue;
+            unsigned mk;
+            V3<R> q = triangle(faces[k][0], faces[k][1], faces[k][2], tmp, mk);
+            R dist = len2(q);
+            if (dist < best) {
+                for (int j = 0; j < 4; j++) w[j] = tmp[j];
+                m = mk; cp = q;
+                best = dist;
+            }
+        }
+        if (m != 0) return cp;
+        w[0] = l0; w[1] = l1; w[2] = l2; w[3] = l3;
+        m = 15;
+        return V3<R>();
+    }
+    // AddVertex (SimplexSolverAB.cs:300-357): false when the origin is enclosed.
+    bool add(const Vertex<R>& x, V3<R>& closest) {
+        int ix[4], used = 0, free_slot = 0;
+        for (int i = 0; i < 4; i++) {
+            if (mask & (1u << i)) ix[used++] = i;
+            else free_slot = i;
+        }
+        ix[used++] = free_slot;
+        v[free_slot] = x;
+        switch (used) {
+            case 1: closest = v[ix[0]].V; mask = 1u << ix[0]; bc[ix[0]] = 1; return true;
+            case 2: closest = segment(ix[0], ix[1], bc, mask); return true;
+            case 3: closest = triangle(ix[0], ix[1], ix[2], bc, mask); return true;
+            default: closest = tetra(bc, mask); return mask != 15;
+        }
+    }
+    // GetClosest (SimplexSolverAB.cs:278-293)
+    void closest_points(V3<R>& pA, V3<R>& pB) const {
+        pA = V3<R>(); pB = V3<R>();
+        for (int i = 0; i < 4; i++) {
+            if (!(mask & (1u << i))) continue;
+            pA = pA + bc[i] * v[i].A;
+            pB = pB + bc[i] * v[i].B;
+        }
+    }
+};
+
+// ---- time of impact (NarrowPhase.Sweep, NarrowPhase.cs:1100-1222) -------------------------
+// Conservative advancement on the Minkowski difference, shape A fixed at the origin: B moves
+// along `sweep`; each support point in front of the current search direction advances the
+// time of impact lambda to the plane it spans, and the simplex is rebuilt around the
+// moved B.  Returns false when B moves away from the current separating plane (no hit);
+// true with lambda = 0 for shapes that already overlap.
+template <class R> bool sweep_local(const Shape<R>& sa, const Shape<R>& sb, Q4<R> qb, V3<R> pb, V3<R> sweep,
+                                    V3<R>& pA, V3<R>& pB, V3<R>& normal, R& lambda) {
+    const R eps = (R)1e-4;
+    int iter = 34;
+    SimplexAB<R> sx;
+    Vertex<R> c;
+    mk_center(sa, sb, qb, pb, c);
+    V3<R> pos = pb;
+    lambda = 0;
+    pA = pB = V3<R>();
+    V3<R> r = sweep;
+    V3<R> v = -c.V;
+    normal = V3<R>();
+    R d2 = len2(v);
+    while (d2 > eps * eps && iter-- != 0) {
+        Vertex<R> x;
+        mk_support(sa, sb, qb, pos, v, x);
+        R vw = -dot(v, x.V);
+        if (vw > (R)0.0) {
+            R vr = dot(v, r);
+            if (vr >= -(R)1e-12) { lambda = std::numeric_limits<R>::infinity(); return false; }
+            lambda -= vw / vr;
+            pos = pb + lambda * r;
+            normal = v;
+        }
+        if (!sx.add(x, v)) break;
+        v = -v;
+        d2 = len2(v);
+    }
+    sx.closest_points(pA, pB);
+    normal = normalize_safe(normal, (R)1e-16);
+    return true;
+}
+// World-space Sweep (NarrowPhase.cs:1100-1136): both bodies move with their linear
+// velocities; the points come back at the bodies' current poses.
+template <class R> bool sweep_world(const Shape<R>& sa, const Shape<R>& sb, Q4<R> qa, Q4<R> qb, V3<R> pa, V3<R> pb,
+                                    V3<R> va, V3<R> vb, V3<R>& pA, V3<R>& pB, V3<R>& normal, R& lambda) {
+    Q4<R> q = qconjmul(qa, qb);
+    V3<R> p = rotate_inv(pb - pa, qa);
+    V3<R> s = rotate_inv(vb - va, qa);
+    if (!sweep_local(sa, sb, q, p, s, pA, pB, normal, lambda)) return false;
+    pA = rotate(pA, qa); pA = pA + pa;
+    pB = rotate(pB, qa); pB = pB + pa;
+    normal = rotate(normal, qa);
+    pB = pB + lambda * (va - vb);
+    return true;
+}
+
 // ---- one-shot manifold (Collision/NarrowPhase/CollisionManifold.cs:22-586) ---------------
 template <class R> struct Manifold {
     static const int MaxSupport = 6, MaxPoints = 12, SolverLimit = 4;

@@ -45,6 +45,7 @@ template <class R> struct Body {
     R lin_damp = (R)0.998, ang_damp = (R)0.995;
     V3<R> force, torque;
     bool gravity = true;
+    bool speculative = false;       // RigidBody.EnableSpeculativeContacts
     int world = 0;
     bool active() const { return (flags & 4) != 0; }
     bool gyroscopic() const { return (flags & 8) != 0; }

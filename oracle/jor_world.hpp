@@ -32,12 +32,14 @@ template <class R> struct World {
     int substeps = 1, iterations = 6, relax = 4;
     bool aux_contacts = true, persistent = true, edge_filter = true;
     R spec_relax = (R)0.9;
+    R spec_threshold = (R)10.0;                // SpeculativeVelocityThreshold
+    R step_dt = 0;                             // dt of the step in progress
     bool external_order = false;               // use ContactData::color / Joint::color
     bool record_residual = false;
     std::vector<R> residuals;                  // first substep, one value per iteration
     MprEpa<R> solver;
     EdgeFilter<R> efilter;
-    int64_t n_pairs = 0, n_colliding = 0, n_points = 0;
+    int64_t n_pairs = 0, n_colliding = 0, n_points = 0, n_speculative = 0;
     int nthreads = 1;
 
     static uint64_t key(int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
@@ -70,6 +72,13 @@ template <class R> struct World {
         for (size_t i = 0; i < shapes.size(); i++) {
             const Body<R>& b = bodies[shape_body[i]];
             out[i] = shape_aabb(shapes[i], b.q, b.pos);
+            if (b.speculative) {
+                // RigidBodyShape.UpdateWorldBoundingBox (RigidBodyShape.cs:37-57): grown by the
+                // distance the linear velocity covers in one step
+                R swept = step_dt * std::sqrt(len2(b.vel));
+                out[i].mn = out[i].mn - V3<R>(swept);
+                out[i].mx = out[i].mx + V3<R>(swept);
+            }
         }
         return out;
     }
@@ -207,6 +216,7 @@ template <class R> struct World {
         V3<R> A[4], B[4];
         V3<R> pA, pB;
         R pen = 0;
+        bool speculative = false;              // registered with SolveMode.Angular removed
     };
     // World.Detect (World.Detect.cs:125-218) up to, not including, RegisterContact.
     DetectResult detect(int sA, int sB, MprEpa<R>& sol) {
@@ -218,7 +228,24 @@ template <class R> struct World {
         V3<R> pA, pB, n;
         R pen;
         bool hit = sol.mpr_epa_world(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, pA, pB, n, pen);
-        if (!hit) return r;
+        if (!hit) {
+            // speculative branch (World.Detect.cs:168-196): a sweep along the relative linear
+            // velocity; a hit within the step registers its one point, linear terms only
+            if (!b1.speculative && !b2.speculative) return r;
+            V3<R> dv = b2.vel - b1.vel;
+            if (len2(dv) < spec_threshold * spec_threshold) return r;
+            R toi;
+            bool ok = sweep_world(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, b1.vel, b2.vel, pA, pB, n, toi);
+            if (!ok || toi > step_dt || toi == (R)0.0) return r;
+            pen = dot(n, pA - pB) * spec_relax;
+            if (edge_filter) {
+                bool tri_dyn = shapes[sA].is_triangle() ? b1.motion == DYNAMIC : b2.motion == DYNAMIC;
+                if (!efilter.filter(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, tri_dyn, sol, pA, pB, n, pen)) return r;
+            }
+            r.hit = true; r.speculative = true; r.n = n; r.pA = pA; r.pB = pB; r.pen = pen;
+            r.count = 1; r.A[0] = pA; r.B[0] = pB;
+            return r;
+        }
         if (edge_filter) {
             bool tri_dyn = shapes[sA].is_triangle() ? b1.motion == DYNAMIC : b2.motion == DYNAMIC;
             if (!efilter.filter(shapes[sA], shapes[sB], b1.q, b2.q, b1.pos, b2.pos, tri_dyn, sol, pA, pB, n, pen)) return r;
@@ -240,18 +267,19 @@ template <class R> struct World {
         ContactData<R>& cd = arbiters[ai];
         if (!persistent) cd.usage = 0;
         reset_mode(cd);
+        if (r.speculative) cd.mode &= ~(ContactData<R>::AngularBody1 | ContactData<R>::AngularBody2);
         for (int e = 0; e < r.count; e++) add_contact(cd, bodies, r.A[e], r.B[e], r.n);
     }
 
     void narrowphase() {
         auto pairs = find_pairs();
         n_pairs = (int64_t)pairs.size();
-        n_colliding = 0; n_points = 0;
+        n_colliding = 0; n_points = 0; n_speculative = 0;
         if (nthreads <= 1) {
             for (auto& p : pairs) {
                 DetectResult r = detect(p.first, p.second, solver);
                 if (!r.hit) continue;
-                n_colliding++; n_points += r.count;
+                n_colliding++; n_points += r.count; n_speculative += r.speculative;
                 register_contact(p.first, p.second, r);
             }
             return;
@@ -263,7 +291,7 @@ template <class R> struct World {
         });
         for (size_t i = 0; i < pairs.size(); i++) {
             if (!res[i].hit) continue;
-            n_colliding++; n_points += res[i].count;
+            n_colliding++; n_points += res[i].count; n_speculative += res[i].speculative;
             register_contact(pairs[i].first, pairs[i].second, res[i]);
         }
     }
@@ -355,6 +383,7 @@ template <class R> struct World {
     void step(R dt, bool narrow = true) {
         if (dt < std::numeric_limits<R>::epsilon()) return;
         TimeStep<R> ts(dt, substeps);
+        step_dt = dt;
         if (narrow) narrowphase();
         build_order();
         for (int s = 0; s < substeps; s++) solve_substep(ts, s == 0);
@@ -428,6 +457,7 @@ template <class R> struct RegularSolver {
     }
     void step(R dt) {
         TimeStep<R> ts(dt, w.substeps);
+        w.step_dt = dt;
         w.narrowphase();
         locks = std::vector<std::atomic<int>>(w.bodies.size());
         for (auto& l : locks) l.store(0);

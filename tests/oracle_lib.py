@@ -39,6 +39,7 @@ def load():
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
+            "jor_world_set_step_dt": (None, [P, F]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
             "jor_world_set_penalty": (None, [P, I, I, D]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
@@ -50,6 +51,7 @@ def load():
             "jor_support": (None, [P, P, P, P]), "jor_aabb": (None, [P, P, P, P, P]),
             "jor_collide": (I, [P, P, P, P, P, P, P, P, D, I, P]),
             "jor_manifold": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
+            "jor_sweep": (I, [P, P, P, P, P, P, P, P, P, P, P]),
             "jor_exact_side": (I, [P, P, P, P]), "jor_filter_side": (I, [P, P, P, P, P]),
             "jor_stable_sincos": (None, [D, P, P]), "jor_stable_atan2": (D, [D, D]),
         }
@@ -129,6 +131,27 @@ def manifold(a, b, qa, qb, pa, pb, pA, pB, n, real="f"):
     k = getattr(lib, "jor_manifold_" + real)(p(sa), p(va), p(sb), p(vb), *[p(x) for x in args], p(out))
     m = out[:6 * k].reshape(k, 6)
     return m[:, :3], m[:, 3:]
+
+
+def aabb(s, q, pos, real="f"):
+    """World bounding box (min, max) of a shape at an orientation and position."""
+    lib = load()
+    sa, va = _shape_args(s)
+    out = np.zeros(6, np.float64)
+    args = [np.ascontiguousarray(x, np.float64) for x in (q, pos)]
+    getattr(lib, "jor_aabb_" + real)(p(sa), p(va), p(args[0]), p(args[1]), p(out))
+    return out[:3], out[3:]
+
+
+def sweep(a, b, qa, qb, pa, pb, va, vb, real="f"):
+    """NarrowPhase.Sweep: (hit, pA, pB, n, toi), points at the bodies' current poses."""
+    lib = load()
+    sa, ra = _shape_args(a)
+    sb, rb = _shape_args(b)
+    out = np.zeros(10, np.float64)
+    args = [np.ascontiguousarray(x, np.float64) for x in (qa, qb, pa, pb, va, vb)]
+    hit = getattr(lib, "jor_sweep_" + real)(p(sa), p(ra), p(sb), p(rb), *[p(x) for x in args], p(out))
+    return bool(hit), out[0:3], out[3:6], out[6:9], out[9]
 
 
 def support(s, d, real="f"):
@@ -239,13 +262,17 @@ class OracleWorld:
         a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, n)]
         self.fn("jor_world_register_contact")(self.h, s1, s2, p(a[0]), p(a[1]), p(a[2]))
 
-    def narrowphase(self):
+    def narrowphase(self, dt=None):
+        """Detection alone; dt is the step length the speculative branch tests against."""
+        if dt is not None:
+            self.fn("jor_world_set_step_dt")(self.h, float(dt))
         self.fn("jor_world_narrowphase")(self.h)
 
     def counters(self):
-        out = np.zeros(7, np.int64)
+        out = np.zeros(8, np.int64)
         self.fn("jor_world_counters")(self.h, p(out))
-        return dict(zip(["pairs", "colliding", "points", "arbiters", "contacts", "epa_calls", "epa_failures"], out.tolist()))
+        return dict(zip(["pairs", "colliding", "points", "arbiters", "contacts", "epa_calls", "epa_failures",
+                         "speculative"], out.tolist()))
 
     def pairs(self, sweep=False):
         name = "jor_world_pairs_sweep" if sweep else "jor_world_pairs"

@@ -48,6 +48,7 @@ def test_default_params_match_world_defaults(built_lib):
     assert (p.substeps, p.solver_iterations, p.relax_iterations) == (1, 6, 4)
     assert p.enable_auxiliary_contacts == 1 and p.persistent_manifold == 1
     assert p.speculative_relaxation == pytest.approx(0.9)
+    assert p.speculative_threshold == pytest.approx(10.0)
 
 
 def test_invalid_arguments_are_rejected_without_a_device(built_lib):
