@@ -63,6 +63,9 @@ extern "C" {
 /* Constraint kinds (Dynamics/Constraints/BallSocket.cs, HingeAngle.cs) */
 #define JG_CONSTRAINT_BALLSOCKET 1
 #define JG_CONSTRAINT_HINGEANGLE 2
+#define JG_CONSTRAINT_DISTANCELIMIT 3   /* Dynamics/Constraints/DistanceLimit.cs */
+#define JG_CONSTRAINT_CONELIMIT 4       /* Dynamics/Constraints/ConeLimit.cs     */
+#define JG_CONSTRAINT_TWISTANGLE 5      /* Dynamics/Constraints/TwistAngle.cs    */
 
 /* ---- plain data structures ------------------------------------------------------- */
 
@@ -215,8 +218,16 @@ int jg_upload_shapes(jg_world* world, const jg_shape_desc* shapes, int32_t count
  * RigidBody.Move (RigidBody.cs:637-648): the body's contact cache is cleared. */
 int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value);
 
-/* World.CreateConstraint<BallSocket/HingeAngle> + Initialize (BallSocket.cs:120-138,
- * HingeAngle.cs:84-110).  init: BallSocket anchor xyz; HingeAngle axis xyz, min, max. */
+/* World.CreateConstraint<T> + Initialize (BallSocket.cs:120-138, HingeAngle.cs:84-110,
+ * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128), world-space init:
+ *   BallSocket     anchor xyz
+ *   HingeAngle     axis xyz, min, max (radians)
+ *   DistanceLimit  anchor1 xyz, anchor2 xyz, min, max (offsets from the initial distance;
+ *                  min >= max fixes it, LinearLimit.Fixed = (1e-6, -1e-6))
+ *   ConeLimit      axis1 xyz, axis2 xyz, min, max (radians, 0 <= min <= max <= pi, not a
+ *                  fixed tilt of 0 or pi)
+ *   TwistAngle     axis1 xyz, axis2 xyz, min, max (radians, finite)
+ * Invalid arguments return JG_ERR_INVALID_ARG (the reference's ArgumentException). */
 int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,
                       const float* init, int32_t* out_id);
 
@@ -267,7 +278,8 @@ int jg_get_arbiter_events(jg_world* world, int32_t* created_pairs, int32_t creat
                           int32_t* n_created, int32_t* removed_pairs, int32_t removed_capacity,
                           int32_t* n_removed);
 /* Constraint state in creation order: the accumulated impulse (BallSocket.Impulse,
- * BallSocket.cs:221; HingeAngle.Impulse, HingeAngle.cs:311) as 3 floats each, and
+ * BallSocket.cs:221; HingeAngle.Impulse, HingeAngle.cs:311) as 3 floats each (the one-row
+ * kinds, DistanceLimit, ConeLimit and TwistAngle, in the first of the three), and
  * the order key of the last step's solve (768 + global colour: constraints sharing a key
  * share no dynamic body). */
 int jg_get_constraints(jg_world* world, int32_t* order_keys, float* impulses, int32_t capacity,

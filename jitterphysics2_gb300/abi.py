@@ -34,7 +34,7 @@ MLP_IN, MLP_HID, MLP_OUT = 24, 64, 3
 MLP_NW = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_OUT * MLP_HID + MLP_OUT  # trainable
 MLP_NPARAM = MLP_NW + MLP_IN + MLP_IN + MLP_OUT  # + feature mean, feature scale, output scale
 WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
-CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE = 1, 2
+CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE, CONSTRAINT_DISTANCELIMIT, CONSTRAINT_CONELIMIT, CONSTRAINT_TWISTANGLE = 1, 2, 3, 4, 5
 
 ERROR_NAMES = {
     JG_ERR_INVALID_ARG: "JG_ERR_INVALID_ARG", JG_ERR_CAPACITY: "JG_ERR_CAPACITY",

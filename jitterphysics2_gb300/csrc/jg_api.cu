@@ -585,9 +585,39 @@ int jg_set_body(jg_world* w, int32_t body, int32_t field, const float* v) {
     return JG_OK;
 }
 
+// JQuaternion.CreateFromToRotation (JQuaternion.cs:84-101)
+static q4 from_to_rotation(v3 from, v3 to) {
+    float d = dot(from, to);
+    if (d < -1.0f + 1e-6f) {
+        v3 ax = create_orthonormal(from);
+        return q4{ax.x, ax.y, ax.z, 0.f};
+    }
+    float s = sqrtf((1.0f + d) * 2.0f);
+    float is = 1.0f / s;
+    v3 c = cross(from, to) * is;
+    return q4{c.x, c.y, c.z, s * 0.5f};
+}
+
 int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
     if (!w || !init) return JG_ERR_INVALID_ARG;
-    if (kind != JG_CONSTRAINT_BALLSOCKET && kind != JG_CONSTRAINT_HINGEANGLE) return JG_ERR_INVALID_ARG;
+    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_TWISTANGLE) return JG_ERR_INVALID_ARG;
+    if (kind >= JG_CONSTRAINT_DISTANCELIMIT) {
+        // the reference's argument checks (DistanceLimit.cs:99-103, ConeLimit.cs:96-99 and
+        // :228-238, TwistAngle.cs:88-92)
+        for (int i = 0; i < 6; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
+        float lo = init[6], hi = init[7];
+        if (kind == JG_CONSTRAINT_DISTANCELIMIT) {
+            if (std::isnan(lo) || std::isnan(hi)) return JG_ERR_INVALID_ARG;
+        } else {
+            if (len2(mk3(init[0], init[1], init[2])) == 0.f || len2(mk3(init[3], init[4], init[5])) == 0.f)
+                return JG_ERR_INVALID_ARG;
+            if (!std::isfinite(lo) || !std::isfinite(hi)) return JG_ERR_INVALID_ARG;
+            const float PI = 3.14159265358979323846f;
+            if (kind == JG_CONSTRAINT_CONELIMIT &&
+                (!(lo >= 0.f && lo <= PI) || !(hi >= lo && hi <= PI) || (lo == hi && (lo == 0.f || lo == PI))))
+                return JG_ERR_INVALID_ARG;
+        }
+    }
     if (b1 < 0 || b2 < 0 || b1 >= w->d.nb || b2 >= w->d.nb || b1 == b2) return JG_ERR_INVALID_ARG;
     if (w->nj_host >= w->d.cap_joints) return JG_ERR_CAPACITY;
     // the two bodies' current poses: from the host copy while it is current, else from the device
@@ -618,6 +648,30 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         J.la1 = f4(rotate_inv(anchor - p1, q1), 0.f);
         J.la2 = f4(rotate_inv(anchor - p2, q2), 0.f);
         J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_DISTANCELIMIT) {
+        // DistanceLimit.Initialize (DistanceLimit.cs:92-117)
+        v3 a1 = mk3(init[0], init[1], init[2]), a2 = mk3(init[3], init[4], init[5]);
+        J.la1 = f4(rotate_inv(a1 - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(a2 - p2, q2), 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+        J.lim = make_float4(init[6], init[7], sqrtf(len2(a2 - a1)), 0.f);
+    } else if (kind == JG_CONSTRAINT_CONELIMIT) {
+        // ConeLimit.Initialize (ConeLimit.cs:92-118)
+        J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
+        J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
+        J.lim = make_float4(init[6], init[7], 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_TWISTANGLE) {
+        // TwistAngle.Initialize (TwistAngle.cs:85-128): Q0 is the initial relative rotation
+        // turned so that body 1's axis lies on body 2's
+        v3 ax1 = normalize(mk3(init[0], init[1], init[2])), ax2 = normalize(mk3(init[3], init[4], init[5]));
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
+        J.lim = make_float4(init[6], init[7], 0.5f * init[6] + 0.5f * init[7], 0.f);
+        v3 u1 = rotate_inv(ax1, q1);
+        v3 B = rotate_inv(ax2, q2);
+        q4 rel = qmul(qconj(q2), q1);
+        J.axis = f4(B, 0.f);
+        J.q0 = f4(qmul(from_to_rotation(rotate(u1, rel), B), rel));
     } else {
         // HingeAngle.Initialize (HingeAngle.cs:84-110)
         v3 axis = normalize(mk3(init[0], init[1], init[2]));

@@ -1,6 +1,14 @@
-// Device BallSocket (Dynamics/Constraints/BallSocket.cs:140-252) and HingeAngle
-// (Dynamics/Constraints/HingeAngle.cs:133-364) rows, solved in the same colours as the
-// contacts.  Included by the solver translation unit.  Matrices are row-major float[3][3].
+// Device constraint rows, solved in the same colours as the contacts: BallSocket
+// (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle (HingeAngle.cs:133-364),
+// DistanceLimit (DistanceLimit.cs:227-391), ConeLimit (ConeLimit.cs:262-404) and TwistAngle
+// (TwistAngle.cs:170-323).  Included by the solver translation unit.  Matrices are
+// row-major float[3][3].
+//
+// JointDev fields of the one-row kinds: la1/la2 anchors (DistanceLimit) or local axes
+// (ConeLimit); axis / q0 the twist axis and reference rotation (TwistAngle); lim = (min, max,
+// distance or fixed angle, clamp); prm = (bias factor, softness); acc.x the accumulated
+// impulse, bias.x the bias, bil.x the effective mass, bil.w the hemisphere (TwistAngle);
+// Jacobian blocks in eff[0..2] and jac[0] (the ConeLimit block persists between steps).
 #pragma once
 
 struct M3x { float a[3][3]; };
@@ -363,13 +371,253 @@ __device__ void hinge_iterate(const WorldDev& w, JointDev& J, const StepParams& 
     if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, mv(jac, lambda)); store_vel(w.body, i2, b2); }
 }
 
+// ---- one-row limits ---------------------------------------------------------------------
+__device__ __forceinline__ float clamp_impulse(int clamp, float acc) {
+    if (clamp == 1) return fminf(acc, 0.0f);
+    if (clamp == 2) return fmaxf(acc, 0.0f);
+    return acc;
+}
+__device__ __forceinline__ float row_mass(float m, float softness, const StepParams& sp) {
+    m += softness * sp.inv_sub_dt;
+    return m > 0 ? 1.0f / m : 0.0f;
+}
+__device__ __forceinline__ sym6 sym_add(const sym6& a, const sym6& b) {
+    sym6 o;
+    o.m11 = a.m11 + b.m11; o.m12 = a.m12 + b.m12; o.m13 = a.m13 + b.m13;
+    o.m22 = a.m22 + b.m22; o.m23 = a.m23 + b.m23; o.m33 = a.m33 + b.m33;
+    return o;
+}
+
+// DistanceLimit.PrepareForIterationDistanceLimit (DistanceLimit.cs:227-306): the distance
+// between the anchors against [distance + min, distance + max]
+__device__ void distance_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 r1 = rotate(mk3(J.la1), mkq(w.q[i1])), r2 = rotate(mk3(J.la2), mkq(w.q[i2]));
+    v3 dp = (mk3(w.pos[i2]) + r2) - (mk3(w.pos[i1]) + r1);
+    float dist = sqrtf(len2(dp));
+    float err = dist - J.lim.z;
+    const float lo = J.lim.x, hi = J.lim.y;
+    int clamp;
+    if (lo >= hi) { err -= 0.5f * lo + 0.5f * hi; clamp = 3; }
+    else if (err >= hi) { clamp = 1; err -= hi; }
+    else if (err <= lo) { clamp = 2; err -= lo; }
+    else { J.lim.w = 0.f; J.acc.x = 0.f; return; }
+    if (dist == 0.0f) { J.lim.w = 0.f; J.acc.x = 0.f; return; }
+    J.lim.w = (float)clamp;
+    v3 n = dp * (1.0f / dist);
+    v3 j0 = -1.0f * n, j1 = -1.0f * cross(r1, n), j2 = 1.0f * n, j3 = cross(r2, n);
+    float m = dot(cmul(j0, b1.im), j0) + dot(cmul(j2, b2.im), j2) + dot(sym_mul(b1.I, j1), j1) + dot(sym_mul(b2.I, j3), j3);
+    float eff = row_mass(m, J.prm.y, sp);
+    float a = eff == 0.0f ? 0.0f : J.acc.x;
+    J.acc.x = a;
+    J.bil.x = eff;
+    J.bias.x = err * J.prm.x * sp.inv_dt;
+    J.eff[0] = f4(j0, 0.f); J.eff[1] = f4(j1, 0.f); J.eff[2] = f4(j2, 0.f); J.jac[0] = f4(j3, 0.f);
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v + cmul(a * j0, b1.im);
+        b1.w = b1.w + sym_mul(b1.I, a * j1);
+        store_vel(w.body, i1, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(a * j2, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, a * j3);
+        store_vel(w.body, i2, b2);
+    }
+}
+// DistanceLimit.IterateDistanceLimit (DistanceLimit.cs:344-391)
+__device__ void distance_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const int clamp = (int)J.lim.w;
+    if (clamp == 0) return;
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 j0 = mk3(J.eff[0]), j1 = mk3(J.eff[1]), j2 = mk3(J.eff[2]), j3 = mk3(J.jac[0]);
+    float jv = dot(b1.v, j0) + dot(b1.w, j1) + dot(b2.v, j2) + dot(b2.w, j3);
+    float soft = J.acc.x * J.prm.y * sp.inv_sub_dt;
+    float lambda = -J.bil.x * (jv + J.bias.x + soft);
+    float old = J.acc.x;
+    J.acc.x = clamp_impulse(clamp, J.acc.x + lambda);
+    lambda = J.acc.x - old;
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v + cmul(lambda * j0, b1.im);
+        b1.w = b1.w + sym_mul(b1.I, lambda * j1);
+        store_vel(w.body, i1, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(lambda * j2, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, lambda * j3);
+        store_vel(w.body, i2, b2);
+    }
+}
+
+// ConeLimit.PrepareForIterationConeLimit (ConeLimit.cs:262-356): the angle between the
+// bodies' axes against [min, max]; the Jacobian row persists, and its sign flip drops the
+// cached impulse
+__device__ void cone_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 a1 = rotate(mk3(J.la1), mkq(w.q[i1])), a2 = rotate(mk3(J.la2), mkq(w.q[i2]));
+    v3 prev = mk3(J.eff[0]);
+    v3 j0 = cross(a2, a1);
+    float cosine = dot(a1, a2);
+    const float minA = J.lim.x, maxA = J.lim.y;
+    float lower = -minA, upper = -maxA;
+    float sine = sqrtf(len2(j0));
+    if (sine > 0) {
+        j0 = j0 * (1.0f / sine);
+    } else {
+        v3 axis = create_orthonormal(a1);
+        v3 other = cross(a1, axis);
+        sym6 I = sym_add(b1.I, b2.I);
+        j0 = dot(sym_mul(I, axis), axis) >= dot(sym_mul(I, other), other) ? axis : other;
+    }
+    v3 j1 = -j0;
+    J.eff[0] = f4(j0, 0.f); J.eff[1] = f4(j1, 0.f);
+    float acc = J.acc.x;
+    if (dot(prev, j0) < 0) acc = 0.f;
+    float err = -StableMathF::atan2(sine, cosine);
+    const float PI = 3.14159265358979323846f;
+    int clamp;
+    if (lower == upper) { clamp = 3; err -= upper; }
+    else if (err <= upper && maxA < PI) { clamp = 1; err -= upper; }
+    else if (err >= lower && minA > 0) { clamp = 2; err -= lower; }
+    else { J.lim.w = 0.f; J.acc.x = 0.f; return; }
+    J.lim.w = (float)clamp;
+    acc = clamp_impulse(clamp, acc);
+    float m = dot(sym_mul(b1.I, j0), j0) + dot(sym_mul(b2.I, j1), j1);
+    float eff = row_mass(m, J.prm.y, sp);
+    if (eff == 0.0f) acc = 0.f;
+    J.acc.x = acc;
+    J.bil.x = eff;
+    J.bias.x = -err * J.prm.x * sp.inv_dt;
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, acc * j0); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w + sym_mul(b2.I, acc * j1); store_vel(w.body, i2, b2); }
+}
+// ConeLimit.IterateConeLimit (ConeLimit.cs:378-404)
+__device__ void cone_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const int clamp = (int)J.lim.w;
+    if (clamp == 0) return;
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 j0 = mk3(J.eff[0]), j1 = mk3(J.eff[1]);
+    float jv = dot(b1.w, j0) + dot(b2.w, j1);
+    float soft = J.acc.x * J.prm.y * sp.inv_sub_dt;
+    float lambda = -J.bil.x * (jv + J.bias.x + soft);
+    float old = J.acc.x;
+    J.acc.x = clamp_impulse(clamp, J.acc.x + lambda);
+    lambda = J.acc.x - old;
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, lambda * j0); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w + sym_mul(b2.I, lambda * j1); store_vel(w.body, i2, b2); }
+}
+
+// QMatrix.ProjectMultiplyLeftRight (QMatrix.cs:112-125): the vector block (rows and columns
+// 1..3) of L(left) R(right), the quaternions' left- and right-multiplication matrices in
+// (w, x, y, z) order, each entry summed over k = 0..3 in order
+__device__ M3x project_left_right(q4 l, q4 r) {
+    const float L[4][4] = {{l.w, -l.x, -l.y, -l.z}, {l.x, l.w, -l.z, l.y}, {l.y, l.z, l.w, -l.x}, {l.z, -l.y, l.x, l.w}};
+    const float Rm[4][4] = {{r.w, -r.x, -r.y, -r.z}, {r.x, r.w, r.z, -r.y}, {r.y, -r.z, r.w, r.x}, {r.z, r.y, -r.x, r.w}};
+    M3x o;
+    for (int i = 1; i < 4; i++)
+        for (int c = 1; c < 4; c++) {
+            float acc = L[i][0] * Rm[0][c];
+            for (int k = 1; k < 4; k++) acc += L[i][k] * Rm[k][c];
+            o.a[i - 1][c - 1] = acc;
+        }
+    return o;
+}
+// AngularConstraintMath.CalculateTwist (AngularConstraintMath.cs:33-64)
+__device__ float calc_twist(q4 left, q4 right, v3 axis, v3& jac, int& hemi) {
+    M3x m = project_left_right(left, right);
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) m.a[i][k] = -0.5f * m.a[i][k];
+    q4 q = qmul(left, right);
+    jac = mtv(m, axis);
+    float proj = dot(axis, mk3(q.x, q.y, q.z));
+    hemi = q.w < 0 ? -1 : 1;
+    if (q.w < 0) {
+        q.x = -q.x; q.y = -q.y; q.z = -q.z; q.w = -q.w;
+        proj = proj * -1.0f;
+        jac = jac * -1.0f;
+    }
+    float d2 = len2(jac);
+    if (d2 > 0) jac = jac * (1.0f / sqrtf(d2));
+    else jac = -rotate(axis, right);
+    v3 perp = mk3(q.x, q.y, q.z) - axis * proj;
+    float cosine = sqrtf(q.w * q.w + len2(perp));
+    return 2.0f * StableMathF::atan2(proj, cosine);
+}
+// TwistAngle.PrepareForIterationTwistAngle (TwistAngle.cs:170-233)
+__device__ void twist_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 jr;
+    int hemi;
+    float err = calc_twist(qmul(mkq(J.q0), qconj(q1)), q2, mk3(J.axis), jr, hemi);
+    J.eff[0] = f4(jr, 0.f);
+    const float lower = J.lim.x, upper = J.lim.y;
+    float acc = J.acc.x;
+    int old_hemi = (int)J.bil.w;
+    if (old_hemi != 0 && old_hemi != hemi) acc = 0.f;
+    J.bil.w = (float)hemi;
+    const float PI = 3.14159265358979323846f;
+    bool full = lower <= -PI && upper >= PI;
+    int clamp;
+    if (lower >= upper) {
+        clamp = 3;
+        float ang = err - J.lim.z;
+        if (!(ang >= -PI && ang <= PI)) {
+            float period = 2 * PI;
+            ang = fmodf(ang, period);
+            if (ang > PI) ang -= period; else if (ang < -PI) ang += period;
+        }
+        err = ang;
+    } else if (!full && err >= upper) { clamp = 1; err -= upper; }
+    else if (!full && err <= lower) { clamp = 2; err -= lower; }
+    else { J.lim.w = 0.f; J.acc.x = 0.f; return; }
+    J.lim.w = (float)clamp;
+    acc = clamp_impulse(clamp, acc);
+    float eff = row_mass(dot(sym_mul(sym_add(b1.I, b2.I), jr), jr), J.prm.y, sp);
+    if (eff == 0.0f) acc = 0.f;
+    J.acc.x = acc;
+    J.bil.x = eff;
+    J.bias.x = err * J.prm.x * sp.inv_dt;
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, acc * jr); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, acc * jr); store_vel(w.body, i2, b2); }
+}
+// TwistAngle.IterateTwistAngle (TwistAngle.cs:296-323)
+__device__ void twist_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const int clamp = (int)J.lim.w;
+    if (clamp == 0) return;
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 jr = mk3(J.eff[0]);
+    float jv = dot(b1.w - b2.w, jr);
+    float soft = J.acc.x * (J.prm.y * sp.inv_sub_dt);
+    float lambda = -J.bil.x * (jv + J.bias.x + soft);
+    float old = J.acc.x;
+    J.acc.x = clamp_impulse(clamp, J.acc.x + lambda);
+    lambda = J.acc.x - old;
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, lambda * jr); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, lambda * jr); store_vel(w.body, i2, b2); }
+}
+
 __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
-    if (J.hdr.x == JG_CONSTRAINT_BALLSOCKET) ballsocket_prepare(w, J, sp);
-    else hinge_prepare(w, J, sp);
+    switch (J.hdr.x) {
+        case JG_CONSTRAINT_BALLSOCKET: ballsocket_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_HINGEANGLE: hinge_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_DISTANCELIMIT: distance_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_CONELIMIT: cone_prepare(w, J, sp); break;
+        default: twist_prepare(w, J, sp); break;
+    }
 }
 __device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
-    if (J.hdr.x == JG_CONSTRAINT_BALLSOCKET) ballsocket_iterate(w, J, sp);
-    else hinge_iterate(w, J, sp);
+    switch (J.hdr.x) {
+        case JG_CONSTRAINT_BALLSOCKET: ballsocket_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_HINGEANGLE: hinge_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_DISTANCELIMIT: distance_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_CONELIMIT: cone_iterate(w, J, sp); break;
+        default: twist_iterate(w, J, sp); break;
+    }
 }

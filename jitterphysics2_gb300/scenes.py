@@ -394,3 +394,53 @@ def bullets(n=256, speed=(60.0, 150.0), speculative=True, seed=12351, spacing=1.
     return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
                 triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[],
                 params=dict(substeps=2, solver_iterations=8, relax_iterations=4), dt=1.0 / 60.0)
+
+
+def limb_chains(n_chains=16, links=6, seed=12352, spacing=1.0):
+    """Chains of boxes hanging from static anchors, each link joined to the next the way a
+    ragdoll limb is: BallSocket at the midpoint, ConeLimit on the chain axis (0 to 0.5 rad)
+    and TwistAngle about it (-0.3 to 0.3 rad); a DistanceLimit from the anchor to the last
+    link keeps it within its initial distance and beyond half of it.  The chains start
+    horizontal with random spin about their axes, so they swing down against the cone
+    limits and twist against the twist limits.  Links are 0.6 long with 0.4 gaps: no
+    contacts inside a chain, and the chains are 8 apart."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    per = links + 1
+    n = n_chains * per
+    bodies = _body(n)
+    shapes = np.zeros(n, abi.SHAPE_DTYPE)
+    joints = []
+    x_axis = (1.0, 0.0, 0.0)
+    for c in range(n_chains):
+        a = c * per
+        base = np.array([0.0, 10.0, 8.0 * c])
+        bodies["position"][a] = base
+        bodies["motion_type"][a] = abi.MOTION_STATIC
+        bodies["inv_mass"][a] = 0.0
+        bodies["inv_inertia"][a] = 0.0
+        shapes["kind"][a] = abi.SHAPE_BOX
+        shapes["body"][a] = a
+        shapes["dims"][a, :3] = (0.2, 0.2, 0.2)
+        for k in range(1, per):
+            i = a + k
+            bodies["position"][i] = base + (spacing * k, 0.0, 0.0)
+            bodies["angular_velocity"][i] = (rng.normal(0.0, 3.0), rng.normal(0.0, 0.5), rng.normal(0.0, 0.5))
+            shapes["kind"][i] = abi.SHAPE_BOX
+            shapes["body"][i] = i
+            shapes["dims"][i, :3] = (0.3, 0.12, 0.12)
+            mid = base + (spacing * (k - 0.5), 0.0, 0.0)
+            joints.append((abi.CONSTRAINT_BALLSOCKET, i - 1, i, tuple(mid)))
+            joints.append((abi.CONSTRAINT_CONELIMIT, i - 1, i, x_axis + x_axis + (0.0, 0.5)))
+            joints.append((abi.CONSTRAINT_TWISTANGLE, i - 1, i, x_axis + x_axis + (-0.3, 0.3)))
+        last = a + links
+        d = spacing * links
+        joints.append((abi.CONSTRAINT_DISTANCELIMIT, a, last,
+                       tuple(base) + tuple(base + (d, 0.0, 0.0)) + (-0.5 * d, 0.0)))
+    _finish_mass(bodies, shapes, np.zeros((0, 3), np.float32), 0, 0, n)
+    for c in range(n_chains):
+        a = c * per
+        bodies["inv_mass"][a] = 0.0
+        bodies["inv_inertia"][a] = 0.0
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=joints,
+                params=dict(substeps=4, solver_iterations=8, relax_iterations=2), dt=1.0 / 60.0)

@@ -85,10 +85,7 @@ class World:
         self.set_bodies(scene["bodies"])
         self.set_shapes(scene["shapes"], scene["hull"], scene["triangles"])
         for kind, b1, b2, init in scene.get("joints", []):
-            if kind == abi.CONSTRAINT_BALLSOCKET:
-                self.add_constraint(kind, b1, b2, np.array(init, np.float32))
-            else:
-                self.add_constraint(kind, b1, b2, np.array(init, np.float32))
+            self.add_constraint(kind, b1, b2, np.array(init, np.float32))
 
     def set_body(self, index, field, value):
         fields = {"position": 0, "orientation": 1, "velocity": 2, "angular_velocity": 3, "force": 4, "torque": 5}

@@ -201,9 +201,24 @@ template <class R> struct Handle {
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         Joint<R> j; j.b1 = b1; j.b2 = b2;                                                                          \
         if (kind == JG_CONSTRAINT_BALLSOCKET) ballsocket_init(j, w.bodies, get3<R>(init));                         \
-        else hinge_init(j, w.bodies, get3<R>(init), (R)init[3], (R)init[4]);                                        \
+        else if (kind == JG_CONSTRAINT_HINGEANGLE) hinge_init(j, w.bodies, get3<R>(init), (R)init[3], (R)init[4]);  \
+        else if (kind == JG_CONSTRAINT_DISTANCELIMIT)                                                              \
+            distance_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                 \
+        else if (kind == JG_CONSTRAINT_CONELIMIT)                                                                  \
+            cone_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                     \
+        else twist_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                   \
         w.joints.push_back(j);                                                                                     \
         return (int)w.joints.size() - 1;                                                                           \
+    }                                                                                                              \
+    /* one Prepare (and, with iterate set, one Iterate) of joint j alone at step dt, bias factor \
+       and softness overridden: the constraint-level calls the reference's own tests make */     \
+    extern "C" void jor_world_joint_solve_##SUF(void* h, int j, float dt, float bias, float soft, int iterate) { \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        Joint<R>& jt = w.joints[j];                                                                                \
+        jt.bias_factor = (R)bias; jt.softness = (R)soft;                                                           \
+        TimeStep<R> ts((R)dt, 1);                                                                                  \
+        joint_prepare(jt, w.bodies, ts);                                                                           \
+        if (iterate) joint_iterate(jt, w.bodies, ts);                                                              \
     }                                                                                                              \
     extern "C" void jor_world_set_joint_colors_##SUF(void* h, const int* colors, int n) {                         \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \

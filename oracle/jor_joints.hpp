@@ -1,7 +1,9 @@
-// Oracle (test infrastructure only): CPU restatement of the two joint kinds the batched
-// world configuration uses: BallSocket (Dynamics/Constraints/BallSocket.cs:140-252) and
-// HingeAngle (Dynamics/Constraints/HingeAngle.cs:84-364), with their math helpers
-// (AngularConstraintMath.cs:13-95, MathHelper.cs:282-372, JMatrix.cs:391-478).
+// Oracle (test infrastructure only): CPU restatement of the joint kinds on the device:
+// BallSocket (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle
+// (Dynamics/Constraints/HingeAngle.cs:84-364), DistanceLimit (DistanceLimit.cs:92-391),
+// ConeLimit (ConeLimit.cs:92-404) and TwistAngle (TwistAngle.cs:85-323), with their math
+// helpers (AngularConstraintMath.cs:13-95, QMatrix.cs:112-125, MathHelper.cs:282-372,
+// JMatrix.cs:391-478, JQuaternion.cs:84-101).
 #pragma once
 #include "jor_dynamics.hpp"
 
@@ -195,7 +197,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
     return mmul(mscale(-(R)0.5, der), Mat<R>::from_m3(mat_from_quat(left)));
 }
 
-enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2 };
+enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -213,6 +215,12 @@ template <class R> struct Joint {
     R coupling_x = 0, coupling_y = 0;
     int clamp = 0;
     short hemisphere = 0;
+    // one-row kinds (DistanceLimitData, ConeLimitData, TwistLimitData): limits in
+    // min_angle / max_angle (and fixed_angle), the row's Jacobian blocks, its effective mass;
+    // the accumulated impulse and bias in acc.x / bias.x
+    R target = 0;                     // DistanceLimit.Distance
+    V3<R> jr[4];
+    R eff1 = 0;
 };
 
 // BallSocket.Initialize (BallSocket.cs:120-138)
@@ -384,11 +392,272 @@ template <class R> void hinge_iterate(Joint<R>& j, std::vector<Body<R>>& bodies,
     if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, mvec(j.jac, lambda));
     if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, mvec(j.jac, lambda));
 }
+// ---- one-row limits ---------------------------------------------------------------------
+// Shared by DistanceLimit, ConeLimit and TwistAngle: the row's clamp rule for the
+// accumulated impulse (1: at the upper limit, impulse <= 0; 2: lower, >= 0; 3: fixed).
+template <class R> R clamp_impulse(int clamp, R acc) {
+    if (clamp == 1) return std::min(acc, (R)0.0);
+    if (clamp == 2) return std::max(acc, (R)0.0);
+    return acc;
+}
+template <class R> R row_mass(R m, R softness, const TimeStep<R>& ts) {
+    m += softness * ts.inv_sub_dt;
+    return m > 0 ? (R)1.0 / m : (R)0.0;
+}
+
+// DistanceLimit.Initialize (DistanceLimit.cs:92-117); limit (min, max), LinearLimit.Fixed
+// is (1e-6, -1e-6)
+template <class R> void distance_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> a1, V3<R> a2, R lo, R hi) {
+    j.kind = DISTANCELIMIT;
+    j.la1 = rotate_inv(a1 - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(a2 - b[j.b2].pos, b[j.b2].q);
+    j.softness = (R)0.00001;
+    j.bias_factor = (R)0.2;
+    j.target = std::sqrt(len2(a2 - a1));
+    j.min_angle = lo; j.max_angle = hi;
+}
+// DistanceLimit.PrepareForIterationDistanceLimit (DistanceLimit.cs:227-306)
+template <class R> void distance_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> r1 = rotate(j.la1, b1.q), r2 = rotate(j.la2, b2.q);
+    V3<R> dp = (b2.pos + r2) - (b1.pos + r1);
+    R dist = std::sqrt(len2(dp));
+    R err = dist - j.target;
+    j.clamp = 0;
+    if (j.min_angle >= j.max_angle) { err -= (R)0.5 * j.min_angle + (R)0.5 * j.max_angle; j.clamp = 3; }
+    else if (err >= j.max_angle) { j.clamp = 1; err -= j.max_angle; }
+    else if (err <= j.min_angle) { j.clamp = 2; err -= j.min_angle; }
+    else { j.acc.x = 0; return; }
+    if (dist == 0) { j.clamp = 0; j.acc.x = 0; return; }
+    V3<R> n = dp * ((R)1.0 / dist);
+    j.jr[0] = -(R)1.0 * n;
+    j.jr[1] = -(R)1.0 * cross(r1, n);
+    j.jr[2] = (R)1.0 * n;
+    j.jr[3] = cross(r2, n);
+    R m = dot(cmul(j.jr[0], b1.inv_mass_vec), j.jr[0]) + dot(cmul(j.jr[2], b2.inv_mass_vec), j.jr[2]) +
+          dot(sym_mul(b1.inv_inertia_world, j.jr[1]), j.jr[1]) + dot(sym_mul(b2.inv_inertia_world, j.jr[3]), j.jr[3]);
+    j.eff1 = row_mass(m, j.softness, ts);
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = err * j.bias_factor * ts.inv_dt;
+    R a = j.acc.x;
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel + cmul(a * j.jr[0], b1.inv_mass_vec);
+        b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, a * j.jr[1]);
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(a * j.jr[2], b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, a * j.jr[3]);
+    }
+}
+// DistanceLimit.IterateDistanceLimit (DistanceLimit.cs:344-391)
+template <class R> void distance_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    if (j.clamp == 0) return;
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(b1.vel, j.jr[0]) + dot(b1.angvel, j.jr[1]) + dot(b2.vel, j.jr[2]) + dot(b2.angvel, j.jr[3]);
+    R soft = j.acc.x * j.softness * ts.inv_sub_dt;
+    R lambda = -j.eff1 * (jv + j.bias.x + soft);
+    R old = j.acc.x;
+    j.acc.x = clamp_impulse(j.clamp, j.acc.x + lambda);
+    lambda = j.acc.x - old;
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel + cmul(lambda * j.jr[0], b1.inv_mass_vec);
+        b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, lambda * j.jr[1]);
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(lambda * j.jr[2], b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, lambda * j.jr[3]);
+    }
+}
+
+// ConeLimit.Initialize (ConeLimit.cs:92-118): world axes of the two bodies, limit (min, max)
+// in radians within [0, pi]
+template <class R> void cone_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R lo, R hi) {
+    j.kind = CONELIMIT;
+    j.la1 = rotate_inv(normalize(ax1), b[j.b1].q);
+    j.la2 = rotate_inv(normalize(ax2), b[j.b2].q);
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    j.min_angle = lo; j.max_angle = hi;
+}
+// ConeLimit.PrepareForIterationConeLimit (ConeLimit.cs:262-356).  The row is the angle
+// between the two axes; its Jacobian persists between steps, and a sign flip of it drops
+// the cached impulse.
+template <class R> void cone_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> a1 = rotate(j.la1, b1.q), a2 = rotate(j.la2, b2.q);
+    V3<R> prev = j.jr[0];
+    j.jr[0] = cross(a2, a1);
+    j.clamp = 0;
+    R cosine = dot(a1, a2);
+    R lower = -j.min_angle, upper = -j.max_angle;
+    R sine = std::sqrt(len2(j.jr[0]));
+    if (sine > 0) {
+        j.jr[0] = j.jr[0] * ((R)1.0 / sine);
+    } else {
+        // at a cusp: the perpendicular axis with the larger response
+        V3<R> axis = create_orthonormal(a1);
+        V3<R> other = cross(a1, axis);
+        Sym3<R> I(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                  b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                  b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+        j.jr[0] = dot(sym_mul(I, axis), axis) >= dot(sym_mul(I, other), other) ? axis : other;
+    }
+    j.jr[1] = -j.jr[0];
+    if (dot(prev, j.jr[0]) < 0) j.acc.x = 0;
+    R err = -StableMath<R>::atan2(sine, cosine);
+    const R PI = (R)3.14159265358979323846;
+    if (lower == upper) { j.clamp = 3; err -= upper; }
+    else if (err <= upper && j.max_angle < PI) { j.clamp = 1; err -= upper; }
+    else if (err >= lower && j.min_angle > 0) { j.clamp = 2; err -= lower; }
+    else { j.acc.x = 0; return; }
+    j.acc.x = clamp_impulse(j.clamp, j.acc.x);
+    R m = dot(sym_mul(b1.inv_inertia_world, j.jr[0]), j.jr[0]) + dot(sym_mul(b2.inv_inertia_world, j.jr[1]), j.jr[1]);
+    j.eff1 = row_mass(m, j.softness, ts);
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = -err * j.bias_factor * ts.inv_dt;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, j.acc.x * j.jr[0]);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j.acc.x * j.jr[1]);
+}
+// ConeLimit.IterateConeLimit (ConeLimit.cs:378-404)
+template <class R> void cone_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    if (j.clamp == 0) return;
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(b1.angvel, j.jr[0]) + dot(b2.angvel, j.jr[1]);
+    R soft = j.acc.x * j.softness * ts.inv_sub_dt;
+    R lambda = -j.eff1 * (jv + j.bias.x + soft);
+    R old = j.acc.x;
+    j.acc.x = clamp_impulse(j.clamp, j.acc.x + lambda);
+    lambda = j.acc.x - old;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, lambda * j.jr[0]);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, lambda * j.jr[1]);
+}
+
+// JQuaternion.CreateFromToRotation (JQuaternion.cs:84-101)
+template <class R> Q4<R> from_to_rotation(V3<R> from, V3<R> to) {
+    R d = dot(from, to);
+    if (d < -(R)1.0 + (R)1e-6) {
+        V3<R> ax = create_orthonormal(from);
+        return Q4<R>(ax.x, ax.y, ax.z, 0);
+    }
+    R s = std::sqrt(((R)1.0 + d) * (R)2.0);
+    R is = (R)1.0 / s;
+    V3<R> c = cross(from, to);
+    V3<R> v = c * is;
+    return Q4<R>(v.x, v.y, v.z, s * (R)0.5);
+}
+// QMatrix.ProjectMultiplyLeftRight (QMatrix.cs:112-125): the vector block (rows and
+// columns 1..3) of L(left) R(right), the left- and right-multiplication matrices of the
+// two quaternions in (w, x, y, z) order, each entry summed over k = 0..3 in order.
+template <class R> Mat<R> project_left_right(Q4<R> l, Q4<R> r) {
+    const R L[4][4] = {{l.w, -l.x, -l.y, -l.z}, {l.x, l.w, -l.z, l.y}, {l.y, l.z, l.w, -l.x}, {l.z, -l.y, l.x, l.w}};
+    const R Rm[4][4] = {{r.w, -r.x, -r.y, -r.z}, {r.x, r.w, r.z, -r.y}, {r.y, -r.z, r.w, r.x}, {r.z, r.y, -r.x, r.w}};
+    Mat<R> o;
+    for (int i = 1; i < 4; i++)
+        for (int c = 1; c < 4; c++) {
+            R acc = L[i][0] * Rm[0][c];
+            for (int k = 1; k < 4; k++) acc += L[i][k] * Rm[k][c];
+            o.a[i - 1][c - 1] = acc;
+        }
+    return o;
+}
+// AngularConstraintMath.CalculateTwist (AngularConstraintMath.cs:33-64): the twist angle of
+// left * right about `axis` and its unit Jacobian row
+template <class R> R calc_twist(Q4<R> left, Q4<R> right, V3<R> axis, V3<R>& jac, short& hemi) {
+    Mat<R> m = mscale(-(R)0.5, project_left_right(left, right));
+    Q4<R> q = qmul(left, right);
+    jac = mtvec(m, axis);
+    R proj = dot(axis, V3<R>(q.x, q.y, q.z));
+    hemi = q.w < 0 ? (short)-1 : (short)1;
+    if (q.w < 0) {
+        q = Q4<R>(-q.x, -q.y, -q.z, -q.w);
+        proj = proj * -(R)1;
+        jac = jac * (R)-1;
+    }
+    R d2 = len2(jac);
+    if (d2 > 0) jac = jac * ((R)1 / std::sqrt(d2));
+    else jac = -rotate(axis, right);
+    V3<R> perp = V3<R>(q.x, q.y, q.z) - axis * proj;
+    R cosine = std::sqrt(q.w * q.w + len2(perp));
+    return (R)2 * StableMath<R>::atan2(proj, cosine);
+}
+// TwistAngle.Initialize (TwistAngle.cs:85-128): world axes of the two bodies, limit
+// (min, max) in radians; Q0 is the initial relative rotation with the axes aligned
+template <class R> void twist_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R lo, R hi) {
+    j.kind = TWISTANGLE;
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    ax1 = normalize(ax1); ax2 = normalize(ax2);
+    j.min_angle = lo; j.max_angle = hi;
+    j.fixed_angle = (R)0.5 * lo + (R)0.5 * hi;
+    Q4<R> q1 = b[j.b1].q, q2 = b[j.b2].q;
+    V3<R> u1 = rotate_inv(ax1, q1);
+    j.axis = rotate_inv(ax2, q2);
+    Q4<R> rel = qmul(qconj(q2), q1);
+    V3<R> u1b2 = rotate(u1, rel);
+    j.q0 = qmul(from_to_rotation(u1b2, j.axis), rel);
+}
+// TwistAngle.PrepareForIterationTwistAngle (TwistAngle.cs:170-233)
+template <class R> void twist_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    short hemi;
+    R err = calc_twist(qmul(j.q0, qconj(b1.q)), b2.q, j.axis, j.jr[0], hemi);
+    R lower = j.min_angle, upper = j.max_angle;
+    if (j.hemisphere != 0 && j.hemisphere != hemi) j.acc.x = 0;
+    j.hemisphere = hemi;
+    j.clamp = 0;
+    const R PI = (R)3.14159265358979323846;
+    bool full = lower <= -PI && upper >= PI;
+    if (lower >= upper) { j.clamp = 3; err = shortest_angle(err - j.fixed_angle, PI); }
+    else if (!full && err >= upper) { j.clamp = 1; err -= upper; }
+    else if (!full && err <= lower) { j.clamp = 2; err -= lower; }
+    else { j.acc.x = 0; return; }
+    j.acc.x = clamp_impulse(j.clamp, j.acc.x);
+    Sym3<R> I(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+              b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+              b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+    j.eff1 = row_mass(dot(sym_mul(I, j.jr[0]), j.jr[0]), j.softness, ts);
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = err * j.bias_factor * ts.inv_dt;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, j.acc.x * j.jr[0]);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, j.acc.x * j.jr[0]);
+}
+// TwistAngle.IterateTwistAngle (TwistAngle.cs:296-323)
+template <class R> void twist_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    if (j.clamp == 0) return;
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(b1.angvel - b2.angvel, j.jr[0]);
+    R soft = j.acc.x * (j.softness * ts.inv_sub_dt);
+    R lambda = -j.eff1 * (jv + j.bias.x + soft);
+    R old = j.acc.x;
+    j.acc.x = clamp_impulse(j.clamp, j.acc.x + lambda);
+    lambda = j.acc.x - old;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, lambda * j.jr[0]);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, lambda * j.jr[0]);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
-    if (j.kind == BALLSOCKET) ballsocket_prepare(j, b, ts); else hinge_prepare(j, b, ts);
+    switch (j.kind) {
+        case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
+        case HINGEANGLE: hinge_prepare(j, b, ts); break;
+        case DISTANCELIMIT: distance_prepare(j, b, ts); break;
+        case CONELIMIT: cone_prepare(j, b, ts); break;
+        default: twist_prepare(j, b, ts); break;
+    }
 }
 template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
-    if (j.kind == BALLSOCKET) ballsocket_iterate(j, b, ts); else hinge_iterate(j, b, ts);
+    switch (j.kind) {
+        case BALLSOCKET: ballsocket_iterate(j, b, ts); break;
+        case HINGEANGLE: hinge_iterate(j, b, ts); break;
+        case DISTANCELIMIT: distance_iterate(j, b, ts); break;
+        case CONELIMIT: cone_iterate(j, b, ts); break;
+        default: twist_iterate(j, b, ts); break;
+    }
 }
 
 }  // namespace jor

@@ -39,7 +39,7 @@ def load():
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
-            "jor_world_set_step_dt": (None, [P, F]),
+            "jor_world_set_step_dt": (None, [P, F]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
             "jor_world_set_penalty": (None, [P, I, I, D]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
@@ -245,6 +245,14 @@ class OracleWorld:
     def set_joint_colors(self, colors):
         c = np.ascontiguousarray(colors, np.int32)
         self.fn("jor_world_set_joint_colors")(self.h, p(c), len(c))
+
+    def joint_solve(self, j, dt, bias, softness, iterate=True):
+        """Prepare (and Iterate) one joint alone, bias factor and softness overridden."""
+        self.fn("jor_world_joint_solve")(self.h, j, dt, bias, softness, 1 if iterate else 0)
+
+    def add_joint(self, kind, b1, b2, init):
+        v = np.ascontiguousarray(init, np.float32)
+        return self.fn("jor_world_add_joint")(self.h, kind, b1, b2, p(v))
 
     def joint_impulses(self, n):
         out = np.zeros((n, 3), np.float32)

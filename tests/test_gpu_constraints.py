@@ -1,0 +1,77 @@
+"""DistanceLimit, ConeLimit and TwistAngle on the GPU against the oracle, through the C ABI.
+
+The limb-chain scene joins boxes the way a ragdoll limb is joined (BallSocket + ConeLimit +
+TwistAngle per joint, a DistanceLimit per chain).  One step from the GPU's state is
+replayed in the oracle in the GPU's order keys, warm-started with the GPU's impulses:
+velocities within 1e-3, impulses within 1e-3 relative.  Over 240 steps the GPU holds the
+limits, and 30 steps from the start it follows the oracle's own run within 2e-3.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi, scenes
+from jitterphysics2_gb300.world import world_for_scene
+from test_oracle_constraints import chain_limits
+
+pytestmark = pytest.mark.gpu
+
+
+def test_one_step_of_limb_chains_matches_the_oracle():
+    sc = scenes.limb_chains(n_chains=16)
+    w = world_for_scene(sc)
+    for _ in range(60):
+        w.step(sc["dt"])
+    b0 = w.bodies()
+    _, j0 = w.constraints()
+    w.step(sc["dt"])
+    b1 = w.bodies()
+    k1, j1 = w.constraints()
+    assert np.abs(j1).max() > 0
+    o = O.OracleWorld(sc, external_order=True)
+    o.set_bodies(b0)
+    o.set_joint_impulses(j0)
+    o.narrowphase()
+    o.set_joint_colors(k1)
+    o.step(sc["dt"], narrow=False)
+    ob = o.bodies()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    err = np.maximum(np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1),
+                     np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1))
+    jerr = np.abs(j1 - o.joint_impulses(len(j1))).max(axis=1) / np.maximum(1e-3, np.abs(j1).max(axis=1))
+    assert err.max() < 1e-3, np.sort(err)[-5:]
+    assert np.mean(jerr < 1e-3) > 0.95, np.sort(jerr)[-5:]
+
+
+def test_limb_chains_hold_their_limits_and_follow_the_oracle():
+    sc = scenes.limb_chains(n_chains=16)
+    w = world_for_scene(sc)
+    o = O.OracleWorld(sc)
+    for _ in range(30):
+        w.step(sc["dt"])
+        o.step(sc["dt"])
+    np.testing.assert_allclose(w.bodies()["position"], o.bodies()["position"], atol=2e-3)
+    for _ in range(210):
+        w.step(sc["dt"])
+    cones, twists, dists = chain_limits(sc, w.bodies())
+    assert cones.max() < 0.5 + 0.03
+    assert np.abs(twists).max() < 0.3 + 0.03
+    assert dists.max() < 6.0 + 0.01 and dists.min() > 3.0 - 0.01
+
+
+@pytest.mark.parametrize("kind, init", [
+    (abi.CONSTRAINT_CONELIMIT, (1, 0, 0, 1, 0, 0, 0.0, 0.0)),          # fixed tilt of zero
+    (abi.CONSTRAINT_CONELIMIT, (1, 0, 0, 1, 0, 0, np.pi, np.pi)),      # fixed tilt of pi
+    (abi.CONSTRAINT_CONELIMIT, (1, 0, 0, 1, 0, 0, 0.6, 0.5)),          # min above max
+    (abi.CONSTRAINT_CONELIMIT, (1, 0, 0, 1, 0, 0, -0.1, 0.5)),         # below zero
+    (abi.CONSTRAINT_CONELIMIT, (0, 0, 0, 1, 0, 0, 0.0, 0.5)),          # zero axis
+    (abi.CONSTRAINT_TWISTANGLE, (1, 0, 0, 1, 0, 0, -np.inf, 0.5)),     # infinite limit
+    (abi.CONSTRAINT_DISTANCELIMIT, (0, 0, 0, 1, 0, 0, np.nan, 0.0)),   # NaN limit
+    (abi.CONSTRAINT_DISTANCELIMIT, (0, np.inf, 0, 1, 0, 0, 0.0, 0.0)),  # infinite anchor
+])
+def test_invalid_constraint_arguments_raise(kind, init):
+    sc = scenes.limb_chains(n_chains=1, links=2)
+    w = world_for_scene(sc)
+    with pytest.raises(abi.JitterError) as e:
+        w.add_constraint(kind, 1, 2, init)
+    assert e.value.code == abi.JG_ERR_INVALID_ARG
