@@ -220,6 +220,22 @@ template <class R> struct Handle {
         joint_prepare(jt, w.bodies, ts);                                                                           \
         if (iterate) joint_iterate(jt, w.bodies, ts);                                                              \
     }                                                                                                              \
+    /* joint row after its last Prepare: out = jr[0], jr[1], effective mass, clamp, impulse */                \
+    extern "C" void jor_world_joint_data_##SUF(void* h, int j, double* out) {                                      \
+        const Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                         \
+        put3d(out, jt.jr[0]); put3d(out + 3, jt.jr[1]);                                                            \
+        out[6] = (double)jt.eff1; out[7] = jt.clamp; out[8] = (double)jt.acc.x;                                   \
+    }                                                                                                              \
+    extern "C" double jor_world_joint_angle_##SUF(void* h, int j) {                                                \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        return (double)joint_angle(w.joints[j], w.bodies);                                                         \
+    }                                                                                                              \
+    /* ConeLimit.Limit / TwistAngle.Limit setters (ConeLimit.cs:196-206, TwistAngle.cs:130-143) */               \
+    extern "C" void jor_world_joint_set_limit_##SUF(void* h, int j, double lo, double hi) {                       \
+        Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                               \
+        jt.min_angle = (R)lo; jt.max_angle = (R)hi;                                                                \
+        jt.fixed_angle = (R)0.5 * (R)lo + (R)0.5 * (R)hi;                                                          \
+    }                                                                                                              \
     extern "C" void jor_world_set_joint_colors_##SUF(void* h, const int* colors, int n) {                         \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         for (int i = 0; i < n && i < (int)w.joints.size(); i++) w.joints[i].color = colors[i];                     \
@@ -264,6 +280,10 @@ template <class R> struct Handle {
     }                                                                                                              \
     extern "C" void jor_world_set_orientation_##SUF(void* h, int b, const float* q) {                             \
         World<R>& w = ((Handle<R>*)h)->w; w.bodies[b].q = Q4<R>(q[0], q[1], q[2], q[3]);                           \
+        update_world_inertia(w.bodies[b]);                                                                         \
+    }                                                                                                              \
+    extern "C" void jor_world_set_orientation_d_##SUF(void* h, int b, const double* q) {                          \
+        World<R>& w = ((Handle<R>*)h)->w; w.bodies[b].q = Q4<R>((R)q[0], (R)q[1], (R)q[2], (R)q[3]);               \
         update_world_inertia(w.bodies[b]);                                                                         \
     }                                                                                                              \
     extern "C" void jor_world_inertia_world_##SUF(void* h, int b, double* out) {                                  \

@@ -641,6 +641,24 @@ template <class R> void twist_iterate(Joint<R>& j, std::vector<Body<R>>& bodies,
     if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, lambda * j.jr[0]);
 }
 
+// ConeLimit.Angle (ConeLimit.cs:137-149) and TwistAngle.Angle (TwistAngle.cs:240-258): the
+// joint's current angle as its public getter reports it (0 for the other kinds).
+template <class R> R joint_angle(const Joint<R>& j, const std::vector<Body<R>>& b) {
+    if (j.kind == CONELIMIT) {
+        V3<R> a1 = rotate(j.la1, b[j.b1].q), a2 = rotate(j.la2, b[j.b2].q);
+        return StableMath<R>::atan2(std::sqrt(len2(cross(a1, a2))), dot(a1, a2));
+    }
+    if (j.kind == TWISTANGLE) {
+        Q4<R> q = qmul(qmul(j.q0, qconj(b[j.b1].q)), b[j.b2].q);
+        if (q.w < (R)0.0) q = Q4<R>(-q.x, -q.y, -q.z, -q.w);
+        V3<R> v(q.x, q.y, q.z);
+        R proj = dot(j.axis, v);
+        V3<R> perp = v - j.axis * proj;
+        return (R)2.0 * StableMath<R>::atan2(proj, std::sqrt(q.w * q.w + len2(perp)));
+    }
+    return 0;
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;

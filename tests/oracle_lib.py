@@ -40,6 +40,8 @@ def load():
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
             "jor_world_set_step_dt": (None, [P, F]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
+            "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
+            "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
             "jor_world_set_penalty": (None, [P, I, I, D]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
@@ -249,6 +251,23 @@ class OracleWorld:
     def joint_solve(self, j, dt, bias, softness, iterate=True):
         """Prepare (and Iterate) one joint alone, bias factor and softness overridden."""
         self.fn("jor_world_joint_solve")(self.h, j, dt, bias, softness, 1 if iterate else 0)
+
+    def joint_data(self, j):
+        """(jr0, jr1, effective mass, clamp, impulse) of a one-row joint after its Prepare."""
+        out = np.zeros(9, np.float64)
+        self.fn("jor_world_joint_data")(self.h, j, p(out))
+        return out[0:3], out[3:6], out[6], int(out[7]), out[8]
+
+    def set_orientation_d(self, body, q):
+        """Set one body's orientation at the oracle's own precision (not through float32)."""
+        v = np.ascontiguousarray(q, np.float64)
+        self.fn("jor_world_set_orientation_d")(self.h, body, p(v))
+
+    def joint_angle(self, j):
+        return self.fn("jor_world_joint_angle")(self.h, j)
+
+    def joint_set_limit(self, j, lo, hi):
+        self.fn("jor_world_joint_set_limit")(self.h, j, float(lo), float(hi))
 
     def add_joint(self, kind, b1, b2, init):
         v = np.ascontiguousarray(init, np.float32)

@@ -1,0 +1,211 @@
+"""The oracle's ConeLimit and TwistAngle rows pinned to the reference's own
+constraint-level tests (AngularCoordinateTests.cs), restated: one Prepare (+ Iterate) of
+the joint alone on bodies with unit inverse mass and identity inverse inertia (the
+reference's default body), body 0 static where the reference uses its NullBody.
+
+- the Jacobian row of each is the derivative of the angle its getter reports, for either
+  body, by central differences (delta 1e-4 and tolerance 0.006 in FP32, 1e-6 and 1e-7 in
+  FP64, the reference's values);
+- softness acts in angle units on both sides of the former thresholds (the velocity left
+  is gamma / (1 + gamma), gamma = softness / dt);
+- a tiny cone limit stays distinct from zero, a fixed tilt holds both directions, an
+  interior boundary stops only the outward rate, the natural 0 and pi bounds leave motion
+  free, and cached impulses keep their units across the former thresholds.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from jitterphysics2_gb300 import abi
+from test_oracle_constraints import _quat_mul
+
+DT = 0.01
+
+
+def _axis_angle(axis, angle):
+    a = np.asarray(axis, np.float64) / np.linalg.norm(axis)
+    return np.array([*(a * np.sin(angle / 2)), np.cos(angle / 2)])
+
+
+def _normalize(q):
+    q = np.asarray(q, np.float64)
+    return q / np.linalg.norm(q)
+
+
+def _world(q1, q2, static_first, w2=(0, 0, 0)):
+    b = np.zeros(2, abi.BODY_DTYPE)
+    b["flags"] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY
+    b["linear_damping"] = b["angular_damping"] = 1.0
+    b["orientation"][0], b["orientation"][1] = q1, q2
+    b["inv_mass"] = 1.0
+    b["inv_inertia"] = (1, 0, 0, 1, 0, 1)
+    if static_first:
+        b["motion_type"][0] = abi.MOTION_STATIC
+        b["inv_mass"][0] = 0.0
+        b["inv_inertia"][0] = 0.0
+    b["angular_velocity"][1] = w2
+    sc = dict(bodies=b, shapes=np.zeros(0, abi.SHAPE_DTYPE), hull=np.zeros((0, 3), np.float32),
+              triangles=np.zeros(0, abi.TRIANGLE_DTYPE))
+    return sc
+
+
+def _set(o, body, q=None, w=None):
+    b = o.bodies()
+    if q is not None:
+        b["orientation"][body] = q
+    if w is not None:
+        b["angular_velocity"][body] = w
+    o.set_bodies(b)
+
+
+def _perp(axis):
+    a = np.asarray(axis, np.float64)
+    t = np.cross(a, (1.0, 0.0, 0.0) if abs(a[0]) < 0.9 else (0.0, 1.0, 0.0))
+    return t / np.linalg.norm(t)
+
+
+PREC = {"f": (1e-4, 0.006), "d": (1e-6, 1e-7)}
+Q1 = _normalize((1, 2, 3, 4))
+Q2 = _normalize((2, -1, 3, 5))
+AXIS = np.array([1.0, 3.0, 2.0]) / np.linalg.norm([1.0, 3.0, 2.0])
+
+
+def _check_jacobian(o, j, jac, perturb_body2, q1, q2, real):
+    # orientations go in at the oracle's precision: a 1e-6 turn is below float32's
+    delta, tol = PREC[real]
+    body = 1 if perturb_body2 else 0
+    orig = q2 if perturb_body2 else q1
+    for direction in np.eye(3):
+        o.set_orientation_d(body, _quat_mul(_axis_angle(direction, delta), orig))
+        plus = o.joint_angle(j)
+        o.set_orientation_d(body, _quat_mul(_axis_angle(direction, -delta), orig))
+        minus = o.joint_angle(j)
+        o.set_orientation_d(body, orig)
+        expected = float(np.dot(jac, direction)) * (-1 if perturb_body2 else 1)
+        assert (plus - minus) / (2 * delta) == pytest.approx(expected, abs=tol)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("perturb_body2", [False, True])
+@pytest.mark.parametrize("angle", [0.2, 2.1, 3.13])
+def test_twist_jacobian_is_the_derivative_of_its_angle(angle, perturb_body2, real):
+    o = O.OracleWorld(_world(Q1, Q2, False), real=real)
+    o.set_orientation_d(0, Q1)
+    o.set_orientation_d(1, Q2)
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, tuple(AXIS) + tuple(AXIS) + (1e-6, -1e-6))
+    q2 = _quat_mul(_axis_angle(AXIS, angle), Q2)
+    q2 = _quat_mul(_axis_angle(_perp(AXIS), 0.3), q2)
+    o.set_orientation_d(1, q2)
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    jac = o.joint_data(j)[0]
+    _check_jacobian(o, j, jac, perturb_body2, Q1, q2, real)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("perturb_body2", [False, True])
+@pytest.mark.parametrize("angle", [0.2, 0.6, 2.1, 3.13])
+def test_cone_jacobian_is_the_derivative_of_its_angle(angle, perturb_body2, real):
+    o = O.OracleWorld(_world(Q1, Q2, False), real=real)
+    o.set_orientation_d(0, Q1)
+    o.set_orientation_d(1, Q2)
+    lim = np.radians(30.0)
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, tuple(AXIS) + tuple(AXIS) + (lim, lim))
+    q2 = _quat_mul(_axis_angle(_perp(AXIS), angle), Q2)
+    o.set_orientation_d(1, q2)
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    jac = o.joint_data(j)[0]
+    _check_jacobian(o, j, jac, perturb_body2, Q1, q2, real)
+
+
+def _gamma(softness):
+    return softness / DT
+
+
+@pytest.mark.parametrize("degrees", [119.99, 120.01, 179.0])
+def test_twist_softness_uses_angle_units(degrees):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, 1e-6, -1e-6))
+    _set(o, 1, q=_axis_angle((0, 0, 1), np.radians(degrees)), w=(0, 0, 1))
+    o.joint_solve(j, DT, 0.0, 0.001)
+    g = _gamma(0.001)
+    assert o.bodies()["angular_velocity"][1, 2] == pytest.approx(g / (1 + g), abs=1e-5)
+
+
+@pytest.mark.parametrize("degrees", [29.99, 30.01, 149.99, 150.01])
+def test_cone_softness_uses_angle_units(degrees):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, 0.0, np.radians(10.0)))
+    _set(o, 1, q=_axis_angle((1, 0, 0), np.radians(degrees)), w=(1, 0, 0))
+    o.joint_solve(j, DT, 0.0, 0.001)
+    g = _gamma(0.001)
+    assert o.bodies()["angular_velocity"][1, 0] == pytest.approx(g / (1 + g), abs=1e-5)
+
+
+@pytest.mark.parametrize("lower", [1e-6, 1e-9])
+def test_tiny_cone_limits_remain_distinct(lower):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, lower, 2 * lower))
+    _set(o, 1, q=_axis_angle((1, 0, 0), 3 * lower))
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    assert o.joint_data(j)[3] == 1
+
+
+@pytest.mark.parametrize("softness", [0.0, 0.001])
+@pytest.mark.parametrize("direction", [-1, 1])
+def test_fixed_cone_tilt_holds_both_directions(direction, softness):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    lim = np.radians(30.0)
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, lim, lim))
+    _set(o, 1, q=_axis_angle((1, 0, 0), np.pi / 6), w=(direction, 0, 0))
+    o.joint_solve(j, DT, 0.0, softness)
+    g = _gamma(softness)
+    assert o.joint_data(j)[3] == 3
+    assert o.bodies()["angular_velocity"][1, 0] == pytest.approx(direction * g / (1 + g), abs=1e-5)
+
+
+@pytest.mark.parametrize("softness", [0.0, 0.001])
+@pytest.mark.parametrize("outgoing", [False, True])
+@pytest.mark.parametrize("upper", [False, True])
+def test_interior_cone_boundary_stops_only_the_outward_rate(upper, outgoing, softness):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, 0.0, np.pi))
+    direction = 1 if upper == outgoing else -1
+    _set(o, 1, q=_axis_angle((1, 0, 0), 0.5), w=(direction, 0, 0))
+    boundary = o.joint_angle(j)
+    if upper:
+        o.joint_set_limit(j, 0.0, boundary)
+    else:
+        o.joint_set_limit(j, boundary, np.float32(np.pi))
+    o.joint_solve(j, DT, 0.0, softness)
+    g = _gamma(softness)
+    expected = direction * (g / (1 + g) if outgoing else 1.0)
+    assert o.bodies()["angular_velocity"][1, 0] == pytest.approx(expected, abs=1e-5)
+
+
+@pytest.mark.parametrize("antiparallel", [False, True])
+def test_natural_cone_bounds_leave_motion_free(antiparallel):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, 0.0, np.float32(np.pi)))
+    _set(o, 1, q=(1, 0, 0, 0) if antiparallel else (0, 0, 0, 1), w=(1, 2, 3))
+    o.joint_solve(j, DT, 0.2, 0.001)
+    assert o.joint_data(j)[3] == 0
+    np.testing.assert_array_equal(o.bodies()["angular_velocity"][1], (1, 2, 3))
+
+
+@pytest.mark.parametrize("twist", [False, True])
+def test_warm_starts_keep_their_units_across_former_thresholds(twist):
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    if twist:
+        j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, 1e-6, -1e-6))
+        axis, before, after, comp = (0, 0, 1), 119.99, 120.01, 2
+    else:
+        lim = np.radians(30.0)
+        j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, lim, lim))
+        axis, before, after, comp = (1, 0, 0), 29.99, 30.01, 0
+    _set(o, 1, q=_axis_angle(axis, np.radians(before)))
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    o.set_joint_impulses([[0.25, 0.0, 0.0]])
+    _set(o, 1, q=_axis_angle(axis, np.radians(after)))
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    assert o.joint_data(j)[4] == pytest.approx(0.25)
+    assert o.bodies()["angular_velocity"][1, comp] == pytest.approx(0.25, abs=1e-5)
