@@ -1,5 +1,10 @@
 """Speculative contacts in the oracle (CPU): the sweep and the detect branch that uses it.
 
+Pinned to the reference's own cases: CollisionTests.SweepTest (the sweep's time of impact,
+points and normal for a turned sphere and box) and
+ContactLifecycleTests.SeparatedContact_UsesOriginalSpeculativeThreshold (the speculative
+bias of a separated contact).
+
 NarrowPhase.Sweep (NarrowPhase.cs:1100-1222) on SimplexSolverAB (SimplexSolverAB.cs) is
 checked against closed-form times of impact; the detect branch (World.Detect.cs:168-196)
 and the swept bounding boxes (RigidBodyShape.cs:37-57) against the behaviour they exist
@@ -134,3 +139,42 @@ def test_swept_boxes_find_the_slab_pairs():
                 want.add(k)
         assert got == want
         assert (len(got) > 10) == spec
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_reference_sweep_case(real):
+    # CollisionTests.SweepTest (Behavior/CollisionTests.cs:143-169): a sphere (r 0.5) and a
+    # box (size 1) both turned 45 degrees about z, closing along the diagonal at speed 3
+    rot = (0.0, 0.0, np.sin(np.pi / 8), np.cos(np.pi / 8))
+    sweep = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0)
+    hit, pA, pB, n, lam = O.sweep(O.sphere(0.5), O.box(0.5, 0.5, 0.5), rot, rot, (1, 1, 3), (11, 11, 3),
+                                  sweep, -2.0 * sweep, real=real)
+    assert hit
+    lam_x = (np.sqrt(200.0) - 1.0) / 3.0
+    point = np.array([1.0, 1.0, 3.0]) + sweep * (0.5 + lam_x)
+    assert np.sum((n - sweep) ** 2) < 1e-4
+    assert np.sum((pA - (point - sweep * lam)) ** 2) < 1e-4
+    assert np.sum((pB - (point + 2.0 * sweep * lam)) ** 2) < 1e-4
+    assert abs(lam - lam_x) < 1e-4
+
+
+@pytest.mark.parametrize("gap, target", [(0.1, -0.9), (0.005, 10.0)])
+def test_separated_contact_uses_the_speculative_threshold(gap, target):
+    # ContactLifecycleTests.SeparatedContact_UsesOriginalSpeculativeThreshold
+    # (Behavior/ContactLifecycleTests.cs:109-146): a contact 0.1 apart at dt 0.1 is
+    # speculative (bias = -gap / dt * 0.9); one 0.005 apart keeps its restitution bias
+    from test_oracle_golden import _two_body_scene
+    null = dict(motion_type=abi.MOTION_STATIC, inv_mass=0.0, inv_inertia=np.zeros(6), friction=0.0, restitution=1.0)
+    inv_i = 1.0 / (0.4 * 1.0 * 0.25 * 0.25)
+    ball = dict(position=(gap, 0, 0), velocity=(-10, 0, 0), inv_mass=1.0, inv_inertia=(inv_i, 0, 0, inv_i, 0, inv_i),
+                friction=0.0, restitution=1.0)
+    w = O.OracleWorld(_two_body_scene(null, ball))
+    w.register_contact(0, 1, [0, 0, 0], [gap, 0, 0], [1, 0, 0])
+    assert w.contacts()[0]["bias"] == pytest.approx(10.0)
+    w.fn("jor_world_prepare")(w.h, 0.1, 1)
+    c = w.contacts()[0]
+    assert c["bias"] == pytest.approx(target, abs=1e-5) and c["penalty_bias"] == 0.0
+    w.fn("jor_world_iterate")(w.h, 1)
+    assert w.bodies()["velocity"][1][0] == pytest.approx(target, abs=1e-5)
+    w.fn("jor_world_iterate")(w.h, 0)
+    assert w.bodies()["velocity"][1][0] == pytest.approx(target, abs=1e-5)
