@@ -265,6 +265,8 @@ template <class R> struct Handle {
         w.register_contact(s1, s2, r);                                                                             \
     }                                                                                                              \
     extern "C" void jor_world_narrowphase_##SUF(void* h) { ((Handle<R>*)h)->w.narrowphase(); }                    \
+    /* World.AllowDeactivation (World.cs:333) for the oracle's island restatement */                           \
+    extern "C" void jor_world_set_deactivation_##SUF(void* h, int on) { ((Handle<R>*)h)->w.allow_deactivation = on != 0; } \
     extern "C" void jor_world_set_step_dt_##SUF(void* h, float dt) { ((Handle<R>*)h)->w.step_dt = (R)dt; }        \
     /* ContactData.PrepareForIteration / Iterate on every arbiter, key order (tests) */                            \
     extern "C" void jor_world_prepare_##SUF(void* h, float dt, int substeps) {                                    \

@@ -47,6 +47,11 @@ template <class R> struct Body {
     bool gravity = true;
     bool speculative = false;       // RigidBody.EnableSpeculativeContacts
     int world = 0;
+    // deactivation (RigidBody.cs:315, :398-400; Island.cs): time at rest, and the two island
+    // flags kept per body (an island's flag is the OR over its bodies): MarkedAsActive and
+    // membership of the active island partition
+    R sleep_time = 0;
+    bool marked = true, island_active = true;
     bool active() const { return (flags & 4) != 0; }
     bool gyroscopic() const { return (flags & 8) != 0; }
     bool has_linear_locks() const { return (flags & (7 << 4)) != 0; }

@@ -34,6 +34,11 @@ template <class R> struct World {
     R spec_relax = (R)0.9;
     R spec_threshold = (R)10.0;                // SpeculativeVelocityThreshold
     R step_dt = 0;                             // dt of the step in progress
+    // World.AllowDeactivation (World.cs:333; the reference's default is on) with the bodies'
+    // default thresholds (RigidBody.cs:398-400)
+    bool allow_deactivation = false;
+    R sleep_lin2 = (R)0.1, sleep_ang2 = (R)0.1, sleep_after = (R)1.0;
+    std::vector<int> created;                  // arbiters created by this step's detection
     bool external_order = false;               // use ContactData::color / Joint::color
     bool record_residual = false;
     std::vector<R> residuals;                  // first substep, one value per iteration
@@ -59,6 +64,7 @@ template <class R> struct World {
         arbiters.push_back(cd);
         int idx = (int)arbiters.size() - 1;
         arb_index[k] = idx;
+        created.push_back(idx);
         return idx;
     }
     // ContactData.ResetMode (Contact.cs:288-296)
@@ -272,6 +278,7 @@ template <class R> struct World {
     }
 
     void narrowphase() {
+        created.clear();
         auto pairs = find_pairs();
         n_pairs = (int64_t)pairs.size();
         n_colliding = 0; n_points = 0; n_speculative = 0;
@@ -296,18 +303,85 @@ template <class R> struct World {
         }
     }
 
+    // ---- islands and deactivation --------------------------------------------------------
+    // The reference keeps islands incrementally (IslandHelper.cs: merge on a new connection,
+    // breadth-first split on a removed one); they are the connected components of the graph
+    // of non-static bodies joined by arbiters and constraints, static bodies alone.  Their
+    // two flags are kept per body here: MarkedAsActive (set by a body still moving,
+    // RigidBody.cs:740-743, and by AddToActiveList) and membership of the active partition
+    // (set by AddToActiveList, World.cs:903-910, cleared when the island goes to sleep).  A
+    // merge ORs both flags and always comes with AddToActiveList; a split copies them to both
+    // parts, and the splits of a step (RemoveBrokenArbiters) follow AddToActiveList on both
+    // bodies of the removed arbiter, so the OR over a component's bodies is the island's flag.
+    static bool non_static(const Body<R>& b) { return b.motion != STATIC; }
+    // AddToActiveList (World.cs:903-910) on the island of body i
+    void add_to_active(int i) { bodies[i].marked = true; bodies[i].island_active = true; }
+    // a row is solved while its non-static bodies are awake (memContacts / constraint
+    // activation follows DeactivateBodyForSleep and activation, World.Step.cs:1247-1275, :1325-1345)
+    bool row_awake(int b1, int b2) const {
+        return (non_static(bodies[b1]) && bodies[b1].active()) || (non_static(bodies[b2]) && bodies[b2].active());
+    }
+    int uf_find(std::vector<int>& p, int x) {
+        while (p[x] != x) { p[x] = p[p[x]]; x = p[x]; }
+        return x;
+    }
+    // CheckDeactivation (World.Step.cs:1289-1371) on the components of the connection graph
+    void check_deactivation() {
+        const int n = (int)bodies.size();
+        std::vector<int> parent(n);
+        std::iota(parent.begin(), parent.end(), 0);
+        auto join = [&](int a, int b) {
+            if (!non_static(bodies[a]) || !non_static(bodies[b])) return;
+            a = uf_find(parent, a); b = uf_find(parent, b);
+            if (a != b) parent[std::max(a, b)] = std::min(a, b);
+        };
+        for (auto& a : arbiters) join(a.b1, a.b2);
+        for (auto& j : joints) join(j.b1, j.b2);
+        std::vector<char> any_active(n, 0), any_marked(n, 0);
+        for (int i = 0; i < n; i++) {
+            int r = uf_find(parent, i);
+            any_active[r] |= bodies[i].island_active;
+            any_marked[r] |= bodies[i].marked;
+        }
+        for (int i = 0; i < n; i++) {
+            Body<R>& b = bodies[i];
+            int r = uf_find(parent, i);
+            if (!any_active[r]) continue;            // a sleeping island is not visited
+            b.marked = false;
+            if (!any_marked[r] && allow_deactivation) {
+                // DeactivateBodyForSleep (World.Step.cs:1247-1287): velocities are kept
+                b.flags &= ~4;
+                b.island_active = false;
+            } else {
+                b.island_active = true;
+                if (!b.active() && b.motion != STATIC) { b.flags |= 4; b.sleep_time = 0; }
+            }
+        }
+    }
+    // RigidBody.Update's rest test (RigidBody.cs:723-743)
+    void sleep_update(Body<R>& b, const TimeStep<R>& ts) {
+        bool kin = b.motion == KINEMATIC;
+        V3<R> zero;
+        bool resting = kin ? (b.angvel == zero && b.vel == zero)
+                           : (len2(b.angvel) < sleep_ang2 && len2(b.vel) < sleep_lin2);
+        b.sleep_time = resting ? b.sleep_time + ts.dt : (R)0;
+        if ((kin && !resting) || b.sleep_time < sleep_after) b.marked = true;
+    }
+
     // Solve order: indices into arbiters and joints, grouped by colour.
     std::vector<std::vector<int>> order_arb, order_joint;
     void build_order() {
         order_arb.clear(); order_joint.clear();
         if (!external_order) {
-            std::vector<int> a(arbiters.size());
-            std::iota(a.begin(), a.end(), 0);
+            std::vector<int> a;
+            for (int i = 0; i < (int)arbiters.size(); i++)
+                if (!allow_deactivation || row_awake(arbiters[i].b1, arbiters[i].b2)) a.push_back(i);
             std::sort(a.begin(), a.end(), [&](int x, int y) {
                 return std::make_pair(arbiters[x].key1, arbiters[x].key2) < std::make_pair(arbiters[y].key1, arbiters[y].key2);
             });
-            std::vector<int> j(joints.size());
-            std::iota(j.begin(), j.end(), 0);
+            std::vector<int> j;
+            for (int i = 0; i < (int)joints.size(); i++)
+                if (!allow_deactivation || row_awake(joints[i].b1, joints[i].b2)) j.push_back(i);
             order_arb.push_back(a);
             order_joint.push_back(std::vector<int>());
             order_arb.push_back(std::vector<int>());
@@ -319,8 +393,10 @@ template <class R> struct World {
         for (auto& j : joints) nc = std::max(nc, j.color + 1);
         order_arb.assign(nc, {});
         order_joint.assign(nc, {});
-        for (size_t i = 0; i < arbiters.size(); i++) order_arb[arbiters[i].color].push_back((int)i);
-        for (size_t i = 0; i < joints.size(); i++) order_joint[joints[i].color].push_back((int)i);
+        for (size_t i = 0; i < arbiters.size(); i++)
+            if (!allow_deactivation || row_awake(arbiters[i].b1, arbiters[i].b2)) order_arb[arbiters[i].color].push_back((int)i);
+        for (size_t i = 0; i < joints.size(); i++)
+            if (!allow_deactivation || row_awake(joints[i].b1, joints[i].b2)) order_joint[joints[i].color].push_back((int)i);
     }
     R residual_norm(std::vector<R>& prev) {
         double d2 = 0, l2 = 0;
@@ -346,8 +422,10 @@ template <class R> struct World {
         return v;
     }
 
+    // bodies the step moves: all, or with deactivation the awake ones (memRigidBodies.Active)
+    bool moves(const Body<R>& b) const { return !allow_deactivation || b.active(); }
     void solve_substep(const TimeStep<R>& ts, bool first) {
-        for (auto& b : bodies) integrate_forces(b);
+        for (auto& b : bodies) if (moves(b)) integrate_forces(b);
         // prepare (World.Step.cs:1155-1172)
         for (size_t c = 0; c < order_arb.size(); c++) {
             for (int i : order_arb[c]) contactdata_prepare(arbiters[i], bodies, ts);
@@ -362,7 +440,7 @@ template <class R> struct World {
             }
             if (first && record_residual) residuals.push_back(residual_norm(prev));
         }
-        for (auto& b : bodies) integrate_velocities(b, ts);
+        for (auto& b : bodies) if (moves(b)) integrate_velocities(b, ts);
         for (int it = 0; it < relax; it++)
             for (size_t c = 0; c < order_arb.size(); c++)
                 for (int i : order_arb[c]) contactdata_iterate(arbiters[i], bodies, false);
@@ -372,7 +450,11 @@ template <class R> struct World {
     void remove_broken() {
         std::vector<ContactData<R>> keep;
         keep.reserve(arbiters.size());
-        for (auto& a : arbiters) if ((a.usage & 15u) != 0) keep.push_back(a);
+        for (auto& a : arbiters) {
+            if ((a.usage & 15u) != 0) { keep.push_back(a); continue; }
+            // AddToActiveList on both islands before the arbiter goes (World.Step.cs:845-846)
+            if (allow_deactivation) { add_to_active(a.b1); add_to_active(a.b2); }
+        }
         arbiters.swap(keep);
         arb_index.clear();
         for (size_t i = 0; i < arbiters.size(); i++) arb_index[key(arbiters[i].key1, arbiters[i].key2)] = (int)i;
@@ -385,11 +467,21 @@ template <class R> struct World {
         TimeStep<R> ts(dt, substeps);
         step_dt = dt;
         if (narrow) narrowphase();
+        if (allow_deactivation) {
+            // HandleDeferredArbiters (World.Step.cs:880-914), then CheckDeactivation
+            for (int i : created) { add_to_active(arbiters[i].b1); add_to_active(arbiters[i].b2); }
+            check_deactivation();
+        }
         build_order();
         for (int s = 0; s < substeps; s++) solve_substep(ts, s == 0);
         remove_broken();
-        for (auto& a : arbiters) contactdata_update_position(a, bodies);
-        for (auto& b : bodies) body_update(b, ts, gravity);
+        for (auto& a : arbiters)
+            if (!allow_deactivation || row_awake(a.b1, a.b2)) contactdata_update_position(a, bodies);
+        for (auto& b : bodies) {
+            if (!moves(b)) continue;
+            if (allow_deactivation) sleep_update(b, ts);
+            body_update(b, ts, gravity);
+        }
     }
 
     // --- threading for the multithreaded Regular-mode restatement ---------------------
