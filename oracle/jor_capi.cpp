@@ -226,6 +226,11 @@ template <class R> struct Handle {
         put3d(out, jt.jr[0]); put3d(out + 3, jt.jr[1]);                                                            \
         out[6] = (double)jt.eff1; out[7] = jt.clamp; out[8] = (double)jt.acc.x;                                   \
     }                                                                                                              \
+    /* Bias / Softness setters of a joint (ConeLimit.cs:358-376, TwistAngle.cs:262-294, ...) */                   \
+    extern "C" void jor_world_joint_params_##SUF(void* h, int j, double bias, double soft) {                       \
+        Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                               \
+        jt.bias_factor = (R)bias; jt.softness = (R)soft;                                                           \
+    }                                                                                                              \
     extern "C" double jor_world_joint_angle_##SUF(void* h, int j) {                                                \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         return (double)joint_angle(w.joints[j], w.bodies);                                                         \

@@ -41,7 +41,7 @@ def load():
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
             "jor_world_set_step_dt": (None, [P, F]), "jor_world_set_deactivation": (None, [P, I]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
-            "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
+            "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
             "jor_world_set_penalty": (None, [P, I, I, D]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
@@ -269,6 +269,9 @@ class OracleWorld:
 
     def joint_angle(self, j):
         return self.fn("jor_world_joint_angle")(self.h, j)
+
+    def joint_params(self, j, bias, softness):
+        self.fn("jor_world_joint_params")(self.h, j, float(bias), float(softness))
 
     def joint_set_limit(self, j, lo, hi):
         self.fn("jor_world_joint_set_limit")(self.h, j, float(lo), float(hi))

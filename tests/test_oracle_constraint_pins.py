@@ -10,7 +10,12 @@ reference's default body), body 0 static where the reference uses its NullBody.
   is gamma / (1 + gamma), gamma = softness / dt);
 - a tiny cone limit stays distinct from zero, a fixed tilt holds both directions, an
   interior boundary stops only the outward rate, the natural 0 and pi bounds leave motion
-  free, and cached impulses keep their units across the former thresholds.
+  free, and cached impulses keep their units across the former thresholds;
+- and from ConstraintSingularityTests.cs, stepped in a world without gravity or damping:
+  a twist recovers from a half turn without a huge angular velocity and honours its range
+  there, a cone recovers from its endpoint poses into its range, the twist Jacobian matches
+  its angle's derivative next to the half turn, and a tiny cone limit corrects a tilt its
+  rounded cosine would hide.
 """
 import numpy as np
 import pytest
@@ -209,3 +214,99 @@ def test_warm_starts_keep_their_units_across_former_thresholds(twist):
     o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
     assert o.joint_data(j)[4] == pytest.approx(0.25)
     assert o.bodies()["angular_velocity"][1, comp] == pytest.approx(0.25, abs=1e-5)
+
+
+# ---- ConstraintSingularityTests.cs: half turns and cone endpoints, stepped ------------------
+# The reference's world for these cases: no gravity, one substep, 8 iterations and no
+# relaxation, no damping, no gyroscopic term (ConstraintSingularityTests.cs:74-87).
+LOCK_ALL_BUT = {"all": 0, "angular_x": 63 ^ 8, "angular_z": 63 ^ 32}
+
+
+def _stepped_world(locks):
+    sc = _world((0, 0, 0, 1), (0, 0, 0, 1), True)
+    b = sc["bodies"]
+    b["flags"][1] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY | (LOCK_ALL_BUT[locks] << abi.BODY_LOCKS_SHIFT)
+    sc["params"] = dict(substeps=1, solver_iterations=8, relax_iterations=0, gravity=(0.0, 0.0, 0.0))
+    return sc
+
+
+def _run_checked(o, steps=100):
+    for _ in range(steps):
+        o.step(0.01)
+        b = o.bodies()
+        assert np.linalg.norm(b["angular_velocity"][1]) < 100.0
+        assert np.isfinite(b["orientation"][1]).all()
+
+
+@pytest.mark.parametrize("locks", ["all", "angular_z"])
+@pytest.mark.parametrize("softness", [0.0, 0.001])
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("offset", [0.0, 1e-5, 0.005])
+def test_twist_recovers_from_a_half_turn(offset, sign, softness, locks):
+    # Twist_HalfTurnRecoversWithoutHugeAngularVelocity (ConstraintSingularityTests.cs:89-112)
+    o = O.OracleWorld(_stepped_world(locks))
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, 1e-6, -1e-6))
+    o.joint_params(j, 0.2, softness)
+    q = (0.0, 0.0, float(sign), 0.0) if offset == 0 else _axis_angle((0, 0, 1), sign * (np.pi - offset))
+    _set(o, 1, q=q)
+    _run_checked(o)
+    assert abs(o.joint_angle(j)) < 0.001
+
+
+@pytest.mark.parametrize("locks", ["all", "angular_x"])
+@pytest.mark.parametrize("softness", [0.0, 0.001])
+@pytest.mark.parametrize("antiparallel", [False, True])
+@pytest.mark.parametrize("offset", [0.0, 1e-5, 0.002, 0.1])
+def test_cone_endpoint_poses_recover_into_the_range(offset, antiparallel, softness, locks):
+    # Cone_EndpointPosesRecoverIntoAllowedRange (ConstraintSingularityTests.cs:114-137)
+    o = O.OracleWorld(_stepped_world(locks))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, np.radians(30.0), np.radians(60.0)))
+    o.joint_params(j, 0.2, softness)
+    if antiparallel and offset == 0:
+        q = (1.0, 0.0, 0.0, 0.0)
+    else:
+        q = _axis_angle((1, 0, 0), np.pi - offset if antiparallel else offset)
+    _set(o, 1, q=q)
+    _run_checked(o)
+    assert np.pi / 6 - 0.001 <= o.joint_angle(j) <= np.pi / 3 + 0.001
+
+
+@pytest.mark.parametrize("swing", [0.0, 0.005])
+def test_twist_jacobian_near_the_half_turn(swing):
+    # Twist_AngleFallbackJacobianMatchesFiniteDifference (ConstraintSingularityTests.cs:139-171)
+    o = O.OracleWorld(_world(Q1, Q1, False))
+    o.set_orientation_d(0, Q1)
+    o.set_orientation_d(1, Q1)
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, tuple(AXIS) + tuple(AXIS) + (1e-6, -1e-6))
+    q2 = _quat_mul(_axis_angle(AXIS, np.pi - 0.01), Q1)
+    q2 = _quat_mul(_axis_angle(_perp(AXIS), swing), q2)
+    o.set_orientation_d(1, q2)
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    jac = o.joint_data(j)[0]
+    for direction in np.eye(3):
+        o.set_orientation_d(0, _quat_mul(_axis_angle(direction, 1e-4), Q1))
+        after = o.joint_angle(j)
+        o.set_orientation_d(0, _quat_mul(_axis_angle(direction, -1e-4), Q1))
+        before = o.joint_angle(j)
+        assert (after - before) / 2e-4 == pytest.approx(float(np.dot(jac, direction)), abs=0.004)
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_twist_half_turn_honours_its_range(sign):
+    # Twist_HalfTurnHonorsRangeLimits (ConstraintSingularityTests.cs:173-185)
+    o = O.OracleWorld(_stepped_world("angular_z"))
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, -np.pi / 6, np.pi / 6))
+    o.joint_params(j, 0.2, 0.0)
+    _set(o, 1, q=(0.0, 0.0, float(sign), 0.0))
+    for _ in range(100):
+        o.step(0.01)
+    assert abs(o.joint_angle(j)) <= np.pi / 6 + 0.001
+
+
+def test_tiny_cone_upper_limit_corrects_a_rounded_tilt():
+    # Cone_TinyUpperLimitCorrectsTiltDespiteRoundedCosine (ConstraintSingularityTests.cs:187-200)
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    j = o.add_joint(abi.CONSTRAINT_CONELIMIT, 0, 1, (0, 0, 1, 0, 0, 1, 0.0, 5e-6))
+    _set(o, 1, q=_axis_angle((1, 0, 0), 1e-5))
+    o.joint_solve(j, DT, 0.2, 0.0)
+    assert o.bodies()["angular_velocity"][1, 0] == pytest.approx(-1e-4, abs=1e-6)
