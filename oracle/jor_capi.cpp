@@ -272,6 +272,12 @@ template <class R> struct Handle {
     extern "C" void jor_world_narrowphase_##SUF(void* h) { ((Handle<R>*)h)->w.narrowphase(); }                    \
     /* World.AllowDeactivation (World.cs:333) for the oracle's island restatement */                           \
     extern "C" void jor_world_set_deactivation_##SUF(void* h, int on) { ((Handle<R>*)h)->w.allow_deactivation = on != 0; } \
+    /* world bounding box of shape s as the step of length dt sees it (out = min, max) */                        \
+    extern "C" void jor_world_shape_box_##SUF(void* h, int s, float dt, double* out) {                            \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        w.step_dt = (R)dt;                                                                                         \
+        Box3<R> b = w.aabbs()[s]; put3d(out, b.mn); put3d(out + 3, b.mx);                                          \
+    }                                                                                                              \
     extern "C" void jor_world_set_step_dt_##SUF(void* h, float dt) { ((Handle<R>*)h)->w.step_dt = (R)dt; }        \
     /* ContactData.PrepareForIteration / Iterate on every arbiter, key order (tests) */                            \
     extern "C" void jor_world_prepare_##SUF(void* h, float dt, int substeps) {                                    \

@@ -39,7 +39,8 @@ def load():
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
-            "jor_world_set_step_dt": (None, [P, F]), "jor_world_set_deactivation": (None, [P, I]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
+            "jor_world_set_step_dt": (None, [P, F]), "jor_world_set_deactivation": (None, [P, I]),
+            "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
@@ -257,6 +258,12 @@ class OracleWorld:
         out = np.zeros(9, np.float64)
         self.fn("jor_world_joint_data")(self.h, j, p(out))
         return out[0:3], out[3:6], out[6], int(out[7]), out[8]
+
+    def shape_box(self, s, dt):
+        """World bounding box (min, max) of shape s for a step of length dt."""
+        out = np.zeros(6, np.float64)
+        self.fn("jor_world_shape_box")(self.h, s, float(dt), p(out))
+        return out[:3], out[3:]
 
     def allow_deactivation(self, on=True):
         """World.AllowDeactivation: islands at rest for the deactivation time go to sleep."""

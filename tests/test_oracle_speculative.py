@@ -178,3 +178,62 @@ def test_separated_contact_uses_the_speculative_threshold(gap, target):
     assert w.bodies()["velocity"][1][0] == pytest.approx(target, abs=1e-5)
     w.fn("jor_world_iterate")(w.h, 0)
     assert w.bodies()["velocity"][1][0] == pytest.approx(target, abs=1e-5)
+
+
+def _one_body(shape_kind, dims, speculative, velocity, angular=(0, 0, 0), position=(0, 0, 0)):
+    b = np.zeros(1, abi.BODY_DTYPE)
+    b["orientation"][0, 3] = 1.0
+    b["inv_mass"] = 1.0
+    b["inv_inertia"] = (1, 0, 0, 1, 0, 1)
+    b["linear_damping"] = b["angular_damping"] = 1.0
+    b["flags"] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY | (abi.BODY_SPECULATIVE if speculative else 0)
+    b["position"] = position
+    b["velocity"] = velocity
+    b["angular_velocity"] = angular
+    s = np.zeros(1, abi.SHAPE_DTYPE)
+    s["kind"] = shape_kind
+    s["dims"][0, :len(dims)] = dims
+    return dict(bodies=b, shapes=s, hull=np.zeros((0, 3), np.float32), triangles=np.zeros(0, abi.TRIANGLE_DTYPE))
+
+
+@pytest.mark.parametrize("linear", [False, True])
+def test_speculative_bounds_use_only_linear_velocity(linear):
+    # BroadPhaseUpdateTests.SpeculativeBoundsUseOnlyLinearVelocity
+    # (Behavior/BroadPhaseUpdateTests.cs:7-36): BoxShape(4, 0.2, 0.2) spinning at 1000 rad/s,
+    # speed 5 or 0, dt 0.02: padding 0.1 or none; without the flag the tight box
+    v = (3.0, 4.0, 0.0) if linear else (0.0, 0.0, 0.0)
+    tight = O.OracleWorld(_one_body(abi.SHAPE_BOX, (2.0, 0.1, 0.1), False, v, (0, 0, 1000))).shape_box(0, 0.02)
+    grown = O.OracleWorld(_one_body(abi.SHAPE_BOX, (2.0, 0.1, 0.1), True, v, (0, 0, 1000))).shape_box(0, 0.02)
+    pad = 0.1 if linear else 0.0
+    assert np.linalg.norm(grown[0] - (tight[0] - pad)) < 1e-5
+    assert np.linalg.norm(grown[1] - (tight[1] + pad)) < 1e-5
+    np.testing.assert_allclose(tight[0], (-2.0, -0.1, -0.1), atol=1e-6)
+
+
+def test_speculative_bullet_stops_at_a_thin_wall_in_one_step():
+    # BroadPhaseUpdateTests.SpeculativeVelocityChangeUpdatesBroadphaseBeforeFirstStep
+    # (Behavior/BroadPhaseUpdateTests.cs:58-90): a 0.1 sphere at 100 m/s toward a 0.02-thick
+    # static wall 0.8 away; one step of 0.01 (default solver settings, no gravity)
+    b = np.zeros(2, abi.BODY_DTYPE)
+    b["orientation"][:, 3] = 1.0
+    b["linear_damping"] = 0.998
+    b["angular_damping"] = 0.995
+    b["flags"] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY
+    b["friction"] = 0.2
+    b["position"][0] = (0, 0, -0.8)
+    b["motion_type"][0] = abi.MOTION_STATIC
+    b["inv_mass"][1] = 1.0
+    b["inv_inertia"][1] = (1, 0, 0, 1, 0, 1)
+    b["velocity"][1] = (0, 0, -100)
+    b["flags"][1] |= abi.BODY_SPECULATIVE
+    s = np.zeros(2, abi.SHAPE_DTYPE)
+    s["kind"] = (abi.SHAPE_BOX, abi.SHAPE_SPHERE)
+    s["body"] = (0, 1)
+    s["dims"][0, :3] = (5.0, 5.0, 0.01)
+    s["dims"][1, 0] = 0.1
+    sc = dict(bodies=b, shapes=s, hull=np.zeros((0, 3), np.float32), triangles=np.zeros(0, abi.TRIANGLE_DTYPE),
+              params=dict(gravity=(0.0, 0.0, 0.0)))
+    o = O.OracleWorld(sc)
+    o.step(0.01)
+    assert o.counters()["speculative"] == 1
+    assert o.bodies()["position"][1, 2] > -0.8
