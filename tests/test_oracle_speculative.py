@@ -1,9 +1,10 @@
 """Speculative contacts in the oracle (CPU): the sweep and the detect branch that uses it.
 
 Pinned to the reference's own cases: CollisionTests.SweepTest (the sweep's time of impact,
-points and normal for a turned sphere and box) and
+points and normal for a turned sphere and box),
 ContactLifecycleTests.SeparatedContact_UsesOriginalSpeculativeThreshold (the speculative
-bias of a separated contact).
+bias of a separated contact) and BroadPhaseUpdateTests (a speculative box grows by dt |v| of
+its linear velocity alone; a bullet stops at a thin wall in its first step).
 
 NarrowPhase.Sweep (NarrowPhase.cs:1100-1222) on SimplexSolverAB (SimplexSolverAB.cs) is
 checked against closed-form times of impact; the detect branch (World.Detect.cs:168-196)
