@@ -269,6 +269,14 @@ template <class R> struct Handle {
         r.A[0] = get3<R>(p1); r.B[0] = get3<R>(p2); r.n = get3<R>(n);                                              \
         w.register_contact(s1, s2, r);                                                                             \
     }                                                                                                              \
+    /* RegisterContact with SolveMode.Angular removed (World.Detect.cs:246-262, removeFlags) */                 \
+    extern "C" void jor_world_register_linear_contact_##SUF(void* h, int s1, int s2, const float* p1,              \
+                                                            const float* p2, const float* n) {                     \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        typename World<R>::DetectResult r; r.hit = true; r.count = 1; r.speculative = true;                        \
+        r.A[0] = get3<R>(p1); r.B[0] = get3<R>(p2); r.n = get3<R>(n);                                              \
+        w.register_contact(s1, s2, r);                                                                             \
+    }                                                                                                              \
     extern "C" void jor_world_narrowphase_##SUF(void* h) { ((Handle<R>*)h)->w.narrowphase(); }                    \
     /* World.AllowDeactivation (World.cs:333) for the oracle's island restatement */                           \
     extern "C" void jor_world_set_deactivation_##SUF(void* h, int on) { ((Handle<R>*)h)->w.allow_deactivation = on != 0; } \
@@ -386,6 +394,14 @@ template <class R> struct Handle {
                                get3d<R>(sb_), pA, pB, n, toi);                                                     \
         put3d(out, pA); put3d(out + 3, pB); put3d(out + 6, n); out[9] = (double)toi;                              \
         return hit ? 1 : 0;                                                                                        \
+    }                                                                                                              \
+    /* SimplexSolverAB.AddVertex over n Minkowski vertices (witness points zero): returns the     \
+       last call's result, out = the closest point it reports */                                   \
+    extern "C" int jor_simplex_##SUF(const double* verts, int n, double* out) {                                    \
+        SimplexAB<R> sx; V3<R> c; bool r = true;                                                                   \
+        for (int i = 0; i < n; i++) { Vertex<R> v; v.V = get3d<R>(verts + 3 * i); r = sx.add(v, c); }           \
+        put3d(out, c);                                                                                             \
+        return r ? 1 : 0;                                                                                          \
     }                                                                                                              \
     extern "C" int jor_manifold_##SUF(const jg_shape_desc* da, const float* va, const jg_shape_desc* db,         \
                                       const float* vb, const double* qa, const double* qb, const double* pa,      \

@@ -39,7 +39,7 @@ def load():
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
-            "jor_world_set_step_dt": (None, [P, F]), "jor_world_set_deactivation": (None, [P, I]),
+            "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]), "jor_world_set_deactivation": (None, [P, I]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
@@ -54,7 +54,7 @@ def load():
             "jor_support": (None, [P, P, P, P]), "jor_aabb": (None, [P, P, P, P, P]),
             "jor_collide": (I, [P, P, P, P, P, P, P, P, D, I, P]),
             "jor_manifold": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
-            "jor_sweep": (I, [P, P, P, P, P, P, P, P, P, P, P]),
+            "jor_sweep": (I, [P, P, P, P, P, P, P, P, P, P, P]), "jor_simplex": (I, [P, I, P]),
             "jor_exact_side": (I, [P, P, P, P]), "jor_filter_side": (I, [P, P, P, P, P]),
             "jor_stable_sincos": (None, [D, P, P]), "jor_stable_atan2": (D, [D, D]),
         }
@@ -155,6 +155,14 @@ def sweep(a, b, qa, qb, pa, pb, va, vb, real="f"):
     args = [np.ascontiguousarray(x, np.float64) for x in (qa, qb, pa, pb, va, vb)]
     hit = getattr(lib, "jor_sweep_" + real)(p(sa), p(ra), p(sb), p(rb), *[p(x) for x in args], p(out))
     return bool(hit), out[0:3], out[3:6], out[6:9], out[9]
+
+
+def simplex(vertices, real="f"):
+    """SimplexSolverAB.AddVertex over the vertices in order: (last result, closest point)."""
+    v = np.ascontiguousarray(vertices, np.float64).reshape(-1, 3)
+    out = np.zeros(3, np.float64)
+    r = getattr(load(), "jor_simplex_" + real)(p(v), len(v), p(out))
+    return bool(r), out
 
 
 def support(s, d, real="f"):
@@ -299,9 +307,11 @@ class OracleWorld:
     def external_order(self, on):
         self.fn("jor_world_external_order")(self.h, 1 if on else 0)
 
-    def register_contact(self, s1, s2, p1, p2, n):
+    def register_contact(self, s1, s2, p1, p2, n, linear_only=False):
+        """World.RegisterContact of one point; linear_only removes SolveMode.Angular."""
         a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, n)]
-        self.fn("jor_world_register_contact")(self.h, s1, s2, p(a[0]), p(a[1]), p(a[2]))
+        name = "jor_world_register_linear_contact" if linear_only else "jor_world_register_contact"
+        self.fn(name)(self.h, s1, s2, p(a[0]), p(a[1]), p(a[2]))
 
     def narrowphase(self, dt=None):
         """Detection alone; dt is the step length the speculative branch tests against."""

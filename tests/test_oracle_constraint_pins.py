@@ -310,3 +310,12 @@ def test_tiny_cone_upper_limit_corrects_a_rounded_tilt():
     _set(o, 1, q=_axis_angle((1, 0, 0), 1e-5))
     o.joint_solve(j, DT, 0.2, 0.0)
     assert o.bodies()["angular_velocity"][1, 0] == pytest.approx(-1e-4, abs=1e-6)
+
+
+def test_twist_created_on_a_pure_swing_starts_at_zero():
+    # HistoricalRegressionTests.TwistAngle_Initialize_WithPureSwing_StartsAtZeroTwist
+    # (Regression/HistoricalRegressionTests.cs:88-105): body 2 turned a quarter about x, the
+    # twist axes y and z of the two bodies: Q0 absorbs the swing, so the twist reads zero
+    o = O.OracleWorld(_world((0, 0, 0, 1), _axis_angle((1, 0, 0), np.pi / 2), False))
+    j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 1, 0, 0, 0, 1, 1e-6, -1e-6))
+    assert abs(o.joint_angle(j)) < 1e-5

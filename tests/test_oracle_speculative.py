@@ -238,3 +238,67 @@ def test_speculative_bullet_stops_at_a_thin_wall_in_one_step():
     o.step(0.01)
     assert o.counters()["speculative"] == 1
     assert o.bodies()["position"][1, 2] > -0.8
+
+
+# ---- the sweep's simplex (Regression/SimplexProjectionTests.cs, the witness-point solver) ---
+def _simplex_all_true(vertices, real="f"):
+    # every AddVertex call of the reference's helper must report "origin not enclosed"
+    for k in range(1, len(vertices) + 1):
+        ok, c = O.simplex(vertices[:k], real=real)
+        assert ok
+    return c
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_simplex_segment_of_large_vertices_keeps_a_small_gap(real):
+    c = _simplex_all_true([(100000, 0.001, 0), (-130000, 0.001, 0)], real)
+    np.testing.assert_allclose(c, (0, np.float32(0.001) if real == "f" else 0.001, 0), atol=1e-9)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+def test_simplex_triangle_of_large_vertices_keeps_a_small_gap(real):
+    off = np.float32(0.001) if real == "f" else 0.001
+    c = _simplex_all_true([(100000, 100000, 0.001), (-130000, 100000, 0.001), (100000, -130000, 0.001)], real)
+    np.testing.assert_allclose(c, (0, 0, off), atol=1e-9)
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_simplex_segment_beyond_an_end_returns_that_end(reverse):
+    near, far = (2, 1, -3), (5, 1, -3)
+    c = _simplex_all_true([far, near] if reverse else [near, far])
+    np.testing.assert_array_equal(c, near)
+    near, far = (0, 2, 3), (4, 2, 3)
+    c = _simplex_all_true([far, near] if reverse else [near, far])
+    np.testing.assert_array_equal(c, near)
+
+
+def test_simplex_tiny_edge_keeps_the_second_vertex():
+    first, second = (2, 1, 3), (2 + 1e-5, 1, 3)
+    np.testing.assert_array_equal(_simplex_all_true([first, second]), np.float32(second))
+    np.testing.assert_array_equal(_simplex_all_true([second, first]), np.float32(first))
+    np.testing.assert_array_equal(_simplex_all_true([first, first]), first)
+
+
+def test_simplex_triangle_falls_back_to_an_edge():
+    np.testing.assert_allclose(_simplex_all_true([(3, -2, 1), (3, 2, 1), (5, 0, 1)]), (3, 0, 1), atol=1e-6)
+    np.testing.assert_allclose(_simplex_all_true([(3, -2, 1), (3, 2, 1), (3, 0, 1)]), (3, 0, 1), atol=1e-6)
+
+
+@pytest.mark.parametrize("gap, target", [(0.005, 2.0), (0.1, -0.9)])
+def test_linear_only_contact_ignores_angular_surface_velocity(gap, target):
+    # ContactLifecycleTests.LinearOnlyContact_IgnoresAngularSurfaceVelocity
+    # (Behavior/ContactLifecycleTests.cs:71-106): a contact registered with SolveMode.Angular
+    # removed (as the speculative branch registers its point) sees neither the spin's surface
+    # velocity in its restitution bias nor changes the spin
+    from test_oracle_golden import _two_body_scene
+    wall = dict(motion_type=abi.MOTION_STATIC, inv_mass=0.0, inv_inertia=np.zeros(6), friction=0.0)
+    ball = dict(velocity=(-2, 0, 0), angular_velocity=(0, 0, 10), inv_mass=1.0, inv_inertia=(2.5, 0, 0, 2.5, 0, 2.5),
+                friction=0.0, restitution=1.0)
+    w = O.OracleWorld(_two_body_scene(wall, ball))
+    w.register_contact(0, 1, [-gap, 1, 0], [0, 1, 0], [1, 0, 0], linear_only=True)
+    assert w.contacts()[0]["bias"] == pytest.approx(2.0, abs=1e-5)
+    w.fn("jor_world_prepare")(w.h, 0.1, 1)
+    w.fn("jor_world_iterate")(w.h, 1)
+    b = w.bodies()
+    assert b["velocity"][1][0] == pytest.approx(target, abs=1e-5)
+    np.testing.assert_array_equal(b["angular_velocity"][1], (0, 0, 10))
