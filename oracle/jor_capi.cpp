@@ -269,6 +269,14 @@ template <class R> struct Handle {
         r.A[0] = get3<R>(p1); r.B[0] = get3<R>(p2); r.n = get3<R>(n);                                              \
         w.register_contact(s1, s2, r);                                                                             \
     }                                                                                                              \
+    /* RegisterContact of a manifold (World.Detect.cs:294-324): n points on A and on B */                        \
+    extern "C" void jor_world_register_manifold_##SUF(void* h, int s1, int s2, const float* pa, const float* pb,   \
+                                                      int n, const float* nrm) {                                   \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        typename World<R>::DetectResult r; r.hit = true; r.count = std::min(n, 4); r.n = get3<R>(nrm);              \
+        for (int i = 0; i < r.count; i++) { r.A[i] = get3<R>(pa + 3 * i); r.B[i] = get3<R>(pb + 3 * i); }           \
+        w.register_contact(s1, s2, r);                                                                             \
+    }                                                                                                              \
     /* RegisterContact with SolveMode.Angular removed (World.Detect.cs:246-262, removeFlags) */                 \
     extern "C" void jor_world_register_linear_contact_##SUF(void* h, int s1, int s2, const float* p1,              \
                                                             const float* p2, const float* n) {                     \

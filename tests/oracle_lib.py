@@ -39,7 +39,8 @@ def load():
             "jor_world_external_order": (None, [P, I]), "jor_world_set_contacts": (None, [P, P, I]),
             "jor_world_get_contacts": (I, [P, P, I]), "jor_world_set_arbiter_color": (None, [P, I, I, I]),
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
-            "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]), "jor_world_set_deactivation": (None, [P, I]),
+            "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]),
+            "jor_world_register_manifold": (None, [P, I, I, P, P, I, P]), "jor_world_set_deactivation": (None, [P, I]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
@@ -312,6 +313,13 @@ class OracleWorld:
         a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, n)]
         name = "jor_world_register_linear_contact" if linear_only else "jor_world_register_contact"
         self.fn(name)(self.h, s1, s2, p(a[0]), p(a[1]), p(a[2]))
+
+    def register_manifold(self, s1, s2, pa, pb, n):
+        """World.RegisterContact of a CollisionManifold (up to four points)."""
+        a = np.ascontiguousarray(pa, np.float32).reshape(-1, 3)
+        b = np.ascontiguousarray(pb, np.float32).reshape(-1, 3)
+        v = np.ascontiguousarray(n, np.float32)
+        self.fn("jor_world_register_manifold")(self.h, s1, s2, p(a), p(b), len(a), p(v))
 
     def narrowphase(self, dt=None):
         """Detection alone; dt is the step length the speculative branch tests against."""
