@@ -446,3 +446,56 @@ def test_box_stack_stays_upright():
         w.step(0.01)
     top = w.bodies()["position"][n]
     assert np.linalg.norm(top - top0) < 1.0
+
+
+@pytest.mark.parametrize("substeps", [1, 3])
+def test_resting_cylinder_does_not_start_rolling(substeps):
+    # ContactSubstepTests.RestingCylinder_DoesNotStartRollingWithAuxiliaryContacts
+    # (Regression/ContactSubstepTests.cs:144-172): a cylinder (height 2, radius 0.5) on its
+    # side, 0.005 into a static floor, no damping, 4 + 2 iterations, auxiliary contacts on
+    bodies = scenes._body(2)
+    shapes = np.zeros(2, abi.SHAPE_DTYPE)
+    scenes.ground(bodies, shapes, 0, 0, size=(200.0, 200.0, 200.0), y=-100.0)
+    shapes["kind"][1] = abi.SHAPE_CYLINDER
+    shapes["body"][1] = 1
+    shapes["dims"][1, :2] = (0.5, 2.0)
+    scenes.set_mass(bodies, shapes, None, 1, 1)
+    bodies["position"][1] = (10.0, 0.495, 0.0)
+    bodies["orientation"][1] = (0.0, 0.0, np.sin(np.pi / 4), np.cos(np.pi / 4))
+    bodies["linear_damping"] = bodies["angular_damping"] = 1.0
+    bodies["restitution"] = 0.0
+    sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32), triangles=np.zeros(0, abi.TRIANGLE_DTYPE),
+              params=dict(substeps=substeps, solver_iterations=4, relax_iterations=2))
+    w = O.OracleWorld(sc)
+    for _ in range(1000):
+        w.step(0.01)
+    b = w.bodies()
+    assert np.linalg.norm(b["velocity"][1]) < 0.02
+    assert np.linalg.norm(b["angular_velocity"][1]) < 0.04
+    assert abs(b["position"][1][1] - 0.495) < 0.001
+
+
+def test_cached_contact_offsets_are_current_after_each_step():
+    # ContactSubstepTests.CachedContact_KeepsOffsetsFixedUntilSolvingFinishes
+    # (Regression/ContactSubstepTests.cs:48-92), its after-step half: detection rejected
+    # (steps without narrowphase), a spinning sphere's registered contact keeps one cached
+    # point whose body-2 offset is the current rotation of the registered point
+    null = dict(motion_type=abi.MOTION_STATIC, inv_mass=0.0, inv_inertia=np.zeros(6), position=(0, -1, 0))
+    inv_i = 1.0 / (0.4 * (4 / 3 * np.pi * 0.125) * 0.25)
+    ball = dict(angular_velocity=(0, 0, 1), inv_mass=1 / (4 / 3 * np.pi * 0.125), inv_inertia=(inv_i, 0, 0, inv_i, 0, inv_i),
+                linear_damping=1.0, angular_damping=1.0, flags=abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY)
+    sc = _two_body_scene(null, ball)
+    sc["params"] = dict(substeps=3, gravity=(0.0, 0.0, 0.0))
+    w = O.OracleWorld(sc)
+    point = np.array([0.0, -0.5, 0.0])
+    w.register_contact(0, 1, point, point, [0, 1, 0])
+    for _ in range(2):
+        w.step(0.01, narrow=False)
+        q = w.bodies()["orientation"][1].astype(np.float64)
+        x, y, z, s = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * s), 2 * (x * z + y * s)],
+                      [2 * (x * y + z * s), 1 - 2 * (x * x + z * z), 2 * (y * z - x * s)],
+                      [2 * (x * z - y * s), 2 * (y * z + x * s), 1 - 2 * (x * x + y * y)]])
+        c = w.contacts()
+        assert len(c) == 1
+        assert np.abs(c[0]["rel_pos2"] - R @ point).max() < 1e-5
