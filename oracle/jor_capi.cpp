@@ -9,6 +9,9 @@
 
 using namespace jor;
 
+// Constraint kinds the oracle restates ahead of the device (ids past the header's).
+#define JOR_CONSTRAINT_FIXEDANGLE 6
+
 namespace {
 
 template <class R> Shape<R> make_shape(const jg_shape_desc& d, const float* hull, const jg_triangle_desc* tris,
@@ -206,7 +209,9 @@ template <class R> struct Handle {
             distance_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                 \
         else if (kind == JG_CONSTRAINT_CONELIMIT)                                                                  \
             cone_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                     \
-        else twist_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                   \
+        else if (kind == JG_CONSTRAINT_TWISTANGLE)                                                                 \
+            twist_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                    \
+        else if (kind == JOR_CONSTRAINT_FIXEDANGLE) fixed_init(j, w.bodies);                                       \
         w.joints.push_back(j);                                                                                     \
         return (int)w.joints.size() - 1;                                                                           \
     }                                                                                                              \

@@ -197,7 +197,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
     return mmul(mscale(-(R)0.5, der), Mat<R>::from_m3(mat_from_quat(left)));
 }
 
-enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5 };
+enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -659,12 +659,57 @@ template <class R> R joint_angle(const Joint<R>& j, const std::vector<Body<R>>& 
     return 0;
 }
 
+// FixedAngle.Initialize (FixedAngle.cs:72-85): Q0 is the initial relative rotation
+template <class R> void fixed_init(Joint<R>& j, const std::vector<Body<R>>& b) {
+    j.kind = FIXEDANGLE;
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    j.q0 = qmul(qconj(b[j.b2].q), b[j.b1].q);
+}
+// FixedAngle.PrepareForIterationFixedAngle (FixedAngle.cs:87-128): three angular rows, the
+// Jacobian -2 x the rotation-log derivative of Q0 conj(q1) q2
+template <class R> void fixed_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> err;
+    short hemi;
+    j.jac = mscale(-(R)2, calc_jacobian(qmul(j.q0, qconj(b1.q)), b2.q, err, hemi));
+    if (j.hemisphere != 0 && j.hemisphere != hemi) j.acc = V3<R>();
+    j.hemisphere = hemi;
+    Sym3<R> isum(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                 b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                 b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+    M3<R> jt3;
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) jt3.m[i][k] = j.jac.a[i][k];
+    j.eff = Mat<R>::from_sym(sym_transform(isum, jt3));
+    R soft = j.softness * ts.inv_sub_dt;
+    j.eff.a[0][0] += soft; j.eff.a[1][1] += soft; j.eff.a[2][2] += soft;
+    j.eff = inverse_symmetric(j.eff);
+    j.bias = -err * j.bias_factor * ts.inv_dt;
+    V3<R> imp = mtvec(j.jac, j.acc);
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, imp);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, imp);
+}
+// FixedAngle.IterateFixedAngle (FixedAngle.cs:159-181)
+template <class R> void fixed_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> jv = mvec(j.jac, b1.angvel - b2.angvel);
+    V3<R> soft = j.acc * (j.softness * ts.inv_sub_dt);
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, jv + j.bias + soft);
+    j.acc = j.acc + lambda;
+    V3<R> imp = mtvec(j.jac, lambda);
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, imp);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, imp);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
         case HINGEANGLE: hinge_prepare(j, b, ts); break;
         case DISTANCELIMIT: distance_prepare(j, b, ts); break;
         case CONELIMIT: cone_prepare(j, b, ts); break;
+        case FIXEDANGLE: fixed_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -674,6 +719,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case HINGEANGLE: hinge_iterate(j, b, ts); break;
         case DISTANCELIMIT: distance_iterate(j, b, ts); break;
         case CONELIMIT: cone_iterate(j, b, ts); break;
+        case FIXEDANGLE: fixed_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }
