@@ -236,6 +236,19 @@ template <class R> struct Handle {
         Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                               \
         jt.bias_factor = (R)bias; jt.softness = (R)soft;                                                           \
     }                                                                                                              \
+    /* HingeAngle LimitBias / LimitSoftness setters (HingeAngle.cs:270-300) */                                   \
+    extern "C" void jor_world_joint_limit_params_##SUF(void* h, int j, double bias, double soft) {                 \
+        Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                               \
+        jt.limit_bias = (R)bias; jt.limit_softness = (R)soft;                                                      \
+    }                                                                                                              \
+    /* three-row joint state after its last Prepare: out = Jacobian (3x3, row-major as stored), \
+       Q0 (x y z w), local axis */                                                                                 \
+    extern "C" void jor_world_joint_matrix_##SUF(void* h, int j, double* out) {                                    \
+        const Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                         \
+        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) out[3 * r + c] = (double)jt.jac.a[r][c];           \
+        out[9] = jt.q0.x; out[10] = jt.q0.y; out[11] = jt.q0.z; out[12] = jt.q0.w;                                 \
+        put3d(out + 13, jt.axis);                                                                                  \
+    }                                                                                                              \
     extern "C" double jor_world_joint_angle_##SUF(void* h, int j) {                                                \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         return (double)joint_angle(w.joints[j], w.bodies);                                                         \

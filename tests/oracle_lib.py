@@ -43,7 +43,8 @@ def load():
             "jor_world_register_manifold": (None, [P, I, I, P, P, I, P]), "jor_world_set_deactivation": (None, [P, I]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
-            "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]), "jor_world_set_orientation_d": (None, [P, I, P]),
+            "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
+            "jor_world_joint_limit_params": (None, [P, I, D, D]), "jor_world_joint_matrix": (None, [P, I, P]), "jor_world_set_orientation_d": (None, [P, I, P]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
             "jor_world_set_penalty": (None, [P, I, I, D]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
@@ -288,6 +289,15 @@ class OracleWorld:
 
     def joint_params(self, j, bias, softness):
         self.fn("jor_world_joint_params")(self.h, j, float(bias), float(softness))
+
+    def joint_limit_params(self, j, bias, softness):
+        self.fn("jor_world_joint_limit_params")(self.h, j, float(bias), float(softness))
+
+    def joint_matrix(self, j):
+        """(Jacobian 3x3 as stored, Q0, local axis) of a three-row joint after its Prepare."""
+        out = np.zeros(16, np.float64)
+        self.fn("jor_world_joint_matrix")(self.h, j, p(out))
+        return out[:9].reshape(3, 3), out[9:13], out[13:16]
 
     def joint_set_limit(self, j, lo, hi):
         self.fn("jor_world_joint_set_limit")(self.h, j, float(lo), float(hi))

@@ -15,7 +15,11 @@ reference's default body), body 0 static where the reference uses its NullBody.
   a twist recovers from a half turn without a huge angular velocity and honours its range
   there, a cone recovers from its endpoint poses into its range, the twist Jacobian matches
   its angle's derivative next to the half turn, and a tiny cone limit corrects a tilt its
-  rounded cosine would hide.
+  rounded cosine would hide;
+- and for the three-row blocks (HingeAngle, a device row, and FixedAngle, restated in the
+  oracle as kind 6): their Jacobians are the derivative of the rotation log for both
+  bodies, they recover from half turns, and crossing the half turn drops the other branch's
+  impulse (for TwistAngle too).
 """
 import numpy as np
 import pytest
@@ -319,3 +323,120 @@ def test_twist_created_on_a_pure_swing_starts_at_zero():
     o = O.OracleWorld(_world((0, 0, 0, 1), _axis_angle((1, 0, 0), np.pi / 2), False))
     j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 1, 0, 0, 0, 1, 1e-6, -1e-6))
     assert abs(o.joint_angle(j)) < 1e-5
+
+
+# ---- three-row angular blocks: HingeAngle (device row) and FixedAngle (oracle, kind 6) -------
+FIXEDANGLE = 6
+
+
+def _rotation_log(q):
+    q = np.asarray(q, np.float64)
+    if q[3] < 0:
+        q = -q
+    s = np.linalg.norm(q[:3])
+    return q[:3] * (np.arctan2(s, q[3]) / s) if s > 0 else np.zeros(3)
+
+
+@pytest.mark.parametrize("real", ["f", "d"])
+@pytest.mark.parametrize("perturb_body2", [False, True])
+@pytest.mark.parametrize("hinge", [False, True])
+@pytest.mark.parametrize("angle", [0.2, 2.1, 3.13])
+def test_rotation_log_jacobian_matches_both_bodies(angle, hinge, perturb_body2, real):
+    # AngularCoordinateTests.RotationLogJacobianMatchesBothBodies (AngularCoordinateTests.cs:17-71)
+    delta, tol = PREC[real]
+    o = O.OracleWorld(_world(Q1, Q2, False), real=real)
+    o.set_orientation_d(0, Q1)
+    o.set_orientation_d(1, Q2)
+    if hinge:
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, tuple(AXIS) + (1e-6, -1e-6))
+    else:
+        j = o.add_joint(FIXEDANGLE, 0, 1, (0, 0, 0))
+    q2 = _quat_mul(_axis_angle(np.array([2.0, 1.0, -3.0]), angle), Q2)
+    o.set_orientation_d(1, q2)
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    jac, q0, local_axis = o.joint_matrix(j)
+    if hinge:
+        # the hinge stores its rows' Jacobians as columns; the reference transposes them
+        rows = jac.T
+        p0 = _orthonormal(local_axis)
+        frame = np.stack([p0, np.cross(local_axis, p0), local_axis])
+    else:
+        rows = jac
+    qs = {0: Q1, 1: q2}
+    body = 1 if perturb_body2 else 0
+    for direction in np.eye(3):
+        logs = []
+        for sgn in (1, -1):
+            qq = dict(qs)
+            qq[body] = _quat_mul(_axis_angle(direction, sgn * delta), qs[body])
+            rel = _quat_mul(_quat_mul(q0, qq[0] * (-1, -1, -1, 1)), qq[1])
+            logs.append(_rotation_log(rel))
+        measured = (logs[0] - logs[1]) / (2 * delta)
+        measured = frame @ measured if hinge else -2 * measured
+        expected = rows @ (direction * (-1 if perturb_body2 else 1))
+        assert np.abs(measured - expected).max() < tol
+
+
+def _orthonormal(v):
+    # MathHelper.CreateOrthonormal (MathHelper.cs:204-254) restated for this test: a unit
+    # vector orthogonal to v chosen from v's smallest component, as the oracle's helper does
+    v = np.asarray(v, np.float64)
+    ax = np.abs(v)
+    if ax[0] <= ax[1] and ax[0] <= ax[2]:
+        r = np.array([0.0, v[2], -v[1]])
+    elif ax[1] <= ax[2]:
+        r = np.array([-v[2], 0.0, v[0]])
+    else:
+        r = np.array([v[1], -v[0], 0.0])
+    return r / np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("offset", [0.0, 1e-5])
+@pytest.mark.parametrize("softness", [0.0, 0.001])
+@pytest.mark.parametrize("pure_twist", [False, True])
+@pytest.mark.parametrize("hinge", [False, True])
+def test_angular_blocks_recover_from_half_turns(hinge, pure_twist, softness, offset):
+    # AngularCoordinateTests.AngularBlocksRecoverFromHalfTurns (AngularCoordinateTests.cs:166-197):
+    # no gravity, one substep, default iterations, no damping, no gyroscopic term
+    sc = _world((0, 0, 0, 1), (0, 0, 0, 1), True)
+    sc["params"] = dict(substeps=1, gravity=(0.0, 0.0, 0.0))
+    o = O.OracleWorld(sc)
+    if hinge:
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, (0, 0, 1, 1e-6, -1e-6))
+        o.joint_params(j, 0.2, softness)
+        o.joint_limit_params(j, 0.1, softness)
+    else:
+        j = o.add_joint(FIXEDANGLE, 0, 1, (0, 0, 0))
+        o.joint_params(j, 0.2, softness)
+    axis = np.array([0.0, 0.0, 1.0]) if pure_twist else np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+    q = np.array([*axis, 0.0]) if offset == 0 else _axis_angle(axis, np.pi - offset)
+    o.set_orientation_d(1, q)
+    for _ in range(200):
+        o.step(0.01)
+        b = o.bodies()
+        assert np.linalg.norm(b["angular_velocity"][1]) < 100.0
+        assert np.isfinite(b["orientation"][1]).all()
+    assert np.linalg.norm(_rotation_log(o.bodies()["orientation"][1])) < 0.001
+
+
+@pytest.mark.parametrize("kind", ["hinge", "fixed", "twist"])
+def test_crossing_the_half_turn_clears_the_other_branch_impulse(kind):
+    # AngularCoordinateTests.CrossingTheHalfTurnClearsThePreviousBranchImpulse
+    # (AngularCoordinateTests.cs:199-240)
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    if kind == "hinge":
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, (0, 0, 1, 1e-6, -1e-6))
+        cached = [0.0, 0.0, 1.0]
+    elif kind == "fixed":
+        j = o.add_joint(FIXEDANGLE, 0, 1, (0, 0, 0))
+        cached = [0.0, 0.0, 1.0]
+    else:
+        j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, 1e-6, -1e-6))
+        cached = [1.0, 0.0, 0.0]
+    o.set_orientation_d(1, _axis_angle((0, 0, 1), np.pi - 0.01))
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    o.set_joint_impulses([cached])
+    o.set_orientation_d(1, _axis_angle((0, 0, 1), np.pi + 0.01))
+    o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+    np.testing.assert_array_equal(o.joint_impulses(1)[0], 0.0)
+    np.testing.assert_array_equal(o.bodies()["angular_velocity"][1], 0.0)
