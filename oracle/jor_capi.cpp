@@ -229,7 +229,7 @@ template <class R> struct Handle {
     extern "C" void jor_world_joint_data_##SUF(void* h, int j, double* out) {                                      \
         const Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                         \
         put3d(out, jt.jr[0]); put3d(out + 3, jt.jr[1]);                                                            \
-        out[6] = (double)jt.eff1; out[7] = jt.clamp; out[8] = (double)jt.acc.x;                                   \
+        out[6] = (double)jt.eff1; out[7] = jt.clamp; out[8] = (double)jt.acc.x; put3d(out + 9, jt.bias);          \
     }                                                                                                              \
     /* Bias / Softness setters of a joint (ConeLimit.cs:358-376, TwistAngle.cs:262-294, ...) */                   \
     extern "C" void jor_world_joint_params_##SUF(void* h, int j, double bias, double soft) {                       \
@@ -449,6 +449,7 @@ template <class R> struct Handle {
     extern "C" void jor_stable_sincos_##SUF(double a, double* s, double* c) {                                     \
         R ss, cc; StableMath<R>::sincos((R)a, ss, cc); *s = ss; *c = cc;                                           \
     }                                                                                                              \
+    extern "C" double jor_shortest_angle_##SUF(double a, double half) { return (double)shortest_angle((R)a, (R)half); } \
     extern "C" double jor_stable_atan2_##SUF(double y, double x) { return (double)StableMath<R>::atan2((R)y, (R)x); }
 
 JOR_DEFINE(f, float)

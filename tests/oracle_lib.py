@@ -59,6 +59,7 @@ def load():
             "jor_sweep": (I, [P, P, P, P, P, P, P, P, P, P, P]), "jor_simplex": (I, [P, I, P]),
             "jor_exact_side": (I, [P, P, P, P]), "jor_filter_side": (I, [P, P, P, P, P]),
             "jor_stable_sincos": (None, [D, P, P]), "jor_stable_atan2": (D, [D, D]),
+            "jor_shortest_angle": (D, [D, D]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name + "_" + suf)
@@ -265,9 +266,15 @@ class OracleWorld:
 
     def joint_data(self, j):
         """(jr0, jr1, effective mass, clamp, impulse) of a one-row joint after its Prepare."""
-        out = np.zeros(9, np.float64)
+        out = np.zeros(12, np.float64)
         self.fn("jor_world_joint_data")(self.h, j, p(out))
         return out[0:3], out[3:6], out[6], int(out[7]), out[8]
+
+    def joint_bias(self, j):
+        """The joint's bias vector after its last Prepare (one-row kinds: the first entry)."""
+        out = np.zeros(12, np.float64)
+        self.fn("jor_world_joint_data")(self.h, j, p(out))
+        return out[9:12]
 
     def shape_box(self, s, dt):
         """World bounding box (min, max) of shape s for a step of length dt."""

@@ -440,3 +440,73 @@ def test_crossing_the_half_turn_clears_the_other_branch_impulse(kind):
     o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
     np.testing.assert_array_equal(o.joint_impulses(1)[0], 0.0)
     np.testing.assert_array_equal(o.bodies()["angular_velocity"][1], 0.0)
+
+
+@pytest.mark.parametrize("velocity_sign", [-1, 1])
+@pytest.mark.parametrize("pose_sign", [-1, 1])
+@pytest.mark.parametrize("hinge", [False, True])
+def test_full_ranges_let_a_half_turn_pass(hinge, pose_sign, velocity_sign):
+    # AngularCoordinateTests.FullHingeAndTwistRangesAllowCrossingHalfTurns (:346-375)
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    if hinge:
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, (0, 0, 1, -np.pi, np.pi))
+        o.joint_limit_params(j, 0.0, 0.001)
+    else:
+        j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, -np.pi, np.pi))
+    _set(o, 1, q=(0, 0, pose_sign, 0), w=(0, 0, velocity_sign))
+    o.joint_solve(j, DT, 0.0, 0.001)
+    assert o.joint_data(j)[3] == 0
+    np.testing.assert_array_equal(o.bodies()["angular_velocity"][1], (0, 0, velocity_sign))
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("hinge", [False, True])
+def test_partial_ranges_keep_the_half_turn_bound_active(hinge, sign):
+    # AngularCoordinateTests.PartialHingeAndTwistRangesKeepTheHalfTurnBoundaryActive (:377-407)
+    lo, hi = (0.0, np.pi) if sign == 1 else (-np.pi, 0.0)
+    o = O.OracleWorld(_world((0, 0, 0, 1), (0, 0, 0, 1), True))
+    if hinge:
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, (0, 0, 1, lo, hi))
+        o.joint_limit_params(j, 0.0, 0.0)
+    else:
+        j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, (0, 0, 1, 0, 0, 1, lo, hi))
+    _set(o, 1, q=(0, 0, sign, 0), w=(0, 0, sign))
+    o.joint_solve(j, DT, 0.0, 0.0)
+    assert o.joint_data(j)[3] == (1 if sign == 1 else 2)
+    assert np.abs(o.bodies()["angular_velocity"][1]).max() < 1e-5
+
+
+@pytest.mark.parametrize("nonidentity", [False, True])
+@pytest.mark.parametrize("qsign", [-1, 1])
+@pytest.mark.parametrize("target_sign", [-1, 1])
+@pytest.mark.parametrize("hinge", [False, True])
+def test_fixed_half_turn_targets_see_no_bias_from_the_quaternion_sign(hinge, target_sign, qsign, nonidentity):
+    # AngularCoordinateTests.FixedHalfTurnTargetsDoNotBiasEquivalentQuaternionRepresentations (:409-442)
+    q1, q2 = (Q1, Q2) if nonidentity else (np.array([0, 0, 0, 1.0]), np.array([0, 0, 0, 1.0]))
+    axis = AXIS if nonidentity else np.array([0.0, 0.0, 1.0])
+    o = O.OracleWorld(_world(q1, q2, False))
+    o.set_orientation_d(0, q1)
+    o.set_orientation_d(1, q2)
+    lim = target_sign * np.pi
+    if hinge:
+        j = o.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, tuple(axis) + (lim, lim))
+    else:
+        j = o.add_joint(abi.CONSTRAINT_TWISTANGLE, 0, 1, tuple(axis) + tuple(axis) + (lim, lim))
+    local = o.joint_matrix(j)[2]
+    o.set_orientation_d(1, _quat_mul(q2, np.array([*(local * qsign), 0.0])))
+    if hinge:
+        o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+        bias = o.joint_bias(j)[2]
+    else:
+        o.joint_solve(j, DT, 0.2, 0.001, iterate=False)
+        bias = o.joint_bias(j)[0]
+    assert abs(bias) < 1e-4
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fixed_target_wrapping_handles_large_finite_values(sign):
+    # AngularCoordinateTests.FixedAngularTargetWrappingHandlesLargeFiniteValues (:444-453)
+    lib = O.load()
+    big = float(np.finfo(np.float32).max) * sign
+    w = lib.jor_shortest_angle_f(big, float(np.float32(np.pi)))
+    assert np.isfinite(w) and -np.pi - 1e-6 <= w <= np.pi + 1e-6
