@@ -78,6 +78,9 @@ template <class R> void set_bodies(World<R>& w, const jg_body_desc* d, int n) {
         b.flags = (s.flags & 0x3f0) | (s.flags & JG_BODY_ACTIVE) | (s.flags & JG_BODY_GYROSCOPIC);
         b.gravity = (s.flags & JG_BODY_NO_GRAVITY) == 0;
         b.speculative = (s.flags & JG_BODY_SPECULATIVE) != 0;
+        // a body made static is deactivated at the next step (DeactivateBodyNextStep,
+        // World.cs:797-800, from the MotionType setter, RigidBody.cs:959-968)
+        if (b.motion == STATIC) b.sleep_time = std::numeric_limits<R>::infinity();
         b.world = s.world;
         // DeltaVelocity/DeltaAngularVelocity: the velocity change queued by the last
         // RigidBody.Update (zero for a body that has not been stepped yet).
@@ -304,6 +307,10 @@ template <class R> struct Handle {
         w.register_contact(s1, s2, r);                                                                             \
     }                                                                                                              \
     extern "C" void jor_world_narrowphase_##SUF(void* h) { ((Handle<R>*)h)->w.narrowphase(); }                    \
+    extern "C" void jor_world_body_deactivation_time_##SUF(void* h, int i, double seconds) {                      \
+        ((Handle<R>*)h)->w.bodies[i].deactivation_time = (R)seconds;                                               \
+    }                                                                                                              \
+    extern "C" void jor_world_activate_body_##SUF(void* h, int i) { ((Handle<R>*)h)->w.activate_body(i); }        \
     /* World.AllowDeactivation (World.cs:333) for the oracle's island restatement */                           \
     extern "C" void jor_world_set_deactivation_##SUF(void* h, int on) { ((Handle<R>*)h)->w.allow_deactivation = on != 0; } \
     /* world bounding box of shape s as the step of length dt sees it (out = min, max) */                        \

@@ -51,6 +51,7 @@ template <class R> struct Body {
     // flags kept per body (an island's flag is the OR over its bodies): MarkedAsActive and
     // membership of the active island partition
     R sleep_time = 0;
+    R deactivation_time = (R)1.0;   // RigidBody.DeactivationTime (RigidBody.cs:400, :476-483)
     bool marked = true, island_active = true;
     bool active() const { return (flags & 4) != 0; }
     bool gyroscopic() const { return (flags & 8) != 0; }

@@ -37,7 +37,7 @@ template <class R> struct World {
     // World.AllowDeactivation (World.cs:333; the reference's default is on) with the bodies'
     // default thresholds (RigidBody.cs:398-400)
     bool allow_deactivation = false;
-    R sleep_lin2 = (R)0.1, sleep_ang2 = (R)0.1, sleep_after = (R)1.0;
+    R sleep_lin2 = (R)0.1, sleep_ang2 = (R)0.1;
     std::vector<int> created;                  // arbiters created by this step's detection
     bool external_order = false;               // use ContactData::color / Joint::color
     bool record_residual = false;
@@ -365,7 +365,15 @@ template <class R> struct World {
         bool resting = kin ? (b.angvel == zero && b.vel == zero)
                            : (len2(b.angvel) < sleep_ang2 && len2(b.vel) < sleep_lin2);
         b.sleep_time = resting ? b.sleep_time + ts.dt : (R)0;
-        if ((kin && !resting) || b.sleep_time < sleep_after) b.marked = true;
+        if ((kin && !resting) || b.sleep_time < b.deactivation_time) b.marked = true;
+    }
+    // World.ActivateBodyNextStep (World.cs:696-720) for a dynamic or kinematic body:
+    // SetActivationState(true) and the setters that wake a body
+    void activate_body(int i) {
+        Body<R>& b = bodies[i];
+        b.sleep_time = 0;
+        if (b.active() || b.motion == STATIC) return;
+        add_to_active(i);
     }
 
     // Solve order: indices into arbiters and joints, grouped by colour.

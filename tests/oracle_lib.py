@@ -41,6 +41,7 @@ def load():
             "jor_world_register_contact": (None, [P, I, I, P, P, P]), "jor_world_narrowphase": (None, [P]),
             "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]),
             "jor_world_register_manifold": (None, [P, I, I, P, P, I, P]), "jor_world_set_deactivation": (None, [P, I]),
+            "jor_world_body_deactivation_time": (None, [P, I, D]), "jor_world_activate_body": (None, [P, I]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
@@ -275,6 +276,14 @@ class OracleWorld:
         out = np.zeros(12, np.float64)
         self.fn("jor_world_joint_data")(self.h, j, p(out))
         return out[9:12]
+
+    def deactivation_time(self, body, seconds):
+        """RigidBody.DeactivationTime of one body."""
+        self.fn("jor_world_body_deactivation_time")(self.h, body, float(seconds))
+
+    def activate(self, body):
+        """RigidBody.SetActivationState(true): the body wakes at the next step."""
+        self.fn("jor_world_activate_body")(self.h, body)
 
     def shape_box(self, s, dt):
         """World bounding box (min, max) of shape s for a step of length dt."""
