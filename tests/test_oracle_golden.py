@@ -499,3 +499,94 @@ def test_cached_contact_offsets_are_current_after_each_step():
         c = w.contacts()
         assert len(c) == 1
         assert np.abs(c[0]["rel_pos2"] - R @ point).max() < 1e-5
+
+
+# ---- locked motion axes (Behavior/AllowedMotionTests.cs) -------------------------------------
+LIN_X, LIN_Y, LIN_Z, ANG = 1, 2, 4, 56
+
+
+def _locked_body_scene(allowed, **fields):
+    """AllowedMotionTests' world and body: no gravity, one substep, no damping, inverse
+    mass 0.5 and zero inverse inertia, plus a static body 0 at the origin."""
+    bodies = scenes._body(2)
+    bodies["motion_type"][0] = abi.MOTION_STATIC
+    bodies["inv_mass"][0] = 0.0
+    bodies["inv_inertia"][0] = 0.0
+    bodies["inv_mass"][1] = 0.5
+    bodies["inv_inertia"][1] = 0.0
+    bodies["linear_damping"] = bodies["angular_damping"] = 1.0
+    bodies["flags"][1] = abi.BODY_ACTIVE | ((63 ^ allowed) << abi.BODY_LOCKS_SHIFT)
+    bodies["friction"] = 0.0
+    for k, v in fields.items():
+        bodies[k][1] = v
+    shapes = np.zeros(2, abi.SHAPE_DTYPE)
+    shapes["kind"] = abi.SHAPE_SPHERE
+    shapes["dims"][:, 0] = 0.5
+    shapes["body"] = [0, 1]
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=[],
+                params=dict(substeps=1, solver_iterations=1, relax_iterations=0, gravity=(0.0, 0.0, 0.0)))
+
+
+def test_forces_and_gravity_respect_locked_axes_across_substeps():
+    # AllowedMotionTests.ForcesAndGravity_RespectWorldAxesAcrossSubsteps (:143-167): the force
+    # and gravity become velocity deltas at the end of a step and act in the next one
+    sc = _locked_body_scene(63 ^ LIN_Y, position=(1, 2, 3), orientation=(0, 0, np.sin(0.6), np.cos(0.6)),
+                            force=(2, 4, 6))
+    sc["bodies"]["flags"][1] &= ~abi.BODY_NO_GRAVITY
+    sc["params"].update(substeps=4, gravity=(3.0, 4.0, 5.0))
+    w = O.OracleWorld(sc)
+    dt = 1.0 / 60.0
+    w.step(dt)
+    w.step(dt)
+    b = w.bodies()
+    assert b["velocity"][1][0] == pytest.approx(4 * dt, abs=1e-5)
+    assert b["velocity"][1][1] == 0.0
+    assert b["velocity"][1][2] == pytest.approx(8 * dt, abs=1e-5)
+    assert b["position"][1][1] == 2.0
+
+
+def test_oblique_contact_uses_the_directional_mass():
+    # AllowedMotionTests.ObliqueContact_UsesDirectionalMassInOneIteration (:215-240)
+    sc = _locked_body_scene(LIN_Y | ANG, velocity=(0, -3, 0))
+    w = O.OracleWorld(sc)
+    n = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0)
+    w.register_contact(0, 1, [0, 0, 0], [0, 0, 0], n)
+    w.fn("jor_world_prepare")(w.h, 0.01, 1)
+    w.fn("jor_world_iterate")(w.h, 0)
+    assert np.abs(w.bodies()["velocity"][1]).max() < 1e-5
+    c = w.contacts()[0]
+    assert c["mass"][0] == pytest.approx(4.0, abs=1e-5)
+    assert c["mass"][2] == 0.0
+
+
+def test_completely_blocked_contact_stays_finite():
+    # AllowedMotionTests.CompletelyBlockedContact_RemainsFinite (:242-268)
+    sc = _locked_body_scene(0)
+    w = O.OracleWorld(sc)
+    w.register_contact(0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0])
+    w.fn("jor_world_set_penalty")(w.h, 0, 0, 1.0)
+    w.fn("jor_world_prepare")(w.h, 0.01, 1)
+    for _ in range(3):
+        w.fn("jor_world_iterate")(w.h, 1)
+    b = w.bodies()
+    np.testing.assert_array_equal(b["velocity"][1], 0.0)
+    np.testing.assert_array_equal(b["angular_velocity"][1], 0.0)
+    c = w.contacts()[0]
+    assert c["accumulated"][0] == 0.0 and c["accumulated"][1] == 0.0
+
+
+def test_a_force_changes_velocity_two_steps_later():
+    # ForceImpulseTests.AddForce_ChangesVelocityAfterStep (Behavior/ForceImpulseTests.cs:126-143)
+    sc = _locked_body_scene(63)
+    sc["bodies"]["inv_mass"][1] = 1.0
+    sc["bodies"]["position"][0] = (0, -100, 0)     # the body alone, as in the reference's world
+    w = O.OracleWorld(sc)
+    w.step(1.0 / 60.0)
+    b = w.bodies()
+    b["force"][1] = (100, 0, 0)
+    w.set_bodies(b)
+    w.step(1.0 / 60.0)
+    assert w.bodies()["velocity"][1][0] == 0.0
+    w.step(1.0 / 60.0)
+    assert w.bodies()["velocity"][1][0] > 0.0
