@@ -329,6 +329,8 @@ template <class R> struct Handle {
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         for (auto& a : w.arbiters) contactdata_iterate(a, w.bodies, bias != 0);                                    \
     }                                                                                                              \
+    /* ContactData.Mode of arbiter a (Contact.cs:37-60): which body velocities the rows update */           \
+    extern "C" void jor_world_set_arbiter_mode_##SUF(void* h, int a, int mode) { ((Handle<R>*)h)->w.arbiters[a].mode = mode; } \
     extern "C" void jor_world_set_penalty_##SUF(void* h, int arb, int slot, double value) {                       \
         ((Handle<R>*)h)->w.arbiters[arb].c[slot].penalty_bias = (R)value;                                         \
     }                                                                                                              \

@@ -47,7 +47,7 @@ def load():
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
             "jor_world_joint_limit_params": (None, [P, I, D, D]), "jor_world_joint_matrix": (None, [P, I, P]), "jor_world_set_orientation_d": (None, [P, I, P]),
             "jor_world_prepare": (None, [P, F, I]), "jor_world_iterate": (None, [P, I]),
-            "jor_world_set_penalty": (None, [P, I, I, D]),
+            "jor_world_set_penalty": (None, [P, I, I, D]), "jor_world_set_arbiter_mode": (None, [P, I, I]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
             "jor_world_step": (None, [P, F, I]), "jor_world_step_mt": (D, [P, F, I]),
             "jor_world_counters": (None, [P, P]), "jor_world_pairs": (I, [P, P, I]),

@@ -590,3 +590,57 @@ def test_a_force_changes_velocity_two_steps_later():
     assert w.bodies()["velocity"][1][0] == 0.0
     w.step(1.0 / 60.0)
     assert w.bodies()["velocity"][1][0] > 0.0
+
+
+@pytest.mark.parametrize("kind", ["DistanceLimit", "BallSocket"])
+def test_joint_stops_the_permitted_velocity_in_one_iteration(kind):
+    # AllowedMotionTests.Joint_StopsPermittedVelocityInOneIteration (:316-372), the kinds the
+    # device has: one step, one iteration, a body free to move along y only
+    axis = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+    pos = axis if kind == "DistanceLimit" else np.zeros(3)
+    sc = _locked_body_scene(LIN_Y | ANG, velocity=(0, -3, 0), position=pos)
+    sc["shapes"] = sc["shapes"][1:]   # the static body has no shape: nothing collides
+    w = O.OracleWorld(sc)
+    if kind == "DistanceLimit":
+        j = w.add_joint(abi.CONSTRAINT_DISTANCELIMIT, 0, 1, (0, 0, 0) + tuple(pos) + (1e-6, -1e-6))
+    else:
+        j = w.add_joint(abi.CONSTRAINT_BALLSOCKET, 0, 1, (0, 0, 0))
+    w.joint_params(j, 0.0, 0.0)
+    w.step(0.01)
+    v = w.bodies()["velocity"][1]
+    assert v[0] == 0.0 and v[2] == 0.0 and abs(v[1]) < 1e-5
+
+
+@pytest.mark.parametrize("linear_locks", [False, True])
+def test_solve_mode_flags_mask_each_body_update(linear_locks):
+    # AllowedMotionTests.AllSolveModes... (:262-314): every ContactData.Mode combination updates
+    # exactly the bodies and parts it names
+    n = np.array([1.0, 1.0, 0.0]) / np.sqrt(2.0) if linear_locks else np.array([1.0, 0.0, 0.0])
+    for bits in range(16):
+        bodies = scenes._body(2)
+        bodies["inv_mass"] = (0.5, 0.25)
+        bodies["inv_inertia"] = 0.0
+        bodies["linear_damping"] = bodies["angular_damping"] = 1.0
+        bodies["friction"] = bodies["restitution"] = 0.0
+        if linear_locks:
+            bodies["flags"] = abi.BODY_ACTIVE | (LIN_Y << abi.BODY_LOCKS_SHIFT)
+        bodies["velocity"][0] = (1, 0, 0)
+        shapes = np.zeros(2, abi.SHAPE_DTYPE)
+        shapes["kind"] = abi.SHAPE_SPHERE
+        shapes["dims"][:, 0] = 0.5
+        shapes["body"] = [0, 1]
+        sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32), triangles=np.zeros(0, abi.TRIANGLE_DTYPE))
+        w = O.OracleWorld(sc)
+        w.register_contact(0, 1, [0, 0, 0], [0, 0, 0], n)
+        w.fn("jor_world_set_arbiter_mode")(w.h, 0, bits)
+        w.fn("jor_world_prepare")(w.h, 0.01, 1)
+        w.fn("jor_world_iterate")(w.h, 0)
+        b = w.bodies()
+        lin1, lin2 = bool(bits & 1), bool(bits & 4)
+        inv = (0.5 if lin1 else 0.0) + (0.25 if lin2 else 0.0)
+        imp = 1.0 / inv if inv > 0 else 0.0
+        e1 = np.array([1.0 - (0.5 * imp if lin1 else 0.0), 0, 0])
+        e2 = np.array([0.25 * imp if lin2 else 0.0, 0, 0])
+        assert np.abs(b["velocity"][0] - e1).max() < 1e-5, bits
+        assert np.abs(b["velocity"][1] - e2).max() < 1e-5, bits
+        np.testing.assert_array_equal(b["angular_velocity"][:2], 0.0)
