@@ -197,7 +197,8 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
     return mmul(mscale(-(R)0.5, der), Mat<R>::from_m3(mat_from_quat(left)));
 }
 
-enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6 };
+enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
+                 POINTONPLANE = 7 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -703,6 +704,53 @@ template <class R> void fixed_iterate(Joint<R>& j, std::vector<Body<R>>& bodies,
     if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, imp);
 }
 
+// PointOnPlane.Initialize (PointOnPlane.cs:96-126): the plane's normal fixed in body 1, an
+// anchor on each body, the signed distance limited to [min, max] (min >= max fixes it)
+template <class R> void plane_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> axis, V3<R> a1, V3<R> a2, R lo, R hi) {
+    j.kind = POINTONPLANE;
+    axis = normalize(axis);
+    j.la1 = rotate_inv(a1 - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(a2 - b[j.b2].pos, b[j.b2].q);
+    j.axis = rotate_inv(axis, b[j.b1].q);
+    j.bias_factor = (R)0.2;
+    j.softness = (R)0.00001;
+    j.min_angle = lo; j.max_angle = hi;
+}
+// PointOnPlane.PrepareForIterationPointOnPlane (PointOnPlane.cs:128-200): one row along the
+// plane normal, the arm of body 1 measured to the second anchor
+template <class R> void plane_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> axis = rotate(j.axis, b1.q);
+    V3<R> r1 = rotate(j.la1, b1.q), r2 = rotate(j.la2, b2.q);
+    V3<R> u = (b2.pos + r2) - (b1.pos + r1);
+    j.clamp = 0;
+    j.jr[0] = -axis;
+    j.jr[1] = -cross(r1 + u, axis);
+    j.jr[2] = axis;
+    j.jr[3] = cross(r2, axis);
+    R err = dot(u, axis);
+    j.eff1 = 1;
+    if (j.min_angle >= j.max_angle) { err -= (R)0.5 * j.min_angle + (R)0.5 * j.max_angle; j.clamp = 3; }
+    else if (err >= j.max_angle) { err -= j.max_angle; j.clamp = 1; }
+    else if (err <= j.min_angle) { err -= j.min_angle; j.clamp = 2; }
+    else { j.acc.x = 0; return; }
+    R m = dot(cmul(j.jr[0], b1.inv_mass_vec), j.jr[0]) + dot(cmul(j.jr[2], b2.inv_mass_vec), j.jr[2]) +
+          dot(sym_mul(b1.inv_inertia_world, j.jr[1]), j.jr[1]) + dot(sym_mul(b2.inv_inertia_world, j.jr[3]), j.jr[3]);
+    j.eff1 = row_mass(m, j.softness, ts);
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = err * j.bias_factor * ts.inv_dt;
+    R a = j.acc.x;
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel + cmul(j.jr[0] * a, b1.inv_mass_vec);
+        b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, j.jr[1] * a);
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(j.jr[2] * a, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j.jr[3] * a);
+    }
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
@@ -710,6 +758,7 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case DISTANCELIMIT: distance_prepare(j, b, ts); break;
         case CONELIMIT: cone_prepare(j, b, ts); break;
         case FIXEDANGLE: fixed_prepare(j, b, ts); break;
+        case POINTONPLANE: plane_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -720,6 +769,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case DISTANCELIMIT: distance_iterate(j, b, ts); break;
         case CONELIMIT: cone_iterate(j, b, ts); break;
         case FIXEDANGLE: fixed_iterate(j, b, ts); break;
+        case POINTONPLANE: distance_iterate(j, b, ts); break;   // PointOnPlane.cs:218-256: the same one-row update
         default: twist_iterate(j, b, ts); break;
     }
 }

@@ -592,10 +592,13 @@ def test_a_force_changes_velocity_two_steps_later():
     assert w.bodies()["velocity"][1][0] > 0.0
 
 
-@pytest.mark.parametrize("kind", ["DistanceLimit", "BallSocket"])
+POINTONPLANE = 7    # restated in the oracle ahead of its device row
+
+
+@pytest.mark.parametrize("kind", ["DistanceLimit", "BallSocket", "PointOnPlane"])
 def test_joint_stops_the_permitted_velocity_in_one_iteration(kind):
     # AllowedMotionTests.Joint_StopsPermittedVelocityInOneIteration (:316-372), the kinds the
-    # device has: one step, one iteration, a body free to move along y only
+    # oracle has: one step, one iteration, a body free to move along y only
     axis = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
     pos = axis if kind == "DistanceLimit" else np.zeros(3)
     sc = _locked_body_scene(LIN_Y | ANG, velocity=(0, -3, 0), position=pos)
@@ -603,6 +606,8 @@ def test_joint_stops_the_permitted_velocity_in_one_iteration(kind):
     w = O.OracleWorld(sc)
     if kind == "DistanceLimit":
         j = w.add_joint(abi.CONSTRAINT_DISTANCELIMIT, 0, 1, (0, 0, 0) + tuple(pos) + (1e-6, -1e-6))
+    elif kind == "PointOnPlane":
+        j = w.add_joint(POINTONPLANE, 0, 1, tuple(axis) + (0, 0, 0, 0, 0, 0, 1e-6, -1e-6))
     else:
         j = w.add_joint(abi.CONSTRAINT_BALLSOCKET, 0, 1, (0, 0, 0))
     w.joint_params(j, 0.0, 0.0)
@@ -644,3 +649,26 @@ def test_solve_mode_flags_mask_each_body_update(linear_locks):
         assert np.abs(b["velocity"][0] - e1).max() < 1e-5, bits
         assert np.abs(b["velocity"][1] - e2).max() < 1e-5, bits
         np.testing.assert_array_equal(b["angular_velocity"][:2], 0.0)
+
+
+def test_point_on_plane_pulls_a_body_onto_its_plane():
+    # AdditionalConstraintBehaviorTests.PointOnPlane_ReducesDistanceToPlane (:86-113): a unit
+    # sphere 3 above the plane y = 0 of a static body, no gravity, 4 substeps, 2 seconds
+    bodies = scenes._body(2)
+    shapes = np.zeros(2, abi.SHAPE_DTYPE)
+    shapes["kind"] = abi.SHAPE_SPHERE
+    shapes["dims"][:, 0] = 1.0
+    shapes["body"] = [0, 1]
+    scenes.set_mass(bodies, shapes, None, 1, 1)
+    bodies["motion_type"][0] = abi.MOTION_STATIC
+    bodies["inv_mass"][0] = 0.0
+    bodies["inv_inertia"][0] = 0.0
+    bodies["position"][1] = (1, 3, 2)
+    sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32), triangles=np.zeros(0, abi.TRIANGLE_DTYPE),
+              params=dict(substeps=4, gravity=(0.0, 0.0, 0.0)))
+    w = O.OracleWorld(sc)
+    w.add_joint(POINTONPLANE, 0, 1, (0, 1, 0, 0, 0, 0, 1, 3, 2, 1e-6, -1e-6))
+    for _ in range(200):
+        w.step(0.01)
+    y = abs(float(w.bodies()["position"][1][1]))
+    assert y < 3.0 and y < 0.2
