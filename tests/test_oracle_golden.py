@@ -672,3 +672,32 @@ def test_point_on_plane_pulls_a_body_onto_its_plane():
         w.step(0.01)
     y = abs(float(w.bodies()["position"][1][1]))
     assert y < 3.0 and y < 0.2
+
+
+def test_hinge_limit_reduces_rotation():
+    # AdditionalConstraintBehaviorTests.HingeAngle_LimitReducesRotationComparedToUnconstrained
+    # (:115-155): a unit sphere spun at 8 rad/s about y for 10 steps, with and without a
+    # hinge about y limited to +-10 degrees
+    def run(constrained):
+        bodies = scenes._body(2)
+        shapes = np.zeros(1, abi.SHAPE_DTYPE)
+        shapes["kind"] = abi.SHAPE_SPHERE
+        shapes["dims"][0, 0] = 1.0
+        shapes["body"] = 1
+        scenes.set_mass(bodies, shapes, None, 1, 0)
+        bodies["motion_type"][0] = abi.MOTION_STATIC
+        bodies["inv_mass"][0] = 0.0
+        bodies["inv_inertia"][0] = 0.0
+        bodies["position"][0] = (0, -50, 0)
+        bodies["angular_velocity"][1] = (0, 8, 0)
+        sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                  triangles=np.zeros(0, abi.TRIANGLE_DTYPE), params=dict(substeps=4, gravity=(0.0, 0.0, 0.0)))
+        w = O.OracleWorld(sc)
+        if constrained:
+            w.add_joint(abi.CONSTRAINT_HINGEANGLE, 0, 1, (0, 1, 0, -np.radians(10), np.radians(10)))
+        for _ in range(10):
+            w.step(0.01)
+        return 2.0 * np.arccos(np.clip(abs(float(w.bodies()["orientation"][1][3])), 0.0, 1.0))
+
+    free, held = run(False), run(True)
+    assert free > 0.4 and held < free and held < 0.4
