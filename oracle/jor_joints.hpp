@@ -198,7 +198,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
 }
 
 enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
-                 POINTONPLANE = 7 };
+                 POINTONPLANE = 7, ANGULARMOTOR = 8 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -751,6 +751,42 @@ template <class R> void plane_prepare(Joint<R>& j, std::vector<Body<R>>& bodies,
     }
 }
 
+// AngularMotor.Initialize (AngularMotor.cs:62-82) with TargetVelocity and MaximumTorque:
+// a velocity drive about an axis of each body (the target in target, the torque limit in
+// max_angle, the impulse limit of a substep in min_angle once prepared)
+template <class R> void motor_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R velocity, R torque) {
+    j.kind = ANGULARMOTOR;
+    j.la1 = rotate_inv(normalize(ax1), b[j.b1].q);
+    j.la2 = rotate_inv(normalize(ax2), b[j.b2].q);
+    j.target = velocity;
+    j.max_angle = torque;
+}
+// AngularMotor.PrepareForIterationAngularMotor (AngularMotor.cs:128-152)
+template <class R> void motor_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> j1 = rotate(j.la1, b1.q), j2 = rotate(j.la2, b2.q);
+    R m = dot(sym_mul(b1.inv_inertia_world, j1), j1) + dot(sym_mul(b2.inv_inertia_world, j2), j2);
+    j.eff1 = m > 0 ? (R)1.0 / m : (R)0;
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.min_angle = ts.sub_dt * j.max_angle;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, j1 * j.acc.x);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j2 * j.acc.x);
+}
+// AngularMotor.IterateAngularMotor (AngularMotor.cs:154-180)
+template <class R> void motor_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>&) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> j1 = rotate(j.la1, b1.q), j2 = rotate(j.la2, b2.q);
+    R jv = dot(-j1, b1.angvel) + dot(j2, b2.angvel);
+    R lambda = -(jv - j.target) * j.eff1;
+    R old = j.acc.x;
+    j.acc.x = std::min(std::max(j.acc.x + lambda, -j.min_angle), j.min_angle);
+    lambda = j.acc.x - old;
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, j1 * lambda);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j2 * lambda);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
@@ -759,6 +795,7 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case CONELIMIT: cone_prepare(j, b, ts); break;
         case FIXEDANGLE: fixed_prepare(j, b, ts); break;
         case POINTONPLANE: plane_prepare(j, b, ts); break;
+        case ANGULARMOTOR: motor_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -770,6 +807,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case CONELIMIT: cone_iterate(j, b, ts); break;
         case FIXEDANGLE: fixed_iterate(j, b, ts); break;
         case POINTONPLANE: distance_iterate(j, b, ts); break;   // PointOnPlane.cs:218-256: the same one-row update
+        case ANGULARMOTOR: motor_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }

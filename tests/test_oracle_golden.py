@@ -701,3 +701,28 @@ def test_hinge_limit_reduces_rotation():
 
     free, held = run(False), run(True)
     assert free > 0.4 and held < free and held < 0.4
+
+
+ANGULARMOTOR = 8    # restated in the oracle ahead of its device row
+
+
+def test_angular_motor_drives_toward_its_target():
+    # AdditionalConstraintBehaviorTests.AngularMotor_DrivesAngularVelocityTowardTarget (:30-52):
+    # target 3 rad/s about y, at most 100 N m, one second, 4 substeps, no gravity
+    bodies = scenes._body(2)
+    shapes = np.zeros(1, abi.SHAPE_DTYPE)
+    shapes["kind"] = abi.SHAPE_SPHERE
+    shapes["dims"][0, 0] = 1.0
+    shapes["body"] = 1
+    scenes.set_mass(bodies, shapes, None, 1, 0)
+    bodies["motion_type"][0] = abi.MOTION_STATIC
+    bodies["inv_mass"][0] = 0.0
+    bodies["inv_inertia"][0] = 0.0
+    bodies["position"][0] = (0, -50, 0)
+    sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+              triangles=np.zeros(0, abi.TRIANGLE_DTYPE), params=dict(substeps=4, gravity=(0.0, 0.0, 0.0)))
+    w = O.OracleWorld(sc)
+    w.add_joint(ANGULARMOTOR, 0, 1, (0, 1, 0, 0, 1, 0, 3.0, 100.0))
+    for _ in range(100):
+        w.step(0.01)
+    assert w.bodies()["angular_velocity"][1][1] == pytest.approx(3.0, abs=0.3)
