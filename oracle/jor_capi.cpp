@@ -13,6 +13,7 @@ using namespace jor;
 #define JOR_CONSTRAINT_FIXEDANGLE 6
 #define JOR_CONSTRAINT_POINTONPLANE 7
 #define JOR_CONSTRAINT_ANGULARMOTOR 8
+#define JOR_CONSTRAINT_LINEARMOTOR 9
 
 namespace {
 
@@ -217,8 +218,9 @@ template <class R> struct Handle {
         else if (kind == JG_CONSTRAINT_TWISTANGLE)                                                                 \
             twist_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                    \
         else if (kind == JOR_CONSTRAINT_FIXEDANGLE) fixed_init(j, w.bodies);                                       \
-        else if (kind == JOR_CONSTRAINT_ANGULARMOTOR)                                                              \
-            motor_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);                    \
+        else if (kind == JOR_CONSTRAINT_ANGULARMOTOR || kind == JOR_CONSTRAINT_LINEARMOTOR)                        \
+            motor_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7],                     \
+                       kind == JOR_CONSTRAINT_LINEARMOTOR);                                                        \
         else if (kind == JOR_CONSTRAINT_POINTONPLANE)                                                              \
             plane_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9], (R)init[10]); \
         w.joints.push_back(j);                                                                                     \

@@ -198,7 +198,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
 }
 
 enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
-                 POINTONPLANE = 7, ANGULARMOTOR = 8 };
+                 POINTONPLANE = 7, ANGULARMOTOR = 8, LINEARMOTOR = 9 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -751,40 +751,54 @@ template <class R> void plane_prepare(Joint<R>& j, std::vector<Body<R>>& bodies,
     }
 }
 
-// AngularMotor.Initialize (AngularMotor.cs:62-82) with TargetVelocity and MaximumTorque:
-// a velocity drive about an axis of each body (the target in target, the torque limit in
-// max_angle, the impulse limit of a substep in min_angle once prepared)
-template <class R> void motor_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R velocity, R torque) {
-    j.kind = ANGULARMOTOR;
+// AngularMotor.Initialize (AngularMotor.cs:62-82) and LinearMotor.Initialize
+// (LinearMotor.cs:97-115) with TargetVelocity and MaximumTorque / MaximumForce: a velocity
+// drive about (along) an axis of each body (the target in target, the torque or force limit
+// in max_angle, the impulse limit of a substep in min_angle once prepared)
+template <class R> void motor_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R velocity, R torque,
+                                   bool linear = false) {
+    j.kind = linear ? LINEARMOTOR : ANGULARMOTOR;
     j.la1 = rotate_inv(normalize(ax1), b[j.b1].q);
     j.la2 = rotate_inv(normalize(ax2), b[j.b2].q);
     j.target = velocity;
     j.max_angle = torque;
 }
-// AngularMotor.PrepareForIterationAngularMotor (AngularMotor.cs:128-152)
+// the response of a body along / about an axis, and the velocity change of an impulse
+template <class R> R motor_response(const Body<R>& b, V3<R> a, bool linear) {
+    return linear ? dot(cmul(a, b.inv_mass_vec), a) : dot(sym_mul(b.inv_inertia_world, a), a);
+}
+template <class R> void motor_push(Body<R>& b, V3<R> imp, bool linear) {
+    if (linear) b.vel = b.vel + cmul(imp, b.inv_mass_vec);
+    else b.angvel = b.angvel + sym_mul(b.inv_inertia_world, imp);
+}
+// AngularMotor.PrepareForIterationAngularMotor (AngularMotor.cs:128-152),
+// LinearMotor.PrepareForIterationLinearMotor (LinearMotor.cs:152-176)
 template <class R> void motor_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    const bool lin = j.kind == LINEARMOTOR;
     Body<R>& b1 = bodies[j.b1];
     Body<R>& b2 = bodies[j.b2];
     V3<R> j1 = rotate(j.la1, b1.q), j2 = rotate(j.la2, b2.q);
-    R m = dot(sym_mul(b1.inv_inertia_world, j1), j1) + dot(sym_mul(b2.inv_inertia_world, j2), j2);
+    R m = motor_response(b1, j1, lin) + motor_response(b2, j2, lin);
     j.eff1 = m > 0 ? (R)1.0 / m : (R)0;
     if (j.eff1 == 0) j.acc.x = 0;
     j.min_angle = ts.sub_dt * j.max_angle;
-    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, j1 * j.acc.x);
-    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j2 * j.acc.x);
+    if (b1.motion == DYNAMIC) motor_push(b1, -(j1 * j.acc.x), lin);
+    if (b2.motion == DYNAMIC) motor_push(b2, j2 * j.acc.x, lin);
 }
-// AngularMotor.IterateAngularMotor (AngularMotor.cs:154-180)
+// AngularMotor.IterateAngularMotor (AngularMotor.cs:154-180),
+// LinearMotor.IterateLinearMotor (LinearMotor.cs:203-231)
 template <class R> void motor_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>&) {
+    const bool lin = j.kind == LINEARMOTOR;
     Body<R>& b1 = bodies[j.b1];
     Body<R>& b2 = bodies[j.b2];
     V3<R> j1 = rotate(j.la1, b1.q), j2 = rotate(j.la2, b2.q);
-    R jv = dot(-j1, b1.angvel) + dot(j2, b2.angvel);
+    R jv = lin ? dot(-j1, b1.vel) + dot(j2, b2.vel) : dot(-j1, b1.angvel) + dot(j2, b2.angvel);
     R lambda = -(jv - j.target) * j.eff1;
     R old = j.acc.x;
     j.acc.x = std::min(std::max(j.acc.x + lambda, -j.min_angle), j.min_angle);
     lambda = j.acc.x - old;
-    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, j1 * lambda);
-    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j2 * lambda);
+    if (b1.motion == DYNAMIC) motor_push(b1, -(j1 * lambda), lin);
+    if (b2.motion == DYNAMIC) motor_push(b2, j2 * lambda, lin);
 }
 
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
@@ -795,7 +809,7 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case CONELIMIT: cone_prepare(j, b, ts); break;
         case FIXEDANGLE: fixed_prepare(j, b, ts); break;
         case POINTONPLANE: plane_prepare(j, b, ts); break;
-        case ANGULARMOTOR: motor_prepare(j, b, ts); break;
+        case ANGULARMOTOR: case LINEARMOTOR: motor_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -807,7 +821,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case CONELIMIT: cone_iterate(j, b, ts); break;
         case FIXEDANGLE: fixed_iterate(j, b, ts); break;
         case POINTONPLANE: distance_iterate(j, b, ts); break;   // PointOnPlane.cs:218-256: the same one-row update
-        case ANGULARMOTOR: motor_iterate(j, b, ts); break;
+        case ANGULARMOTOR: case LINEARMOTOR: motor_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }

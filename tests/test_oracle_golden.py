@@ -726,3 +726,28 @@ def test_angular_motor_drives_toward_its_target():
     for _ in range(100):
         w.step(0.01)
     assert w.bodies()["angular_velocity"][1][1] == pytest.approx(3.0, abs=0.3)
+
+
+LINEARMOTOR = 9     # restated in the oracle ahead of its device row
+
+
+def test_linear_motor_drives_toward_its_target():
+    # AdditionalConstraintBehaviorTests.LinearMotor_DrivesBodyTowardTargetVelocity (:7-28):
+    # target 2 m/s along x, at most 100 N, one second, 4 substeps, no gravity
+    bodies = scenes._body(2)
+    shapes = np.zeros(1, abi.SHAPE_DTYPE)
+    shapes["kind"] = abi.SHAPE_SPHERE
+    shapes["dims"][0, 0] = 1.0
+    shapes["body"] = 1
+    scenes.set_mass(bodies, shapes, None, 1, 0)
+    bodies["motion_type"][0] = abi.MOTION_STATIC
+    bodies["inv_mass"][0] = 0.0
+    bodies["inv_inertia"][0] = 0.0
+    bodies["position"][0] = (0, -50, 0)
+    sc = dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+              triangles=np.zeros(0, abi.TRIANGLE_DTYPE), params=dict(substeps=4, gravity=(0.0, 0.0, 0.0)))
+    w = O.OracleWorld(sc)
+    w.add_joint(LINEARMOTOR, 0, 1, (1, 0, 0, 1, 0, 0, 2.0, 100.0))
+    for _ in range(100):
+        w.step(0.01)
+    assert w.bodies()["velocity"][1][0] == pytest.approx(2.0, abs=0.2)
