@@ -236,6 +236,12 @@ template <class R> struct Handle {
         joint_prepare(jt, w.bodies, ts);                                                                           \
         if (iterate) joint_iterate(jt, w.bodies, ts);                                                              \
     }                                                                                                              \
+    /* one Iterate of joint j alone (after a Prepare) at step dt */                                              \
+    extern "C" void jor_world_joint_iterate_##SUF(void* h, int j, float dt) {                                      \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        TimeStep<R> ts((R)dt, 1);                                                                                  \
+        joint_iterate(w.joints[j], w.bodies, ts);                                                                  \
+    }                                                                                                              \
     /* joint row after its last Prepare: out = jr[0], jr[1], effective mass, clamp, impulse */                \
     extern "C" void jor_world_joint_data_##SUF(void* h, int j, double* out) {                                      \
         const Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                         \

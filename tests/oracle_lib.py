@@ -42,7 +42,7 @@ def load():
             "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]),
             "jor_world_register_manifold": (None, [P, I, I, P, P, I, P]), "jor_world_set_deactivation": (None, [P, I]),
             "jor_world_body_deactivation_time": (None, [P, I, D]), "jor_world_activate_body": (None, [P, I]),
-            "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]),
+            "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]), "jor_world_joint_iterate": (None, [P, I, F]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
             "jor_world_joint_limit_params": (None, [P, I, D, D]), "jor_world_joint_matrix": (None, [P, I, P]), "jor_world_set_orientation_d": (None, [P, I, P]),
@@ -264,6 +264,10 @@ class OracleWorld:
     def joint_solve(self, j, dt, bias, softness, iterate=True):
         """Prepare (and Iterate) one joint alone, bias factor and softness overridden."""
         self.fn("jor_world_joint_solve")(self.h, j, dt, bias, softness, 1 if iterate else 0)
+
+    def joint_iterate(self, j, dt):
+        """One Iterate of joint j alone."""
+        self.fn("jor_world_joint_iterate")(self.h, j, dt)
 
     def joint_data(self, j):
         """(jr0, jr1, effective mass, clamp, impulse) of a one-row joint after its Prepare."""
