@@ -197,6 +197,16 @@ int jg_create(const jg_world_params* params, jg_world** out_world);
 /* World.Dispose (World.cs:281-299). */
 int jg_destroy(jg_world* world);
 
+/* The World property setters: SolverIterations (World.cs:346-369), SubstepCount
+ * (World.cs:378-391), Gravity (World.cs:397-403), EnableAuxiliaryContactPoints,
+ * PersistentContactManifold, SpeculativeRelaxationFactor, SpeculativeVelocityThreshold
+ * (World.Detect.cs:88-122), plus the device settings.  The reference's
+ * ArgumentOutOfRangeException cases (solver iterations below one, negative relaxation
+ * iterations, substeps below one, a non-finite gravity) return JG_ERR_INVALID_ARG, and so does
+ * a change of the pool capacities, which are fixed at creation.  jg_get_params reads them. */
+int jg_set_params(jg_world* world, const jg_world_params* params);
+int jg_get_params(jg_world* world, jg_world_params* out);
+
 /* ---- state upload / download -------------------------------------------------------- */
 
 /* World.CreateRigidBody + RigidBody setters (World.cs:930-965, RigidBody.cs:503-760).
@@ -294,7 +304,16 @@ int jg_get_residuals(jg_world* world, float* out, int32_t capacity, int32_t* out
 /* Full state dump for checkpoints and one-step comparisons (no reference counterpart;
  * World.Stabilize, World.Step.cs:318-392, re-solves restored contacts). */
 int jg_export_state(jg_world* world, void* buffer, int64_t capacity, int64_t* out_size);
+/* Validates the blob (jg_check_state against the world's counts and pools) before it
+ * changes anything; a rejected blob leaves the world as it was. */
 int jg_import_state(jg_world* world, const void* buffer, int64_t size);
+/* Host-only check of a state blob for a world of n_bodies bodies and n_shapes shapes with
+ * the given arbiter and constraint pools: its size covers the counts in its header, the
+ * counts are not negative, and every arbiter's shapes and bodies and every constraint's
+ * kind and bodies lie inside the world.  JG_ERR_INVALID_ARG (or JG_ERR_CAPACITY when
+ * the counts exceed the pools) otherwise.  Needs no device. */
+int jg_check_state(const void* buffer, int64_t size, int32_t n_bodies, int32_t n_shapes, int32_t arbiter_capacity,
+                   int32_t constraint_capacity);
 
 /* ---- learned warm start (no reference counterpart) ---------------------------------------- */
 

@@ -97,6 +97,8 @@ SIGNATURES = {
     "jg_default_params": (_I, [_P]),
     "jg_create": (_I, [_P, ctypes.POINTER(_P)]),
     "jg_destroy": (_I, [_P]),
+    "jg_set_params": (_I, [_P, _P]),
+    "jg_get_params": (_I, [_P, _P]),
     "jg_upload_bodies": (_I, [_P, _P, _I]),
     "jg_download_bodies": (_I, [_P, _P, _I]),
     "jg_upload_shapes": (_I, [_P, _P, _I, _P, _I, _P, _I]),
@@ -114,6 +116,7 @@ SIGNATURES = {
     "jg_get_residuals": (_I, [_P, _P, _I, _PI]),
     "jg_export_state": (_I, [_P, _P, _I64, ctypes.POINTER(_I64)]),
     "jg_import_state": (_I, [_P, _P, _I64]),
+    "jg_check_state": (_I, [_P, _I64, _I, _I, _I, _I]),
     "jg_mlp_load": (_I, [_P, _P, _I]),
     "jg_mlp_predict": (_I, [_P, _P, _I, _P]),
     "jg_mlp_train_step": (_I, [_P, _P, _P, _I, _F, _PF]),

@@ -13,16 +13,18 @@
 #include <mutex>
 #include <climits>
 
-void jg_contacts_set_scratch(int2* created, int2* removed, int* remaining, int* dst_index);
 void jg_flip_store(WorldDev& w);
 void jg_launch_count_contacts(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_update_contacts(WorldDev& w, cudaStream_t s, int nsm);
-void jg_solver_reset_launch_cache();
+void jg_solver_reset_launch_cache(WorldDev& w);
+int jg_solver_init();
+int jg_schedule_init();
 int jg_mlp_step_hook(jg_world* w, const StepParams& p);
 void jg_mlp_free(void* mlp);
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
                              cudaStream_t s, int nsm);
 int jg_schedule_launches(const StepParams& p);
+int jg_narrowphase_init();
 
 static thread_local std::string g_err;
 
@@ -36,9 +38,6 @@ struct jg_world {
     jg_body_desc* d_stage = nullptr;  // an upload lands here and becomes d_desc once it is valid
     int* d_bad = nullptr;             // first invalid body of an upload: index * 4 + reason
     int* h_bad = nullptr;             // pinned
-    int2 *ev_created = nullptr, *ev_removed = nullptr;
-    int* remaining = nullptr;
-    int* dst_index = nullptr;
     std::vector<jg_body_desc> host_bodies;
     bool host_current = false;         // host_bodies equals the device state (no step since the upload)
     std::vector<jg_shape_desc> host_shapes;
@@ -60,6 +59,10 @@ struct jg_world {
     int q_cap = 0;
     void* mlp = nullptr;              // learned warm start state (jg_mlp.cu)
 };
+
+extern "C" {
+static void invalidate_graphs(jg_world* w);
+}
 
 namespace {
 
@@ -148,7 +151,7 @@ int allocate(jg_world* w) {
     DA(d.sc_task, JG_SCHED_MAXTASKS); DA(d.sc_cursor, JG_SCHED_MAXTASKS); DA(d.sc_tnc, JG_SCHED_MAXTASKS);
     DA(d.sc_tcell, JG_SCHED_MAXTASKS); DA(d.sc_tdep, 2 * JG_SCHED_MAXTASKS); DA(d.sc_done, JG_SCHED_MAXTASKS);
     DA(d.sc_tcol, (size_t)JG_SCHED_MAXTASKS * (JG_TASK_MAXC + 1));
-    DA(w->ev_created, d.cap_arb); DA(w->ev_removed, d.cap_arb); DA(w->remaining, 2); DA(w->dst_index, d.cap_arb);
+    DA(d.ev_created, d.cap_arb); DA(d.ev_removed, d.cap_arb); DA(d.remaining, 2); DA(d.dst_index, d.cap_arb);
     CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));
     memset(w->h_ctr, 0, sizeof(DevCounters));
     DA(w->d_desc, d.cap_bodies); DA(w->d_stage, d.cap_bodies); DA(w->d_bad, 1);
@@ -237,7 +240,6 @@ StepParams make_params(const jg_world* w, float dt) {
 int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     WorldDev& d = w->d;
     cudaStream_t s = w->stream;
-    jg_contacts_set_scratch(w->ev_created, w->ev_removed, w->remaining, w->dst_index);
     if (timed) cudaEventRecord(w->ev[0], s);
     k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
     if (sp.record_residual) cudaMemsetAsync(d.resid, 0, sizeof(float) * 2 * JG_RESID_MAX, s);
@@ -254,7 +256,10 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     w->launches += jg_mlp_step_hook(w, sp);
     if (timed) cudaEventRecord(w->ev[3], s);
     jg_launch_schedule(d, sp, s, w->nsm);
-    jg_launch_color(d, s, w->nsm);
+    if (jg_launch_color(d, s, w->nsm) < 0) {
+        g_err = "cooperative launch of the colouring failed";
+        return JG_ERR_CUDA;
+    }
     jg_flip_store(d);
     if (timed) cudaEventRecord(w->ev[4], s);
     jg_launch_count_contacts(d, s, w->nsm);
@@ -338,6 +343,11 @@ int jg_create(const jg_world_params* params, jg_world** out) {
     cudaGetDeviceProperties(&prop, w->device);
     if (prop.major < 10) { delete w; g_err = "needs an sm_103a (Blackwell) device"; return JG_ERR_NOT_SUPPORTED; }
     w->nsm = prop.multiProcessorCount;
+    if (jg_narrowphase_init() != 0 || jg_solver_init() != 0 || jg_schedule_init() != 0) {
+        delete w;
+        g_err = "shared memory attribute refused";
+        return JG_ERR_CUDA;
+    }
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { delete w; return JG_ERR_CUDA; }
     for (int i = 0; i < 9; i++) cudaEventCreate(&w->ev[i]);
     int r = allocate(w);
@@ -345,6 +355,33 @@ int jg_create(const jg_world_params* params, jg_world** out) {
     w->d.nworlds = 1;
     cudaStreamSynchronize(w->stream);
     *out = w;
+    return JG_OK;
+}
+
+// The World property setters (World.cs:346-403, World.Detect.cs:88-122): solver
+// iterations at least one, relaxation iterations not negative, substeps at least one, a
+// finite gravity; the pool capacities are fixed at creation.
+int jg_set_params(jg_world* w, const jg_world_params* p) {
+    if (!w || !p) return JG_ERR_INVALID_ARG;
+    if (p->substeps < 1 || p->solver_iterations < 1 || p->solver_iterations > 4096 || p->relax_iterations < 0 ||
+        !std::isfinite(p->gravity[0]) || !std::isfinite(p->gravity[1]) || !std::isfinite(p->gravity[2])) {
+        g_err = "jg_set_params: invalid solver settings";
+        return JG_ERR_INVALID_ARG;
+    }
+    const jg_world_params& c = w->prm;
+    if (p->max_bodies != c.max_bodies || p->max_shapes != c.max_shapes || p->max_pairs != c.max_pairs ||
+        p->max_arbiters != c.max_arbiters || p->max_constraints != c.max_constraints) {
+        g_err = "jg_set_params: pool capacities are fixed when the world is created";
+        return JG_ERR_INVALID_ARG;
+    }
+    w->prm = *p;
+    invalidate_graphs(w);
+    return JG_OK;
+}
+
+int jg_get_params(jg_world* w, jg_world_params* out) {
+    if (!w || !out) return JG_ERR_INVALID_ARG;
+    *out = w->prm;
     return JG_OK;
 }
 
@@ -921,13 +958,22 @@ int jg_get_arbiter_events(jg_world* w, int32_t* created, int32_t ccap, int32_t* 
     int a = (int)std::min<int64_t>(w->counters.created_arbiters, w->d.cap_arb);
     int b = (int)std::min<int64_t>(w->counters.removed_arbiters, w->d.cap_arb);
     *nc = a; *nr = b;
-    if (created && ccap > 0) CK(cudaMemcpy(created, w->ev_created, sizeof(int2) * std::min(a, ccap), cudaMemcpyDeviceToHost));
-    if (removed && rcap > 0) CK(cudaMemcpy(removed, w->ev_removed, sizeof(int2) * std::min(b, rcap), cudaMemcpyDeviceToHost));
+    if (created && ccap > 0) CK(cudaMemcpy(created, w->d.ev_created, sizeof(int2) * std::min(a, ccap), cudaMemcpyDeviceToHost));
+    if (removed && rcap > 0) CK(cudaMemcpy(removed, w->d.ev_removed, sizeof(int2) * std::min(b, rcap), cudaMemcpyDeviceToHost));
     return JG_OK;
 }
 
 // State blob: header, bodies (jg_body_desc), arbiter store of the live buffer, joints.
 struct StateHeader { int magic, version, nb, narb, nj, cap_arb; };
+
+// Layout of a state blob: the header, nb body descriptors, narb arbiters (key, bodies,
+// info, material, then 8 contact fields x 4 slots of float4) and nj joint records.
+static int64_t state_blob_size(int nb, int narb, int nj) {
+    const int64_t per_arb = sizeof(int2) * 2 + sizeof(int4) + sizeof(float4) + 32 * sizeof(float4);
+    return (int64_t)sizeof(StateHeader) + (int64_t)sizeof(jg_body_desc) * nb + per_arb * narb +
+           (int64_t)sizeof(JointDev) * nj;
+}
+
 
 int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
     if (!w || !size) return JG_ERR_INVALID_ARG;
@@ -937,8 +983,7 @@ int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
     int narb = 0;
     CK(cudaMemcpy(&narb, &D.ctr->narb, sizeof(int), cudaMemcpyDeviceToHost));
     narb = std::min(narb, D.cap_arb);
-    size_t per_arb = sizeof(int2) * 2 + sizeof(int4) + sizeof(float4) + 32 * sizeof(float4);
-    int64_t need = sizeof(StateHeader) + sizeof(jg_body_desc) * (int64_t)D.nb + (int64_t)per_arb * narb + sizeof(JointDev) * (int64_t)D.nj;
+    int64_t need = state_blob_size(D.nb, narb, D.nj);
     *size = need;
     if (!buf) return JG_OK;
     if (cap < need) return JG_ERR_CAPACITY;
@@ -966,18 +1011,50 @@ int jg_export_state(jg_world* w, void* buf, int64_t cap, int64_t* size) {
     return JG_OK;
 }
 
+int jg_check_state(const void* buf, int64_t size, int32_t nb, int32_t ns, int32_t cap_arb, int32_t cap_joints) {
+    if (!buf || size < (int64_t)sizeof(StateHeader)) { g_err = "state blob shorter than its header"; return JG_ERR_INVALID_ARG; }
+    StateHeader h;
+    memcpy(&h, buf, sizeof(h));
+    if (h.magic != 0x4a475331 || h.version != 1) { g_err = "not a state blob of this version"; return JG_ERR_INVALID_ARG; }
+    if (h.nb != nb || h.narb < 0 || h.nj < 0) { g_err = "state blob counts do not fit the world"; return JG_ERR_INVALID_ARG; }
+    if (h.narb > cap_arb || h.nj > cap_joints) { g_err = "state blob exceeds the world's pools"; return JG_ERR_CAPACITY; }
+    if (size < state_blob_size(h.nb, h.narb, h.nj)) { g_err = "state blob truncated"; return JG_ERR_INVALID_ARG; }
+    const char* p = (const char*)buf + sizeof(StateHeader) + sizeof(jg_body_desc) * (size_t)h.nb;
+    const int2* key = (const int2*)p;
+    const int2* body = key + h.narb;
+    for (int a = 0; a < h.narb; a++) {
+        int2 k, b;
+        memcpy(&k, key + a, sizeof(k));
+        memcpy(&b, body + a, sizeof(b));
+        if (k.x < 0 || k.x >= ns || k.y < 0 || k.y >= ns || b.x < 0 || b.x >= nb || b.y < 0 || b.y >= nb) {
+            g_err = "state blob arbiter " + std::to_string(a) + " names a shape or body outside the world";
+            return JG_ERR_INVALID_ARG;
+        }
+    }
+    const char* jp = (const char*)buf + state_blob_size(h.nb, h.narb, 0);
+    for (int j = 0; j < h.nj; j++) {
+        int4 hd;
+        memcpy(&hd, jp + sizeof(JointDev) * (size_t)j, sizeof(hd));
+        if (hd.x < JG_CONSTRAINT_BALLSOCKET || hd.x > JG_CONSTRAINT_TWISTANGLE || hd.y < 0 || hd.y >= nb || hd.z < 0 ||
+            hd.z >= nb) {
+            g_err = "state blob joint " + std::to_string(j) + " has an invalid kind or body";
+            return JG_ERR_INVALID_ARG;
+        }
+    }
+    return JG_OK;
+}
+
 int jg_import_state(jg_world* w, const void* buf, int64_t size) {
-    if (!w || !buf || size < (int64_t)sizeof(StateHeader)) return JG_ERR_INVALID_ARG;
+    if (!w) return JG_ERR_INVALID_ARG;
+    int chk = jg_check_state(buf, size, w->d.nb, w->d.ns, w->d.cap_arb, w->d.cap_joints);
+    if (chk) return chk;
     int fr = flush_joints(w);
     if (fr) return fr;
     w->host_current = false;
     const char* p = (const char*)buf;
     StateHeader h;
     memcpy(&h, p, sizeof(h)); p += sizeof(h);
-    if (h.magic != 0x4a475331 || h.version != 1) return JG_ERR_INVALID_ARG;
     WorldDev& D = w->d;
-    if (h.nb != D.nb) return JG_ERR_INVALID_ARG;
-    if (h.narb > D.cap_arb || h.nj > D.cap_joints) return JG_ERR_CAPACITY;
     int r = jg_upload_bodies(w, (const jg_body_desc*)p, h.nb);
     if (r) return r;
     p += sizeof(jg_body_desc) * h.nb;
@@ -1028,7 +1105,7 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
             w->prm.solver_block = b;
             w->prm.solver_ctas_per_sm = c;
             w->prm.use_graph = 0;
-            jg_solver_reset_launch_cache();
+            jg_solver_reset_launch_cache(w->d);
             if ((r = jg_import_state(w, snap.data(), size))) return r;
             if ((r = jg_step(w, dt))) continue;  // warm-up
             cudaEvent_t e0, e1;
@@ -1046,7 +1123,7 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     w->prm = saved;
     w->prm.solver_block = bb;
     w->prm.solver_ctas_per_sm = bc;
-    jg_solver_reset_launch_cache();
+    jg_solver_reset_launch_cache(w->d);
     invalidate_graphs(w);
     r = jg_import_state(w, snap.data(), size);
     if (chosen) *chosen = w->prm;
@@ -1058,7 +1135,7 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
 // accessors for the MLP translation unit
 void*& jg_world_mlp(jg_world* w) { return w->mlp; }
 void jg_world_invalidate_graphs(jg_world* w) { invalidate_graphs(w); }
-int* jg_world_dst_index(jg_world* w) { return w->dst_index; }
+int* jg_world_dst_index(jg_world* w) { return w->d.dst_index; }
 void jg_set_error(const char* msg) { g_err = msg; }
 WorldDev& jg_world_dev(jg_world* w) { return w->d; }
 cudaStream_t jg_world_stream(jg_world* w) { return w->stream; }

@@ -475,37 +475,30 @@ __global__ void k_update_contacts(WorldDev w) {
 
 }  // namespace
 
-// Scratch arrays owned by the API layer, passed through these setters.
-static int2* g_ev_created = nullptr;
-static int2* g_ev_removed = nullptr;
-static int* g_remaining = nullptr;
-static int* g_dst_index = nullptr;
-void jg_contacts_set_scratch(int2* created, int2* removed, int* remaining, int* dst_index) {
-    g_ev_created = created; g_ev_removed = removed; g_remaining = remaining; g_dst_index = dst_index;
-}
-
 void jg_launch_merge(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm) {
     int blocks = nsm * 4;
     k_hash_clear<<<blocks, 256, 0, s>>>(w);
     k_hash_build<<<blocks, 256, 0, s>>>(w);
-    k_merge<<<blocks, 128, 0, s>>>(w, p, g_ev_created);
+    k_merge<<<blocks, 128, 0, s>>>(w, p, w.ev_created);
 }
 
-static int g_color_grid = 0;
-void jg_launch_color(WorldDev& w, cudaStream_t s, int nsm) {
-    if (g_color_grid == 0) {
+// Returns 0, or -1 when the cooperative colouring launch is refused.
+int jg_launch_color(WorldDev& w, cudaStream_t s, int nsm) {
+    if (w.lc_color_grid == 0) {
         int occ = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_color, 256, 0);
         if (occ < 1) occ = 1;
-        g_color_grid = nsm * (occ < 2 ? occ : 2);
+        w.lc_color_grid = nsm * (occ < 2 ? occ : 2);
     }
     cudaMemsetAsync(w.bar_count, 0, sizeof(unsigned) * 2, s);
-    int* rem = g_remaining;
+    int* rem = w.remaining;
     void* args[] = {(void*)&w, (void*)&rem};
-    cudaLaunchCooperativeKernel((const void*)k_color, dim3(g_color_grid), dim3(256), args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_color, dim3(w.lc_color_grid), dim3(256), args, 0, s);
+    if (e != cudaSuccess) return -1;
     k_jcursor_clear<<<1, 128, 0, s>>>(w);
-    k_permute<<<nsm * 4, 256, 0, s>>>(w, g_ev_removed, g_dst_index);
+    k_permute<<<nsm * 4, 256, 0, s>>>(w, w.ev_removed, w.dst_index);
     k_permute_done<<<1, 1, 0, s>>>(w);
+    return 0;
 }
 
 void jg_flip_store(WorldDev& w) { w.cur = 1 - w.cur; }

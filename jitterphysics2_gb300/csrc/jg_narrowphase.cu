@@ -18,6 +18,7 @@
 // warranty; altered source versions must be plainly marked as such; this notice may not
 // be removed or altered from any source distribution.
 #include "jg_shapes.cuh"
+#include <math_constants.h>
 
 namespace {
 
@@ -104,8 +105,9 @@ struct Exp {
         double t = det[cnt - 1];
         return t > 0 ? 1 : (t < 0 ? -1 : 0);
     }
-    // ExpansionArithmetic.Normal (ExpansionArithmetic.cs:43-55)
-    __device__ __noinline__ static v3 normal(v3 a, v3 b, v3 c) {
+    // ExpansionArithmetic.Normal (ExpansionArithmetic.cs:43-55): each component of
+    // (a-b) x (a-c) as an exact expansion, summed from the least significant part up
+    __device__ __noinline__ static void normal(v3 a, v3 b, v3 c, double& x, double& y, double& z) {
         double ux[2], uy[2], uz[2], vx[2], vy[2], vz[2], cr[16];
         int nx = diff(a.x, b.x, ux), ny = diff(a.y, b.y, uy), nz = diff(a.z, b.z, uz);
         int mx = diff(a.x, c.x, vx), my = diff(a.y, c.y, vy), mz = diff(a.z, c.z, vz);
@@ -116,10 +118,7 @@ struct Exp {
         s = 0; for (int i = 0; i < len; i++) s += cr[i]; r[1] = s;
         len = crossterm(ux, nx, vy, my, uy, ny, vx, mx, cr);
         s = 0; for (int i = 0; i < len; i++) s += cr[i]; r[2] = s;
-        // scale by the largest component in double before rounding to float
-        double m = fmax(fabs(r[0]), fmax(fabs(r[1]), fabs(r[2])));
-        if (!(m > 0)) return mk3(0.f);
-        return mk3((float)(r[0] / m), (float)(r[1] / m), (float)(r[2] / m));
+        x = r[0]; y = r[1]; z = r[2];
     }
 };
 
@@ -162,11 +161,19 @@ __device__ __forceinline__ bool ffilter_side(v3 a, v3 b, v3 c, v3 p, int& sign) 
     return true;
 }
 
+// Per-warp EPA polytope, in dynamic shared memory.  Vertices and faces at the reference's
+// capacity (ConvexPolytope.cs:53-54).  Each face keeps what the reference's Triangle and
+// FaceData keep for the search: the squared distance of its closest point in FP64 (the
+// closest-face choice compares these), and the closest point and its squared distance
+// rounded to FP32 (the support direction and the convergence test).  Everything else a
+// face has in FP64 (plane normal, barycentric coordinates) is a deterministic function of
+// its corners and is recomputed, bit for bit, where it is needed: for the rare search
+// along a face normal and for the witness points of the final face.
 struct EpaSmem {
     float4 vV[JG_EPA_MAXV], vA[JG_EPA_MAXV], vB[JG_EPA_MAXV];
-    float4 fn[JG_EPA_MAXT];     // scaled normal xyz, normal_sq
-    float4 fc[JG_EPA_MAXT];     // closest point xyz, closest_sq
-    uchar4 fi[JG_EPA_MAXT];     // a, b, c, facing origin
+    double fd[JG_EPA_MAXT];     // squared distance of the closest point (FP64)
+    float4 fc[JG_EPA_MAXT];     // closest point xyz, squared distance (both rounded to FP32)
+    uchar4 fi[JG_EPA_MAXT];     // a, b, c, flags (1: facing the origin, 2: corners swapped)
     unsigned char ea[3 * JG_EPA_MAXT], eb[3 * JG_EPA_MAXT];
     unsigned lit[JG_EPA_MAXT / 32];
     int nv, nt, ne, enclosed;
@@ -174,12 +181,16 @@ struct EpaSmem {
     float4 mA[12], mB[12];
     float4 left[6], right[6];
 };
+#define EPA_FACING 1
+#define EPA_SWAPPED 2
 
 enum { ADDED = 0, NO_HORIZON = 1, DEGENERATE = 2, CAPACITY = 3, NUMERICAL = 4 };
 
 struct NpStats { int exact; };
 
-// ConvexPolytope.Side (ConvexPolytope.cs:321-327): orientation of point p relative to face (a,b,c).
+// ConvexPolytope.Side (ConvexPolytope.cs:321-327): orientation of point p relative to face
+// (a,b,c).  Every filter that answers is certified, so the sign is the exact one whichever
+// answers: the FP32 filter first, then the reference's FP64 filter, then exact expansions.
 __device__ __forceinline__ int side_pt(v3 a, v3 b, v3 c, v3 p, NpStats& st) {
     if (p == a || p == b || p == c) return 0;
     int s;
@@ -189,75 +200,121 @@ __device__ __forceinline__ int side_pt(v3 a, v3 b, v3 c, v3 p, NpStats& st) {
     return Exp::side(a, b, c, p);
 }
 
+// PlaneFilter.IsSafe (ExactArithmetic/PlaneFilter.cs:73-77) for float coordinates.
 __device__ __forceinline__ bool safe_coord(float v) {
     float a = fabsf(v);
     return v == 0.f || (a >= 1e-30f && a <= 1e30f);
 }
 __device__ __forceinline__ bool is_safe(v3 p) { return safe_coord(p.x) && safe_coord(p.y) && safe_coord(p.z); }
 
-// ConvexPolytope.CalcBarycentric (ConvexPolytope.cs:328-395), in FP32.
-__device__ bool calc_bary(v3 a, v3 b, v3 c, v3 n, float nscale, float nsq, v3& out) {
-    v3 u = a - b, v = a - c;
-    float gamma = (dot(cross(u, a), n) / nsq) / nscale;
-    float beta = (dot(cross(a, v), n) / nsq) / nscale;
-    float alpha = 1.f - gamma - beta;
+// FP64 vector helpers in the reference's evaluation order (ConvexPolytope.Double3).
+struct d3 { double x, y, z; };
+__device__ __forceinline__ d3 dv(v3 v) { return d3{(double)v.x, (double)v.y, (double)v.z}; }
+__device__ __forceinline__ double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ d3 dcross(d3 a, d3 b) { return d3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ d3 dsub(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ d3 dadd(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ d3 dmul(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ bool dfinite(d3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+__device__ __forceinline__ double dclamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+// ConvexPolytope.CalcBarycentric (ConvexPolytope.cs:328-395), FP64.
+__device__ bool calc_bary(d3 a, d3 b, d3 c, d3 n, double nscale, double nsq, d3& out) {
+    d3 u = dsub(a, b), v = dsub(a, c);
+    double gamma = (ddot(dcross(u, a), n) / nsq) / nscale;
+    double beta = (ddot(dcross(a, v), n) / nsq) / nscale;
+    double alpha = 1.0 - gamma - beta;
     bool clamped = false;
     if (alpha >= 0 && beta < 0) {
-        float t = dot(a, u);
-        if (gamma < 0 && t > 0) { beta = fminf(1.f, t / dot(u, u)); alpha = 1 - beta; gamma = 0; }
-        else { gamma = fminf(fmaxf(dot(a, v) / dot(v, v), 0.f), 1.f); alpha = 1 - gamma; beta = 0; }
+        double t = ddot(a, u);
+        if (gamma < 0 && t > 0) { beta = fmin(1.0, t / ddot(u, u)); alpha = 1 - beta; gamma = 0; }
+        else { gamma = dclamp01(ddot(a, v) / ddot(v, v)); alpha = 1 - gamma; beta = 0; }
         clamped = true;
     } else if (beta >= 0 && gamma < 0) {
-        v3 w = b - c;
-        float t = dot(b, w);
-        if (alpha < 0 && t > 0) { gamma = fminf(1.f, t / dot(w, w)); beta = 1 - gamma; alpha = 0; }
-        else { alpha = fminf(fmaxf(-dot(b, u) / dot(u, u), 0.f), 1.f); beta = 1 - alpha; gamma = 0; }
+        d3 w = dsub(b, c);
+        double t = ddot(b, w);
+        if (alpha < 0 && t > 0) { gamma = fmin(1.0, t / ddot(w, w)); beta = 1 - gamma; alpha = 0; }
+        else { alpha = dclamp01(-ddot(b, u) / ddot(u, u)); beta = 1 - alpha; gamma = 0; }
         clamped = true;
     } else if (gamma >= 0 && alpha < 0) {
-        v3 w = b - c;
-        float t = -dot(c, v);
-        if (beta < 0 && t > 0) { alpha = fminf(1.f, t / dot(v, v)); gamma = 1 - alpha; beta = 0; }
-        else { beta = fminf(fmaxf(-dot(c, w) / dot(w, w), 0.f), 1.f); gamma = 1 - beta; alpha = 0; }
+        d3 w = dsub(b, c);
+        double t = -ddot(c, v);
+        if (beta < 0 && t > 0) { alpha = fmin(1.0, t / ddot(v, v)); gamma = 1 - alpha; beta = 0; }
+        else { beta = dclamp01(-ddot(c, w) / ddot(w, w)); gamma = 1 - beta; alpha = 0; }
         clamped = true;
     }
-    out = mk3(alpha, beta, gamma);
+    out = d3{alpha, beta, gamma};
     return clamped;
+}
+
+// The FP64 geometry of a face (ConvexPolytope.CreateTriangle, ConvexPolytope.cs:267-318):
+// p0, p1, p2 are the corners in creation order; `swapped` when the orientation test
+// exchanged the first two.  The raw normal is the FP64 plane filter's cross product of the
+// creation order (PlaneFilter.cs:29-45), negated on a swap, and replaced by the exact
+// expansion normal of the final order when the filter calls it unreliable
+// (PlaneFilter.cs:24-27).  Returns false on a numerical failure.
+struct FaceGeo { d3 sn; double nscale, nsq; d3 bc, cl; double d2; };
+__device__ __noinline__ bool face_geo(v3 p0, v3 p1, v3 p2, bool swapped, FaceGeo& g, NpStats& st) {
+    const double EF = 16 * 1.1102230246251565e-16;
+    double ux = (double)p0.x - p1.x, uy = (double)p0.y - p1.y, uz = (double)p0.z - p1.z;
+    double vx = (double)p0.x - p2.x, vy = (double)p0.y - p2.y, vz = (double)p0.z - p2.z;
+    double yz = uy * vz, zy = uz * vy, zx = uz * vx, xz = ux * vz, xy = ux * vy, yx = uy * vx;
+    d3 raw{yz - zy, zx - xz, xy - yx};
+    double ex = EF * (fabs(yz) + fabs(zy)), ey = EF * (fabs(zx) + fabs(xz)), ez = EF * (fabs(xy) + fabs(yx));
+    if (swapped) raw = d3{-raw.x, -raw.y, -raw.z};
+    v3 a = swapped ? p1 : p0, b = swapped ? p0 : p1, c = p2;
+    if (!(fmax(fabs(raw.x), fmax(fabs(raw.y), fabs(raw.z))) > 1048576 * fmax(ex, fmax(ey, ez)))) {
+        st.exact++;
+        Exp::normal(a, b, c, raw.x, raw.y, raw.z);
+    }
+    double ns = fmax(fabs(raw.x), fmax(fabs(raw.y), fabs(raw.z)));
+    if (!(ns > 0) || !isfinite(ns)) return false;
+    g.nscale = ns;
+    g.sn = d3{raw.x / ns, raw.y / ns, raw.z / ns};
+    g.nsq = ddot(g.sn, g.sn);
+    d3 va = dv(a), vb = dv(b), vc = dv(c);
+    bool clamped = calc_bary(va, vb, vc, g.sn, ns, g.nsq, g.bc);
+    g.cl = clamped ? dadd(dadd(dmul(va, g.bc.x), dmul(vb, g.bc.y)), dmul(vc, g.bc.z))
+                   : dmul(g.sn, ddot(g.sn, va) / g.nsq);
+    g.d2 = ddot(g.cl, g.cl);
+    return dfinite(g.cl) && dfinite(g.bc) && isfinite(g.d2);
+}
+
+// The face's geometry from its stored corners and flags.
+__device__ __forceinline__ bool face_geo_of(const EpaSmem& E, int f, FaceGeo& g, NpStats& st) {
+    uchar4 t = E.fi[f];
+    bool sw = (t.w & EPA_SWAPPED) != 0;
+    int p0 = sw ? t.y : t.x, p1 = sw ? t.x : t.y;
+    return face_geo(mk3(E.vV[p0]), mk3(E.vV[p1]), mk3(E.vV[t.z]), sw, g, st);
+}
+
+// The FP32 normal of a face and its squared length (Triangle.Normal / NormalSq).
+__device__ __forceinline__ float4 face_normal32(const FaceGeo& g) {
+    v3 n = mk3((float)g.sn.x, (float)g.sn.y, (float)g.sn.z);
+    return f4(n, len2(n));
 }
 
 // ConvexPolytope.CreateTriangle (ConvexPolytope.cs:267-318), one lane per face.
 __device__ __noinline__ int create_tri(EpaSmem& E, int a, int b, int c, int slot, NpStats& st) {
     v3 va = mk3(E.vV[a]), vb = mk3(E.vV[b]), vc = mk3(E.vV[c]);
+    v3 p0 = va, p1 = vb;
     int orient = 0;
     for (int i = 0; i < 4 && orient == 0; i++) {
         if (i == a || i == b || i == c) continue;
         orient = -side_pt(va, vb, vc, mk3(E.vV[i]), st);
     }
     if (orient == 0) return DEGENERATE;
-    if (orient < 0) { int t = a; a = b; b = t; v3 tv = va; va = vb; vb = tv; }
+    const bool swapped = orient < 0;
+    if (swapped) { int t = a; a = b; b = t; v3 tv = va; va = vb; vb = tv; }
     bool facing = side_pt(va, vb, vc, mk3(0.f), st) <= 0;
-    // raw normal (a-b) x (a-c) with its filter error; recompute exactly when cancelled
-    float ux = va.x - vb.x, uy = va.y - vb.y, uz = va.z - vb.z;
-    float vx = va.x - vc.x, vy = va.y - vc.y, vz = va.z - vc.z;
-    float yz = uy * vz, zy = uz * vy, zx = uz * vx, xz = ux * vz, xy = ux * vy, yx = uy * vx;
-    v3 raw = mk3(yz - zy, zx - xz, xy - yx);
-    const float EF = 16.0f * 5.9604645e-08f;
-    float err = EF * fmaxf(fabsf(yz) + fabsf(zy), fmaxf(fabsf(zx) + fabsf(xz), fabsf(xy) + fabsf(yx)));
-    float nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
-    if (!(nmax > 4096.0f * err)) {
-        st.exact++;
-        raw = Exp::normal(va, vb, vc);
-        nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
-    }
-    if (!(nmax > 0) || !isfinite(nmax)) return NUMERICAL;
-    v3 sn = mk3(raw.x / nmax, raw.y / nmax, raw.z / nmax);
-    float nsq = dot(sn, sn);
-    v3 bc;
-    bool clamped = calc_bary(va, vb, vc, sn, nmax, nsq, bc);
-    v3 cl = clamped ? (va * bc.x + vb * bc.y) + vc * bc.z : sn * (dot(sn, va) / nsq);
-    float d2 = dot(cl, cl);
+    FaceGeo g;
+    if (!face_geo(p0, p1, vc, swapped, g, st)) return NUMERICAL;
+    v3 cl = mk3((float)g.cl.x, (float)g.cl.y, (float)g.cl.z);
+    float d2 = (float)g.d2;
     if (!isfinite(cl.x) || !isfinite(cl.y) || !isfinite(cl.z) || !isfinite(d2)) return NUMERICAL;
-    E.fi[slot] = make_uchar4((unsigned char)a, (unsigned char)b, (unsigned char)c, facing ? 1 : 0);
-    E.fn[slot] = f4(sn, len2(sn));
+    E.fi[slot] = make_uchar4((unsigned char)a, (unsigned char)b, (unsigned char)c,
+                             (unsigned char)((facing ? EPA_FACING : 0) | (swapped ? EPA_SWAPPED : 0)));
+    E.fd[slot] = g.d2;
     E.fc[slot] = f4(cl, d2);
     return ADDED;
 }
@@ -280,20 +337,21 @@ __device__ bool epa_init(EpaSmem& E, NpStats& st) {
     return ok;
 }
 
-// ConvexPolytope.GetClosestTriangle (ConvexPolytope.cs:147-166): first minimum wins.
+// ConvexPolytope.GetClosestTriangle (ConvexPolytope.cs:147-166): the smallest FP64 squared
+// distance, the first such face on a tie.
 __device__ int epa_closest(EpaSmem& E) {
     const int lane = threadIdx.x & 31;
-    float best = 3.402823466e+38f;
+    double best = CUDART_INF;
     int bi = 0x7fffffff;
     bool notfacing = false;
     int nt = E.nt;
     for (int i = lane; i < nt; i += 32) {
-        float d = E.fc[i].w;
-        if (d < best || (d == best && i < bi)) { best = d; bi = i; }
-        if (!E.fi[i].w) notfacing = true;
+        double d = E.fd[i];
+        if (d < best) { best = d; bi = i; }
+        if (!(E.fi[i].w & EPA_FACING)) notfacing = true;
     }
     for (int off = 16; off > 0; off >>= 1) {
-        float ob = __shfl_xor_sync(FULL, best, off);
+        double ob = __shfl_xor_sync(FULL, best, off);
         int oi = __shfl_xor_sync(FULL, bi, off);
         if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
     }
@@ -361,12 +419,12 @@ __device__ __noinline__ int epa_add(EpaSmem& E, const MV& v, NpStats& st) {
     for (int base = 0; base < nt; base += 32) {
         int i = base + lane;
         bool keep = i < nt && !((E.lit[i >> 5] >> (i & 31)) & 1u);
-        uchar4 fi; float4 fn, fc;
-        if (keep) { fi = E.fi[i]; fn = E.fn[i]; fc = E.fc[i]; }
+        uchar4 fi; float4 fc; double fd;
+        if (keep) { fi = E.fi[i]; fc = E.fc[i]; fd = E.fd[i]; }
         unsigned m = __ballot_sync(FULL, keep);
         int dst = surv + __popc(m & ((1u << lane) - 1u));
         __syncwarp();
-        if (keep) { E.fi[dst] = fi; E.fn[dst] = fn; E.fc[dst] = fc; }
+        if (keep) { E.fi[dst] = fi; E.fc[dst] = fc; E.fd[dst] = fd; }
         surv += __popc(m);
         __syncwarp();
     }
@@ -403,11 +461,17 @@ __device__ __noinline__ bool solve_epa(EpaSmem& E, const ShapeRef& sa, const Sha
     int ci = 0;
     while (++iter < maxIter) {
         ci = epa_closest(E);
-        float4 fc = E.fc[ci], fn = E.fn[ci];
+        float4 fc = E.fc[ci];
         v3 sd = mk3(fc), cl = mk3(fc);
         float sdsq = fc.w;
         if (!E.enclosed) sd = -sd;
-        if (fc.w < 1e-16f) { sd = mk3(fn); sdsq = fn.w; }
+        if (fc.w < 1e-16f) {
+            // search along the face normal (Triangle.Normal / NormalSq)
+            FaceGeo g;
+            face_geo_of(E, ci, g, st);
+            float4 fn = face_normal32(g);
+            sd = mk3(fn); sdsq = fn.w;
+        }
         MV v;
         mk_support(sa, sb, qb, pb, sd, v);
         float delta = dot(cl - v.V, sd);
@@ -422,23 +486,18 @@ __device__ __noinline__ bool solve_epa(EpaSmem& E, const ShapeRef& sa, const Sha
 converged:
     if (!E.enclosed) return false;
     {
-        // ConvexPolytope.CalculatePoints (ConvexPolytope.cs:169-185)
+        // ConvexPolytope.CalculatePoints (ConvexPolytope.cs:169-185): the FP64 barycentric
+        // combination of the corners' support points, rounded to FP32
         uchar4 f = E.fi[ci];
-        float4 fn = E.fn[ci], fc = E.fc[ci];
-        v3 va = mk3(E.vV[f.x]), vb = mk3(E.vV[f.y]), vc = mk3(E.vV[f.z]);
-        v3 sn = mk3(fn);
-        // rebuild the normal scale the face was built with
-        float ux = va.x - vb.x, uy = va.y - vb.y, uz = va.z - vb.z;
-        float vx = va.x - vc.x, vy = va.y - vc.y, vz = va.z - vc.z;
-        v3 raw = mk3(uy * vz - uz * vy, uz * vx - ux * vz, ux * vy - uy * vx);
-        float nmax = fmaxf(fabsf(raw.x), fmaxf(fabsf(raw.y), fabsf(raw.z)));
-        if (!(nmax > 0)) nmax = 1.f;
-        v3 bc;
-        calc_bary(va, vb, vc, sn, nmax, dot(sn, sn), bc);
-        p1 = (mk3(E.vA[f.x]) * bc.x + mk3(E.vA[f.y]) * bc.y) + mk3(E.vA[f.z]) * bc.z;
-        p2 = (mk3(E.vB[f.x]) * bc.x + mk3(E.vB[f.y]) * bc.y) + mk3(E.vB[f.z]) * bc.z;
-        n = sn * (1.0f / sqrtf(fn.w));
-        pen = sqrtf(fc.w);
+        FaceGeo g;
+        face_geo_of(E, ci, g, st);
+        d3 a = dadd(dadd(dmul(dv(mk3(E.vA[f.x])), g.bc.x), dmul(dv(mk3(E.vA[f.y])), g.bc.y)), dmul(dv(mk3(E.vA[f.z])), g.bc.z));
+        d3 b = dadd(dadd(dmul(dv(mk3(E.vB[f.x])), g.bc.x), dmul(dv(mk3(E.vB[f.y])), g.bc.y)), dmul(dv(mk3(E.vB[f.z])), g.bc.z));
+        p1 = mk3((float)a.x, (float)a.y, (float)a.z);
+        p2 = mk3((float)b.x, (float)b.y, (float)b.z);
+        float4 fn = face_normal32(g);
+        n = mk3(fn) * (1.0f / sqrtf(fn.w));
+        pen = sqrtf(E.fc[ci].w);
     }
     return true;
 }
@@ -1302,7 +1361,8 @@ __device__ __forceinline__ int next_item(int* cursor, int lane) {
 }
 
 __global__ void __launch_bounds__(NP_WARPS * 32) k_epa(WorldDev w) {
-    __shared__ EpaSmem smem[NP_WARPS];
+    extern __shared__ __align__(16) unsigned char np_smem_raw[];
+    EpaSmem* smem = reinterpret_cast<EpaSmem*>(np_smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     EpaSmem& E = smem[wib];
@@ -1419,7 +1479,8 @@ __global__ void __launch_bounds__(128) k_manifold(WorldDev w, StepParams sp) {
 // (rerun of MPR/EPA with threshold zero, normal snapping; TriangleEdgeCollisionFilter.cs:
 // 294-420) and the manifold.
 __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams sp) {
-    __shared__ EpaSmem smem[NP_WARPS];
+    extern __shared__ __align__(16) unsigned char np_smem_raw[];
+    EpaSmem* smem = reinterpret_cast<EpaSmem*>(np_smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     EpaSmem& E = smem[wib];
@@ -1512,7 +1573,8 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_edge(WorldDev w, StepParams s
 // written, so neither buffer needs clearing.
 __global__ void __launch_bounds__(NP_WARPS * 32) k_collide_query(WorldDev w, const int2* pairs, int n, float threshold,
                                                                  float* out, int* hit) {
-    __shared__ EpaSmem smem[NP_WARPS];
+    extern __shared__ __align__(16) unsigned char np_smem_raw[];
+    EpaSmem* smem = reinterpret_cast<EpaSmem*>(np_smem_raw);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     EpaSmem& E = smem[wib];
@@ -1538,14 +1600,26 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_collide_query(WorldDev w, con
     }
 }
 
+// Dynamic shared memory of the warp-per-pair kernels: one polytope per warp.
+constexpr int kNpSmem = NP_WARPS * (int)sizeof(EpaSmem);
+
 }  // namespace
+
+// Lets the warp-per-pair kernels take their polytopes' shared memory (above the 48 KB
+// default) on the current device; called when a world is created.
+int jg_narrowphase_init() {
+    cudaError_t e = cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, kNpSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_edge, cudaFuncAttributeMaxDynamicSharedMemorySize, kNpSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_collide_query, cudaFuncAttributeMaxDynamicSharedMemorySize, kNpSmem);
+    return e == cudaSuccess ? 0 : -1;
+}
 
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
                              cudaStream_t s, int nsm) {
     if (n <= 0) return;
     int blocks = (n + NP_WARPS - 1) / NP_WARPS;
     if (blocks > nsm * 4) blocks = nsm * 4;
-    k_collide_query<<<blocks, NP_WARPS * 32, 0, s>>>(w, pairs, n, threshold, out, hit);
+    k_collide_query<<<blocks, NP_WARPS * 32, kNpSmem, s>>>(w, pairs, n, threshold, out, hit);
 }
 
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile) {
@@ -1556,7 +1630,7 @@ void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int
     k_pair_scatter<<<nsm * 4, 256, 0, s>>>(w);
     k_mpr<<<nsm * 8, 256, 0, s>>>(w);
     k_sweep<<<nsm * 2, 128, 0, s>>>(w, p);
-    k_epa<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w);
+    k_epa<<<nsm * 4, NP_WARPS * 32, kNpSmem, s>>>(w);
     k_manifold<<<nsm * 16, 128, 0, s>>>(w, p);
-    k_edge<<<nsm * 4, NP_WARPS * 32, 0, s>>>(w, p);
+    k_edge<<<nsm * 4, NP_WARPS * 32, kNpSmem, s>>>(w, p);
 }

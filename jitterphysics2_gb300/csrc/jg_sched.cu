@@ -437,13 +437,20 @@ void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int ns
         k_sched_tasks<<<1, 1024, 0, s>>>(w, p);
         k_sched_scatter<<<nsm * 4, 256, 0, s>>>(w);
         size_t smem = jg_task_color_smem(p.task_maxb);
-        static size_t s_attr = 0;
-        if (s_attr != smem) {
-            cudaFuncSetAttribute(k_task_color, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            s_attr = smem;
-        }
         k_task_color<<<nsm * 2, TC_THREADS, smem, s>>>(w, p);
     }
+}
+
+// Lets the local colouring take all the dynamic shared memory the current device allows,
+// once per device (called when a world is created).
+int jg_schedule_init() {
+    int dev = 0, pb = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&pb, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void*)k_task_color) != cudaSuccess) return -1;
+    return cudaFuncSetAttribute(k_task_color, cudaFuncAttributeMaxDynamicSharedMemorySize, pb - (int)fa.sharedSizeBytes)
+               == cudaSuccess ? 0 : -1;
 }
 
 // Kernels launched by jg_launch_schedule.

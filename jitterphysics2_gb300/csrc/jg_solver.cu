@@ -704,17 +704,27 @@ __global__ void k_update_bodies(WorldDev w, StepParams sp) {
 
 }  // namespace
 
+// Shared memory limits of the current device.
 static void smem_limits(int& per_block, int& per_sm) {
-    static int b = 0, m = 0;
-    if (!b) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&b, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        if (b <= 0) b = 48 * 1024;
-        if (m <= 0) m = b;
-    }
+    int b = 0, m = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (b <= 0) b = 48 * 1024;
+    if (m <= 0) m = b;
     per_block = b; per_sm = m;
+}
+
+// Lets the task solve take all the dynamic shared memory the current device allows, once
+// per device (called when a world is created), so that worlds with different launch
+// shapes never have to change the attribute under each other.
+int jg_solver_init() {
+    int pb, psm;
+    smem_limits(pb, psm);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void*)k_solve_tasks) != cudaSuccess) return -1;
+    int dyn = pb - (int)fa.sharedSizeBytes;
+    return cudaFuncSetAttribute(k_solve_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) == cudaSuccess ? 0 : -1;
 }
 
 // Bodies a task can stage next to the arbiter ring of `block` threads when
@@ -734,48 +744,48 @@ static size_t task_smem(const StepParams& p, int block) {
     return ((size_t)4 * p.task_maxb + (size_t)JG_TASK_RING * block * JG_TASK_STAGE_F4) * 16;
 }
 
-static int g_solve_grid = 0, g_solve_block = 0, g_tasks_grid = 0, g_tasks_block = 0;
-static size_t g_tasks_smem = 0;
+// The cooperative grid of each solve kernel is sized once per world (its device, block,
+// shared memory and CTAs per SM) and kept in the world's launch cache.
 int jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm) {
     if (p.partition) {
         if (block <= 0) block = JG_TASK_BLOCK;
         if (ctas_per_sm <= 0) ctas_per_sm = JG_TASK_CTAS;
         size_t smem = task_smem(p, block);
-        if (g_tasks_block != block || g_tasks_smem != smem || g_tasks_grid == 0) {
-            cudaFuncSetAttribute(k_solve_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (w.lc_tasks_block != block || w.lc_tasks_smem != smem || w.lc_tasks_ctas != ctas_per_sm || w.lc_tasks_grid == 0) {
             int occ = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve_tasks, block, smem);
             if (occ < 1) return -1;
-            if (ctas_per_sm > 0 && occ > ctas_per_sm) occ = ctas_per_sm;
-            g_tasks_grid = nsm * occ;
-            g_tasks_block = block;
-            g_tasks_smem = smem;
+            if (occ > ctas_per_sm) occ = ctas_per_sm;
+            w.lc_tasks_grid = nsm * occ;
+            w.lc_tasks_block = block;
+            w.lc_tasks_smem = smem;
+            w.lc_tasks_ctas = ctas_per_sm;
         }
         cudaMemsetAsync(w.bar_count, 0, sizeof(unsigned) * 2, s);
         StepParams sp = p;
         void* args[] = {(void*)&w, (void*)&sp};
-        cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_solve_tasks, dim3(g_tasks_grid), dim3(block), args, smem, s);
-        return e == cudaSuccess ? g_tasks_grid : -1;
+        cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_solve_tasks, dim3(w.lc_tasks_grid), dim3(block), args, smem, s);
+        return e == cudaSuccess ? w.lc_tasks_grid : -1;
     }
     if (block <= 0) block = 256;
     if (ctas_per_sm <= 0) ctas_per_sm = 2;
-    if (g_solve_block != block || g_solve_grid == 0) {
+    if (w.lc_solve_block != block || w.lc_solve_ctas != ctas_per_sm || w.lc_solve_grid == 0) {
         int occ = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve, block, 0);
         if (occ < 1) occ = 1;
-        if (ctas_per_sm > occ) ctas_per_sm = occ;
-        g_solve_grid = nsm * ctas_per_sm;
-        g_solve_block = block;
+        w.lc_solve_grid = nsm * (ctas_per_sm > occ ? occ : ctas_per_sm);
+        w.lc_solve_block = block;
+        w.lc_solve_ctas = ctas_per_sm;
     }
     cudaMemsetAsync(w.bar_count, 0, sizeof(unsigned) * 2, s);
     StepParams sp = p;
     void* args[] = {(void*)&w, (void*)&sp};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_solve, dim3(g_solve_grid), dim3(block), args, 0, s);
-    return e == cudaSuccess ? g_solve_grid : -1;
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_solve, dim3(w.lc_solve_grid), dim3(block), args, 0, s);
+    return e == cudaSuccess ? w.lc_solve_grid : -1;
 }
 
 void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm) {
     k_update_bodies<<<nsm * 4, 256, 0, s>>>(w, p);
 }
 
-void jg_solver_reset_launch_cache() { g_solve_grid = 0; g_tasks_grid = 0; }
+void jg_solver_reset_launch_cache(WorldDev& w) { w.lc_solve_grid = 0; w.lc_tasks_grid = 0; w.lc_color_grid = 0; }

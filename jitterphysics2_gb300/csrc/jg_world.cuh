@@ -15,8 +15,8 @@
 #define JG_MAX_COLORS 128
 #define JG_RESID_MAX 2048       // iterations whose residual a step records (record_residual)
 #define JG_HULL_MAX 64          // point-cloud vertices per shape handled on the device
-#define JG_EPA_MAXV 64          // EPA polytope capacity on the device (reference: 128/256)
-#define JG_EPA_MAXT 128
+#define JG_EPA_MAXV 128         // EPA polytope capacity (ConvexPolytope.cs:53-54)
+#define JG_EPA_MAXT 256
 
 struct __align__(16) SBody {
     float4 v;   // velocity xyz, inverse mass x
@@ -213,6 +213,17 @@ struct WorldDev {
     int* sc_dst;                 // [cap_arb] final slot of a task arbiter, -1 for the remainder
     int* sc_lcol;                // [cap_arb] local colour of a task arbiter
     int4* sc_ls;                 // [cap_arb] body slots of a task arbiter
+    // per-step scratch of the cache merge and the colour permutation (each world its own)
+    int2* ev_created;            // [cap_arb] keys of the arbiters created this step
+    int2* ev_removed;            // [cap_arb] keys of the arbiters removed this step
+    int* remaining;              // [2] colouring: constraints still without a colour
+    int* dst_index;              // [cap_arb] slot of each arbiter after the permutation, -1 if removed
+    // launch shapes of the cooperative kernels, sized once per world on its device (host
+    // side only; a world is driven by one host thread)
+    int lc_color_grid;
+    int lc_solve_grid, lc_solve_block, lc_solve_ctas;
+    int lc_tasks_grid, lc_tasks_block, lc_tasks_ctas;
+    size_t lc_tasks_smem;
     // learned warm start: for the contacts created this step (arbiter before the colouring
     // permutation, slot), the accumulated impulse after the first substep's iterations
     // is copied to rec_tgt (training targets); rec_on enables it
@@ -257,7 +268,7 @@ void jg_launch_aabb(WorldDev& w, float dt, cudaStream_t s);
 int  jg_launch_broadphase(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_narrowphase(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int tile);
 void jg_launch_merge(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
-void jg_launch_color(WorldDev& w, cudaStream_t s, int nsm);
+int  jg_launch_color(WorldDev& w, cudaStream_t s, int nsm);
 void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 int  jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm);
 void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);

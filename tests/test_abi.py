@@ -107,3 +107,45 @@ def test_heightfield_neighbours_are_symmetric():
         for j in nb:
             if j >= 0:
                 assert i in t["neighbor"][j]
+
+
+JOINT_RECORD_BYTES = 304  # JointDev: a kind/bodies/colour header and 18 float4 rows
+
+
+def state_blob(nb, keys, bodies, joints):
+    """A state blob in the jg_export_state layout: header, body descriptors, arbiters
+    (key, bodies, info, material, 32 contact float4), joint records."""
+    narb, nj = len(keys), len(joints)
+    hdr = np.array([0x4a475331, 1, nb, narb, nj, 16], np.int32).tobytes()
+    b = np.zeros(nb, abi.BODY_DTYPE).tobytes()
+    arb = (np.asarray(keys, np.int32).reshape(-1, 2).tobytes() + np.asarray(bodies, np.int32).reshape(-1, 2).tobytes()
+           + np.zeros((narb, 4), np.int32).tobytes() + np.zeros((narb, 4), np.float32).tobytes()
+           + np.zeros((32, narb, 4), np.float32).tobytes())
+    jr = b""
+    for kind, b1, b2 in joints:
+        rec = np.zeros(JOINT_RECORD_BYTES // 4, np.int32)
+        rec[:4] = (kind, b1, b2, 0)
+        jr += rec.tobytes()
+    return np.frombuffer(hdr + b + arb + jr, np.uint8).copy()
+
+
+def test_state_blob_checks_without_a_device(built_lib):
+    """jg_import_state validates a blob on the host before touching the world: sizes,
+    counts and every arbiter's and constraint's indices."""
+    nb, ns = 4, 5
+    check = lambda blob, n=None: built_lib.jg_check_state(abi.ptr(blob), len(blob) if n is None else n, nb, ns, 16, 16)
+    good = state_blob(nb, [(0, 1), (2, 4)], [(0, 1), (2, 3)], [(abi.CONSTRAINT_BALLSOCKET, 1, 2)])
+    assert check(good) == abi.JG_OK
+    assert check(good, len(good) - 1) == abi.JG_ERR_INVALID_ARG          # truncated
+    assert check(good[:20]) == abi.JG_ERR_INVALID_ARG                    # shorter than the header
+    neg = good.copy()
+    neg[12:16] = np.frombuffer(np.int32(-3).tobytes(), np.uint8)         # negative arbiter count
+    assert check(neg) == abi.JG_ERR_INVALID_ARG
+    assert check(state_blob(nb, [(0, 1)], [(0, 4)], [])) == abi.JG_ERR_INVALID_ARG    # body out of range
+    assert check(state_blob(nb, [(0, 5)], [(0, 1)], [])) == abi.JG_ERR_INVALID_ARG    # shape out of range
+    assert check(state_blob(nb, [(0, 1)], [(-1, 1)], [])) == abi.JG_ERR_INVALID_ARG   # negative body
+    assert check(state_blob(nb, [], [], [(abi.CONSTRAINT_BALLSOCKET, 0, 9)])) == abi.JG_ERR_INVALID_ARG
+    assert check(state_blob(nb, [], [], [(99, 0, 1)])) == abi.JG_ERR_INVALID_ARG       # unknown kind
+    assert check(state_blob(3, [], [], [])) == abi.JG_ERR_INVALID_ARG                   # other body count
+    many = state_blob(nb, [(0, 1)] * 17, [(0, 1)] * 17, [])
+    assert check(many) == abi.JG_ERR_CAPACITY

@@ -85,4 +85,4 @@ def test_batched_worlds_without_joints_hand_off_and_match_the_oracle():
     c = w.counters()
     assert c["status"] == 0 and c["colors"] == 0 and c["task_arbiters"] == c["arbiters"], c
     err = _one_step_velocity_errors(sc, w)
-    assert np.mean(err < 1e-3) > 0.9, (np.mean(err < 1e-3), np.sort(err)[-5:])
+    assert np.mean(err < 1e-3) >= 0.999, (np.mean(err < 1e-3), np.sort(err)[-5:])

@@ -1,10 +1,9 @@
 """jg_collide_pairs (batched NarrowPhase.MprEpa) against the oracle's MprEpa.
 
-Contact normal, depth and points within 1e-4 (relative to max(1, |x|)).  Pairs the MPR
-settles alone (penetration <= the EPA threshold 0.02) run the same FP32 arithmetic on
-both sides; deeper pairs run EPA, whose face data is FP32 on the device and FP64 in the
-oracle (as in the reference's ConvexPolytope), so those are held to the same bound for
-nearly all pairs.
+Contact normal, depth and points within 1e-4 (relative to max(1, |x|)) for at least
+99.9 % of colliding pairs.  Pairs the MPR settles alone (penetration <= the EPA threshold
+0.02) run the same FP32 arithmetic on both sides; deeper pairs run EPA, whose face data is
+FP64 on both sides (as in the reference's ConvexPolytope), so those agree as closely.
 """
 import numpy as np
 import pytest
@@ -75,7 +74,7 @@ def test_collide_pairs_matches_oracle_on_resting_contacts():
     pairs = candidate_pairs(sc, np.random.default_rng(1))
     shallow, deep, errs, _, _ = compare(sc, w, pairs)
     assert shallow.sum() > 300, shallow.sum()
-    assert np.mean(errs[shallow] < 1e-4) > 0.995, np.sort(errs[shallow])[-10:]
+    assert np.mean(errs[shallow] < 1e-4) >= 0.999, np.sort(errs[shallow])[-10:]
 
 
 def test_collide_pairs_matches_oracle_on_deep_overlaps():
@@ -85,10 +84,8 @@ def test_collide_pairs_matches_oracle_on_deep_overlaps():
     w = world_for_scene(sc)
     shallow, deep, errs, pen, op = compare(sc, w, pairs)
     assert deep.sum() > 500, deep.sum()
-    assert np.mean(errs[deep] < 1e-4) > 0.9, (np.mean(errs[deep] < 1e-4), np.sort(errs[deep])[-10:])
-    # where EPA results differ, nearly all still give the same depth within 5%
-    dd = np.abs(pen[deep] - op[deep]) / np.maximum(op[deep], 0.1)
-    assert np.mean(dd < 0.05) > 0.98, (np.mean(dd < 0.05), np.sort(dd)[-10:], op[deep][np.argsort(dd)[-10:]])
+    bad = np.nonzero(deep & (errs >= 1e-4))[0]
+    assert np.mean(errs[deep] < 1e-4) >= 0.999, (np.mean(errs[deep] < 1e-4), [(tuple(pairs[i]), errs[i]) for i in bad[:10]])
 
 
 def test_collide_pairs_rejects_bad_input():

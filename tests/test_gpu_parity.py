@@ -60,7 +60,18 @@ def test_narrowphase_matches_oracle_on_a_pile():
     o.narrowphase()
     oc = o.contacts()
     assert len(gc) > 100 and len(oc) > 100
+    stats = compare_contact_caches(gc, oc)
+    # the same colliding pairs and slots, contact normal and point within 1e-4 (relative)
+    # for at least 99.9 % of contacts
+    assert stats["common_keys"] >= 0.999 * stats["keys"], stats
+    assert stats["slot_mismatch"] <= 0.001 * stats["common_keys"], stats
+    assert stats["normal_ok"] >= 0.999 and stats["point_ok"] >= 0.999, stats
 
+
+def compare_contact_caches(gc, oc):
+    """Contact caches of the GPU and the oracle, matched by (shape1, shape2, slot): pair
+    and slot agreement, and per matched contact the normal error and the local point
+    error relative to max(1, |point|)."""
     def index(rows):
         d = {}
         for r in rows:
@@ -70,21 +81,10 @@ def test_narrowphase_matches_oracle_on_a_pile():
     G, Oo = index(gc), index(oc)
     keys = set(G) | set(Oo)
     common = set(G) & set(Oo)
-    # the same colliding pairs (MPR decisions are the same FP32 arithmetic)
-    assert len(common) >= 0.98 * len(keys), (len(common), len(keys))
-    nrm_err, pt_err = [], []
-    shallow, deep, mis_shallow, mis_deep, details = 0, 0, 0, 0, []
+    nrm_err, pt_err, mismatch = [], [], []
     for k in common:
-        d = o.detect(*k)
-        is_deep = d is not None and d["pen"] > 0.02  # EPA ran: FP32 faces here, FP64 faces in the oracle
-        deep += is_deep
-        shallow += not is_deep
         if set(G[k]) != set(Oo[k]):
-            if is_deep:
-                mis_deep += 1
-            else:
-                mis_shallow += 1
-            details.append((k, sorted(G[k]), sorted(Oo[k]), d["pen"] if d else None))
+            mismatch.append((k, sorted(G[k]), sorted(Oo[k])))
             continue
         for slot, r in G[k].items():
             q = Oo[k][slot]
@@ -92,11 +92,12 @@ def test_narrowphase_matches_oracle_on_a_pile():
             scale = max(1.0, np.abs(q["pos1_local"]).max())
             pt_err.append(np.abs(np.asarray(r["pos1_local"], np.float64) - q["pos1_local"]).max() / scale)
     nrm_err, pt_err = np.array(nrm_err), np.array(pt_err)
-    # contact normal and point within 1e-4 (relative) for nearly all contacts
-    assert np.mean(nrm_err < 1e-4) > 0.97, np.sort(nrm_err)[-10:]
-    assert np.mean(pt_err < 1e-4) > 0.95, np.sort(pt_err)[-10:]
-    assert mis_shallow <= 0.02 * max(shallow, 1), details[:10]
-    assert mis_deep <= 0.25 * max(deep, 1) + 2, details[:10]
+    return {"keys": len(keys), "common_keys": len(common), "slot_mismatch": len(mismatch),
+            "mismatch_examples": mismatch[:5], "contacts": len(nrm_err),
+            "normal_ok": float(np.mean(nrm_err < 1e-4)) if len(nrm_err) else 1.0,
+            "point_ok": float(np.mean(pt_err < 1e-4)) if len(pt_err) else 1.0,
+            "normal_err_max": float(nrm_err.max()) if len(nrm_err) else 0.0,
+            "point_err_max": float(pt_err.max()) if len(pt_err) else 0.0}
 
 
 def _one_step_velocity_errors(sc, w):
@@ -154,11 +155,11 @@ def test_partitioned_schedule_covers_a_wide_pile():
 
 
 def test_one_step_solve_matches_oracle_on_a_pile():
-    # mixed pile: deep contacts run EPA (FP32 faces on the GPU, FP64 in the oracle), which
-    # can change a manifold sample of a few pairs; all other bodies agree within 1e-3
+    # mixed pile with deep contacts (EPA with FP64 face data on both sides): post-solve
+    # velocities within 1e-3 for at least 99.9 % of bodies
     sc, w = _settled_pile(seed=11)
     err = _one_step_velocity_errors(sc, w)
-    assert np.mean(err < 1e-3) > 0.9, (np.mean(err < 1e-3), np.sort(err)[-5:])
+    assert np.mean(err < 1e-3) >= 0.999, (np.mean(err < 1e-3), np.sort(err)[-5:])
 
 
 def test_one_step_solve_with_joints_matches_oracle():
@@ -190,8 +191,8 @@ def test_one_step_solve_with_joints_matches_oracle():
     err = np.maximum(np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1),
                      np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1))
     jerr = np.abs(j1 - o.joint_impulses(len(j1))).max(axis=1) / np.maximum(1.0, np.abs(j1).max(axis=1))
-    assert np.mean(err < 1e-3) > 0.95, (np.mean(err < 1e-3), np.sort(err)[-5:])
-    assert np.mean(jerr < 1e-3) > 0.95, np.sort(jerr)[-5:]
+    assert np.mean(err < 1e-3) >= 0.999, (np.mean(err < 1e-3), np.sort(err)[-5:])
+    assert np.mean(jerr < 1e-3) >= 0.999, np.sort(jerr)[-5:]
 
 
 def test_colours_are_conflict_free():
