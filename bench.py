@@ -49,10 +49,15 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 N_BODIES = 100000
 SETTLE_STEPS = 800
 SEED = 12347
+# Both arms time the same formed pile: whichever arm forms it first stores the body state
+# here, and the other loads it (the driver runs the reference arm first on the same box).
+STATE_CACHE = os.environ.get("JG_BENCH_CACHE", "/tmp/jitter_gb300_bench")
 
-
-SOLVE_DRAM_BYTES = 0.371e9
-MPR_FMA_PIPE_PCT = 33.5
+# Figures from ncu captures (profiles/), labelled with the commit they were taken at:
+# they do not follow later code changes.
+CAPTURE = {"k_solve_tasks_dram_bytes": 0.371e9, "k_mpr_fma_pipe_pct": 33.5,
+           "source": "ncu capture of the 100k pile at commit aaaddb4 (profiles/k_solve_tasks_pile100k.md, "
+                     "profiles/k_mpr_k_epa_pile100k.md); the code has changed since"}
 
 
 def peaks():
@@ -113,6 +118,39 @@ def make_scene(n=N_BODIES):
 # The workload's configurations; c3 (the 100k pile) is the headline line, the others
 # are run with --config for the results table.  Settle steps before timing:
 CONFIG_SETTLE = {"c3": SETTLE_STEPS, "c1": 300, "c2": 600, "c4": 200, "c5": 100}
+
+
+def c3_config(n_bodies, settle):
+    """The workload object both arms print for the 100k pile."""
+    return {"name": "c3", "workload": "mixed pile, %d bodies, 120x200x120 over ground + heightfield, formed in %d "
+                                      "steps; dt 0.01, 4 substeps, (8,4) iterations" % (n_bodies, settle),
+            "bodies": n_bodies, "settle_steps": settle, "parallelism": "replicas only",
+            "l2": "working set above L2 (bodies, contact cache and schedule, several hundred MB); "
+                  "the GPU arm also writes 256 MiB between timed steps"}
+
+
+def state_path(n, settle):
+    return os.path.join(STATE_CACHE, "c3_seed%d_n%d_settle%d.npy" % (SEED, n, settle))
+
+
+def load_state(n, settle):
+    """The formed pile's bodies stored by an earlier arm on this machine, or None."""
+    from jitterphysics2_gb300 import abi
+    p = state_path(n, settle)
+    if not os.path.exists(p):
+        return None
+    b = np.load(p)
+    return b if b.dtype == abi.BODY_DTYPE and len(b) == n + 2 else None
+
+
+def store_state(bodies, n, settle):
+    try:
+        os.makedirs(STATE_CACHE, exist_ok=True)
+        tmp = state_path(n, settle) + ".%d.tmp" % os.getpid()
+        np.save(tmp, bodies)
+        os.replace(tmp + ".npy" if not tmp.endswith(".npy") else tmp, state_path(n, settle))
+    except OSError:
+        pass
 
 
 def config_scene(name, n):
@@ -258,24 +296,29 @@ def reduce_over_ranks(total_ms, contacts, dist, device="cuda"):
 
 
 def run_reference(args):
+    """The CPU arm: the oracle's multithreaded Regular-mode restatement of World.Step on
+    all host threads, on the same formed pile as the GPU arm.  It loads only the oracle
+    library (scene construction and parameters are pure Python)."""
     rank, ws, dist = dist_setup(args.gpus)
     if rank != 0:
         return
     import oracle_lib as O
-    from jitterphysics2_gb300 import abi
     sc = make_scene(args.bodies)
     threads = os.cpu_count() or 1
-    # Settling the pile at the workload's solver settings takes the CPU far longer than
-    # the run allows, so the restatement settles it with 1 substep and 2 iterations (the
-    # pile forms the same way; only the converged detail differs) for up to `settle`
-    # steps or 200 s, then times full-setting steps of that pile.
-    o = O.OracleWorld(sc, substeps=1, solver_iterations=2, relax_iterations=0)
-    t0, settled = time.perf_counter(), 0
-    while settled < args.settle and time.perf_counter() - t0 < 200.0:
-        o.step_mt(sc["dt"], threads)
-        settled += 1
-    full = abi.default_params(**sc["params"])
-    o.fn("jor_world_config")(o.h, ctypes.byref(full))
+    bodies = load_state(args.bodies, args.settle)
+    state = "loaded (formed by the other arm on this machine)"
+    if bodies is None:
+        t0 = time.perf_counter()
+        o = O.OracleWorld(sc)
+        for _ in range(args.settle):
+            o.step_mt(sc["dt"], threads)
+        bodies = o.bodies()
+        store_state(bodies, args.bodies, args.settle)
+        state = "formed here by the CPU restatement in %.0f s" % (time.perf_counter() - t0)
+    else:
+        sc = dict(sc)
+        sc["bodies"] = bodies
+        o = O.OracleWorld(sc)
     for _ in range(args.warmup):
         o.step_mt(sc["dt"], threads)
     total_t, total_c = 0.0, 0
@@ -286,17 +329,15 @@ def run_reference(args):
     line = {"metric": "contacts/s @100k bodies", "value": v, "unit": "contacts/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": "mixed pile, %d bodies, 120x200x120, dt 1/100, 4 substeps, (8,4) iterations"
-                                   % len(sc["bodies"]),
-                       "bodies": len(sc["bodies"]), "settle_steps": settled,
-                       "contacts_per_step": total_c / max(args.steps, 1),
-                       "note": "C++ restatement of Jitter2 (Regular mode, grid broadphase); the C# reference "
-                       "needs a .NET runtime, absent on both machines"},
+            "impl": "reference", "config": c3_config(len(bodies) - 2, args.settle),
+            "contacts_per_step": total_c / max(args.steps, 1), "state": state,
+            "note": "C++ restatement of Jitter2 World.Step (Regular mode, grid broadphase); the C# reference needs "
+                    "a .NET runtime, absent on both machines",
             "cpu_baseline": {"value": v, "unit": "contacts/s", "cores": threads, "kind": "port",
-                             "sample": "%d settle steps (1 substep, 2 iterations), then %d warm-up + %d timed "
-                                       "multithreaded steps at the workload's settings" % (settled, args.warmup, args.steps)},
-            "e2e": {"value": v, "unit": "contacts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": "%d warm-up + %d timed multithreaded steps of the formed pile at the "
+                                       "workload's settings" % (args.warmup, args.steps)},
+            "e2e": {"value": v, "unit": "contacts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
     print(json.dumps(line), flush=True)
 
 
@@ -326,9 +367,27 @@ def main():
     sc, _, workload = config_scene(args.config, args.bodies)
     prm = sc["params"]
     S, I, R = prm.get("substeps", 1), prm.get("solver_iterations", 6), prm.get("relax_iterations", 4)
-    w = world_for_scene(sc)
-    for _ in range(args.settle):
-        w.step(sc["dt"])
+    state = None
+    if args.config == "c3":
+        # the formed pile: from the other arm when it formed it on this machine, else
+        # formed here with the same settings and stored for the other arm
+        bodies = load_state(args.bodies, args.settle) if rank == 0 or ws == 1 else None
+        if bodies is not None:
+            sc = dict(sc)
+            sc["bodies"] = bodies
+            w = world_for_scene(sc)
+            state = "loaded (formed by the other arm on this machine)"
+        else:
+            w = world_for_scene(sc)
+            for _ in range(args.settle):
+                w.step(sc["dt"])
+            if rank == 0:
+                store_state(w.bodies(), args.bodies, args.settle)
+            state = "formed here on the device"
+    else:
+        w = world_for_scene(sc)
+        for _ in range(args.settle):
+            w.step(sc["dt"])
     for _ in range(max(3, args.warmup)):
         w.step(sc["dt"])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -380,28 +439,32 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene)",
-            "config": {"name": args.config,
+            "config": c3_config(nb - 2, args.settle) if args.config == "c3" else
+                      {"name": args.config,
                        "workload": "%s; dt %.5g, %d substeps, (%d,%d) iterations" % (workload % nb if "%d" in workload
                                                                                     else workload, sc["dt"], S, I, R),
                        "bodies": nb, "settle_steps": args.settle, "parallelism": "replicas only",
-                       "l2": "flushed between steps (256 MiB write)",
-                       "contacts_per_step": contacts / args.steps, "arbiters": cnt["arbiters"],
-                       "solver_tasks": cnt["solver_tasks"], "task_colors": cnt["task_colors"]},
+                       "l2": "flushed between steps (256 MiB write)"},
+            "state": state,
+            "contacts_per_step": contacts / args.steps, "arbiters": cnt["arbiters"],
+            "solver_tasks": cnt["solver_tasks"], "task_colors": cnt["task_colors"],
+            "task_arbiters": cnt["task_arbiters"], "remainder_colors": cnt["colors"],
             "body_steps_per_s": nb * args.steps * ws / (total_ms / 1e3),
             "e2e": {"value": e2e_c / e2e_s, "unit": "contacts/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "roofline": {"bound": "hbm", "kernel": "k_solve_tasks", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         # DRAM bytes read + written by one k_solve_tasks launch of the settled
-                         # 100k pile, from an ncu capture of this command (rows stay in L2
-                         # across passes, so DRAM traffic is below the algorithmic bytes)
-                         "traffic": SOLVE_DRAM_BYTES if args.config == "c3" and nb == N_BODIES + 2 else None,
+                         # DRAM bytes read + written by one k_solve_tasks launch of the formed
+                         # 100k pile, from an ncu capture (rows stay in L2 across passes, so
+                         # DRAM traffic is below the algorithmic bytes)
+                         "traffic": CAPTURE["k_solve_tasks_dram_bytes"] if args.config == "c3" and nb == N_BODIES + 2
+                         else None, "traffic_source": CAPTURE["source"],
                          "solve_ms_per_step": float(np.mean(solve_ms)),
                          "bytes_model": "S*((I+R)*276*C + 320*C + 116*N) + 52*N"},
             # the narrowphase is bound by the FP32 pipe, not HBM: FMA-pipe cycles active of the
             # MPR kernel from an ncu capture of this workload
-            "narrowphase": {"bound": "fp32 pipe", "kernel": "k_mpr", "fma_pipe_active_pct": MPR_FMA_PIPE_PCT,
-                            "ms_per_step": stage_ms["narrowphase"]}
+            "narrowphase": {"bound": "fp32 pipe", "kernel": "k_mpr", "fma_pipe_active_pct": CAPTURE["k_mpr_fma_pipe_pct"],
+                            "fma_source": CAPTURE["source"], "ms_per_step": stage_ms["narrowphase"]}
             if args.config == "c3" and nb == N_BODIES + 2 else None,
             "clocks": clk, "gpu_launches": launches,
             "stage_ms": stage_ms}

@@ -169,6 +169,27 @@ def ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
+# The values jg_default_params writes (a freshly constructed World, World.cs:333-416,
+# World.Detect.cs:88-122), for callers that fill a jg_world_params without loading the
+# library (the CPU oracle and the reference arm of the benchmark).
+PARAM_DEFAULTS = dict(gravity=(0.0, -9.81, 0.0), substeps=1, solver_iterations=6, relax_iterations=4,
+                      enable_auxiliary_contacts=1, persistent_manifold=1, speculative_relaxation=0.9,
+                      speculative_threshold=10.0, edge_filter=1, warm_start_mode=1, narrow_tile=32,
+                      partitioned_solve=1)
+
+
+def params_struct(**kw):
+    """A jg_world_params with the defaults of jg_default_params and the given fields,
+    built without loading libjitter_gpu.so."""
+    p = WorldParams()
+    for k, v in dict(PARAM_DEFAULTS, **kw).items():
+        if k == "gravity":
+            p.gravity[0], p.gravity[1], p.gravity[2] = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
 def default_params(**kw):
     p = WorldParams()
     load().jg_default_params(ctypes.byref(p))

@@ -409,13 +409,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
             atomicMax(&w.ctr->task_colors, nc);
         }
         __syncthreads();
+        // body slots packed with the arbiter's rank among its body's arbiters in colour
+        // order (the colours a body's arbiters take are distinct, so the rank is the number
+        // of the body's colours below this one): slot | rank << 16, -1 for a non-dynamic body
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             int c = s_col[i];
             int p = atomicAdd(&s_cur[c], 1);
             int a = s_a[i];
+            const unsigned long long below = (1ull << c) - 1ull;
+            int l1 = s_l1[i], l2 = s_l2[i];
+            int p1 = l1 >= 0 ? (l1 | __popcll(s_mask[l1] & below) << 16) : -1;
+            int p2 = l2 >= 0 ? (l2 | __popcll(s_mask[l2] & below) << 16) : -1;
             w.sc_dst[a] = T.x + p;
             w.sc_lcol[a] = g * 256 + c;
-            w.sc_ls[a] = make_int4(s_l1[i], s_l2[i], g, 0);
+            w.sc_ls[a] = make_int4(p1, p2, g, 0);
         }
         __syncthreads();
     }

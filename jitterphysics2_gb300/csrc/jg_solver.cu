@@ -386,16 +386,48 @@ __device__ __forceinline__ LBody fixed_body(float4 v, float4 wv) {
 
 enum { PASS_PREPARE = 0, PASS_ITERATE = 1, PASS_RELAX = 2 };
 
-// Iterate / relax colours of one task (its bodies already staged or in flight).
+// Order inside a task.  sver[slot] (shared memory) counts the task arbiters on that body
+// finished in the current pass.  A task arbiter carries, per dynamic body, the body's slot
+// and its rank among the body's arbiters in colour order (slot | rank << 16, -1 for a
+// non-dynamic body); it runs once each body's count equals its rank, then raises it.  So
+// every body sees its arbiters in colour order, the order a block barrier between colours
+// gives, and the results are the same bits, but an arbiter waits only for the earlier
+// arbiters on its own two bodies.
+__device__ __forceinline__ int slot_of(int packed) { return packed & 0xffff; }
+__device__ __forceinline__ int rank_of(int packed) { return packed >> 16; }
+__device__ __forceinline__ bool deps_ready(const volatile int* sver, int p1, int p2) {
+    return (p1 < 0 || sver[slot_of(p1)] == rank_of(p1)) && (p2 < 0 || sver[slot_of(p2)] == rank_of(p2));
+}
+__device__ __forceinline__ void deps_release(volatile int* sver, int p1, int p2) {
+    __threadfence_block();  // the bodies' new velocities before the counts
+    if (p1 >= 0) sver[slot_of(p1)] = rank_of(p1) + 1;
+    if (p2 >= 0) sver[slot_of(p2)] = rank_of(p2) + 1;
+}
+// A warp that could run none of its lanes' arbiters backs off; after about 2^20 such
+// rounds (far beyond any legitimate wait) the task is abandoned with JG_ERR_TIMEOUT.
+__device__ __forceinline__ bool backoff(unsigned& idle, volatile int* abort_flag, int* status) {
+    if (*abort_flag) return false;
+    if (++idle > (1u << 20)) {
+        *abort_flag = 1;
+        atomicCAS(status, 0, JG_ERR_TIMEOUT);
+        return false;
+    }
+    __nanosleep(idle < 8 ? 16 : 64);
+    return true;
+}
+
+// Iterate / relax pass of one task (its bodies already staged or in flight).  Returns
+// false when the task was abandoned.
 template <bool kResid>
-__device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStore& A, int4 T, int nc, const int* tc,
-                                                bool bias, float4* sbody, int sst, float4* ring, float& d2, float& l2) {
+__device__ __forceinline__ bool iterate_task(const WorldDev& w, const ArbStore& A, int4 T, bool bias, float4* sbody,
+                                             int sst, float4* ring, volatile int* sver, volatile int* abort_flag,
+                                             int* status, float& d2, float& l2) {
     const int cap = w.cap_arb, bs = blockDim.x, tid = threadIdx.x;
-    // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order),
-    // so consecutive colours are spread over different threads.  Each thread keeps
-    // its next JG_TASK_RING arbiters in flight (one cp.async group per arbiter, empty
-    // groups past the end keep the count uniform): the ring holds bs * JG_TASK_RING
-    // arbiters, several colours ahead of the one being solved.
+    // Thread tid owns the task's arbiters tid, tid + bs, tid + 2 bs, ... (colour order)
+    // and runs them in that order.  Each thread keeps its next JG_TASK_RING arbiters in
+    // flight (one cp.async group per arbiter, empty groups past the end keep the count
+    // uniform).  Every wait is on an arbiter of a smaller index, whose owner runs its
+    // arbiters in order too, so the smallest unfinished arbiter can always run.
     const int n = T.y;
     for (int m = 0; m < JG_TASK_RING; m++) {
         int j = m * bs + tid;
@@ -403,20 +435,30 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
         cp_async_commit();
     }
     cp_async_wait_bodies();  // this thread's body copies have landed
-    __syncthreads();         // ... and everyone's
-    int m = 0;  // next owned arbiter: j = m * bs + tid
-    for (int c = 0; c < nc; c++) {
-        const int cend = tc[c + 1];
-        for (; m * bs + tid < cend; m++) {
-            const int j = m * bs + tid, d = T.x + j;
-            float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
+    __syncthreads();         // ... and everyone's, with the zeroed counts
+    int m = 0;               // next owned arbiter: j = m * bs + tid
+    unsigned idle = 0;
+    for (;;) {
+        const int j = m * bs + tid;
+        const bool active = j < n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        float4* r = ring + ((size_t)(m % JG_TASK_RING) * bs + tid) * JG_TASK_STAGE_F4;
+        bool go = false;
+        float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (active) {
+            cp_async_wait_ring();
+            r0 = r[0];
+            go = deps_ready(sver, __float_as_int(r0.x), __float_as_int(r0.y));
+        }
+        if (go) {
+            __threadfence_block();  // the counts before the bodies they guard
+            const int d = T.x + j;
             // header word of the arbiter this slot is refilled with, loaded now and used
             // after the compute below, so its latency stays off the critical path
             const int jn = j + JG_TASK_RING * bs;
             const int un = jn < n ? __ldg(&A.lslot[T.x + jn].z) : 0;
-            cp_async_wait_ring();
-            const float4 r0 = r[0];
-            const int l1 = __float_as_int(r0.x), l2s = __float_as_int(r0.y), hz = __float_as_int(r0.z);
+            const int p1 = __float_as_int(r0.x), p2 = __float_as_int(r0.y), hz = __float_as_int(r0.z);
+            const int l1 = p1 >= 0 ? slot_of(p1) : -1, l2s = p2 >= 0 ? slot_of(p2) : -1;
             const int usage = hz & 15, mode = (hz >> 4) & 15;
             const float fr = r0.w;
             LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[1], r[2]);
@@ -431,27 +473,74 @@ __device__ __forceinline__ void iterate_colours(const WorldDev& w, const ArbStor
             }
             if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);
             if ((mode & 12) && l2s >= 0) sbody_store(sbody, l2s, sst, b2);
+            deps_release(sver, p1, p2);
             // refill the slot just consumed (its values are in registers by now)
             if (jn < n) stage_arbiter(r, A, T.x + jn, cap, un);
             cp_async_commit();
+            m++;
         }
-        __syncthreads();
+        if (__any_sync(0xffffffffu, go)) idle = 0;
+        else if (!backoff(idle, abort_flag, status)) return false;
     }
+    return true;
 }
 
-// One task in one pass: bodies staged into shared memory, colours in order with a block
-// barrier between them, bodies written back.  Iterations stage each (colour, chunk) step's
-// rows with cp.async while the previous step computes.
-__device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind,
-                                         float4* sbody, float4* ring, int* tc, float& d2, float& l2) {
+// Prepare pass of one task (bodies, positions and orientations staged).
+__device__ __forceinline__ bool prepare_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int4 T,
+                                             float4* sbody, int sst, const float4* spos, const float4* sq, bool staged,
+                                             volatile int* sver, volatile int* abort_flag, int* status) {
+    const int cap = w.cap_arb, bs = blockDim.x, tid = threadIdx.x;
+    int m = 0;
+    unsigned idle = 0;
+    int4 ls = make_int4(-1, -1, 0, 0);
+    int loaded = -1;
+    for (;;) {
+        const int j = m * bs + tid;
+        const bool active = j < T.y;
+        if (!__any_sync(0xffffffffu, active)) break;
+        const int d = T.x + j;
+        bool go = false;
+        if (active) {
+            if (loaded != m) { ls = A.lslot[d]; loaded = m; }
+            go = deps_ready(sver, ls.x, ls.y);
+        }
+        if (go) {
+            __threadfence_block();
+            int4 info = A.info[d];
+            int usage = info.x & 15, mode = info.y;
+            int2 bb = A.body[d];
+            const int l1 = ls.x >= 0 ? slot_of(ls.x) : -1, l2 = ls.y >= 0 ? slot_of(ls.y) : -1;
+            LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
+            LBody b2 = l2 >= 0 ? sbody_load(sbody, l2, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
+            float spec = A.mat[d].z;
+            const bool s1 = staged && l1 >= 0, s2 = staged && l2 >= 0;
+            v3 pos1 = mk3(s1 ? spos[l1] : w.pos[bb.x]), pos2 = mk3(s2 ? spos[l2] : w.pos[bb.y]);
+            q4 q1 = mkq(s1 ? sq[l1] : w.q[bb.x]), q2 = mkq(s2 ? sq[l2] : w.q[bb.y]);
+            for (int k = 0; k < 4; k++)
+                if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
+            if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);
+            if ((mode & 12) && l2 >= 0) sbody_store(sbody, l2, sst, b2);
+            deps_release(sver, ls.x, ls.y);
+            m++;
+        }
+        if (__any_sync(0xffffffffu, go)) idle = 0;
+        else if (!backoff(idle, abort_flag, status)) return false;
+    }
+    return true;
+}
+
+// One task in one pass: bodies staged into shared memory, arbiters in per-body colour
+// order, bodies written back.  Iterations stage each thread's next arbiter's rows with
+// cp.async while the current one computes.  Returns false when the task was abandoned
+// (JG_ERR_TIMEOUT recorded).
+__device__ __forceinline__ bool run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind,
+                                         float4* sbody, float4* ring, volatile int* sver, volatile int* abort_flag,
+                                         float& d2, float& l2) {
     const int4 T = w.sc_task[t];
-    const int nc = w.sc_tnc[t];
-    const int cap = w.cap_arb;
     const int bs = blockDim.x, tid = threadIdx.x;
     const int sst = sp.task_maxb;  // stride of the staged body arrays
-    // the task's colour boundaries, read once into shared memory (visible after the
-    // barrier that follows the body staging)
-    for (int c = tid; c <= nc; c += bs) tc[c] = w.sc_tcol[t * (JG_TASK_MAXC + 1) + c];
+    int* status = &w.ctr->status;
+    for (int i = tid; i < T.w; i += bs) sver[i] = 0;
     // the task's bodies, one cp.async group per thread (the arbiter ring, in iterations,
     // follows as later groups so that both loads are in flight together)
     for (int i = tid; i < T.w; i += bs) {
@@ -462,6 +551,7 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
     // (the bodies' group: committed with the positions below in Prepare, here otherwise,
     // so that the arbiter ring of the iterations follows as later groups)
     if (kind != PASS_PREPARE) cp_async_commit();
+    bool ok = true;
     if (kind == PASS_PREPARE) {
         // Prepare also needs the bodies' positions and orientations: staged into the
         // arbiter ring, which Prepare does not use, when they fit
@@ -477,31 +567,12 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
         cp_async_commit();
         cp_async_wait_0();
         __syncthreads();
-        for (int c = 0; c < nc; c++) {
-            for (int j = tc[c] + tid; j < tc[c + 1]; j += bs) {
-                int d = T.x + j;
-                int4 info = A.info[d];
-                int usage = info.x & 15, mode = info.y;
-                int4 ls = A.lslot[d];
-                int2 bb = A.body[d];
-                LBody b1 = ls.x >= 0 ? sbody_load(sbody, ls.x, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
-                LBody b2 = ls.y >= 0 ? sbody_load(sbody, ls.y, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
-                float spec = A.mat[d].z;
-                const bool s1 = staged && ls.x >= 0, s2 = staged && ls.y >= 0;
-                v3 pos1 = mk3(s1 ? spos[ls.x] : w.pos[bb.x]), pos2 = mk3(s2 ? spos[ls.y] : w.pos[bb.y]);
-                q4 q1 = mkq(s1 ? sq[ls.x] : w.q[bb.x]), q2 = mkq(s2 ? sq[ls.y] : w.q[bb.y]);
-                for (int k = 0; k < 4; k++)
-                    if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
-                if ((mode & 3) && ls.x >= 0) sbody_store(sbody, ls.x, sst, b1);
-                if ((mode & 12) && ls.y >= 0) sbody_store(sbody, ls.y, sst, b2);
-            }
-            __syncthreads();
-        }
-    } else if (nc > 0) {
+        ok = prepare_task(w, A, sp, T, sbody, sst, spos, sq, staged, sver, abort_flag, status);
+    } else if (T.y > 0) {
         if (sp.record_residual)
-            iterate_colours<true>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, sst, ring, d2, l2);
+            ok = iterate_task<true>(w, A, T, kind == PASS_ITERATE, sbody, sst, ring, sver, abort_flag, status, d2, l2);
         else
-            iterate_colours<false>(w, A, T, nc, tc, kind == PASS_ITERATE, sbody, sst, ring, d2, l2);
+            ok = iterate_task<false>(w, A, T, kind == PASS_ITERATE, sbody, sst, ring, sver, abort_flag, status, d2, l2);
     }
     cp_async_wait_0();  // no copy into shared memory outlives the task
     __syncthreads();
@@ -511,6 +582,7 @@ __device__ __forceinline__ void run_task(const WorldDev& w, const ArbStore& A, c
         dst[1] = sbody[sst + i];
     }
     __syncthreads();
+    return ok && !*abort_flag;
 }
 
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
@@ -566,7 +638,10 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     extern __shared__ float4 solve_smem[];
     float4* sbody = solve_smem;
     float4* ring = solve_smem + 4 * sp.task_maxb;
-    __shared__ int s_tc[JG_TASK_MAXC + 1];
+    volatile int* sver = (volatile int*)(ring + (size_t)JG_TASK_RING * blockDim.x * JG_TASK_STAGE_F4);
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) s_abort = 0;
+    __syncthreads();
     const ArbStore& A = w.arb[w.cur];
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int* status = &w.ctr->status;
@@ -592,7 +667,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
                 for (int g = 0; g < JG_SCHED_GRIDS; g++, level++) {
                     for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x) {
                         if (!wait_deps(w, t, level, status)) return;
-                        run_task(w, A, sp, t, kind, sbody, ring, s_tc, d2, l2);
+                        if (!run_task(w, A, sp, t, kind, sbody, ring, sver, &s_abort, d2, l2)) return;
                         if (threadIdx.x == 0) {  // run_task ended with a block barrier
                             __threadfence();
                             st_release_u32(&w.sc_done[t], level + 1);
@@ -624,7 +699,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
             for (int g = 0; g < JG_SCHED_GRIDS; g++) {
                 if (ntask[g] == 0) continue;
                 for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x)
-                    run_task(w, A, sp, t, kind, sbody, ring, s_tc, d2, l2);
+                    if (!run_task(w, A, sp, t, kind, sbody, ring, sver, &s_abort, d2, l2)) return;
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }
             if (!remainder_pass(w, A, sp, pass == 0 ? 0 : 1, !relax, !relax, tid, nth, d2, l2)) return;
@@ -735,13 +810,13 @@ int jg_solver_task_maxb(int block, int ctas_per_sm) {
     if (ctas_per_sm < 1) ctas_per_sm = 1;
     long long avail = std::min<long long>(pb, psm / ctas_per_sm - 1024);
     long long ring = (long long)JG_TASK_RING * block * JG_TASK_STAGE_F4 * 16;
-    long long m = (avail - ring - (JG_TASK_MAXC + 1) * 4 - 256) / 64;  // minus the static shared memory
+    long long m = (avail - ring - 256) / 68;  // 64 B of staged body and a 4 B order count per slot
     if (m > 4096) m = 4096;
     return m > 0 ? (int)m : 0;
 }
 
 static size_t task_smem(const StepParams& p, int block) {
-    return ((size_t)4 * p.task_maxb + (size_t)JG_TASK_RING * block * JG_TASK_STAGE_F4) * 16;
+    return ((size_t)4 * p.task_maxb + (size_t)JG_TASK_RING * block * JG_TASK_STAGE_F4) * 16 + (size_t)4 * p.task_maxb;
 }
 
 // The cooperative grid of each solve kernel is sized once per world (its device, block,

@@ -17,7 +17,7 @@ world and the CPU oracle.
 """
 import numpy as np
 
-from . import abi
+from . import abi, massprops
 
 GROUND_FLAGS = abi.BODY_ACTIVE
 
@@ -51,7 +51,7 @@ def inverse_sym(I6):
 def set_mass(bodies, shapes, hull, body_index, shape_index, mass=None):
     """RigidBody.SetMassInertia() / SetMassInertia(mass) (RigidBody.cs:1575-1633) for a
     body with one shape."""
-    I6, com, m = abi.mass_inertia(shapes[shape_index], hull)
+    I6, com, m = mass_inertia(shapes[shape_index], hull)
     inv = inverse_sym(I6)
     inv_mass = 1.0 / m
     if mass is not None:
@@ -160,21 +160,38 @@ def _mixed_shapes(rng, n, hull_list, hull_base):
     return recs
 
 
+def mass_inertia(rec, hull=None):
+    """(inertia6, centre, mass) of one shape record: CalculateMassInertia of its shape at
+    density 1 (jitterphysics2_gb300.massprops)."""
+    if rec["kind"] == abi.SHAPE_POINTCLOUD:
+        o, n = int(rec["data_offset"]), int(rec["data_count"])
+        I6, com, m = massprops.hull_mass_properties(np.asarray(hull, np.float32)[None, o:o + n], rec["dims"][:3])
+        return I6[0], com[0], m[0]
+    return massprops.analytic_mass_properties(int(rec["kind"]), rec["dims"])
+
+
 def _finish_mass(bodies, shapes, hull, first_body, first_shape, count):
+    """RigidBody.SetMassInertia() of bodies with one shape each (density 1); point-cloud
+    shapes also get their centre of mass (GetCenter)."""
     cache = {}
-    for i in range(count):
-        bi, si = first_body + i, first_shape + i
-        rec = shapes[si]
-        key = (int(rec["kind"]), tuple(np.round(rec["dims"], 7)), int(rec["data_offset"])) if rec["kind"] == abi.SHAPE_POINTCLOUD else \
-              (int(rec["kind"]), tuple(rec["dims"].tolist()))
+    recs = shapes[first_shape:first_shape + count]
+    clouds = np.nonzero(recs["kind"] == abi.SHAPE_POINTCLOUD)[0]
+    if len(clouds):
+        counts = recs["data_count"][clouds]
+        assert (counts == counts[0]).all(), "point clouds of one scene share a vertex count"
+        idx = recs["data_offset"][clouds][:, None] + np.arange(counts[0])[None, :]
+        I6, com, m = massprops.hull_mass_properties(np.asarray(hull, np.float32)[idx])
+        for j, i in enumerate(clouds):
+            bodies["inv_inertia"][first_body + i] = inverse_sym(I6[j])
+            bodies["inv_mass"][first_body + i] = 1.0 / m[j]
+            shapes["center"][first_shape + i] = com[j]
+    for i in np.nonzero(recs["kind"] != abi.SHAPE_POINTCLOUD)[0]:
+        rec = recs[i]
+        key = (int(rec["kind"]), tuple(rec["dims"].tolist()))
         if key not in cache:
-            I6, com, m = abi.mass_inertia(rec, hull)
-            cache[key] = (inverse_sym(I6), 1.0 / m, com)
-        inv, im, com = cache[key]
-        bodies["inv_inertia"][bi] = inv
-        bodies["inv_mass"][bi] = im
-        if rec["kind"] == abi.SHAPE_POINTCLOUD:
-            shapes["center"][si] = com
+            I6, com, m = massprops.analytic_mass_properties(int(rec["kind"]), rec["dims"])
+            cache[key] = (inverse_sym(I6), 1.0 / m)
+        bodies["inv_inertia"][first_body + i], bodies["inv_mass"][first_body + i] = cache[key]
 
 
 def mixed_pile(n=20000, box=(60.0, 120.0, 60.0), y0=2.0, seed=12346, cells=64, amplitude=2.0, friction=0.6,

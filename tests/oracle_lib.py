@@ -186,7 +186,7 @@ class OracleWorld:
         self.h = getattr(self.lib, "jor_world_create_" + real)()
         prm = dict(scene.get("params", {}))
         prm.update(params)
-        wp = abi.default_params(**prm)
+        wp = abi.params_struct(**prm)
         getattr(self.lib, "jor_world_config_" + real)(self.h, ctypes.byref(wp))
         self.n = len(scene["bodies"])
         b = np.ascontiguousarray(scene["bodies"], abi.BODY_DTYPE)

@@ -51,6 +51,40 @@ def test_default_params_match_world_defaults(built_lib):
     assert p.speculative_threshold == pytest.approx(10.0)
 
 
+def test_python_params_equal_the_library_defaults(built_lib):
+    # the oracle and the benchmark's reference arm fill jg_world_params without the library
+    a, b = abi.default_params(), abi.params_struct()
+    for name, _ in abi.WorldParams._fields_:
+        va, vb = getattr(a, name), getattr(b, name)
+        if name == "gravity":
+            va, vb = tuple(va), tuple(vb)
+        assert va == vb, name
+
+
+def test_scene_mass_properties_agree_with_the_library(built_lib):
+    # scenes take their mass properties from numpy (massprops); the C ABI's host utility
+    # evaluates the same formulas: analytic shapes bit for bit, point clouds to summation order
+    from jitterphysics2_gb300 import massprops
+    rng = np.random.default_rng(3)
+    for kind in (abi.SHAPE_BOX, abi.SHAPE_SPHERE, abi.SHAPE_CAPSULE, abi.SHAPE_CYLINDER, abi.SHAPE_CONE):
+        for _ in range(20):
+            rec = np.zeros(1, abi.SHAPE_DTYPE)
+            rec["kind"] = kind
+            rec["dims"][0, :3] = rng.uniform(0.2, 1.5, 3)
+            I6, com, m = abi.mass_inertia(rec[0])
+            J6, com2, m2 = massprops.analytic_mass_properties(kind, rec["dims"][0])
+            assert np.array_equal(I6, J6) and np.float32(m) == m2
+    pts = rng.normal(size=(40, 32, 3))
+    pts = (pts / np.linalg.norm(pts, axis=2, keepdims=True) * rng.uniform(0.5, 1.5, (40, 1, 1))).astype(np.float32)
+    J6, com2, m2 = massprops.hull_mass_properties(pts)
+    for h in range(40):
+        rec = np.zeros(1, abi.SHAPE_DTYPE)
+        rec["kind"], rec["data_count"] = abi.SHAPE_POINTCLOUD, 32
+        I6, com, m = abi.mass_inertia(rec[0], pts[h])
+        assert np.allclose(I6, J6[h], rtol=1e-6, atol=1e-7) and np.allclose(com, com2[h], atol=1e-6)
+        assert abs(m - m2[h]) <= 1e-6 * m
+
+
 def test_invalid_arguments_are_rejected_without_a_device(built_lib):
     assert built_lib.jg_create(None, None) == abi.JG_ERR_INVALID_ARG
     assert built_lib.jg_step(None, ctypes.c_float(0.01)) == abi.JG_ERR_INVALID_ARG
