@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
     int* s_l2 = s_l1 + JG_TASK_MAXA;                                // [MAXA]
     int* s_a = s_l2 + JG_TASK_MAXA;                                 // [MAXA]
     unsigned char* s_col = (unsigned char*)(s_a + JG_TASK_MAXA);    // [MAXA]
-    __shared__ int s_cnt[JG_TASK_MAXC + 1], s_cur[JG_TASK_MAXC + 1];
+    __shared__ int s_cnt[JG_TASK_MAXC + 1], s_cur[4 * JG_TASK_MAXC];
     const ArbStore& A = w.arb[w.cur];
     const SchedInfo* S = w.sc;
     const int cb = w.cap_bodies;
@@ -322,7 +322,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
         const int n = T.y, nb = T.w;
         const int g = t >= S->task_base[2] && S->ntask[2] ? 2 : (t >= S->task_base[1] && S->ntask[1] ? 1 : 0);
         for (int i = threadIdx.x; i < nb; i += blockDim.x) { s_mask[i] = 0ull; s_own[i] = 0ull; s_deg[i] = 0; }
-        for (int i = threadIdx.x; i <= JG_TASK_MAXC; i += blockDim.x) { s_cnt[i] = 0; s_cur[i] = 0; }
+        for (int i = threadIdx.x; i <= JG_TASK_MAXC; i += blockDim.x) s_cnt[i] = 0;
+        for (int i = threadIdx.x; i < 4 * JG_TASK_MAXC; i += blockDim.x) s_cur[i] = 0;
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             int a = w.sc_tlist[T.x + i];
@@ -387,20 +388,29 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
             todo &= ~won;
             left = __syncthreads_count(todo != 0) ? 1 : 0;
         }
-        // colour counts, offsets, placement
+        // colour counts, offsets, placement.  Inside a colour the arbiters with more
+        // contacts come first, so that the lanes of a warp mostly run the same number of
+        // contact rows (any order inside a colour is the same solve).
+        auto bucket = [&](int i) {
+            int pc = __popc(A.info[s_a[i]].x & 15);
+            return 4 * s_col[i] + (pc >= 4 ? 0 : (pc <= 1 ? 3 : 4 - pc));
+        };
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             if (s_col[i] >= JG_TASK_MAXC) { s_col[i] = JG_TASK_MAXC - 1; atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); }
             atomicAdd(&s_cnt[s_col[i]], 1);
+            atomicAdd(&s_cur[bucket(i)], 1);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             int acc = 0, nc = 0;
             for (int c = 0; c < JG_TASK_MAXC; c++) {
-                int k = s_cnt[c];
-                if (k) nc = c + 1;
-                s_cur[c] = acc;
+                if (s_cnt[c]) nc = c + 1;
                 w.sc_tcol[t * (JG_TASK_MAXC + 1) + c] = acc;
-                acc += k;
+                for (int q = 0; q < 4; q++) {
+                    int kq = s_cur[4 * c + q];
+                    s_cur[4 * c + q] = acc;
+                    acc += kq;
+                }
             }
             w.sc_tcol[t * (JG_TASK_MAXC + 1) + JG_TASK_MAXC] = acc;
             for (int c = nc; c <= JG_TASK_MAXC; c++) w.sc_tcol[t * (JG_TASK_MAXC + 1) + c] = acc;
@@ -414,7 +424,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_task_color(WorldDev w, StepParam
         // of the body's colours below this one): slot | rank << 16, -1 for a non-dynamic body
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             int c = s_col[i];
-            int p = atomicAdd(&s_cur[c], 1);
+            int p = atomicAdd(&s_cur[bucket(i)], 1);
             int a = s_a[i];
             const unsigned long long below = (1ull << c) - 1ull;
             int l1 = s_l1[i], l2 = s_l2[i];
