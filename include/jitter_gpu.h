@@ -280,6 +280,22 @@ int jg_collide_pairs(jg_world* world, const int32_t* shape_pairs, int32_t count,
 int jg_collide_pairs_noalloc(jg_world* world, const int32_t* shape_pairs, int32_t count,
                              float* results, int32_t* hits);
 
+/* CollisionManifold.BuildManifold (CollisionManifold.cs:393-566) on the world's shapes at
+ * the bodies' current poses, for given witness points: points holds 9 floats per pair
+ * (pointA, pointB, normal, world frame, as NarrowPhase.MprEpa returns them); out receives
+ * 24 floats per pair (up to four point pairs, A xyz then B xyz) and counts the number of
+ * pairs (ManifoldCount).  The step's manifold stage runs the same device function.  Host
+ * buffers; synchronous; allocates its device buffers for the call. */
+int jg_manifold_pairs(jg_world* world, const int32_t* shape_pairs, int32_t count, const float* points,
+                      float* results, int32_t* counts);
+
+/* The broadphase pair list of the last step (DynamicTree.EnumerateOverlaps with the
+ * default filter, DynamicTree.cs:266-286, World.cs:447-455): every shape pair with
+ * non-disjoint world bounding boxes, on different bodies, at least one active and one
+ * dynamic, as 2 shape indices per pair in no particular order.  Writes up to capacity
+ * pairs; *out_count receives the number of pairs. */
+int jg_get_pairs(jg_world* world, int32_t* pairs, int32_t capacity, int32_t* out_count);
+
 /* Arbiter/ContactData view (World.RawData, World.cs:95-141).  Writes up to capacity
  * entries; *out_count receives the number of active contact points. */
 int jg_get_contacts(jg_world* world, jg_contact_view* out, int32_t capacity, int32_t* out_count);

@@ -108,6 +108,8 @@ SIGNATURES = {
     "jg_step_host": (_I, [_P, _F, _P, _I]),
     "jg_collide_pairs": (_I, [_P, _P, _I, _P, _P]),
     "jg_collide_pairs_noalloc": (_I, [_P, _P, _I, _P, _P]),
+    "jg_manifold_pairs": (_I, [_P, _P, _I, _P, _P, _P]),
+    "jg_get_pairs": (_I, [_P, _P, _I, _PI]),
     "jg_get_contacts": (_I, [_P, _P, _I, _PI]),
     "jg_get_arbiter_events": (_I, [_P, _P, _I, _PI, _P, _I, _PI]),
     "jg_get_constraints": (_I, [_P, _P, _P, _I, _PI]),

@@ -25,6 +25,8 @@ void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float thresh
                              cudaStream_t s, int nsm);
 int jg_schedule_launches(const StepParams& p);
 int jg_narrowphase_init();
+void jg_launch_manifold_query(WorldDev& w, const int2* pairs, int n, const float* in, float* out, int* count,
+                              cudaStream_t s, int nsm);
 
 static thread_local std::string g_err;
 
@@ -904,6 +906,41 @@ int jg_collide_pairs_noalloc(jg_world* w, const int32_t* pairs, int32_t n, float
         base = (unsigned char*)g_collide_scratch_addr[dev];
     }
     return run_query(w, pairs, n, out, hit, (int2*)(base + kNaPairs), (float*)(base + kNaOut), (int*)(base + kNaHit));
+}
+
+int jg_manifold_pairs(jg_world* w, const int32_t* pairs, int32_t n, const float* points, float* out, int32_t* counts) {
+    int r = check_query_args("jg_manifold_pairs", w, pairs, n, out, counts);
+    if (r || n == 0) return r;
+    if (!points) { g_err = "jg_manifold_pairs: null points"; return JG_ERR_INVALID_ARG; }
+    int2* d_pairs = nullptr;
+    float *d_in = nullptr, *d_out = nullptr;
+    int* d_cnt = nullptr;
+    cudaStream_t s = w->stream;
+    cudaError_t e = cudaMalloc((void**)&d_pairs, sizeof(int2) * n);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_in, sizeof(float) * 9 * n);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, sizeof(float) * 24 * n);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_cnt, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pairs, pairs, sizeof(int2) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, points, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        jg_launch_manifold_query(w->d, d_pairs, n, d_in, d_out, d_cnt, s, w->nsm);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(float) * 24 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_pairs); cudaFree(d_in); cudaFree(d_out); cudaFree(d_cnt);
+    return e == cudaSuccess ? JG_OK : cuda_fail(e, "jg_manifold_pairs");
+}
+
+int jg_get_pairs(jg_world* w, int32_t* out, int32_t cap, int32_t* count) {
+    if (!w || !count || cap < 0 || (cap > 0 && !out)) return JG_ERR_INVALID_ARG;
+    int n = 0;
+    CK(cudaMemcpy(&n, &w->d.ctr->npairs, sizeof(int), cudaMemcpyDeviceToHost));
+    n = std::min(n, w->d.cap_pairs);
+    *count = n;
+    if (cap > 0 && n > 0) CK(cudaMemcpy(out, w->d.pairs, sizeof(int2) * std::min(n, cap), cudaMemcpyDeviceToHost));
+    return JG_OK;
 }
 
 int jg_get_contacts(jg_world* w, jg_contact_view* out, int32_t cap, int32_t* count) {

@@ -1600,6 +1600,32 @@ __global__ void __launch_bounds__(NP_WARPS * 32) k_collide_query(WorldDev w, con
     }
 }
 
+// Batched CollisionManifold.BuildManifold (CollisionManifold.cs:393-566) for given witness
+// points, one thread per pair, the same function the step's manifold stage runs.  in holds
+// 9 floats per pair (pointA, pointB, normal, world frame); out receives 24 floats per pair
+// (up to four point pairs A, B) and count the number of pairs.
+__global__ void __launch_bounds__(128) k_manifold_query(WorldDev w, const int2* pairs, int n, const float* in, float* out,
+                                                        int* count) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int2 pr = pairs[i];
+        ShapeRef sa = load_shape(w, pr.x), sb = load_shape(w, pr.y);
+        int b1 = w.sinfo[pr.x].y, b2 = w.sinfo[pr.y].y;
+        q4 qa = mkq(w.q[b1]), qb = mkq(w.q[b2]);
+        v3 pa = mk3(w.pos[b1]), pb = mk3(w.pos[b2]);
+        const float* c = in + 9 * (size_t)i;
+        float4 oA[4], oB[4];
+        int cnt = manifold_thread(sa, sb, qa, qb, pa, pb, mk3(c[0], c[1], c[2]), mk3(c[3], c[4], c[5]), mk3(c[6], c[7], c[8]),
+                                  oA, oB);
+        float* o = out + 24 * (size_t)i;
+        for (int k = 0; k < 4; k++) {
+            float4 a = k < cnt ? oA[k] : make_float4(0.f, 0.f, 0.f, 0.f), b = k < cnt ? oB[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+            o[6 * k + 0] = a.x; o[6 * k + 1] = a.y; o[6 * k + 2] = a.z;
+            o[6 * k + 3] = b.x; o[6 * k + 4] = b.y; o[6 * k + 5] = b.z;
+        }
+        count[i] = cnt;
+    }
+}
+
 // Dynamic shared memory of the warp-per-pair kernels: one polytope per warp.
 constexpr int kNpSmem = NP_WARPS * (int)sizeof(EpaSmem);
 
@@ -1612,6 +1638,14 @@ int jg_narrowphase_init() {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_edge, cudaFuncAttributeMaxDynamicSharedMemorySize, kNpSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_collide_query, cudaFuncAttributeMaxDynamicSharedMemorySize, kNpSmem);
     return e == cudaSuccess ? 0 : -1;
+}
+
+void jg_launch_manifold_query(WorldDev& w, const int2* pairs, int n, const float* in, float* out, int* count,
+                              cudaStream_t s, int nsm) {
+    if (n <= 0) return;
+    int blocks = (n + 127) / 128;
+    if (blocks > nsm * 8) blocks = nsm * 8;
+    k_manifold_query<<<blocks, 128, 0, s>>>(w, pairs, n, in, out, count);
 }
 
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,

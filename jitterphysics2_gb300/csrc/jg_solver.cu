@@ -213,6 +213,95 @@ __device__ __forceinline__ void integrate_forces_all(const WorldDev& w, int tid,
     }
 }
 
+// float.IsNormal
+__device__ __forceinline__ bool is_normal_f(float x) { return isfinite(x) && fabsf(x) >= 1.17549435e-38f; }
+
+// JSymmetricMatrix.TryInverseUnscaled / Inverse (JSymmetricMatrix.cs:104-178): zero when
+// neither the matrix nor its scaled copy inverts
+__device__ bool sym_try_inverse_unscaled(const sym6& m, sym6& o) {
+    float det = m.m11 * (m.m22 * m.m33 - m.m23 * m.m23) + m.m12 * (m.m23 * m.m13 - m.m12 * m.m33) +
+                m.m13 * (m.m12 * m.m23 - m.m22 * m.m13);
+    float idet = 1.0f / det;
+    if (!is_normal_f(idet)) return false;
+    o.m11 = (m.m22 * m.m33 - m.m23 * m.m23) * idet;
+    o.m12 = (m.m13 * m.m23 - m.m12 * m.m33) * idet;
+    o.m13 = (m.m12 * m.m23 - m.m22 * m.m13) * idet;
+    o.m22 = (m.m11 * m.m33 - m.m13 * m.m13) * idet;
+    o.m23 = (m.m13 * m.m12 - m.m23 * m.m11) * idet;
+    o.m33 = (m.m11 * m.m22 - m.m12 * m.m12) * idet;
+    return isfinite(o.m11) && isfinite(o.m12) && isfinite(o.m13) && isfinite(o.m22) && isfinite(o.m23) && isfinite(o.m33);
+}
+__device__ sym6 sym_inverse_ref(const sym6& m) {
+    sym6 o;
+    if (sym_try_inverse_unscaled(m, o)) return o;
+    float s = fmaxf(fabsf(m.m11), fmaxf(fabsf(m.m12), fabsf(m.m13)));
+    s = fmaxf(s, fmaxf(fabsf(m.m22), fmaxf(fabsf(m.m23), fabsf(m.m33))));
+    if (s > 0 && isfinite(s)) {
+        sym6 n{m.m11 / s, m.m12 / s, m.m13 / s, m.m22 / s, m.m23 / s, m.m33 / s};
+        if (sym_try_inverse_unscaled(n, o)) {
+            o = sym6{o.m11 / s, o.m12 / s, o.m13 / s, o.m22 / s, o.m23 / s, o.m33 / s};
+            if (isfinite(o.m11) && isfinite(o.m12) && isfinite(o.m13) && isfinite(o.m22) && isfinite(o.m23) && isfinite(o.m33))
+                return o;
+        }
+    }
+    return sym6{0, 0, 0, 0, 0, 0};
+}
+
+// JMatrix.Determinant / TryInverseUnscaled / Inverse (JMatrix.cs:391-478)
+__device__ bool mat_try_inverse_unscaled(const float M[3][3], float o[3][3]) {
+    float det = M[0][0] * M[1][1] * M[2][2] + M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                M[2][0] * M[1][1] * M[0][2] - M[2][1] * M[1][2] * M[0][0] - M[2][2] * M[1][0] * M[0][1];
+    float idet = 1.0f / det;
+    if (!is_normal_f(idet)) return false;
+    float n[3][3];
+    n[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+    n[0][1] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+    n[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
+    n[1][0] = M[1][2] * M[2][0] - M[2][2] * M[1][0];
+    n[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
+    n[1][2] = M[0][2] * M[1][0] - M[1][2] * M[0][0];
+    n[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
+    n[2][1] = M[0][1] * M[2][0] - M[2][1] * M[0][0];
+    n[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
+    bool fin = true;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) { o[r][c] = n[r][c] * idet; fin = fin && isfinite(o[r][c]); }
+    return fin;
+}
+__device__ bool mat_inverse(const float M[3][3], float o[3][3]) {
+    if (mat_try_inverse_unscaled(M, o)) return true;
+    float s = fmaxf(fabsf(M[0][0]), fmaxf(fabsf(M[0][1]), fabsf(M[0][2])));
+    s = fmaxf(s, fmaxf(fabsf(M[1][0]), fmaxf(fabsf(M[1][1]), fabsf(M[1][2]))));
+    s = fmaxf(s, fmaxf(fabsf(M[2][0]), fmaxf(fabsf(M[2][1]), fabsf(M[2][2]))));
+    if (!(s > 0 && isfinite(s))) return false;
+    float nm[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) nm[r][c] = M[r][c] / s;
+    if (!mat_try_inverse_unscaled(nm, o)) return false;
+    bool fin = true;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) { o[r][c] = o[r][c] / s; fin = fin && isfinite(o[r][c]); }
+    return fin;
+}
+
+// World.SolveGyroscopic (World.Step.cs:1075-1104): one implicit Newton step on the
+// gyroscopic term with the world inertia held fixed
+__device__ __noinline__ v3 solve_gyroscopic(const sym6& I, v3 av, float dt) {
+    v3 Iw = sym_mul(I, av);
+    v3 f = dt * cross(av, Iw);
+    const float M[3][3] = {{I.m11, I.m12, I.m13}, {I.m12, I.m22, I.m23}, {I.m13, I.m23, I.m33}};
+    const float W[3][3] = {{0, -av.z, av.y}, {av.z, 0, -av.x}, {-av.y, av.x, 0}};
+    const float L[3][3] = {{0, -Iw.z, Iw.y}, {Iw.z, 0, -Iw.x}, {-Iw.y, Iw.x, 0}};
+    float J[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) J[r][c] = M[r][c] + dt * ((W[r][0] * M[0][c] + W[r][1] * M[1][c] + W[r][2] * M[2][c]) - L[r][c]);
+    float inv[3][3];
+    if (!mat_inverse(J, inv)) return av;
+    v3 d = mk3(inv[0][0] * f.x + inv[0][1] * f.y + inv[0][2] * f.z, inv[1][0] * f.x + inv[1][1] * f.y + inv[1][2] * f.z,
+               inv[2][0] * f.x + inv[2][1] * f.y + inv[2][2] * f.z);
+    return av - d;
+}
+
 // IntegrateVelocities (World.Step.cs:1106-1133) with SolveGyroscopic (World.Step.cs:1075-1104).
 __device__ __forceinline__ void integrate_velocities_all(const WorldDev& w, const StepParams& sp, int tid, int nth) {
     for (int i = tid; i < w.nb; i += nth) {
@@ -226,46 +315,10 @@ __device__ __forceinline__ void integrate_velocities_all(const WorldDev& w, cons
         q4 q = qnormalize(qmul(rq, mkq(w.q[i])));
         w.q[i] = f4(q);
         if ((bi.y & JG_BODY_GYROSCOPIC) && ((bi.y >> 4) & 63) == 0) {
-            // one implicit Newton step on the gyroscopic term
+            // JSymmetricMatrix.Inverse of the world inverse inertia, then SolveGyroscopic
             sym6 Ii;
             Ii.m11 = b.i0.x; Ii.m12 = b.i0.y; Ii.m13 = b.i0.z; Ii.m22 = b.i0.w; Ii.m23 = b.i1.x; Ii.m33 = b.i1.y;
-            float det = Ii.m11 * (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) + Ii.m12 * (Ii.m23 * Ii.m13 - Ii.m12 * Ii.m33) +
-                        Ii.m13 * (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13);
-            float id = 1.0f / det;
-            if (isfinite(id) && id != 0.f) {
-                sym6 I;
-                I.m11 = (Ii.m22 * Ii.m33 - Ii.m23 * Ii.m23) * id; I.m12 = (Ii.m13 * Ii.m23 - Ii.m12 * Ii.m33) * id;
-                I.m13 = (Ii.m12 * Ii.m23 - Ii.m22 * Ii.m13) * id; I.m22 = (Ii.m11 * Ii.m33 - Ii.m13 * Ii.m13) * id;
-                I.m23 = (Ii.m13 * Ii.m12 - Ii.m23 * Ii.m11) * id; I.m33 = (Ii.m11 * Ii.m22 - Ii.m12 * Ii.m12) * id;
-                v3 Iw = sym_mul(I, av);
-                v3 f = sp.sub_dt * cross(av, Iw);
-                float M[3][3] = {{I.m11, I.m12, I.m13}, {I.m12, I.m22, I.m23}, {I.m13, I.m23, I.m33}};
-                float W[3][3] = {{0, -av.z, av.y}, {av.z, 0, -av.x}, {-av.y, av.x, 0}};
-                float L[3][3] = {{0, -Iw.z, Iw.y}, {Iw.z, 0, -Iw.x}, {-Iw.y, Iw.x, 0}};
-                float J[3][3];
-                for (int r = 0; r < 3; r++)
-                    for (int c = 0; c < 3; c++)
-                        J[r][c] = M[r][c] + sp.sub_dt * ((W[r][0] * M[0][c] + W[r][1] * M[1][c] + W[r][2] * M[2][c]) - L[r][c]);
-                float jd = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-                if (jd != 0.f && isfinite(jd)) {
-                    float ij = 1.0f / jd;
-                    float inv[3][3];
-                    inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * ij;
-                    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * ij;
-                    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * ij;
-                    inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * ij;
-                    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * ij;
-                    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * ij;
-                    inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * ij;
-                    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * ij;
-                    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * ij;
-                    v3 d = mk3(f.x * inv[0][0] + f.y * inv[0][1] + f.z * inv[0][2], f.x * inv[1][0] + f.y * inv[1][1] + f.z * inv[1][2],
-                               f.x * inv[2][0] + f.y * inv[2][1] + f.z * inv[2][2]);
-                    v3 nw = av - d;
-                    w.body[i].w = f4(nw, b.w.w);
-                }
-            }
+            w.body[i].w = f4(solve_gyroscopic(sym_inverse_ref(Ii), av, sp.sub_dt), b.w.w);
         }
     }
 }

@@ -124,6 +124,25 @@ class World:
         check(getattr(self._lib, name)(self._h, ptr(pr), n, ptr(out), ptr(hit)), name)
         return hit[:n] != 0, out[:n, 0:3], out[:n, 3:6], out[:n, 6:9], out[:n, 9]
 
+    def manifold_pairs(self, pairs, points):
+        """CollisionManifold.BuildManifold for shape-index pairs at the current poses, given
+        (pointA, pointB, normal) per pair.  Returns a list of (A [k,3], B [k,3]) arrays."""
+        pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 9)
+        n = len(pr)
+        out = np.zeros((max(n, 1), 4, 6), np.float32)
+        cnt = np.zeros(max(n, 1), np.int32)
+        check(self._lib.jg_manifold_pairs(self._h, ptr(pr), n, ptr(pts), ptr(out), ptr(cnt)), "jg_manifold_pairs")
+        return [(out[i, :cnt[i], :3].copy(), out[i, :cnt[i], 3:].copy()) for i in range(n)]
+
+    def pairs(self):
+        """The broadphase pair list of the last step, [n, 2] shape indices."""
+        n = ctypes.c_int32()
+        check(self._lib.jg_get_pairs(self._h, None, 0, ctypes.byref(n)), "jg_get_pairs")
+        out = np.zeros((max(n.value, 1), 2), np.int32)
+        check(self._lib.jg_get_pairs(self._h, ptr(out), n.value, ctypes.byref(n)), "jg_get_pairs")
+        return out[:n.value]
+
     def contacts(self):
         n = ctypes.c_int32()
         check(self._lib.jg_get_contacts(self._h, None, 0, ctypes.byref(n)), "jg_get_contacts")

@@ -362,7 +362,49 @@ template <class R> void integrate_forces(Body<R>& b) {
     b.angvel = b.angvel + b.dangvel;
     b.vel = b.vel + b.dvel;
 }
-// World.SolveGyroscopic (World.Step.cs:1075-1104)
+// JMatrix.Determinant (JMatrix.cs:391-395) and JMatrix.TryInverseUnscaled (JMatrix.cs:448-478)
+template <class R> R mat_det(const R M[3][3]) {
+    return M[0][0] * M[1][1] * M[2][2] + M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+           M[2][0] * M[1][1] * M[0][2] - M[2][1] * M[1][2] * M[0][0] - M[2][2] * M[1][0] * M[0][1];
+}
+template <class R> bool mat_try_inverse_unscaled(const R M[3][3], R out[3][3]) {
+    R idet = (R)1.0 / mat_det(M);
+    if (!std::isnormal(idet)) return false;
+    R n[3][3];
+    n[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+    n[0][1] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+    n[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
+    n[1][0] = M[1][2] * M[2][0] - M[2][2] * M[1][0];
+    n[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
+    n[1][2] = M[0][2] * M[1][0] - M[1][2] * M[0][0];
+    n[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
+    n[2][1] = M[0][1] * M[2][0] - M[2][1] * M[0][0];
+    n[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
+    bool fin = true;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) { out[i][j] = n[i][j] * idet; fin = fin && std::isfinite(out[i][j]); }
+    return fin;
+}
+// JMatrix.Inverse (JMatrix.cs:404-440): unscaled, else on the matrix scaled by its largest entry
+template <class R> bool mat_inverse(const R M[3][3], R out[3][3]) {
+    if (mat_try_inverse_unscaled(M, out)) return true;
+    R s = std::max(std::abs(M[0][0]), std::max(std::abs(M[0][1]), std::abs(M[0][2])));
+    s = std::max(s, std::max(std::abs(M[1][0]), std::max(std::abs(M[1][1]), std::abs(M[1][2]))));
+    s = std::max(s, std::max(std::abs(M[2][0]), std::max(std::abs(M[2][1]), std::abs(M[2][2]))));
+    if (s > 0 && std::isfinite(s)) {
+        R nm[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) nm[i][j] = M[i][j] / s;
+        if (mat_try_inverse_unscaled(nm, out)) {
+            bool fin = true;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) { out[i][j] /= s; fin = fin && std::isfinite(out[i][j]); }
+            if (fin) return true;
+        }
+    }
+    return false;
+}
+// World.SolveGyroscopic (World.Step.cs:1075-1104): one implicit Newton step
 template <class R> V3<R> solve_gyroscopic(const Sym3<R>& Iw, V3<R> w, R dt) {
     V3<R> Iwv = sym_mul(Iw, w);
     V3<R> f = dt * cross(w, Iwv);
@@ -375,22 +417,10 @@ template <class R> V3<R> solve_gyroscopic(const Sym3<R>& Iw, V3<R> w, R dt) {
             R wi = W[i][0] * I[0][j] + W[i][1] * I[1][j] + W[i][2] * I[2][j];
             J[i][j] = I[i][j] + dt * (wi - L[i][j]);
         }
-    R det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-    if (!(std::abs(det) > 0) || !std::isfinite(det)) return w;
-    R id = (R)1.0 / det;
     R inv[3][3];
-    inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
-    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-    inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
-    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-    inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
-    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-    V3<R> d(f.x * inv[0][0] + f.y * inv[0][1] + f.z * inv[0][2], f.x * inv[1][0] + f.y * inv[1][1] + f.z * inv[1][2],
-            f.x * inv[2][0] + f.y * inv[2][1] + f.z * inv[2][2]);
+    if (!mat_inverse(J, inv)) return w;
+    V3<R> d(inv[0][0] * f.x + inv[0][1] * f.y + inv[0][2] * f.z, inv[1][0] * f.x + inv[1][1] * f.y + inv[1][2] * f.z,
+            inv[2][0] * f.x + inv[2][1] * f.y + inv[2][2] * f.z);
     return w - d;
 }
 // World.IntegrateVelocities (World.Step.cs:1106-1133)
