@@ -18,7 +18,10 @@ colouring, substepped solve + integration, contact and body update.
           S * ((I + R) * 276 * C + 320 * C + 116 * N) + 52 * N
   cpu_baseline  the oracle's multithreaded Regular-mode restatement of the reference
           (C++ restatement of Jitter2, all host threads) on 2 steps of the same state
-  fp64_error  one step from the timed state replayed by the FP64 oracle in the GPU's order
+  fp64_error  one step from the timed state replayed by the FP64 oracle in the GPU's order:
+          errors in contact normal, depth, point, impulse, velocity and position
+  fp64_drift  a 4000-body pile stepped 1000 times on the GPU and in the FP64 oracle: the
+          gaps of kinetic and potential energy and the final momenta
   learned_warm_start  the learned against the plain warm start on 50 towers + 49k rubble:
           residual after 8 and 64 iterations, iterations to 1e-4 and 1e-3 (cap 2048),
           contacts/s of both
@@ -251,27 +254,39 @@ def learned_section(eval_steps=10):
 
 
 def fp64_section(scene, bodies, contacts_before, contacts_after, gpu_after):
-    """One step from the GPU's state replayed by the FP64 oracle in the GPU's solve
-    order: velocity and position error of the FP32 path against double precision."""
-    import oracle_lib as O
-    from jitterphysics2_gb300 import abi
+    """One step from the GPU's state replayed by the FP64 oracle in the GPU's solve order:
+    errors of the FP32 path in contact normal, depth, point, impulse, velocity and position."""
+    import precision_lib
     t0 = time.perf_counter()
-    o = O.OracleWorld(scene, real="d", external_order=True)
-    o.set_bodies(bodies)
-    o.set_contacts(contacts_before)
-    o.narrowphase()
-    for c in contacts_after:
-        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
-    o.step(scene["dt"], narrow=False)
-    ob = o.bodies_d()
-    dyn = gpu_after["motion_type"] == abi.MOTION_DYNAMIC
-    dv = np.maximum(np.abs(gpu_after["velocity"][dyn] - ob["velocity"][dyn]).max(1),
-                    np.abs(gpu_after["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(1))
-    dx = np.abs(gpu_after["position"][dyn] - ob["position"][dyn]).max(1)
-    return {"velocity_err_max": float(dv.max()), "velocity_err_mean": float(dv.mean()),
-            "velocity_err_median": float(np.median(dv)), "velocity_within_1e-3": float(np.mean(dv < 1e-3)),
-            "position_err_max": float(dx.max()), "seconds": time.perf_counter() - t0,
-            "sample": "one step of the settled pile from identical state, FP64 oracle in the GPU's order"}
+    r = precision_lib.one_step_errors(scene, bodies, contacts_before, contacts_after, gpu_after)
+    r["seconds"] = time.perf_counter() - t0
+    r["sample"] = "one step of the formed pile from identical state, FP64 oracle in the GPU's order"
+    return r
+
+
+def drift_section(n=4000, steps=1000):
+    """Momentum and energy of a pile (the 20k pile's recipe at n bodies, gravity, ground and
+    heightfield) over `steps` steps from the seeded start, FP32 on the GPU against the FP64
+    oracle (multithreaded): the relative gaps of kinetic and potential energy."""
+    import precision_lib
+    from jitterphysics2_gb300 import scenes
+    from jitterphysics2_gb300.world import world_for_scene
+    t0 = time.perf_counter()
+    sc = scenes.mixed_pile(n=n, box=(30.0, 60.0, 30.0), seed=12350)
+    w = world_for_scene(sc)
+    d = precision_lib.drift(sc, w, steps, threads=os.cpu_count() or 1)
+    w.close()
+    u0 = abs(d["u_fp64"][0])
+    k_scale = max(float(np.max(d["k_fp64"])), 1e-9)
+    return {"workload": "mixed pile, %d bodies, 30x60x30 over ground + heightfield, %d steps from the seeded start"
+                        % (n, steps),
+            "potential_gap_final": float(abs(d["u_gpu"][-1] - d["u_fp64"][-1]) / u0),
+            "potential_gap_max": float(np.max(np.abs(d["u_gpu"] - d["u_fp64"])) / u0),
+            "kinetic_gap_max_of_peak": float(np.max(np.abs(d["k_gpu"] - d["k_fp64"])) / k_scale),
+            "kinetic_final_gpu": float(d["k_gpu"][-1]), "kinetic_final_fp64": float(d["k_fp64"][-1]),
+            "momentum_final_gpu": float(np.linalg.norm(d["p_gpu"][-1])),
+            "momentum_final_fp64": float(np.linalg.norm(d["p_fp64"][-1])),
+            "seconds": time.perf_counter() - t0}
 
 
 def dist_setup(n_gpus):
@@ -477,6 +492,7 @@ def main():
         line["cpu_baseline"] = cpu_baseline(sc, w.bodies(), w.contacts())
     w.close()
     if extras:
+        line["fp64_drift"] = drift_section()
         line["learned_warm_start"] = learned_section()
     if rank == 0:
         print(json.dumps(line), flush=True)

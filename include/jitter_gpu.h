@@ -93,6 +93,7 @@ typedef struct jg_world_params {
     int32_t deterministic;              /* sort new arbiters by key every step          */
     int32_t partitioned_solve;          /* 1 (default): spatial tasks in shared memory   */
     float   speculative_threshold;      /* SpeculativeVelocityThreshold, default 10      */
+    int32_t allow_deactivation;         /* AllowDeactivation, default 1 (World.cs:333)   */
 } jg_world_params;
 
 /* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the
@@ -222,6 +223,18 @@ int jg_download_bodies(jg_world* world, jg_body_desc* bodies, int32_t count);
 int jg_upload_shapes(jg_world* world, const jg_shape_desc* shapes, int32_t count,
                      const float* hull_vertices, int32_t hull_vertex_count,
                      const jg_triangle_desc* triangles, int32_t triangle_count);
+
+/* World.ActivateBodyNextStep (World.cs:696-720), RigidBody.SetActivationState(true): the
+ * body's sleep time restarts and, when it sleeps and is not static, its island joins the
+ * active list at the next step.  Only matters with allow_deactivation. */
+int jg_activate_body(jg_world* world, int32_t body);
+/* RigidBody.DeactivationTime (RigidBody.cs:476-483, seconds, default 1) and
+ * RigidBody.DeactivationThreshold (RigidBody.cs:497-508, angular and linear speeds, default
+ * sqrt(0.1) each): a body whose speeds stay below the thresholds for the deactivation time
+ * stops keeping its island awake.  Negative or NaN values return JG_ERR_INVALID_ARG.  An upload
+ * of a different number of bodies restarts every body's sleep time. */
+int jg_set_body_sleep(jg_world* world, int32_t body, float deactivation_time, float linear_threshold,
+                      float angular_threshold);
 
 /* RigidBody.Position/Orientation/Velocity setters; field: 0 position, 1 orientation,
  * 2 velocity, 3 angular velocity, 4 force, 5 torque.  Position/orientation follow

@@ -52,6 +52,7 @@ PARAMS_FIELDS = [
     ("narrow_tile", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_residual", ctypes.c_int32),
     ("deterministic", ctypes.c_int32),
     ("partitioned_solve", ctypes.c_int32), ("speculative_threshold", ctypes.c_float),
+    ("allow_deactivation", ctypes.c_int32),
 ]
 
 
@@ -103,6 +104,8 @@ SIGNATURES = {
     "jg_download_bodies": (_I, [_P, _P, _I]),
     "jg_upload_shapes": (_I, [_P, _P, _I, _P, _I, _P, _I]),
     "jg_set_body": (_I, [_P, _I, _I, _P]),
+    "jg_activate_body": (_I, [_P, _I]),
+    "jg_set_body_sleep": (_I, [_P, _I, _F, _F, _F]),
     "jg_add_constraint": (_I, [_P, _I, _I, _I, _P, _PI]),
     "jg_step": (_I, [_P, _F]),
     "jg_step_host": (_I, [_P, _F, _P, _I]),
@@ -176,7 +179,7 @@ def ptr(a):
 # library (the CPU oracle and the reference arm of the benchmark).
 PARAM_DEFAULTS = dict(gravity=(0.0, -9.81, 0.0), substeps=1, solver_iterations=6, relax_iterations=4,
                       enable_auxiliary_contacts=1, persistent_manifold=1, speculative_relaxation=0.9,
-                      speculative_threshold=10.0, edge_filter=1, warm_start_mode=1, narrow_tile=32,
+                      speculative_threshold=10.0, edge_filter=1, warm_start_mode=1, narrow_tile=32, allow_deactivation=1,
                       partitioned_solve=1)
 
 

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libjitter_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["jg_api.cu", "jg_broadphase.cu", "jg_narrowphase.cu", "jg_contacts.cu", "jg_sched.cu", "jg_solver.cu",
-              "jg_mlp.cu"]
+              "jg_mlp.cu", "jg_islands.cu"]
 CPP_SOURCES = ["jg_host.cpp"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC", "-Xptxas", "-v"]

@@ -19,6 +19,9 @@ void jg_launch_update_contacts(WorldDev& w, cudaStream_t s, int nsm);
 void jg_solver_reset_launch_cache(WorldDev& w);
 int jg_solver_init();
 int jg_schedule_init();
+void jg_launch_activate(WorldDev& w, int body, cudaStream_t s);
+void jg_launch_sleep_settings(WorldDev& w, int body, float t, float lin2, float ang2, cudaStream_t s);
+void jg_launch_sleep_init(float4* sleep, int n, cudaStream_t s);
 int jg_mlp_step_hook(jg_world* w, const StepParams& p);
 void jg_mlp_free(void* mlp);
 void jg_launch_collide_query(WorldDev& w, const int2* pairs, int n, float threshold, float* out, int* hit,
@@ -111,6 +114,8 @@ int allocate(jg_world* w) {
     DA(d.body, d.cap_bodies); DA(d.pos, d.cap_bodies); DA(d.q, d.cap_bodies); DA(d.dv, d.cap_bodies);
     DA(d.dw, d.cap_bodies); DA(d.il0, d.cap_bodies); DA(d.il1, d.cap_bodies); DA(d.force, d.cap_bodies);
     DA(d.torque, d.cap_bodies); DA(d.mat, d.cap_bodies); DA(d.binfo, d.cap_bodies);
+    DA(d.sleep, d.cap_bodies); DA(d.uf, d.cap_bodies); DA(d.ufl, d.cap_bodies);
+    jg_launch_sleep_init(d.sleep, d.cap_bodies, w->stream);
     DA(d.sinfo, d.cap_shapes); DA(d.sdims, d.cap_shapes); DA(d.scenter, d.cap_shapes);
     DA(d.amin, d.cap_shapes); DA(d.amax, d.cap_shapes);
     DA(d.mkey, d.cap_shapes); DA(d.mkey_alt, d.cap_shapes); DA(d.midx, d.cap_shapes); DA(d.midx_alt, d.cap_shapes);
@@ -232,6 +237,7 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.warm_start = p.warm_start_mode;
     sp.record_residual = p.record_residual;
     sp.partition = p.partitioned_solve ? 1 : 0;
+    sp.allow_deact = p.allow_deactivation ? 1 : 0;
     sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : JG_TASK_BLOCK,
                                        p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
@@ -254,8 +260,13 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     if (timed) cudaEventRecord(w->ev[1], s);
     jg_launch_narrowphase(d, sp, s, w->nsm, w->prm.narrow_tile);
     if (timed) cudaEventRecord(w->ev[2], s);
+    d.allow_deact = sp.allow_deact;
     jg_launch_merge(d, sp, s, w->nsm);
     w->launches += jg_mlp_step_hook(w, sp);
+    if (sp.allow_deact) {
+        jg_launch_islands(d, s, w->nsm);  // HandleDeferredArbiters done in the merge, then CheckDeactivation
+        w->launches += 4;
+    }
     if (timed) cudaEventRecord(w->ev[3], s);
     jg_launch_schedule(d, sp, s, w->nsm);
     if (jg_launch_color(d, s, w->nsm) < 0) {
@@ -323,6 +334,7 @@ int jg_default_params(jg_world_params* p) {
     p->persistent_manifold = 1;
     p->speculative_relaxation = 0.9f;
     p->speculative_threshold = 10.0f;
+    p->allow_deactivation = 1;
     p->edge_filter = 1;
     p->warm_start_mode = JG_WARMSTART_CACHED;
     p->narrow_tile = 32;
@@ -440,7 +452,10 @@ __global__ void k_bodies_check(const jg_body_desc* d, int n, int nworlds, int* b
     }
 }
 
-__global__ void k_bodies_in(const jg_body_desc* d, int n, WorldDev D, const int* bad) {
+// keep: the upload refreshes the same bodies (the host-buffer step), so each body keeps its
+// sleep time and island flags; otherwise they start afresh (sleep time 0, infinite for a
+// static body, island marked and in the active list).
+__global__ void k_bodies_in(const jg_body_desc* d, int n, WorldDev D, const int* bad, int keep) {
     if (*bad != INT_MAX) return;  // an invalid body: the state stays as it was
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const jg_body_desc& b = d[i];
@@ -464,7 +479,10 @@ __global__ void k_bodies_in(const jg_body_desc* d, int n, WorldDev D, const int*
         D.force[i] = make_float4(b.force[0], b.force[1], b.force[2], 0.f);
         D.torque[i] = make_float4(b.torque[0], b.torque[1], b.torque[2], 0.f);
         D.mat[i] = make_float4(b.friction, b.restitution, b.linear_damping, b.angular_damping);
-        D.binfo[i] = make_int4(b.motion_type, b.flags, b.world, 0);
+        int island = 3;
+        if (keep) island = D.binfo[i].w;
+        else D.sleep[i].x = b.motion_type == JG_MOTION_STATIC ? INFINITY : 0.f;
+        D.binfo[i] = make_int4(b.motion_type, b.flags, b.world, island);
     }
 }
 
@@ -482,6 +500,7 @@ __global__ void k_bodies_out(jg_body_desc* d, int n, WorldDev D) {
         o.delta_angular_velocity[0] = dw.x; o.delta_angular_velocity[1] = dw.y; o.delta_angular_velocity[2] = dw.z;
         o.force[0] = o.force[1] = o.force[2] = 0.f;
         o.torque[0] = o.torque[1] = o.torque[2] = 0.f;
+        o.flags = D.binfo[i].y;  // RigidBody.IsActive may have changed (sleeping)
     }
 }
 
@@ -494,7 +513,7 @@ int upload_bodies_device(jg_world* w, const jg_body_desc* b, int32_t n) {
     if (n > 0) {
         CK(cudaMemcpyAsync(w->d_stage, b, sizeof(jg_body_desc) * n, cudaMemcpyHostToDevice, s));
         k_bodies_check<<<blocks, 256, 0, s>>>(w->d_stage, n, w->nworlds, w->d_bad);
-        k_bodies_in<<<blocks, 256, 0, s>>>(w->d_stage, n, D, w->d_bad);
+        k_bodies_in<<<blocks, 256, 0, s>>>(w->d_stage, n, D, w->d_bad, D.nb == n ? 1 : 0);
     }
     CK(cudaMemcpyAsync(w->h_bad, w->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -782,6 +801,25 @@ int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
     r = jg_step(w, dt);
     if (r) return r;
     return download_bodies_device(w, bodies, n);
+}
+
+int jg_activate_body(jg_world* w, int32_t body) {
+    if (!w || body < 0 || body >= w->d.nb) return JG_ERR_INVALID_ARG;
+    jg_launch_activate(w->d, body, w->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(w->stream));
+    w->host_current = false;
+    return JG_OK;
+}
+
+int jg_set_body_sleep(jg_world* w, int32_t body, float deactivation_time, float linear_threshold, float angular_threshold) {
+    if (!w || body < 0 || body >= w->d.nb) return JG_ERR_INVALID_ARG;
+    if (!(deactivation_time >= 0) || !(linear_threshold >= 0) || !(angular_threshold >= 0)) return JG_ERR_INVALID_ARG;
+    jg_launch_sleep_settings(w->d, body, deactivation_time, linear_threshold * linear_threshold,
+                             angular_threshold * angular_threshold, w->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(w->stream));
+    return JG_OK;
 }
 
 int jg_get_constraints(jg_world* w, int32_t* keys, float* imp, int32_t cap, int32_t* count) {

@@ -165,6 +165,10 @@ __global__ void k_merge(WorldDev w, StepParams sp, int2* ev_created) {
         if (a < 0) {
             a = atomicAdd(&w.ctr->narb, 1);
             if (a >= w.cap_arb) { atomicCAS(&w.ctr->status, 0, JG_ERR_CAPACITY); continue; }
+            if (w.allow_deact) {  // HandleDeferredArbiters: AddToActiveList on both islands (World.Step.cs:880-914)
+                atomicOr(&w.binfo[b1].w, 3);
+                atomicOr(&w.binfo[b2].w, 3);
+            }
             A.key[a] = key;
             A.body[a] = make_int2(b1, b2);
             A.mat[a] = make_float4(fmaxf(m1.x, m2.x), fmaxf(m1.y, m2.y), sp.spec_relax, 0.f);
@@ -381,6 +385,11 @@ __global__ void k_permute(WorldDev w, int2* ev_removed, int* dst_index) {
             int e = atomicAdd(&w.ctr->nremoved, 1);
             if (e < cap) ev_removed[e] = S.key[a];
             dst_index[a] = -1;
+            if (w.allow_deact) {  // RemoveBrokenArbiters: AddToActiveList on both islands (World.Step.cs:845-846)
+                int2 bb = S.body[a];
+                atomicOr(&w.binfo[bb.x].w, 3);
+                atomicOr(&w.binfo[bb.y].w, 3);
+            }
             continue;
         } else {
             int col = st & 255;
@@ -391,13 +400,20 @@ __global__ void k_permute(WorldDev w, int2* ev_removed, int* dst_index) {
         dst_index[a] = d;
         int4 info = S.info[a];
         int2 bb = S.body[a];
+        // a row is solved and updated while one of its bodies is an awake non-static body
+        // (memContacts activation follows the bodies, World.Step.cs:1247-1275, :1325-1345)
+        bool asleep = false;
+        if (w.allow_deact) {
+            int4 i1 = w.binfo[bb.x], i2 = w.binfo[bb.y];
+            asleep = !((i1.x != JG_MOTION_STATIC && (i1.y & JG_BODY_ACTIVE)) || (i2.x != JG_MOTION_STATIC && (i2.y & JG_BODY_ACTIVE)));
+        }
         D.key[d] = S.key[a];
         D.body[d] = bb;
-        D.info[d] = make_int4(info.x, info.y, key, info.w);
+        D.info[d] = make_int4(info.x, (info.y & 0xffff) | (asleep ? JG_ARB_ASLEEP : 0), key, info.w);
         // velocities of a non-dynamic body stay constant through the solve
         int nd = w.binfo[bb.x].x != JG_MOTION_DYNAMIC ? bb.x : (w.binfo[bb.y].x != JG_MOTION_DYNAMIC ? bb.y : -1);
         // task arbiters: what the iterations read besides the rows, in one record
-        if (st == -4) ls = make_int4(ls.x, ls.y, (info.x & 15) | ((info.y & 15) << 4) | (nd >= 0 ? 256 : 0),
+        if (st == -4) ls = make_int4(ls.x, ls.y, (info.x & 15) | ((info.y & 15) << 4) | (nd >= 0 ? 256 : 0) | (asleep ? JG_TASK_ASLEEP : 0),
                                      __float_as_int(S.mat[a].x));
         D.lslot[d] = ls;
         D.sv[d] = nd >= 0 ? w.body[nd].v : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -443,6 +459,7 @@ __global__ void k_update_contacts(WorldDev w) {
     const int n = w.ctr->narb, cap = w.cap_arb;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
         int4 info = A.info[a];
+        if (info.y & JG_ARB_ASLEEP) continue;  // sleeping contacts keep their points
         int usage = info.x & 15;
         usage |= usage << 4;
         int2 b = A.body[a];

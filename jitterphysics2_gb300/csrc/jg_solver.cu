@@ -169,8 +169,8 @@ __device__ __forceinline__ void solve_arbiter(const WorldDev& w, const ArbStore&
                                               bool bias, float& d2, float& l2) {
     int4 info = A.info[a];
     int usage = info.x & 15;
-    if (!usage) return;
-    int mode = info.y;
+    if (!usage || (info.y & JG_ARB_ASLEEP)) return;
+    int mode = info.y & 15;
     int2 bb = A.body[a];
     LBody b1 = load_body(w.body, bb.x), b2 = load_body(w.body, bb.y);
     const int cap = w.cap_arb;
@@ -201,9 +201,10 @@ __device__ __forceinline__ void block_reduce_add(float a, float b, float* out) {
 }
 
 // IntegrateForces (World.Step.cs:1060-1072): v += dv, w += dw for dynamic bodies.
-__device__ __forceinline__ void integrate_forces_all(const WorldDev& w, int tid, int nth) {
+__device__ __forceinline__ void integrate_forces_all(const WorldDev& w, const StepParams& sp, int tid, int nth) {
     for (int i = tid; i < w.nb; i += nth) {
-        if (w.binfo[i].x != JG_MOTION_DYNAMIC) continue;
+        const int4 bi = w.binfo[i];
+        if (bi.x != JG_MOTION_DYNAMIC || (sp.allow_deact && !(bi.y & JG_BODY_ACTIVE))) continue;
         SBody b = w.body[i];
         float4 dv = w.dv[i], dw = w.dw[i];
         b.w = make_float4(b.w.x + dw.x, b.w.y + dw.y, b.w.z + dw.z, b.w.w);
@@ -306,7 +307,7 @@ __device__ __noinline__ v3 solve_gyroscopic(const sym6& I, v3 av, float dt) {
 __device__ __forceinline__ void integrate_velocities_all(const WorldDev& w, const StepParams& sp, int tid, int nth) {
     for (int i = tid; i < w.nb; i += nth) {
         int4 bi = w.binfo[i];
-        if (bi.x == JG_MOTION_STATIC) continue;
+        if (bi.x == JG_MOTION_STATIC || (sp.allow_deact && !(bi.y & JG_BODY_ACTIVE))) continue;
         SBody b = w.body[i];
         v3 lv = mk3(b.v), av = mk3(b.w);
         float4 p = w.pos[i];
@@ -335,8 +336,14 @@ __device__ __forceinline__ bool remainder_pass(const WorldDev& w, const ArbStore
         if (beg == end && jb == je) continue;
         for (int a = beg + tid; a < end; a += nth) solve_arbiter(w, A, a, phase, sp, bias, d2, l2);
         for (int j = jb + tid; j < je; j += nth) {
-            if (phase == 0) joint_prepare(w, w.jorder[j], sp);
-            else joint_iterate(w, w.jorder[j], sp);
+            const int jj = w.jorder[j];
+            if (sp.allow_deact) {  // a constraint is solved while one of its bodies is awake and non-static
+                const int4 h = w.joints[jj].hdr, i1 = w.binfo[h.y], i2 = w.binfo[h.z];
+                if (!((i1.x != JG_MOTION_STATIC && (i1.y & JG_BODY_ACTIVE)) || (i2.x != JG_MOTION_STATIC && (i2.y & JG_BODY_ACTIVE))))
+                    continue;
+            }
+            if (phase == 0) joint_prepare(w, jj, sp);
+            else joint_iterate(w, jj, sp);
         }
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return false;
     }
@@ -361,7 +368,7 @@ __global__ void k_solve(WorldDev w, StepParams sp) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int* status = &w.ctr->status;
     for (int s = 0; s < sp.substeps; s++) {
-        integrate_forces_all(w, tid, nth);
+        integrate_forces_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int it = 0; it < 1 + sp.iterations; it++) {
             float d2 = 0.f, l2 = 0.f;
@@ -512,7 +519,7 @@ __device__ __forceinline__ bool iterate_task(const WorldDev& w, const ArbStore& 
             const int un = jn < n ? __ldg(&A.lslot[T.x + jn].z) : 0;
             const int p1 = __float_as_int(r0.x), p2 = __float_as_int(r0.y), hz = __float_as_int(r0.z);
             const int l1 = p1 >= 0 ? slot_of(p1) : -1, l2s = p2 >= 0 ? slot_of(p2) : -1;
-            const int usage = hz & 15, mode = (hz >> 4) & 15;
+            const int usage = (hz & JG_TASK_ASLEEP) ? 0 : hz & 15, mode = (hz >> 4) & 15;
             const float fr = r0.w;
             LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[1], r[2]);
             LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s, sst) : fixed_body(r[1], r[2]);
@@ -560,7 +567,7 @@ __device__ __forceinline__ bool prepare_task(const WorldDev& w, const ArbStore& 
         if (go) {
             __threadfence_block();
             int4 info = A.info[d];
-            int usage = info.x & 15, mode = info.y;
+            int usage = (info.y & JG_ARB_ASLEEP) ? 0 : info.x & 15, mode = info.y & 15;
             int2 bb = A.body[d];
             const int l1 = ls.x >= 0 ? slot_of(ls.x) : -1, l2 = ls.y >= 0 ? slot_of(ls.y) : -1;
             LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(A.sv[d], A.sv[cap + d]);
@@ -711,7 +718,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     if (w.ctr->ncolors == 0) {
         unsigned level = 0;  // grid phases started so far in this launch
         for (int s = 0; s < sp.substeps; s++) {
-            integrate_forces_all(w, tid, nth);
+            integrate_forces_all(w, sp, tid, nth);
             if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             for (int pass = 0; pass < npass; pass++) {
                 const bool relax = pass > sp.iterations;
@@ -743,7 +750,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     // With a remainder: the three grids as three phases per pass with a grid barrier after
     // each, then the remainder in global colours.
     for (int s = 0; s < sp.substeps; s++) {
-        integrate_forces_all(w, tid, nth);
+        integrate_forces_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int pass = 0; pass < npass; pass++) {
             const bool relax = pass > sp.iterations;
@@ -770,11 +777,24 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
 __global__ void k_update_bodies(WorldDev w, StepParams sp) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.nb; i += gridDim.x * blockDim.x) {
         int4 bi = w.binfo[i];
+        if (sp.allow_deact && !(bi.y & JG_BODY_ACTIVE)) continue;  // only active bodies update
         SBody b = w.body[i];
         int axes = 63 ^ ((bi.y >> 4) & 63);
         v3 v = mk3(b.v), av = mk3(b.w);
         if ((axes & 7) != 7) { if (!(axes & 1)) v.x = 0; if (!(axes & 2)) v.y = 0; if (!(axes & 4)) v.z = 0; }
         if ((axes & 56) != 56) { if (!(axes & 8)) av.x = 0; if (!(axes & 16)) av.y = 0; if (!(axes & 32)) av.z = 0; }
+        if (sp.allow_deact) {
+            // the rest test of RigidBody.Update (RigidBody.cs:723-743): a kinematic body rests only
+            // when it does not move, a dynamic one below the thresholds; resting accumulates the
+            // sleep time, and a body that moved or has not rested long enough marks its island
+            float4 sl = w.sleep[i];
+            const bool kin = bi.x == JG_MOTION_KINEMATIC;
+            const v3 zero = mk3(0.f);
+            const bool resting = kin ? (av == zero && v == zero) : (len2(av) < sl.w && len2(v) < sl.z);
+            sl.x = resting ? sl.x + sp.dt : 0.f;
+            w.sleep[i].x = sl.x;
+            if ((kin && !resting) || sl.x < sl.y) w.binfo[i].w = bi.w | 1;
+        }
         if (bi.x == JG_MOTION_DYNAMIC) {
             float4 il0 = w.il0[i], il1 = w.il1[i];
             sym6 L; L.m11 = il0.x; L.m12 = il0.y; L.m13 = il0.z; L.m22 = il0.w; L.m23 = il1.x; L.m33 = il1.y;

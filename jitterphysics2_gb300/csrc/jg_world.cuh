@@ -132,7 +132,11 @@ struct WorldDev {
     // bodies
     SBody* body;
     float4 *pos, *q, *dv, *dw, *il0, *il1, *force, *torque, *mat;
-    int4* binfo;                 // motion, flags, world, 0
+    int4* binfo;                 // motion, flags, world, island flags (1 marked, 2 in the active list)
+    float4* sleep;               // sleep time, deactivation time, squared linear / angular rest thresholds
+    int* uf;                     // [cap_bodies] islands: union-find parent, then root
+    int* ufl;                    // [cap_bodies] island flags at each root
+    int allow_deact;             // World.AllowDeactivation for this step
     // shapes
     int4* sinfo;                 // kind, body, data offset, data count
     float4 *sdims, *scenter, *hull;
@@ -249,6 +253,7 @@ struct StepParams {
     int warm_start;
     int record_residual;
     int partition;               // 1: partitioned solve (tasks + remainder), 0: global colours only
+    int allow_deact;             // World.AllowDeactivation: sleeping bodies and rows are skipped
     int task_maxb;               // bodies a task may hold in the solver's shared memory
 };
 
@@ -273,3 +278,10 @@ void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int ns
 int  jg_launch_solve(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm, int block, int ctas_per_sm);
 void jg_launch_update(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
 void jg_launch_mlp_warmstart(WorldDev& w, const StepParams& p, cudaStream_t s, int nsm);
+void jg_launch_islands(WorldDev& w, cudaStream_t s, int nsm);
+
+// Arbiter mode word (ArbStore::info.y): SolveMode bits 0-3, and this bit when neither body
+// is an awake non-static body (the row is neither solved nor updated while it sleeps).
+#define JG_ARB_ASLEEP (1 << 16)
+// Staged header bit of a task arbiter that sleeps.
+#define JG_TASK_ASLEEP 512

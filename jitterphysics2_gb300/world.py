@@ -92,6 +92,16 @@ class World:
         v = np.ascontiguousarray(value, np.float32)
         check(self._lib.jg_set_body(self._h, index, fields[field], ptr(v)), "jg_set_body")
 
+    def activate_body(self, index):
+        """World.ActivateBodyNextStep: wakes the body's island at the next step."""
+        check(self._lib.jg_activate_body(self._h, index), "jg_activate_body")
+
+    def set_body_sleep(self, index, deactivation_time=1.0, linear_threshold=0.1 ** 0.5, angular_threshold=0.1 ** 0.5):
+        """RigidBody.DeactivationTime (seconds) and DeactivationThreshold (speeds)."""
+        check(self._lib.jg_set_body_sleep(self._h, index, ctypes.c_float(deactivation_time),
+                                          ctypes.c_float(linear_threshold), ctypes.c_float(angular_threshold)),
+              "jg_set_body_sleep")
+
     # -- stepping -----------------------------------------------------------------------
     def step(self, dt):
         """World.Step(dt) (World.Step.cs:141-296) on the device."""
@@ -252,7 +262,8 @@ class World:
 def world_for_scene(scene, **overrides):
     """A World sized for a scene from jitterphysics2_gb300.scenes, with its solver settings."""
     nb, ns = len(scene["bodies"]), len(scene["shapes"])
-    kw = dict(scene.get("params", {}))
+    # the workloads are stepped without deactivation unless a scene asks for it
+    kw = dict(dict(allow_deactivation=0), **scene.get("params", {}))
     kw.update(overrides)
     w = World(max_bodies=nb, max_shapes=ns, max_constraints=max(16, len(scene.get("joints", []))),
               n_worlds=scene.get("n_worlds", 1), **kw)

@@ -325,6 +325,10 @@ template <class R> struct Handle {
         ((Handle<R>*)h)->w.bodies[i].deactivation_time = (R)seconds;                                               \
     }                                                                                                              \
     extern "C" void jor_world_activate_body_##SUF(void* h, int i) { ((Handle<R>*)h)->w.activate_body(i); }        \
+    extern "C" void jor_world_body_sleep_thresholds_##SUF(void* h, int i, double lin, double ang) {                \
+        ((Handle<R>*)h)->w.bodies[i].sleep_lin2 = (R)(lin * lin);                                                   \
+        ((Handle<R>*)h)->w.bodies[i].sleep_ang2 = (R)(ang * ang);                                                   \
+    }                                                                                                              \
     /* World.AllowDeactivation (World.cs:333) for the oracle's island restatement */                           \
     extern "C" void jor_world_set_deactivation_##SUF(void* h, int on) { ((Handle<R>*)h)->w.allow_deactivation = on != 0; } \
     /* world bounding box of shape s as the step of length dt sees it (out = min, max) */                        \

@@ -52,6 +52,7 @@ template <class R> struct Body {
     // membership of the active island partition
     R sleep_time = 0;
     R deactivation_time = (R)1.0;   // RigidBody.DeactivationTime (RigidBody.cs:400, :476-483)
+    R sleep_lin2 = (R)0.1, sleep_ang2 = (R)0.1;  // squared rest thresholds (RigidBody.cs:398-399, :497-508)
     bool marked = true, island_active = true;
     bool active() const { return (flags & 4) != 0; }
     bool gyroscopic() const { return (flags & 8) != 0; }

@@ -359,11 +359,13 @@ template <class R> struct World {
         }
     }
     // RigidBody.Update's rest test (RigidBody.cs:723-743)
+    // (on the velocities restricted to the allowed motion axes, as Update restricts them first)
     void sleep_update(Body<R>& b, const TimeStep<R>& ts) {
         bool kin = b.motion == KINEMATIC;
-        V3<R> zero;
-        bool resting = kin ? (b.angvel == zero && b.vel == zero)
-                           : (len2(b.angvel) < sleep_ang2 && len2(b.vel) < sleep_lin2);
+        V3<R> zero, v = b.vel, av = b.angvel;
+        restrict_linear(v, b.allowed());
+        restrict_angular(av, b.allowed());
+        bool resting = kin ? (av == zero && v == zero) : (len2(av) < b.sleep_ang2 && len2(v) < b.sleep_lin2);
         b.sleep_time = resting ? b.sleep_time + ts.dt : (R)0;
         if ((kin && !resting) || b.sleep_time < b.deactivation_time) b.marked = true;
     }

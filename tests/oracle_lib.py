@@ -42,6 +42,7 @@ def load():
             "jor_world_set_step_dt": (None, [P, F]), "jor_world_register_linear_contact": (None, [P, I, I, P, P, P]),
             "jor_world_register_manifold": (None, [P, I, I, P, P, I, P]), "jor_world_set_deactivation": (None, [P, I]),
             "jor_world_body_deactivation_time": (None, [P, I, D]), "jor_world_activate_body": (None, [P, I]),
+            "jor_world_body_sleep_thresholds": (None, [P, I, D, D]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]), "jor_world_joint_iterate": (None, [P, I, F]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
@@ -199,6 +200,8 @@ class OracleWorld:
             v = np.ascontiguousarray(init, np.float32)
             getattr(self.lib, "jor_world_add_joint_" + real)(self.h, kind, b1, b2, p(v))
         getattr(self.lib, "jor_world_external_order_" + real)(self.h, 1 if external_order else 0)
+        # World.AllowDeactivation: off unless the scene asks for it, as world_for_scene does
+        self.allow_deactivation(bool(prm.get("allow_deactivation", 0)))
 
     def fn(self, name):
         return getattr(self.lib, name + "_" + self.s)

@@ -103,3 +103,40 @@ def test_one_step_error_against_fp64():
     assert np.median(err) < 1e-4
     assert np.mean(err < 1e-3) > 0.9
     assert dx.max() < 1e-3
+
+
+def test_one_step_contact_errors_against_fp64():
+    """One step from a formed pile: contact normal, depth, point and accumulated impulse of
+    the FP32 device against the FP64 oracle replaying the device's order."""
+    import precision_lib
+    sc = scenes.mixed_pile(n=400, box=(20.0, 3.0, 20.0), y0=0.0, cells=8, seed=17, lattice=3.0)
+    w = world_for_scene(sc)
+    for _ in range(200):
+        w.step(sc["dt"])
+    b0, c0 = w.bodies(), w.contacts()
+    w.step(sc["dt"])
+    r = precision_lib.one_step_errors(sc, b0, c0, w.contacts(), w.bodies())
+    print("one step vs fp64:", r)
+    assert r["contacts_compared"] > 300
+    assert r["contacts_only_fp32"] + r["contacts_only_fp64"] <= 0.01 * r["contacts_compared"]
+    for k in ("normal", "depth", "point"):
+        assert r[k]["median"] < 1e-5 and r[k]["within"] >= 0.99, (k, r[k])
+    assert r["impulse"]["within"] >= 0.99 and r["velocity"]["within"] >= 0.99, r
+
+
+def test_pile_energy_over_1000_steps_against_fp64():
+    """A pile with gravity, ground and heightfield falling and settling for 1000 steps on the
+    device (FP32) and in the FP64 oracle: the potential energy (the pile's height) and the
+    kinetic energy follow the same course; both come to rest."""
+    import precision_lib
+    sc = scenes.mixed_pile(n=300, box=(12.0, 24.0, 12.0), cells=8, seed=41)
+    w = world_for_scene(sc)
+    d = precision_lib.drift(sc, w, 1000)
+    u0 = abs(d["u_fp64"][0])
+    gap_u = np.abs(d["u_gpu"] - d["u_fp64"]) / u0
+    k_peak = d["k_fp64"].max()
+    print("potential gap final %.3g max %.3g; kinetic final gpu %.3g fp64 %.3g (peak %.3g)"
+          % (gap_u[-1], gap_u.max(), d["k_gpu"][-1], d["k_fp64"][-1], k_peak))
+    assert w.counters()["status"] == 0
+    assert gap_u[-1] < 0.02 and gap_u.max() < 0.05
+    assert d["k_gpu"][-1] < 0.02 * k_peak and d["k_fp64"][-1] < 0.02 * k_peak
