@@ -66,6 +66,10 @@ extern "C" {
 #define JG_CONSTRAINT_DISTANCELIMIT 3   /* Dynamics/Constraints/DistanceLimit.cs */
 #define JG_CONSTRAINT_CONELIMIT 4       /* Dynamics/Constraints/ConeLimit.cs     */
 #define JG_CONSTRAINT_TWISTANGLE 5      /* Dynamics/Constraints/TwistAngle.cs    */
+#define JG_CONSTRAINT_FIXEDANGLE 6      /* Dynamics/Constraints/FixedAngle.cs    */
+#define JG_CONSTRAINT_POINTONPLANE 7    /* Dynamics/Constraints/PointOnPlane.cs  */
+#define JG_CONSTRAINT_ANGULARMOTOR 8    /* Dynamics/Constraints/AngularMotor.cs  */
+#define JG_CONSTRAINT_LINEARMOTOR 9     /* Dynamics/Constraints/LinearMotor.cs   */
 
 /* ---- plain data structures ------------------------------------------------------- */
 
@@ -242,7 +246,8 @@ int jg_set_body_sleep(jg_world* world, int32_t body, float deactivation_time, fl
 int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value);
 
 /* World.CreateConstraint<T> + Initialize (BallSocket.cs:120-138, HingeAngle.cs:84-110,
- * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128), world-space init:
+ * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128, FixedAngle.cs:72-85,
+ * PointOnPlane.cs:89-126, AngularMotor.cs:62-82, LinearMotor.cs:97-115), world-space init:
  *   BallSocket     anchor xyz
  *   HingeAngle     axis xyz, min, max (radians)
  *   DistanceLimit  anchor1 xyz, anchor2 xyz, min, max (offsets from the initial distance;
@@ -250,6 +255,11 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
  *   ConeLimit      axis1 xyz, axis2 xyz, min, max (radians, 0 <= min <= max <= pi, not a
  *                  fixed tilt of 0 or pi)
  *   TwistAngle     axis1 xyz, axis2 xyz, min, max (radians, finite)
+ *   FixedAngle     nothing read (the current relative rotation is kept)
+ *   PointOnPlane   axis xyz (plane normal, fixed in body 1), anchor1 xyz, anchor2 xyz,
+ *                  min, max (signed distance; min >= max fixes it)
+ *   AngularMotor,  axis1 xyz, axis2 xyz, target velocity, maximum torque (force) >= 0
+ *   LinearMotor
  * Invalid arguments return JG_ERR_INVALID_ARG (the reference's ArgumentException). */
 int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,
                       const float* init, int32_t* out_id);

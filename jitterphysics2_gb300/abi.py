@@ -35,6 +35,7 @@ MLP_NW = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_OUT * ML
 MLP_NPARAM = MLP_NW + MLP_IN + MLP_IN + MLP_OUT  # + feature mean, feature scale, output scale
 WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
 CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE, CONSTRAINT_DISTANCELIMIT, CONSTRAINT_CONELIMIT, CONSTRAINT_TWISTANGLE = 1, 2, 3, 4, 5
+CONSTRAINT_FIXEDANGLE, CONSTRAINT_POINTONPLANE, CONSTRAINT_ANGULARMOTOR, CONSTRAINT_LINEARMOTOR = 6, 7, 8, 9
 
 ERROR_NAMES = {
     JG_ERR_INVALID_ARG: "JG_ERR_INVALID_ARG", JG_ERR_CAPACITY: "JG_ERR_CAPACITY",

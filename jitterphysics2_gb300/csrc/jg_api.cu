@@ -658,8 +658,19 @@ static q4 from_to_rotation(v3 from, v3 to) {
 
 int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
     if (!w || !init) return JG_ERR_INVALID_ARG;
-    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_TWISTANGLE) return JG_ERR_INVALID_ARG;
-    if (kind >= JG_CONSTRAINT_DISTANCELIMIT) {
+    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_LINEARMOTOR) return JG_ERR_INVALID_ARG;
+    if (kind == JG_CONSTRAINT_POINTONPLANE) {
+        // PointOnPlane.Initialize (PointOnPlane.cs:89-100): a non-zero finite axis, finite
+        // anchors, limits that are not NaN
+        for (int i = 0; i < 9; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
+        if (len2(mk3(init[0], init[1], init[2])) == 0.f || std::isnan(init[9]) || std::isnan(init[10])) return JG_ERR_INVALID_ARG;
+    } else if (kind == JG_CONSTRAINT_ANGULARMOTOR || kind == JG_CONSTRAINT_LINEARMOTOR) {
+        // AngularMotor.Initialize (AngularMotor.cs:62-82), LinearMotor.Initialize
+        // (LinearMotor.cs:97-115): non-zero finite axes; MaximumTorque / MaximumForce >= 0
+        for (int i = 0; i < 6; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
+        if (len2(mk3(init[0], init[1], init[2])) == 0.f || len2(mk3(init[3], init[4], init[5])) == 0.f) return JG_ERR_INVALID_ARG;
+        if (!std::isfinite(init[6]) || !(init[7] >= 0.f)) return JG_ERR_INVALID_ARG;
+    } else if (kind >= JG_CONSTRAINT_DISTANCELIMIT && kind <= JG_CONSTRAINT_TWISTANGLE) {
         // the reference's argument checks (DistanceLimit.cs:99-103, ConeLimit.cs:96-99 and
         // :228-238, TwistAngle.cs:88-92)
         for (int i = 0; i < 6; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
@@ -719,6 +730,23 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
         J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
         J.lim = make_float4(init[6], init[7], 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_FIXEDANGLE) {
+        // FixedAngle.Initialize (FixedAngle.cs:72-85): Q0 is the current relative rotation
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
+        J.q0 = f4(qmul(qconj(q2), q1));
+    } else if (kind == JG_CONSTRAINT_POINTONPLANE) {
+        // PointOnPlane.Initialize (PointOnPlane.cs:100-126)
+        v3 axis = normalize(mk3(init[0], init[1], init[2]));
+        J.la1 = f4(rotate_inv(mk3(init[3], init[4], init[5]) - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(mk3(init[6], init[7], init[8]) - p2, q2), 0.f);
+        J.axis = f4(rotate_inv(axis, q1), 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+        J.lim = make_float4(init[9], init[10], 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_ANGULARMOTOR || kind == JG_CONSTRAINT_LINEARMOTOR) {
+        // AngularMotor / LinearMotor Initialize with TargetVelocity and MaximumTorque (Force)
+        J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
+        J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
+        J.lim = make_float4(0.f, init[7], init[6], 0.f);
     } else if (kind == JG_CONSTRAINT_TWISTANGLE) {
         // TwistAngle.Initialize (TwistAngle.cs:85-128): Q0 is the initial relative rotation
         // turned so that body 1's axis lies on body 2's
@@ -1110,7 +1138,7 @@ int jg_check_state(const void* buf, int64_t size, int32_t nb, int32_t ns, int32_
     for (int j = 0; j < h.nj; j++) {
         int4 hd;
         memcpy(&hd, jp + sizeof(JointDev) * (size_t)j, sizeof(hd));
-        if (hd.x < JG_CONSTRAINT_BALLSOCKET || hd.x > JG_CONSTRAINT_TWISTANGLE || hd.y < 0 || hd.y >= nb || hd.z < 0 ||
+        if (hd.x < JG_CONSTRAINT_BALLSOCKET || hd.x > JG_CONSTRAINT_LINEARMOTOR || hd.y < 0 || hd.y >= nb || hd.z < 0 ||
             hd.z >= nb) {
             g_err = "state blob joint " + std::to_string(j) + " has an invalid kind or body";
             return JG_ERR_INVALID_ARG;

@@ -1,7 +1,9 @@
 // Device constraint rows, solved in the same colours as the contacts: BallSocket
 // (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle (HingeAngle.cs:133-364),
-// DistanceLimit (DistanceLimit.cs:227-391), ConeLimit (ConeLimit.cs:262-404) and TwistAngle
-// (TwistAngle.cs:170-323).  Included by the solver translation unit.  Matrices are
+// DistanceLimit (DistanceLimit.cs:227-391), ConeLimit (ConeLimit.cs:262-404), TwistAngle
+// (TwistAngle.cs:170-323), FixedAngle (FixedAngle.cs:87-181), PointOnPlane
+// (PointOnPlane.cs:128-256), AngularMotor (AngularMotor.cs:128-180) and LinearMotor
+// (LinearMotor.cs:152-231).  Included by the solver translation unit.  Matrices are
 // row-major float[3][3].
 //
 // JointDev fields of the one-row kinds: la1/la2 anchors (DistanceLimit) or local axes
@@ -601,6 +603,128 @@ __device__ void twist_iterate(const WorldDev& w, JointDev& J, const StepParams& 
     if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, lambda * jr); store_vel(w.body, i2, b2); }
 }
 
+// ---- FixedAngle, PointOnPlane, AngularMotor, LinearMotor ------------------------------------
+// FixedAngle.PrepareForIterationFixedAngle (FixedAngle.cs:87-128): three angular rows, the
+// Jacobian -2 x the rotation-log derivative of Q0 conj(q1) q2 (q0), softness prm.y, bias
+// factor prm.x; Jacobian in jac[0..2], inverse effective mass in eff[0..2], hemisphere bil.w
+__device__ void fixed_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 err;
+    int hemi;
+    M3x m = calc_jacobian(qmul(mkq(J.q0), qconj(mkq(w.q[i1]))), mkq(w.q[i2]), err, hemi);
+    M3x jac;
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) jac.a[i][k] = -2.0f * m.a[i][k];
+    v3 acc = mk3(J.acc);
+    int old_hemi = (int)J.bil.w;
+    if (old_hemi != 0 && old_hemi != hemi) acc = mk3(0.f);
+    M3x eff = sym_transform_full(sym_add(b1.I, b2.I), jac);
+    float soft = J.prm.y * sp.inv_sub_dt;
+    eff.a[0][0] += soft; eff.a[1][1] += soft; eff.a[2][2] += soft;
+    eff = inv_symmetric(eff);
+    v3 bias = (-err) * J.prm.x * sp.inv_dt;
+    v3 imp = mtv(jac, acc);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, imp); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, imp); store_vel(w.body, i2, b2); }
+    J.acc = f4(acc, 0.f);
+    J.bias = f4(bias, 0.f);
+    jstore_m(J.eff, eff);
+    jstore_m(J.jac, jac);
+    J.bil = make_float4(0.f, 0.f, 0.f, (float)hemi);
+}
+// FixedAngle.IterateFixedAngle (FixedAngle.cs:159-181)
+__device__ void fixed_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    M3x jac = jload_m(J.jac), eff = jload_m(J.eff);
+    v3 jv = mv(jac, b1.w - b2.w);
+    v3 acc = mk3(J.acc);
+    v3 soft = acc * (J.prm.y * sp.inv_sub_dt);
+    v3 lambda = -1.0f * mv(eff, (jv + mk3(J.bias)) + soft);
+    J.acc = f4(acc + lambda, 0.f);
+    v3 imp = mtv(jac, lambda);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, imp); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, imp); store_vel(w.body, i2, b2); }
+}
+
+// PointOnPlane.PrepareForIterationPointOnPlane (PointOnPlane.cs:128-200): one row along the
+// plane normal (axis, local to body 1), the arm of body 1 measured to the second anchor; the
+// same row layout and iteration as DistanceLimit (PointOnPlane.cs:218-256)
+__device__ void plane_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 axis = rotate(mk3(J.axis), q1);
+    v3 r1 = rotate(mk3(J.la1), q1), r2 = rotate(mk3(J.la2), q2);
+    v3 u = (mk3(w.pos[i2]) + r2) - (mk3(w.pos[i1]) + r1);
+    v3 j0 = -axis, j1 = -cross(r1 + u, axis), j2 = axis, j3 = cross(r2, axis);
+    J.eff[0] = f4(j0, 0.f); J.eff[1] = f4(j1, 0.f); J.eff[2] = f4(j2, 0.f); J.jac[0] = f4(j3, 0.f);
+    float err = dot(u, axis);
+    const float lo = J.lim.x, hi = J.lim.y;
+    int clamp;
+    if (lo >= hi) { err -= 0.5f * lo + 0.5f * hi; clamp = 3; }
+    else if (err >= hi) { err -= hi; clamp = 1; }
+    else if (err <= lo) { err -= lo; clamp = 2; }
+    else { J.lim.w = 0.f; J.acc.x = 0.f; J.bil.x = 1.0f; return; }
+    J.lim.w = (float)clamp;
+    float m = dot(cmul(j0, b1.im), j0) + dot(cmul(j2, b2.im), j2) + dot(sym_mul(b1.I, j1), j1) + dot(sym_mul(b2.I, j3), j3);
+    float eff = row_mass(m, J.prm.y, sp);
+    if (eff == 0.0f) J.acc.x = 0.f;
+    J.bil.x = eff;
+    J.bias.x = err * J.prm.x * sp.inv_dt;
+    const float a = J.acc.x;
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v + cmul(j0 * a, b1.im);
+        b1.w = b1.w + sym_mul(b1.I, j1 * a);
+        store_vel(w.body, i1, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(j2 * a, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, j3 * a);
+        store_vel(w.body, i2, b2);
+    }
+}
+
+// AngularMotor (AngularMotor.cs:128-180) and LinearMotor (LinearMotor.cs:152-231): a velocity
+// drive about (along) an axis of each body (la1, la2 local); lim = (impulse limit of the
+// substep, maximum torque or force, target velocity); the world axes in eff[0], eff[1], the
+// effective mass in bil.x, the accumulated impulse in acc.x
+__device__ __forceinline__ float motor_response(const LBody& b, v3 a, bool linear) {
+    return linear ? dot(cmul(a, b.im), a) : dot(sym_mul(b.I, a), a);
+}
+__device__ __forceinline__ void motor_push(LBody& b, v3 imp, bool linear) {
+    if (linear) b.v = b.v + cmul(imp, b.im);
+    else b.w = b.w + sym_mul(b.I, imp);
+}
+__device__ void motor_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const bool lin = J.hdr.x == JG_CONSTRAINT_LINEARMOTOR;
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 j1 = rotate(mk3(J.la1), mkq(w.q[i1])), j2 = rotate(mk3(J.la2), mkq(w.q[i2]));
+    float m = motor_response(b1, j1, lin) + motor_response(b2, j2, lin);
+    float eff = m > 0 ? 1.0f / m : 0.0f;
+    if (eff == 0.0f) J.acc.x = 0.f;
+    J.bil.x = eff;
+    J.lim.x = sp.sub_dt * J.lim.y;
+    J.eff[0] = f4(j1, 0.f); J.eff[1] = f4(j2, 0.f);
+    const float a = J.acc.x;
+    if (b1.flags & SB_DYNAMIC) { motor_push(b1, -(j1 * a), lin); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { motor_push(b2, j2 * a, lin); store_vel(w.body, i2, b2); }
+}
+__device__ void motor_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const bool lin = J.hdr.x == JG_CONSTRAINT_LINEARMOTOR;
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 j1 = mk3(J.eff[0]), j2 = mk3(J.eff[1]);
+    float jv = lin ? dot(-j1, b1.v) + dot(j2, b2.v) : dot(-j1, b1.w) + dot(j2, b2.w);
+    float lambda = -(jv - J.lim.z) * J.bil.x;
+    float old = J.acc.x;
+    J.acc.x = fminf(fmaxf(J.acc.x + lambda, -J.lim.x), J.lim.x);
+    lambda = J.acc.x - old;
+    if (b1.flags & SB_DYNAMIC) { motor_push(b1, -(j1 * lambda), lin); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { motor_push(b2, j2 * lambda, lin); store_vel(w.body, i2, b2); }
+}
+
 __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
     switch (J.hdr.x) {
@@ -608,6 +732,9 @@ __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_HINGEANGLE: hinge_prepare(w, J, sp); break;
         case JG_CONSTRAINT_DISTANCELIMIT: distance_prepare(w, J, sp); break;
         case JG_CONSTRAINT_CONELIMIT: cone_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_FIXEDANGLE: fixed_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_POINTONPLANE: plane_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_ANGULARMOTOR: case JG_CONSTRAINT_LINEARMOTOR: motor_prepare(w, J, sp); break;
         default: twist_prepare(w, J, sp); break;
     }
 }
@@ -618,6 +745,9 @@ __device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_HINGEANGLE: hinge_iterate(w, J, sp); break;
         case JG_CONSTRAINT_DISTANCELIMIT: distance_iterate(w, J, sp); break;
         case JG_CONSTRAINT_CONELIMIT: cone_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_FIXEDANGLE: fixed_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_POINTONPLANE: distance_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_ANGULARMOTOR: case JG_CONSTRAINT_LINEARMOTOR: motor_iterate(w, J, sp); break;
         default: twist_iterate(w, J, sp); break;
     }
 }

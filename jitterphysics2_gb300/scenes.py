@@ -413,6 +413,54 @@ def bullets(n=256, speed=(60.0, 150.0), speculative=True, seed=12351, spacing=1.
                 params=dict(substeps=2, solver_iterations=8, relax_iterations=4), dt=1.0 / 60.0)
 
 
+def mechanism_chains(n_chains=16, seed=12353, spacing=1.0):
+    """Chains of four boxes hanging from static anchors, one of each device row kind the
+    limb chains do not use: link 1 hangs on a BallSocket and is spun about the chain axis by
+    an AngularMotor; link 2 is welded to it (BallSocket + FixedAngle); link 3 is held on
+    link 2's horizontal plane by a fixed PointOnPlane, kept at its distance by a fixed
+    DistanceLimit and pushed along the chain by a LinearMotor; link 4 is welded to link 3.
+    Links are 0.6 long with 0.4 gaps and the chains are 8 apart: no contacts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    per = 5
+    n = n_chains * per
+    bodies = _body(n)
+    shapes = np.zeros(n, abi.SHAPE_DTYPE)
+    joints = []
+    x_axis, y_axis = (1.0, 0.0, 0.0), (0.0, 1.0, 0.0)
+    for c in range(n_chains):
+        a = c * per
+        base = np.array([0.0, 10.0, 8.0 * c])
+        bodies["position"][a] = base
+        bodies["motion_type"][a] = abi.MOTION_STATIC
+        bodies["inv_mass"][a] = 0.0
+        bodies["inv_inertia"][a] = 0.0
+        shapes["kind"][a] = abi.SHAPE_BOX
+        shapes["body"][a] = a
+        shapes["dims"][a, :3] = (0.2, 0.2, 0.2)
+        for k in range(1, per):
+            i = a + k
+            bodies["position"][i] = base + (spacing * k, 0.0, 0.0)
+            bodies["angular_velocity"][i] = rng.normal(0.0, 1.0, 3)
+            shapes["kind"][i] = abi.SHAPE_BOX
+            shapes["body"][i] = i
+            shapes["dims"][i, :3] = (0.3, 0.12, 0.12)
+        mid = lambda k: tuple(base + (spacing * (k - 0.5), 0.0, 0.0))
+        pos = lambda k: tuple(base + (spacing * k, 0.0, 0.0))
+        joints.append((abi.CONSTRAINT_BALLSOCKET, a, a + 1, mid(1)))
+        joints.append((abi.CONSTRAINT_ANGULARMOTOR, a, a + 1, x_axis + x_axis + (2.0, 5.0)))
+        joints.append((abi.CONSTRAINT_BALLSOCKET, a + 1, a + 2, mid(2)))
+        joints.append((abi.CONSTRAINT_FIXEDANGLE, a + 1, a + 2, (0.0,)))
+        joints.append((abi.CONSTRAINT_POINTONPLANE, a + 2, a + 3, y_axis + pos(2) + pos(3) + (0.0, 0.0)))
+        joints.append((abi.CONSTRAINT_DISTANCELIMIT, a + 2, a + 3, pos(2) + pos(3) + (1e-6, -1e-6)))
+        joints.append((abi.CONSTRAINT_LINEARMOTOR, a + 2, a + 3, x_axis + x_axis + (0.5, 3.0)))
+        joints.append((abi.CONSTRAINT_BALLSOCKET, a + 3, a + 4, mid(4)))
+        joints.append((abi.CONSTRAINT_FIXEDANGLE, a + 3, a + 4, (0.0,)))
+    _finish_mass(bodies, shapes, np.zeros((0, 3), np.float32), 0, 0, n)
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=joints,
+                params=dict(substeps=4, solver_iterations=8, relax_iterations=4), dt=1.0 / 100.0)
+
+
 def limb_chains(n_chains=16, links=6, seed=12352, spacing=1.0):
     """Chains of boxes hanging from static anchors, each link joined to the next the way a
     ragdoll limb is: BallSocket at the midpoint, ConeLimit on the chain axis (0 to 0.5 rad)

@@ -82,3 +82,90 @@ def test_invalid_constraint_arguments_raise(kind, init):
     with pytest.raises(abi.JitterError) as e:
         w.add_constraint(kind, 1, 2, init)
     assert e.value.code == abi.JG_ERR_INVALID_ARG
+
+
+# ---- FixedAngle, PointOnPlane, AngularMotor, LinearMotor ----------------------------------
+def _quat_rotate(q, v):
+    q = np.asarray(q, np.float64)
+    u, w = q[..., :3], q[..., 3:]
+    t = 2 * np.cross(u, v)
+    return v + w * t + np.cross(u, t)
+
+
+def test_one_step_of_mechanism_chains_matches_the_oracle():
+    """Motor, weld, plane and slider rows (scenes.mechanism_chains): one step from the GPU's
+    state replayed in the oracle in the GPU's order keys, warm-started with the GPU's
+    impulses."""
+    sc = scenes.mechanism_chains(n_chains=16)
+    w = world_for_scene(sc)
+    for _ in range(40):
+        w.step(sc["dt"])
+    b0 = w.bodies()
+    _, j0 = w.constraints()
+    w.step(sc["dt"])
+    b1 = w.bodies()
+    k1, j1 = w.constraints()
+    o = O.OracleWorld(sc, external_order=True)
+    o.set_bodies(b0)
+    o.set_joint_impulses(j0)
+    o.narrowphase()
+    o.set_joint_colors(k1)
+    o.step(sc["dt"], narrow=False)
+    ob = o.bodies()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    err = np.maximum(np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1),
+                     np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1))
+    jo = o.joint_impulses(len(j1))
+    jerr = np.abs(j1 - jo).max(axis=1) / np.maximum(1e-3, np.abs(j1).max(axis=1))
+    kinds = np.array([j[0] for j in sc["joints"]])
+    for kind in (abi.CONSTRAINT_FIXEDANGLE, abi.CONSTRAINT_POINTONPLANE, abi.CONSTRAINT_ANGULARMOTOR,
+                 abi.CONSTRAINT_LINEARMOTOR):
+        assert np.abs(j1[kinds == kind]).max() > 0, kind     # every kind carries an impulse
+    assert err.max() < 1e-3, np.sort(err)[-5:]
+    assert np.mean(jerr < 1e-3) >= 0.999, np.sort(jerr)[-5:]
+
+
+def test_mechanism_chains_keep_their_welds_planes_and_drives():
+    sc = scenes.mechanism_chains(n_chains=8)
+    w = world_for_scene(sc)
+    q0 = sc["bodies"]["orientation"].astype(np.float64)
+    for _ in range(200):
+        w.step(sc["dt"])
+    b = w.bodies()
+    assert w.counters()["status"] == 0
+    q = b["orientation"].astype(np.float64)
+    per = 5
+    for c in range(8):
+        a = c * per
+        # welded links keep their relative rotation: conj(q1) q2 unchanged
+        for l1, l2 in ((a + 1, a + 2), (a + 3, a + 4)):
+            def rel(qq):
+                x1 = np.array([-qq[l1][0], -qq[l1][1], -qq[l1][2], qq[l1][3]])
+                x2 = qq[l2]
+                return np.array([x1[3] * x2[0] + x1[0] * x2[3] + x1[1] * x2[2] - x1[2] * x2[1],
+                                 x1[3] * x2[1] - x1[0] * x2[2] + x1[1] * x2[3] + x1[2] * x2[0],
+                                 x1[3] * x2[2] + x1[0] * x2[1] - x1[1] * x2[0] + x1[2] * x2[3],
+                                 x1[3] * x2[3] - x1[0] * x2[0] - x1[1] * x2[1] - x1[2] * x2[2]])
+            r0, r1 = rel(q0), rel(q)
+            assert min(np.abs(r1 - r0).max(), np.abs(r1 + r0).max()) < 0.02
+        # the plane of link 2 holds link 3's anchor (its centre) at zero height in link 2's frame
+        n = _quat_rotate(q[a + 2], np.array([0.0, 1.0, 0.0]))
+        assert abs((b["position"][a + 3] - b["position"][a + 2]) @ n) < 0.02
+        # the angular motor spins link 1 about the chain axis at its target (2 rad/s)
+        axis0 = _quat_rotate(q[a], np.array([1.0, 0.0, 0.0]))
+        axis1 = _quat_rotate(q[a + 1], np.array([1.0, 0.0, 0.0]))
+        assert abs(b["angular_velocity"][a + 1] @ axis1 - b["angular_velocity"][a] @ axis0 - 2.0) < 0.2
+
+
+@pytest.mark.parametrize("kind, init", [
+    (abi.CONSTRAINT_POINTONPLANE, (0, 0, 0) + (0, 0, 0) + (1, 0, 0) + (0.0, 0.0)),    # zero axis
+    (abi.CONSTRAINT_POINTONPLANE, (0, 1, 0) + (0, 0, 0) + (1, 0, 0) + (np.nan, 0.0)), # NaN limit
+    (abi.CONSTRAINT_ANGULARMOTOR, (1, 0, 0, 0, 0, 0, 1.0, 1.0)),                      # zero axis
+    (abi.CONSTRAINT_LINEARMOTOR, (1, 0, 0, 1, 0, 0, 1.0, -1.0)),                      # negative force
+])
+def test_invalid_mechanism_arguments_raise(kind, init):
+    sc = scenes.mechanism_chains(n_chains=1)
+    w = world_for_scene(sc)
+    with pytest.raises(abi.JitterError) as e:
+        w.add_constraint(kind, 1, 2, init)
+    assert e.value.code == abi.JG_ERR_INVALID_ARG
