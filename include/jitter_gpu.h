@@ -271,6 +271,15 @@ int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body
  * colouring, substepped solve + integration, contact and body update. */
 int jg_step(jg_world* world, float dt);
 
+/* World.Stabilize (World.Step.cs:318-392): CheckDeactivation, then for each substep the
+ * solve (prepare, solver_iterations iterations) and relaxation_iterations relaxation passes
+ * over the contacts and constraints already present (restored with jg_import_state, for
+ * example), with no collision detection and no integration of forces, velocities or
+ * positions.  The reference's ArgumentException cases (dt negative or not finite, solver
+ * iterations below one, negative relaxation) return JG_ERR_INVALID_ARG / JG_ERR_NONFINITE.
+ * Arbiters left without contact points are dropped here rather than at the next step. */
+int jg_stabilize(jg_world* world, float dt, int32_t solver_iterations, int32_t relaxation_iterations);
+
 /* Like jg_step but with the body state taken from and returned to host buffers
  * (copies included), the call a host that keeps its own bodies makes: one copy of the array
  * each way (pinned memory copies fastest), validated as jg_upload_bodies does. */
@@ -378,11 +387,14 @@ int jg_collect_training(jg_world* world, float* features, float* targets, int32_
 /* ---- batched worlds (no reference counterpart) ---------------------------------------------- */
 
 /* Many independent worlds stepped by one captured launch sequence.  Bodies, shapes and
- * constraints carry their world index; all worlds share params and dt. */
+ * constraints carry their world index; all worlds share params and dt.  jg_batch_step runs
+ * the step as one CUDA-graph launch (captured once per arbiter-buffer parity and dt, and
+ * again after uploads that change the world's shape); its timings hold only the total. */
 int jg_batch_create(const jg_world_params* params, int32_t n_worlds, jg_world** out_world);
 int jg_batch_step(jg_world* world, float dt);
-/* Autotunes solver block shape / CTAs per SM and narrowphase tile for this world by
- * timing a few steps of a copy of its state; writes the chosen values into params. */
+/* Autotunes the solve for this world by timing a few steps of a copy of its state: the
+ * solve's form (partitioned tasks or global colours) and its launch shape (threads per CTA,
+ * CTAs per SM); writes the chosen values into params and keeps them. */
 int jg_autotune(jg_world* world, float dt, int32_t steps, jg_world_params* chosen);
 
 /* ---- host utilities ------------------------------------------------------------------------- */

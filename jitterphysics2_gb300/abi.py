@@ -110,6 +110,7 @@ SIGNATURES = {
     "jg_add_constraint": (_I, [_P, _I, _I, _I, _P, _PI]),
     "jg_step": (_I, [_P, _F]),
     "jg_step_host": (_I, [_P, _F, _P, _I]),
+    "jg_stabilize": (_I, [_P, _F, _I, _I]),
     "jg_collide_pairs": (_I, [_P, _P, _I, _P, _P]),
     "jg_collide_pairs_noalloc": (_I, [_P, _P, _I, _P, _P]),
     "jg_manifold_pairs": (_I, [_P, _P, _I, _P, _P, _P]),

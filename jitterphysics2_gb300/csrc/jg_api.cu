@@ -238,6 +238,7 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.record_residual = p.record_residual;
     sp.partition = p.partitioned_solve ? 1 : 0;
     sp.allow_deact = p.allow_deactivation ? 1 : 0;
+    sp.stabilize = 0;
     sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : JG_TASK_BLOCK,
                                        p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
@@ -288,7 +289,8 @@ int launch_step(jg_world* w, const StepParams& sp, bool timed) {
     return JG_OK;
 }
 
-int finish_step(jg_world* w, bool timed) {
+// timed: stage times from the stage events; graph_timed: only the total (a graph replay)
+int finish_step(jg_world* w, bool timed, bool graph_timed = false) {
     CK(cudaMemcpyAsync(w->h_ctr, w->d.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream));
     CK(cudaStreamSynchronize(w->stream));
     CK(cudaGetLastError());
@@ -307,6 +309,10 @@ int finish_step(jg_world* w, bool timed) {
         jg_timings& tm = w->timings;
         tm.broadphase = t[0]; tm.narrowphase = t[1]; tm.add_arbiter = t[2]; tm.coloring = t[3];
         tm.solve = t[4]; tm.update_contacts = t[5]; tm.update_bodies = t[6];
+        cudaEventElapsedTime(&tm.total, w->ev[0], w->ev[7]);
+    } else if (graph_timed) {
+        jg_timings& tm = w->timings;
+        tm = jg_timings{};
         cudaEventElapsedTime(&tm.total, w->ev[0], w->ev[7]);
     }
     if (c.status != 0) {
@@ -784,7 +790,10 @@ static int flush_joints(jg_world* w) {
     return JG_OK;
 }
 
-int jg_step(jg_world* w, float dt) {
+// One step as a stream of launches (stage times recorded) or, with `graph`, as the replay of
+// the step captured for the current arbiter-buffer parity (recaptured when dt or the world's
+// shape changes), timed as a whole.
+static int step_impl(jg_world* w, float dt, bool graph) {
     if (!w) return JG_ERR_INVALID_ARG;
     if (!std::isfinite(dt)) return JG_ERR_NONFINITE;
     if (dt < 0) return JG_ERR_INVALID_ARG;
@@ -795,7 +804,7 @@ int jg_step(jg_world* w, float dt) {
     StepParams sp = make_params(w, dt);
     if (w->d.ns == 0 && w->d.nb == 0) return JG_OK;
     int parity = w->d.cur;
-    if (w->prm.use_graph) {
+    if (graph) {
         if (!w->graph[parity] || w->graph_dt[parity] != dt) {
             if (w->graph[parity]) { cudaGraphExecDestroy(w->graph[parity]); w->graph[parity] = nullptr; }
             cudaGraph_t g;
@@ -810,15 +819,54 @@ int jg_step(jg_world* w, float dt) {
         } else {
             jg_flip_store(w->d);
         }
+        CK(cudaEventRecord(w->ev[0], w->stream));
         CK(cudaGraphLaunch(w->graph[parity], w->stream));
-        return finish_step(w, false);
+        CK(cudaEventRecord(w->ev[7], w->stream));
+        return finish_step(w, false, true);
     }
     int r = launch_step(w, sp, true);
     if (r) return r;
     return finish_step(w, true);
 }
 
-int jg_batch_step(jg_world* w, float dt) { return jg_step(w, dt); }
+int jg_step(jg_world* w, float dt) { return step_impl(w, dt, w && w->prm.use_graph != 0); }
+
+// Batched worlds always step as one graph launch: every world of the batch in the captured
+// sequence, the solve one persistent cooperative kernel over all worlds (one task each).
+int jg_batch_step(jg_world* w, float dt) { return step_impl(w, dt, true); }
+
+// World.Stabilize (World.Step.cs:318-392): the island check, then per substep the prepare,
+// solver_iterations iterations and relaxation_iterations relaxation passes over the present
+// contacts and constraints, with no detection and no integration of forces or velocities.
+int jg_stabilize(jg_world* w, float dt, int32_t iterations, int32_t relax) {
+    if (!w) return JG_ERR_INVALID_ARG;
+    if (!std::isfinite(dt)) return JG_ERR_NONFINITE;
+    if (dt < 0 || iterations < 1 || iterations > 4096 || relax < 0) return JG_ERR_INVALID_ARG;
+    if (dt < 1.401298e-45f) return JG_OK;
+    int fr = flush_joints(w);
+    if (fr) return fr;
+    w->host_current = false;
+    StepParams sp = make_params(w, dt);
+    sp.iterations = iterations;
+    sp.relax = relax;
+    sp.stabilize = 1;
+    sp.record_residual = 0;
+    WorldDev& d = w->d;
+    cudaStream_t s = w->stream;
+    d.allow_deact = sp.allow_deact;
+    k_reset_counters<<<1, 1, 0, s>>>(d.ctr);
+    if (sp.allow_deact) jg_launch_islands(d, s, w->nsm);
+    jg_launch_schedule(d, sp, s, w->nsm);
+    if (jg_launch_color(d, s, w->nsm) < 0) { g_err = "cooperative launch of the colouring failed"; return JG_ERR_CUDA; }
+    jg_flip_store(d);
+    jg_launch_count_contacts(d, s, w->nsm);
+    if (jg_launch_solve(d, sp, s, w->nsm, w->prm.solver_block, w->prm.solver_ctas_per_sm) < 0) {
+        g_err = "cooperative launch of the solver failed";
+        return JG_ERR_CUDA;
+    }
+    invalidate_graphs(w);  // the arbiter store parity changed outside a captured step
+    return finish_step(w, false);
+}
 
 int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
     if (!w || !bodies || n != w->d.nb) return JG_ERR_INVALID_ARG;
@@ -1191,20 +1239,19 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     if (r) return r;
     std::vector<char> snap(size);
     if ((r = jg_export_state(w, snap.data(), size, &size))) return r;
-    // partitioned solve: threads per task CTA (one CTA per SM, shared memory bound);
-    // global-colour solve: threads per CTA x CTAs per SM
-    const bool part = w->prm.partitioned_solve != 0;
+    // the solve's form (spatial tasks with their bodies in shared memory, or global colours)
+    // and its launch shape: threads per task CTA x task CTAs per SM (shared memory bound),
+    // or threads per CTA x CTAs per SM
     const int pblocks[] = {64, 96, 128}, gblocks[] = {128, 256, 512};
     const int pctas[] = {1, 2}, gctas[] = {1, 2, 4};
-    const int* blocks = part ? pblocks : gblocks;
-    const int* ctas = part ? pctas : gctas;
-    const int nbk = 3, nct = part ? 2 : 3;
     float best = 1e30f;
-    int bb = part ? JG_TASK_BLOCK : 256, bc = part ? JG_TASK_CTAS : 2;
+    int bp = w->prm.partitioned_solve != 0, bb = bp ? JG_TASK_BLOCK : 256, bc = bp ? JG_TASK_CTAS : 2;
     jg_world_params saved = w->prm;
-    for (int ib = 0; ib < nbk; ib++)
-        for (int ic = 0; ic < nct; ic++) {
-            const int b = blocks[ib], c = ctas[ic];
+    for (int part = 1; part >= 0; part--)
+    for (int ib = 0; ib < 3; ib++)
+        for (int ic = 0; ic < (part ? 2 : 3); ic++) {
+            const int b = part ? pblocks[ib] : gblocks[ib], c = part ? pctas[ic] : gctas[ic];
+            w->prm.partitioned_solve = part;
             w->prm.solver_block = b;
             w->prm.solver_ctas_per_sm = c;
             w->prm.use_graph = 0;
@@ -1221,9 +1268,10 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             cudaEventDestroy(e0); cudaEventDestroy(e1);
-            if (ok && ms < best) { best = ms; bb = b; bc = c; }
+            if (ok && ms < best) { best = ms; bb = b; bc = c; bp = part; }
         }
     w->prm = saved;
+    w->prm.partitioned_solve = bp;
     w->prm.solver_block = bb;
     w->prm.solver_ctas_per_sm = bc;
     jg_solver_reset_launch_cache(w->d);

@@ -368,7 +368,7 @@ __global__ void k_solve(WorldDev w, StepParams sp) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int* status = &w.ctr->status;
     for (int s = 0; s < sp.substeps; s++) {
-        integrate_forces_all(w, sp, tid, nth);
+        if (!sp.stabilize) integrate_forces_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int it = 0; it < 1 + sp.iterations; it++) {
             float d2 = 0.f, l2 = 0.f;
@@ -376,7 +376,7 @@ __global__ void k_solve(WorldDev w, StepParams sp) {
             if (sp.record_residual && s == 0 && it > 0 && it <= JG_RESID_MAX) block_reduce_add(d2, l2, w.resid + 2 * (it - 1));
         }
         if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
-        integrate_velocities_all(w, sp, tid, nth);
+        if (!sp.stabilize) integrate_velocities_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int it = 0; it < sp.relax; it++) {
             float d2 = 0.f, l2 = 0.f;
@@ -718,7 +718,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     if (w.ctr->ncolors == 0) {
         unsigned level = 0;  // grid phases started so far in this launch
         for (int s = 0; s < sp.substeps; s++) {
-            integrate_forces_all(w, sp, tid, nth);
+            if (!sp.stabilize) integrate_forces_all(w, sp, tid, nth);
             if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             for (int pass = 0; pass < npass; pass++) {
                 const bool relax = pass > sp.iterations;
@@ -739,7 +739,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
                 if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
                     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;  // every task of the pass
                     if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
-                    integrate_velocities_all(w, sp, tid, nth);
+                    if (!sp.stabilize) integrate_velocities_all(w, sp, tid, nth);
                     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
                 }
             }
@@ -750,7 +750,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     // With a remainder: the three grids as three phases per pass with a grid barrier after
     // each, then the remainder in global colours.
     for (int s = 0; s < sp.substeps; s++) {
-        integrate_forces_all(w, sp, tid, nth);
+        if (!sp.stabilize) integrate_forces_all(w, sp, tid, nth);
         if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
         for (int pass = 0; pass < npass; pass++) {
             const bool relax = pass > sp.iterations;
@@ -766,7 +766,7 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
             if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= JG_RESID_MAX) block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
             if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
                 if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
-                integrate_velocities_all(w, sp, tid, nth);
+                if (!sp.stabilize) integrate_velocities_all(w, sp, tid, nth);
                 if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
             }
         }

@@ -254,6 +254,7 @@ struct StepParams {
     int record_residual;
     int partition;               // 1: partitioned solve (tasks + remainder), 0: global colours only
     int allow_deact;             // World.AllowDeactivation: sleeping bodies and rows are skipped
+    int stabilize;               // World.Stabilize: solve only, no force or velocity integration
     int task_maxb;               // bodies a task may hold in the solver's shared memory
 };
 

@@ -38,6 +38,7 @@ class World:
             check(lib.jg_create(ctypes.byref(p), ctypes.byref(h)), "jg_create")
         self._h = h
         self._lib = lib
+        self.n_worlds = n_worlds
         self.n_bodies = 0
         self.n_shapes = 0
         self.n_joints = 0
@@ -109,7 +110,20 @@ class World:
             raise ArgumentException("Time step must be finite.")
         if dt < 0:
             raise ArgumentException("Time step cannot be negative.")
-        check(self._lib.jg_step(self._h, ctypes.c_float(dt)), "jg_step")
+        if self.n_worlds > 1:  # batched worlds: one graph launch per step
+            check(self._lib.jg_batch_step(self._h, ctypes.c_float(dt)), "jg_batch_step")
+        else:
+            check(self._lib.jg_step(self._h, ctypes.c_float(dt)), "jg_step")
+
+    def stabilize(self, dt, solver_iterations, relaxation_iterations=0):
+        """World.Stabilize (World.Step.cs:318-392): the present contacts and constraints
+        re-solved at the velocity level, without detection or integration."""
+        if not np.isfinite(dt):
+            raise ArgumentException("Time step must be finite.")
+        if dt < 0 or solver_iterations < 1 or relaxation_iterations < 0:
+            raise ArgumentException("Invalid time step or iteration count.")
+        check(self._lib.jg_stabilize(self._h, ctypes.c_float(dt), solver_iterations, relaxation_iterations),
+              "jg_stabilize")
 
     def step_host(self, dt, bodies):
         """One step with the body state copied in from and back to a host array."""
@@ -208,7 +222,7 @@ class World:
     def autotune(self, dt, steps=3):
         chosen = abi.WorldParams()
         check(self._lib.jg_autotune(self._h, ctypes.c_float(dt), steps, ctypes.byref(chosen)), "jg_autotune")
-        return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile")}
+        return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile", "partitioned_solve")}
 
     # -- learned warm start (no reference counterpart) ------------------------------------
     def mlp_load(self, params):

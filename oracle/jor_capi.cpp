@@ -365,6 +365,9 @@ template <class R> struct Handle {
         out[0] = I.m11; out[1] = I.m12; out[2] = I.m13; out[3] = I.m22; out[4] = I.m23; out[5] = I.m33;            \
     }                                                                                                              \
     extern "C" void jor_world_step_##SUF(void* h, float dt, int narrow) { ((Handle<R>*)h)->w.step((R)dt, narrow != 0); } \
+    extern "C" void jor_world_stabilize_##SUF(void* h, float dt, int iterations, int relax) {                    \
+        ((Handle<R>*)h)->w.stabilize((R)dt, iterations, relax);                                                    \
+    }                                                                                                              \
     extern "C" double jor_world_step_mt_##SUF(void* h, float dt, int threads) {                                   \
         World<R>& w = ((Handle<R>*)h)->w;                                                                          \
         w.nthreads = threads;                                                                                      \

@@ -434,8 +434,8 @@ template <class R> struct World {
 
     // bodies the step moves: all, or with deactivation the awake ones (memRigidBodies.Active)
     bool moves(const Body<R>& b) const { return !allow_deactivation || b.active(); }
-    void solve_substep(const TimeStep<R>& ts, bool first) {
-        for (auto& b : bodies) if (moves(b)) integrate_forces(b);
+    void solve_substep(const TimeStep<R>& ts, bool first, bool integrate = true) {
+        if (integrate) for (auto& b : bodies) if (moves(b)) integrate_forces(b);
         // prepare (World.Step.cs:1155-1172)
         for (size_t c = 0; c < order_arb.size(); c++) {
             for (int i : order_arb[c]) contactdata_prepare(arbiters[i], bodies, ts);
@@ -450,10 +450,27 @@ template <class R> struct World {
             }
             if (first && record_residual) residuals.push_back(residual_norm(prev));
         }
-        for (auto& b : bodies) if (moves(b)) integrate_velocities(b, ts);
+        if (integrate) for (auto& b : bodies) if (moves(b)) integrate_velocities(b, ts);
         for (int it = 0; it < relax; it++)
             for (size_t c = 0; c < order_arb.size(); c++)
                 for (int i : order_arb[c]) contactdata_iterate(arbiters[i], bodies, false);
+    }
+
+    // World.Stabilize (World.Step.cs:318-392), Regular mode: CheckDeactivation, then per substep
+    // SolveVelocities and RelaxVelocities on the present contacts and constraints, with no
+    // detection and no integration
+    void stabilize(R dt, int solver_iterations, int relaxation_iterations) {
+        if (dt < std::numeric_limits<R>::epsilon()) return;
+        TimeStep<R> ts(dt, substeps);
+        step_dt = dt;
+        if (allow_deactivation) check_deactivation();
+        const int it = iterations, rx = relax;
+        iterations = solver_iterations;
+        relax = relaxation_iterations;
+        build_order();
+        for (int s = 0; s < substeps; s++) solve_substep(ts, false, false);
+        iterations = it;
+        relax = rx;
     }
 
     // RemoveBrokenArbiters (World.Step.cs:839-860): arbiters still without contacts.

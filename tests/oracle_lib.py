@@ -51,6 +51,7 @@ def load():
             "jor_world_set_penalty": (None, [P, I, I, D]), "jor_world_set_arbiter_mode": (None, [P, I, I]),
             "jor_world_set_orientation": (None, [P, I, P]), "jor_world_inertia_world": (None, [P, I, P]),
             "jor_world_step": (None, [P, F, I]), "jor_world_step_mt": (D, [P, F, I]),
+            "jor_world_stabilize": (None, [P, F, I, I]),
             "jor_world_counters": (None, [P, P]), "jor_world_pairs": (I, [P, P, I]),
             "jor_world_pairs_sweep": (I, [P, P, I]),
             "jor_world_residuals": (I, [P, P, I]), "jor_world_detect": (I, [P, I, I, P]),
@@ -214,6 +215,10 @@ class OracleWorld:
 
     def step(self, dt, narrow=True):
         self.fn("jor_world_step")(self.h, dt, 1 if narrow else 0)
+
+    def stabilize(self, dt, iterations, relax=0):
+        """World.Stabilize: the present contacts and constraints re-solved, no integration."""
+        self.fn("jor_world_stabilize")(self.h, dt, iterations, relax)
 
     def step_mt(self, dt, threads):
         return self.fn("jor_world_step_mt")(self.h, dt, threads)

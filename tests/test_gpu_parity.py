@@ -263,3 +263,29 @@ def test_state_export_import_round_trip():
     w.step(sc["dt"])
     b = w.bodies()
     assert np.array_equal(a["position"], b["position"])
+
+
+def test_stabilize_matches_the_oracle():
+    """World.Stabilize on a formed pile: the present contacts re-solved with 10 iterations and
+    2 relaxation passes, no integration; the oracle replays it in the GPU's order."""
+    sc, w = _settled_pile(n=300, steps=120, seed=43)
+    b0, c0 = w.bodies(), w.contacts()
+    w.stabilize(sc["dt"], 10, 2)
+    b1, c1 = w.bodies(), w.contacts()
+    assert np.array_equal(b0["position"], b1["position"]) and np.array_equal(b0["orientation"], b1["orientation"])
+    assert w.counters()["status"] == 0 and len(c1) > 100
+    o = O.OracleWorld(sc, external_order=True)
+    o.set_bodies(b0)
+    o.set_contacts(c0)
+    for c in c1:
+        o.set_arbiter_color(c["shape1"], c["shape2"], c["color"])
+    o.stabilize(sc["dt"], 10, 2)
+    ob = o.bodies()
+    dyn = b1["motion_type"] == abi.MOTION_DYNAMIC
+    err = np.maximum(np.abs(b1["velocity"][dyn] - ob["velocity"][dyn]).max(axis=1),
+                     np.abs(b1["angular_velocity"][dyn] - ob["angular_velocity"][dyn]).max(axis=1))
+    assert np.mean(err < 1e-3) >= 0.999, np.sort(err)[-5:]
+    from jitterphysics2_gb300.world import ArgumentException
+    for args in ((-0.01, 4, 0), (0.01, 0, 0), (0.01, 4, -1), (float("nan"), 4, 0)):
+        with pytest.raises(ArgumentException):
+            w.stabilize(*args)
