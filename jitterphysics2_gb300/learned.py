@@ -31,11 +31,11 @@ def collect(scene, steps, start=0):
     """Steps a world of `scene` and returns the (features, converged impulse) pairs of
     every contact created during steps start..steps-1."""
     w = world_for_scene(scene)
-    w.collect_training()  # arm
+    w.collect_training(capacity=1 << 17)  # arm
     xs, ts = [], []
     for s in range(steps):
         w.step(scene["dt"])
-        x, t = w.collect_training()
+        x, t = w.collect_training(capacity=1 << 17)
         if s >= start and len(x):
             xs.append(x)
             ts.append(t)
@@ -43,6 +43,19 @@ def collect(scene, steps, start=0):
     if not xs:
         return np.zeros((0, abi.MLP_IN), np.float32), np.zeros((0, abi.MLP_OUT), np.float32)
     return np.concatenate(xs), np.concatenate(ts)
+
+
+def collect_many(make_scene, seeds, steps, start, target_pairs):
+    """collect() over scenes of successive seeds until target_pairs pairs are gathered."""
+    xs, ts, n = [], [], 0
+    for seed in seeds:
+        x, t = collect(make_scene(seed), steps=steps, start=start)
+        xs.append(x)
+        ts.append(t)
+        n += len(x)
+        if n >= target_pairs:
+            break
+    return np.concatenate(xs)[:target_pairs], np.concatenate(ts)[:target_pairs]
 
 
 def train(world, X, T, epochs=20, batch=4096, lr=2e-3, seed=0):
@@ -69,6 +82,29 @@ def iterations_to(resid, tol=1e-4):
         if r <= tol:
             return k + 1
     return len(resid) + 1
+
+
+def iterations_to_match(resid_learned, resid_plain, k):
+    """Per step, the iterations the learned warm start needs to reach the residual the plain
+    one has after k iterations (len + 1 when it never does)."""
+    return np.array([iterations_to(rl, rp[k - 1]) for rl, rp in zip(resid_learned, resid_plain)])
+
+
+def throughput(scene, state, params, iterations, steps, learned_start):
+    """Contacts per second over `steps` steps from `state` at `iterations` solver
+    iterations, plain or learned warm start."""
+    mode = abi.WARMSTART_MLP if learned_start else abi.WARMSTART_CACHED
+    w = world_for_scene(scene, warm_start_mode=mode, solver_iterations=iterations)
+    if learned_start:
+        w.mlp_load(params)
+    w.import_state(state)
+    ms, cnt = 0.0, 0
+    for _ in range(steps):
+        w.step(scene["dt"])
+        ms += w.timings()["total"]
+        cnt += w.counters()["contacts"]
+    w.close()
+    return cnt / (ms / 1e3)
 
 
 def paired_residuals(scene, params, steps, settle, iterations=32, tol=1e-4):
