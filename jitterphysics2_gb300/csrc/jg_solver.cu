@@ -523,9 +523,10 @@ __device__ __forceinline__ bool iterate_task(const WorldDev& w, const ArbStore& 
             const float fr = r0.w;
             LBody b1 = l1 >= 0 ? sbody_load(sbody, l1, sst) : fixed_body(r[1], r[2]);
             LBody b2 = l2s >= 0 ? sbody_load(sbody, l2s, sst) : fixed_body(r[1], r[2]);
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (!(usage & (1 << k))) continue;
+            // over the set usage bits only: a warp runs as many rows as its fullest arbiter
+            // has contacts, not one per slot position any of its lanes uses
+            for (unsigned um = (unsigned)usage; um; um &= um - 1) {
+                const int k = __ffs(um) - 1;
                 const float4* q = r + 3 + 5 * k;
                 const float4 cn = q[0], ct1 = q[1];
                 const float4 ct2 = f4(cross(mk3(ct1), mk3(cn)), 0.f);  // bit-identical to the stored tangent 2
@@ -576,8 +577,10 @@ __device__ __forceinline__ bool prepare_task(const WorldDev& w, const ArbStore& 
             const bool s1 = staged && l1 >= 0, s2 = staged && l2 >= 0;
             v3 pos1 = mk3(s1 ? spos[l1] : w.pos[bb.x]), pos2 = mk3(s2 ? spos[l2] : w.pos[bb.y]);
             q4 q1 = mkq(s1 ? sq[l1] : w.q[bb.x]), q2 = mkq(s2 ? sq[l2] : w.q[bb.y]);
-            for (int k = 0; k < 4; k++)
-                if (usage & (1 << k)) prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
+            for (unsigned um = (unsigned)usage; um; um &= um - 1) {
+                const int k = __ffs(um) - 1;
+                prepare_contact(A, k * cap + d, mode, spec, b1, b2, pos1, q1, pos2, q2, sp);
+            }
             if ((mode & 3) && l1 >= 0) sbody_store(sbody, l1, sst, b1);
             if ((mode & 12) && l2 >= 0) sbody_store(sbody, l2, sst, b2);
             deps_release(sver, ls.x, ls.y);
