@@ -70,6 +70,10 @@ extern "C" {
 #define JG_CONSTRAINT_POINTONPLANE 7    /* Dynamics/Constraints/PointOnPlane.cs  */
 #define JG_CONSTRAINT_ANGULARMOTOR 8    /* Dynamics/Constraints/AngularMotor.cs  */
 #define JG_CONSTRAINT_LINEARMOTOR 9     /* Dynamics/Constraints/LinearMotor.cs   */
+#define JG_CONSTRAINT_ANGULARSERVO 10   /* Dynamics/Constraints/AngularServo.cs  */
+#define JG_CONSTRAINT_LINEARSERVO 11    /* Dynamics/Constraints/LinearServo.cs   */
+#define JG_CONSTRAINT_LINEARAXISSERVO 12 /* Dynamics/Constraints/LinearAxisServo.cs */
+#define JG_CONSTRAINT_TWISTSERVO 13     /* Dynamics/Constraints/TwistServo.cs    */
 
 /* ---- plain data structures ------------------------------------------------------- */
 
@@ -247,7 +251,8 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
 
 /* World.CreateConstraint<T> + Initialize (BallSocket.cs:120-138, HingeAngle.cs:84-110,
  * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128, FixedAngle.cs:72-85,
- * PointOnPlane.cs:89-126, AngularMotor.cs:62-82, LinearMotor.cs:97-115), world-space init:
+ * PointOnPlane.cs:89-126, AngularMotor.cs:62-82, LinearMotor.cs:97-115, AngularServo.cs:55-77,
+ * LinearServo.cs:60-73, LinearAxisServo.cs:61-78, TwistServo.cs:69-87), world-space init:
  *   BallSocket     anchor xyz
  *   HingeAngle     axis xyz, min, max (radians)
  *   DistanceLimit  anchor1 xyz, anchor2 xyz, min, max (offsets from the initial distance;
@@ -260,9 +265,23 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
  *                  min, max (signed distance; min >= max fixes it)
  *   AngularMotor,  axis1 xyz, axis2 xyz, target velocity, maximum torque (force) >= 0
  *   LinearMotor
+ *   AngularServo   target relative orientation xyzw (body 2 in body 1's frame, unit; all
+ *                  zero = the current one), maximum torque
+ *   LinearServo    anchor1 xyz, anchor2 xyz, target position xyz (body 1's frame), maximum force
+ *   LinearAxisServo axis xyz (fixed in body 1), anchor1 xyz, anchor2 xyz, target position,
+ *                  maximum force
+ *   TwistServo     axis1 xyz, axis2 xyz, target angle (radians, in [-pi, pi]), maximum torque
+ * A servo's maximum is >= 0 and may be +inf; 0 (the reference's default) applies no impulse.
  * Invalid arguments return JG_ERR_INVALID_ARG (the reference's ArgumentException). */
 int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,
                       const float* init, int32_t* out_id);
+
+/* A servo's target and maximum, the TargetRelativeOrientation / TargetPosition / TargetAngle and
+ * MaximumTorque / MaximumForce setters (AngularServo.cs:79-98, LinearServo.cs:103-124,
+ * LinearAxisServo.cs:131-152, TwistServo.cs:89-112): target is xyzw (AngularServo), xyz
+ * (LinearServo) or one value (LinearAxisServo position, TwistServo angle).  A changed target
+ * drops the servo's warm start; both wake its inactive dynamic bodies (ServoMath.cs:22-28). */
+int jg_set_servo(jg_world* world, int32_t constraint, const float* target, float maximum);
 
 /* ---- the step ------------------------------------------------------------------------- */
 

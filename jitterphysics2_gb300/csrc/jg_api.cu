@@ -20,6 +20,7 @@ void jg_solver_reset_launch_cache(WorldDev& w);
 int jg_solver_init();
 int jg_schedule_init();
 void jg_launch_activate(WorldDev& w, int body, cudaStream_t s);
+void jg_launch_wake_dynamic(WorldDev& w, int body, cudaStream_t s);
 void jg_launch_sleep_settings(WorldDev& w, int body, float t, float lin2, float ang2, cudaStream_t s);
 void jg_launch_sleep_init(float4* sleep, int n, cudaStream_t s);
 int jg_mlp_step_hook(jg_world* w, const StepParams& p);
@@ -662,10 +663,44 @@ static q4 from_to_rotation(v3 from, v3 to) {
     return q4{c.x, c.y, c.z, s * 0.5f};
 }
 
+// The servos' argument checks: ArgumentCheck.UnitQuaternion (ArgumentCheck.cs:157-167, squared
+// length within 1e-3 of 1), NonZero and Finite vectors, a twist target in [-pi, pi]
+// (TwistServo.cs:73), ServoMath.CheckMaximum (ServoMath.cs:15-20: not NaN, >= 0, +inf allowed).
+static bool servo_maximum_ok(float m) { return !std::isnan(m) && m >= 0.f; }
+static int check_servo_init(int kind, const float* init) {
+    const float PI = 3.14159265358979323846f;
+    auto finite = [&](int a, int n) { for (int i = a; i < a + n; i++) if (!std::isfinite(init[i])) return false; return true; };
+    auto nonzero = [&](int a) { return finite(a, 3) && len2(mk3(init[a], init[a + 1], init[a + 2])) != 0.f; };
+    switch (kind) {
+        case JG_CONSTRAINT_ANGULARSERVO: {
+            const bool keep = init[0] == 0.f && init[1] == 0.f && init[2] == 0.f && init[3] == 0.f;
+            if (!keep) {
+                if (!finite(0, 4)) return JG_ERR_INVALID_ARG;
+                float l2 = init[0] * init[0] + init[1] * init[1] + init[2] * init[2] + init[3] * init[3];
+                if (std::fabs(l2 - 1.0f) > 1e-3f) return JG_ERR_INVALID_ARG;
+            }
+            return servo_maximum_ok(init[4]) ? JG_OK : JG_ERR_INVALID_ARG;
+        }
+        case JG_CONSTRAINT_LINEARSERVO:
+            return finite(0, 9) && servo_maximum_ok(init[9]) ? JG_OK : JG_ERR_INVALID_ARG;
+        case JG_CONSTRAINT_LINEARAXISSERVO:
+            return nonzero(0) && finite(3, 7) && servo_maximum_ok(init[10]) ? JG_OK : JG_ERR_INVALID_ARG;
+        case JG_CONSTRAINT_TWISTSERVO:
+            return nonzero(0) && nonzero(3) && std::isfinite(init[6]) && init[6] >= -PI && init[6] <= PI &&
+                           servo_maximum_ok(init[7])
+                       ? JG_OK
+                       : JG_ERR_INVALID_ARG;
+    }
+    return JG_ERR_INVALID_ARG;
+}
+
 int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
     if (!w || !init) return JG_ERR_INVALID_ARG;
-    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_LINEARMOTOR) return JG_ERR_INVALID_ARG;
-    if (kind == JG_CONSTRAINT_POINTONPLANE) {
+    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_TWISTSERVO) return JG_ERR_INVALID_ARG;
+    if (kind >= JG_CONSTRAINT_ANGULARSERVO) {
+        int r = check_servo_init(kind, init);
+        if (r) return r;
+    } else if (kind == JG_CONSTRAINT_POINTONPLANE) {
         // PointOnPlane.Initialize (PointOnPlane.cs:89-100): a non-zero finite axis, finite
         // anchors, limits that are not NaN
         for (int i = 0; i < 9; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
@@ -752,6 +787,37 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         // AngularMotor / LinearMotor Initialize with TargetVelocity and MaximumTorque (Force)
         J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
         J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
+        J.lim = make_float4(0.f, init[7], init[6], 0.f);
+    } else if (kind == JG_CONSTRAINT_ANGULARSERVO) {
+        // AngularServo.Initialize (AngularServo.cs:55-77): the given target relative
+        // orientation, or the current one (conj(q1) q2) when all four are zero
+        q4 t{init[0], init[1], init[2], init[3]};
+        if (init[0] == 0.f && init[1] == 0.f && init[2] == 0.f && init[3] == 0.f) t = qmul(qconj(q1), q2);
+        J.q0 = f4(t);
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
+        J.lim = make_float4(0.f, init[4], 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_LINEARSERVO) {
+        // LinearServo.Initialize (LinearServo.cs:60-73) with TargetPosition and MaximumForce
+        J.la1 = f4(rotate_inv(mk3(init[0], init[1], init[2]) - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(mk3(init[3], init[4], init[5]) - p2, q2), 0.f);
+        J.axis = make_float4(init[6], init[7], init[8], 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+        J.lim = make_float4(0.f, init[9], 0.f, 0.f);
+    } else if (kind == JG_CONSTRAINT_LINEARAXISSERVO) {
+        // LinearAxisServo.Initialize (LinearAxisServo.cs:61-78) with MaximumForce
+        J.axis = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
+        J.la1 = f4(rotate_inv(mk3(init[3], init[4], init[5]) - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(mk3(init[6], init[7], init[8]) - p2, q2), 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.f, 0.f);
+        J.lim = make_float4(0.f, init[10], init[9], 0.f);
+    } else if (kind == JG_CONSTRAINT_TWISTSERVO) {
+        // TwistServo.Initialize (TwistServo.cs:69-87) with MaximumTorque: body 2's axis, and the
+        // reference rotation that turns body 1's axis (expressed in body 2's frame) onto it
+        v3 ax1 = normalize(mk3(init[0], init[1], init[2])), ax2 = normalize(mk3(init[3], init[4], init[5]));
+        v3 B = rotate_inv(ax2, q2);
+        J.axis = f4(B, 0.f);
+        J.q0 = f4(qmul(from_to_rotation(rotate_inv(ax1, q2), B), qmul(qconj(q2), q1)));
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
         J.lim = make_float4(0.f, init[7], init[6], 0.f);
     } else if (kind == JG_CONSTRAINT_TWISTANGLE) {
         // TwistAngle.Initialize (TwistAngle.cs:85-128): Q0 is the initial relative rotation
@@ -877,6 +943,53 @@ int jg_step_host(jg_world* w, float dt, jg_body_desc* bodies, int32_t n) {
     r = jg_step(w, dt);
     if (r) return r;
     return download_bodies_device(w, bodies, n);
+}
+
+// The servos' TargetRelativeOrientation / TargetPosition / TargetAngle and MaximumTorque /
+// MaximumForce setters (AngularServo.cs:79-98, LinearServo.cs:103-124, LinearAxisServo.cs:131-152,
+// TwistServo.cs:89-112): a changed target drops the warm start (and the AngularServo's
+// hemisphere), and both setters wake the servo's dynamic bodies (ServoMath.cs:22-28).
+int jg_set_servo(jg_world* w, int32_t id, const float* target, float maximum) {
+    if (!w || !target || id < 0) return JG_ERR_INVALID_ARG;
+    int r = flush_joints(w);
+    if (r) return r;
+    if (id >= w->nj_host) return JG_ERR_INVALID_ARG;
+    JointDev J;
+    CK(cudaMemcpy(&J, w->d.joints + id, sizeof(JointDev), cudaMemcpyDeviceToHost));
+    const int kind = J.hdr.x;
+    if (kind < JG_CONSTRAINT_ANGULARSERVO || kind > JG_CONSTRAINT_TWISTSERVO || !servo_maximum_ok(maximum))
+        return JG_ERR_INVALID_ARG;
+    const float PI = 3.14159265358979323846f;
+    bool changed;
+    if (kind == JG_CONSTRAINT_ANGULARSERVO) {
+        for (int i = 0; i < 4; i++) if (!std::isfinite(target[i])) return JG_ERR_INVALID_ARG;
+        float l2 = target[0] * target[0] + target[1] * target[1] + target[2] * target[2] + target[3] * target[3];
+        if (std::fabs(l2 - 1.0f) > 1e-3f) return JG_ERR_INVALID_ARG;
+        float4 t = make_float4(target[0], target[1], target[2], target[3]);
+        changed = memcmp(&t, &J.q0, sizeof(t)) != 0;
+        J.q0 = t;
+        if (changed) J.bil.w = 0.f;
+    } else if (kind == JG_CONSTRAINT_LINEARSERVO) {
+        for (int i = 0; i < 3; i++) if (!std::isfinite(target[i])) return JG_ERR_INVALID_ARG;
+        float4 t = make_float4(target[0], target[1], target[2], 0.f);
+        changed = memcmp(&t, &J.axis, sizeof(t)) != 0;
+        J.axis = t;
+    } else {
+        if (!std::isfinite(target[0])) return JG_ERR_INVALID_ARG;
+        if (kind == JG_CONSTRAINT_TWISTSERVO && !(target[0] >= -PI && target[0] <= PI)) return JG_ERR_INVALID_ARG;
+        changed = memcmp(&target[0], &J.lim.z, sizeof(float)) != 0;
+        J.lim.z = target[0];
+    }
+    if (changed) J.acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    J.lim.y = maximum;
+    CK(cudaMemcpy(w->d.joints + id, &J, sizeof(JointDev), cudaMemcpyHostToDevice));
+    for (int b : {J.hdr.y, J.hdr.z}) {
+        jg_launch_wake_dynamic(w->d, b, w->stream);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(w->stream));
+    w->host_current = false;
+    return JG_OK;
 }
 
 int jg_activate_body(jg_world* w, int32_t body) {

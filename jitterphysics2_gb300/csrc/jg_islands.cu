@@ -107,6 +107,16 @@ __global__ void k_activate(WorldDev w, int b) {
     w.binfo[b] = bi;
 }
 
+// ServoMath.WakeBodies (ServoMath.cs:22-28): an inactive dynamic body is activated at the
+// next step; other bodies are left alone
+__global__ void k_wake_dynamic(WorldDev w, int b) {
+    int4 bi = w.binfo[b];
+    if (bi.x != JG_MOTION_DYNAMIC || (bi.y & JG_BODY_ACTIVE)) return;
+    w.sleep[b].x = 0.f;
+    bi.w |= 3;  // AddToActiveList
+    w.binfo[b] = bi;
+}
+
 __global__ void k_sleep_settings(WorldDev w, int b, float deactivation_time, float lin2, float ang2) {
     float4 s = w.sleep[b];
     w.sleep[b] = make_float4(s.x, deactivation_time, lin2, ang2);
@@ -127,6 +137,7 @@ void jg_launch_islands(WorldDev& w, cudaStream_t s, int nsm) {
     k_uf_apply<<<blocks, 256, 0, s>>>(w);
 }
 void jg_launch_activate(WorldDev& w, int body, cudaStream_t s) { k_activate<<<1, 1, 0, s>>>(w, body); }
+void jg_launch_wake_dynamic(WorldDev& w, int body, cudaStream_t s) { k_wake_dynamic<<<1, 1, 0, s>>>(w, body); }
 void jg_launch_sleep_settings(WorldDev& w, int body, float t, float lin2, float ang2, cudaStream_t s) {
     k_sleep_settings<<<1, 1, 0, s>>>(w, body, t, lin2, ang2);
 }

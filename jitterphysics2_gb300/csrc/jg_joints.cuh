@@ -2,8 +2,10 @@
 // (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle (HingeAngle.cs:133-364),
 // DistanceLimit (DistanceLimit.cs:227-391), ConeLimit (ConeLimit.cs:262-404), TwistAngle
 // (TwistAngle.cs:170-323), FixedAngle (FixedAngle.cs:87-181), PointOnPlane
-// (PointOnPlane.cs:128-256), AngularMotor (AngularMotor.cs:128-180) and LinearMotor
-// (LinearMotor.cs:152-231).  Included by the solver translation unit.  Matrices are
+// (PointOnPlane.cs:128-256), AngularMotor (AngularMotor.cs:128-180), LinearMotor
+// (LinearMotor.cs:152-231), AngularServo (AngularServo.cs:125-172), LinearServo
+// (LinearServo.cs:149-201), LinearAxisServo (LinearAxisServo.cs:169-224) and TwistServo
+// (TwistServo.cs:150-192).  Included by the solver translation unit.  Matrices are
 // row-major float[3][3].
 //
 // JointDev fields of the one-row kinds: la1/la2 anchors (DistanceLimit) or local axes
@@ -725,6 +727,204 @@ __device__ void motor_iterate(const WorldDev& w, JointDev& J, const StepParams& 
     if (b2.flags & SB_DYNAMIC) { motor_push(b2, j2 * lambda, lin); store_vel(w.body, i2, b2); }
 }
 
+// ---- servos: AngularServo, LinearServo, LinearAxisServo, TwistServo ------------------------
+// ServoMath (Internal/ServoMath.cs:30-49): the impulse limit of a substep, and the clamps of a
+// vector impulse (its length) and of an angular one (the length of J^T imp)
+__device__ __forceinline__ float servo_max_impulse(float maximum, float dt) { return dt > 0.f ? maximum * dt : 0.f; }
+__device__ __forceinline__ float net_clamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ bool pos_inf(float x) { return isinf(x) && x > 0.f; }
+__device__ __forceinline__ v3 servo_clamp_magnitude(v3 imp, float maxi) {
+    if (pos_inf(maxi)) return imp;
+    const float l2 = dot(imp, imp);
+    return l2 > maxi * maxi ? imp * (maxi / sqrtf(l2)) : imp;
+}
+__device__ __forceinline__ v3 servo_clamp_angular(v3 imp, const M3x& jac, float maxi) {
+    if (pos_inf(maxi)) return imp;
+    const v3 a = mtv(jac, imp);
+    const float l2 = dot(a, a);
+    return l2 > maxi * maxi ? imp * (maxi / sqrtf(l2)) : imp;
+}
+
+// AngularServo (AngularServo.cs:125-172): three angular rows towards the target relative
+// orientation q0; Jacobian in jac[0..2], inverse effective mass in eff[0..2], maximum torque
+// lim.y, hemisphere bil.w
+__device__ void angular_servo_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 err;
+    int hemi;
+    M3x m = calc_jacobian(qmul(qconj(mkq(J.q0)), qconj(mkq(w.q[i1]))), mkq(w.q[i2]), err, hemi);
+    M3x jac;
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) jac.a[i][k] = -2.0f * m.a[i][k];
+    v3 acc = mk3(J.acc);
+    int old_hemi = (int)J.bil.w;
+    if (old_hemi != 0 && old_hemi != hemi) acc = mk3(0.f);
+    M3x eff = sym_transform_full(sym_add(b1.I, b2.I), jac);
+    float soft = J.prm.y * sp.inv_sub_dt;
+    eff.a[0][0] += soft; eff.a[1][1] += soft; eff.a[2][2] += soft;
+    eff = inv_symmetric(eff);
+    v3 bias = (-err) * J.prm.x * sp.inv_dt;
+    acc = servo_clamp_angular(acc, jac, servo_max_impulse(J.lim.y, sp.sub_dt));
+    v3 imp = mtv(jac, acc);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, imp); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, imp); store_vel(w.body, i2, b2); }
+    J.acc = f4(acc, 0.f);
+    J.bias = f4(bias, 0.f);
+    jstore_m(J.eff, eff);
+    jstore_m(J.jac, jac);
+    J.bil = make_float4(0.f, 0.f, 0.f, (float)hemi);
+}
+__device__ void angular_servo_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    M3x jac = jload_m(J.jac), eff = jload_m(J.eff);
+    v3 jv = mv(jac, b1.w - b2.w);
+    v3 acc = mk3(J.acc);
+    v3 soft = acc * (J.prm.y * sp.inv_sub_dt);
+    v3 lambda = -1.0f * mv(eff, (jv + mk3(J.bias)) + soft);
+    v3 next = servo_clamp_angular(acc + lambda, jac, servo_max_impulse(J.lim.y, sp.sub_dt));
+    J.acc = f4(next, 0.f);
+    v3 imp = mtv(jac, next - acc);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, imp); store_vel(w.body, i1, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, imp); store_vel(w.body, i2, b2); }
+}
+
+// LinearServo (LinearServo.cs:149-201): three linear rows pulling anchor 2 to anchor 1 offset
+// by the target (axis, body 1's frame); arms in r1, r2, inverse effective mass in eff[0..2],
+// maximum force lim.y
+__device__ __forceinline__ void linear_servo_apply(const WorldDev& w, const JointDev& J, LBody& b1, LBody& b2, v3 r1,
+                                                   v3 r2, v3 imp) {
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v - cmul(imp, b1.im);
+        b1.w = b1.w - sym_mul(b1.I, cross(r1, imp));
+        store_vel(w.body, J.hdr.y, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(imp, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, cross(r2, imp));
+        store_vel(w.body, J.hdr.z, b2);
+    }
+}
+__device__ void linear_servo_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 r1 = rotate(mk3(J.la1) + mk3(J.axis), q1), r2 = rotate(mk3(J.la2), q2);
+    M3x cr1 = mskew(r1), cr2 = mskew(r2);
+    M3x t1 = sym_transform_full(b1.I, cr1), t2 = sym_transform_full(b2.I, cr2);
+    // ((Scale(m1) + T1) + Scale(m2)) + T2, component-wise, in the reference's order
+    M3x e;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) e.a[i][j] = t1.a[i][j] + t2.a[i][j];
+    e.a[0][0] = ((b1.im.x + t1.a[0][0]) + b2.im.x) + t2.a[0][0];
+    e.a[1][1] = ((b1.im.y + t1.a[1][1]) + b2.im.y) + t2.a[1][1];
+    e.a[2][2] = ((b1.im.z + t1.a[2][2]) + b2.im.z) + t2.a[2][2];
+    float soft = J.prm.y * sp.inv_sub_dt;
+    e.a[0][0] += soft; e.a[1][1] += soft; e.a[2][2] += soft;
+    jstore_m(J.eff, inv_symmetric(e));
+    v3 bias = (((mk3(w.pos[i2]) + r2) - mk3(w.pos[i1])) - r1) * (J.prm.x * sp.inv_dt);
+    v3 acc = servo_clamp_magnitude(mk3(J.acc), servo_max_impulse(J.lim.y, sp.sub_dt));
+    linear_servo_apply(w, J, b1, b2, r1, r2, acc);
+    J.r1 = f4(r1, 0.f); J.r2 = f4(r2, 0.f);
+    J.acc = f4(acc, 0.f);
+    J.bias = f4(bias, 0.f);
+}
+__device__ void linear_servo_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 r1 = mk3(J.r1), r2 = mk3(J.r2);
+    v3 jv = ((-b1.v - cross(b1.w, r1)) + b2.v) + cross(b2.w, r2);
+    v3 acc = mk3(J.acc);
+    v3 soft = acc * (J.prm.y * sp.inv_sub_dt);
+    v3 lambda = -1.0f * mv(jload_m(J.eff), (jv + mk3(J.bias)) + soft);
+    v3 next = servo_clamp_magnitude(acc + lambda, servo_max_impulse(J.lim.y, sp.sub_dt));
+    J.acc = f4(next, 0.f);
+    linear_servo_apply(w, J, b1, b2, r1, r2, next - acc);
+}
+
+// LinearAxisServo (LinearAxisServo.cs:169-224): one row along an axis of body 1 (axis, local),
+// target position lim.z, maximum force lim.y; Jacobian blocks in eff[0..2] and jac[0], the
+// effective mass in bil.x
+__device__ __forceinline__ void axis_servo_apply(const WorldDev& w, const JointDev& J, LBody& b1, LBody& b2, float a) {
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v + cmul(mk3(J.eff[0]) * a, b1.im);
+        b1.w = b1.w + sym_mul(b1.I, mk3(J.eff[1]) * a);
+        store_vel(w.body, J.hdr.y, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(mk3(J.eff[2]) * a, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, mk3(J.jac[0]) * a);
+        store_vel(w.body, J.hdr.z, b2);
+    }
+}
+__device__ void linear_axis_servo_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    v3 axis = rotate(mk3(J.axis), q1);
+    v3 r1 = rotate(mk3(J.la1), q1), r2 = rotate(mk3(J.la2), q2);
+    v3 sep = ((mk3(w.pos[i2]) + r2) - mk3(w.pos[i1])) - r1;
+    v3 j0 = -axis, j1 = -cross(r1 + sep, axis), j2 = axis, j3 = cross(r2, axis);
+    J.eff[0] = f4(j0, 0.f); J.eff[1] = f4(j1, 0.f); J.eff[2] = f4(j2, 0.f); J.jac[0] = f4(j3, 0.f);
+    float m = dot(cmul(j0, b1.im), j0) + dot(cmul(j2, b2.im), j2) + dot(sym_mul(b1.I, j1), j1) + dot(sym_mul(b2.I, j3), j3) +
+              J.prm.y * sp.inv_sub_dt;
+    float eff = m > 0.f ? 1.0f / m : 0.0f;
+    float acc = eff == 0.0f ? 0.0f : J.acc.x;
+    J.bil.x = eff;
+    J.bias.x = (dot(sep, axis) - J.lim.z) * J.prm.x * sp.inv_dt;
+    const float maxi = servo_max_impulse(J.lim.y, sp.sub_dt);
+    acc = net_clamp(acc, -maxi, maxi);
+    J.acc.x = acc;
+    axis_servo_apply(w, J, b1, b2, acc);
+}
+__device__ void linear_axis_servo_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    float jv = dot(mk3(J.eff[0]), b1.v) + dot(mk3(J.eff[1]), b1.w) + dot(mk3(J.eff[2]), b2.v) + dot(mk3(J.jac[0]), b2.w);
+    float lambda = -(jv + J.bias.x + J.acc.x * J.prm.y * sp.inv_sub_dt) * J.bil.x;
+    const float prev = J.acc.x, maxi = servo_max_impulse(J.lim.y, sp.sub_dt);
+    J.acc.x = net_clamp(prev + lambda, -maxi, maxi);
+    axis_servo_apply(w, J, b1, b2, J.acc.x - prev);
+}
+
+// TwistServo (TwistServo.cs:150-192): the twist about body 2's axis (axis, local) towards the
+// target angle lim.z, reference rotation q0, maximum torque lim.y; Jacobian row jac[0],
+// effective mass bil.x, hemisphere bil.w
+__device__ __forceinline__ void twist_servo_apply(const WorldDev& w, const JointDev& J, LBody& b1, LBody& b2, float a) {
+    const v3 jr = mk3(J.jac[0]);
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, jr * a); store_vel(w.body, J.hdr.y, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, jr * a); store_vel(w.body, J.hdr.z, b2); }
+}
+__device__ void twist_servo_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    v3 jr;
+    int hemi;
+    float angle = calc_twist(qmul(mkq(J.q0), qconj(mkq(w.q[i1]))), mkq(w.q[i2]), mk3(J.axis), jr, hemi);
+    float acc = J.acc.x;
+    int old_hemi = (int)J.bil.w;
+    if (old_hemi != 0 && old_hemi != hemi) acc = 0.f;
+    float m = dot(sym_mul(sym_add(b1.I, b2.I), jr), jr) + J.prm.y * sp.inv_sub_dt;
+    float eff = m > 0.f ? 1.0f / m : 0.0f;
+    if (eff == 0.0f) acc = 0.f;
+    J.jac[0] = f4(jr, 0.f);
+    J.bil = make_float4(eff, 0.f, 0.f, (float)hemi);
+    float error = angle - J.lim.z;
+    J.bias.x = error * J.prm.x * sp.inv_dt;
+    const float maxi = servo_max_impulse(J.lim.y, sp.sub_dt);
+    acc = net_clamp(acc, -maxi, maxi);
+    J.acc.x = acc;
+    twist_servo_apply(w, J, b1, b2, acc);
+}
+__device__ void twist_servo_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    float jv = dot(b1.w - b2.w, mk3(J.jac[0]));
+    float lambda = -J.bil.x * (jv + J.bias.x + J.acc.x * J.prm.y * sp.inv_sub_dt);
+    const float prev = J.acc.x, maxi = servo_max_impulse(J.lim.y, sp.sub_dt);
+    J.acc.x = net_clamp(prev + lambda, -maxi, maxi);
+    twist_servo_apply(w, J, b1, b2, J.acc.x - prev);
+}
+
 __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
     switch (J.hdr.x) {
@@ -735,6 +935,10 @@ __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_FIXEDANGLE: fixed_prepare(w, J, sp); break;
         case JG_CONSTRAINT_POINTONPLANE: plane_prepare(w, J, sp); break;
         case JG_CONSTRAINT_ANGULARMOTOR: case JG_CONSTRAINT_LINEARMOTOR: motor_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_ANGULARSERVO: angular_servo_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_LINEARSERVO: linear_servo_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_TWISTSERVO: twist_servo_prepare(w, J, sp); break;
         default: twist_prepare(w, J, sp); break;
     }
 }
@@ -748,6 +952,10 @@ __device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_FIXEDANGLE: fixed_iterate(w, J, sp); break;
         case JG_CONSTRAINT_POINTONPLANE: distance_iterate(w, J, sp); break;
         case JG_CONSTRAINT_ANGULARMOTOR: case JG_CONSTRAINT_LINEARMOTOR: motor_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_ANGULARSERVO: angular_servo_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_LINEARSERVO: linear_servo_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_TWISTSERVO: twist_servo_iterate(w, J, sp); break;
         default: twist_iterate(w, J, sp); break;
     }
 }

@@ -461,6 +461,56 @@ def mechanism_chains(n_chains=16, seed=12353, spacing=1.0):
                 params=dict(substeps=4, solver_iterations=8, relax_iterations=4), dt=1.0 / 100.0)
 
 
+def servo_chains(n_chains=16, seed=12354, spacing=1.0):
+    """Chains of four boxes hanging from static anchors, one servo of each kind: link 1 hangs
+    on a BallSocket and is turned by an AngularServo towards a rotation of 0.3 rad about z
+    (maximum torque 5); link 2 is held by a LinearServo at an offset of (1, 0.2, 0) from link
+    1 in link 1's frame (maximum force 20); link 3 hangs on a BallSocket from link 2 and is
+    twisted about the chain axis by a TwistServo towards 0.6 rad (maximum torque 3); link 4
+    is pushed along link 3's x axis by a LinearAxisServo towards 1.1 (maximum force 10) and
+    kept within reach by a DistanceLimit.  Links are 0.6 long with 0.4 gaps and the chains
+    are 8 apart: no contacts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    per = 5
+    n = n_chains * per
+    bodies = _body(n)
+    shapes = np.zeros(n, abi.SHAPE_DTYPE)
+    joints = []
+    x_axis = (1.0, 0.0, 0.0)
+    h = 0.15
+    q_target = (0.0, 0.0, float(np.sin(h)), float(np.cos(h)))
+    for c in range(n_chains):
+        a = c * per
+        base = np.array([0.0, 10.0, 8.0 * c])
+        bodies["position"][a] = base
+        bodies["motion_type"][a] = abi.MOTION_STATIC
+        bodies["inv_mass"][a] = 0.0
+        bodies["inv_inertia"][a] = 0.0
+        shapes["kind"][a] = abi.SHAPE_BOX
+        shapes["body"][a] = a
+        shapes["dims"][a, :3] = (0.2, 0.2, 0.2)
+        for k in range(1, per):
+            i = a + k
+            bodies["position"][i] = base + (spacing * k, 0.0, 0.0)
+            bodies["angular_velocity"][i] = rng.normal(0.0, 1.0, 3)
+            shapes["kind"][i] = abi.SHAPE_BOX
+            shapes["body"][i] = i
+            shapes["dims"][i, :3] = (0.3, 0.12, 0.12)
+        mid = lambda k: tuple(base + (spacing * (k - 0.5), 0.0, 0.0))
+        pos = lambda k: tuple(base + (spacing * k, 0.0, 0.0))
+        joints.append((abi.CONSTRAINT_BALLSOCKET, a, a + 1, mid(1)))
+        joints.append((abi.CONSTRAINT_ANGULARSERVO, a, a + 1, q_target + (5.0,)))
+        joints.append((abi.CONSTRAINT_LINEARSERVO, a + 1, a + 2, pos(1) + pos(2) + (spacing, 0.2, 0.0, 20.0)))
+        joints.append((abi.CONSTRAINT_BALLSOCKET, a + 2, a + 3, mid(3)))
+        joints.append((abi.CONSTRAINT_TWISTSERVO, a + 2, a + 3, x_axis + x_axis + (0.6, 3.0)))
+        joints.append((abi.CONSTRAINT_LINEARAXISSERVO, a + 3, a + 4, x_axis + pos(3) + pos(4) + (1.1 * spacing, 10.0)))
+        joints.append((abi.CONSTRAINT_DISTANCELIMIT, a + 3, a + 4, pos(3) + pos(4) + (-0.2, 0.2)))
+    _finish_mass(bodies, shapes, np.zeros((0, 3), np.float32), 0, 0, n)
+    return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
+                triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=joints,
+                params=dict(substeps=4, solver_iterations=8, relax_iterations=4), dt=1.0 / 100.0)
+
+
 def limb_chains(n_chains=16, links=6, seed=12352, spacing=1.0):
     """Chains of boxes hanging from static anchors, each link joined to the next the way a
     ragdoll limb is: BallSocket at the midpoint, ConeLimit on the chain axis (0 to 0.5 rad)

@@ -82,6 +82,12 @@ class World:
         self.n_joints += 1
         return out.value
 
+    def set_servo(self, constraint, target, maximum):
+        """A servo's target and maximum torque / force (the servos' Target* and Maximum*
+        setters): target is xyzw (AngularServo), xyz (LinearServo) or one value."""
+        v = np.ascontiguousarray(np.atleast_1d(target), np.float32)
+        check(self._lib.jg_set_servo(self._h, constraint, ptr(v), ctypes.c_float(maximum)), "jg_set_servo")
+
     def load_scene(self, scene):
         self.set_bodies(scene["bodies"])
         self.set_shapes(scene["shapes"], scene["hull"], scene["triangles"])

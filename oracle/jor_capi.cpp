@@ -14,6 +14,10 @@ using namespace jor;
 #define JOR_CONSTRAINT_POINTONPLANE 7
 #define JOR_CONSTRAINT_ANGULARMOTOR 8
 #define JOR_CONSTRAINT_LINEARMOTOR 9
+#define JOR_CONSTRAINT_ANGULARSERVO 10
+#define JOR_CONSTRAINT_LINEARSERVO 11
+#define JOR_CONSTRAINT_LINEARAXISSERVO 12
+#define JOR_CONSTRAINT_TWISTSERVO 13
 
 namespace {
 
@@ -223,6 +227,18 @@ template <class R> struct Handle {
                        kind == JOR_CONSTRAINT_LINEARMOTOR);                                                        \
         else if (kind == JOR_CONSTRAINT_POINTONPLANE)                                                              \
             plane_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9], (R)init[10]); \
+        else if (kind == JOR_CONSTRAINT_ANGULARSERVO) {                                                            \
+            Q4<R> t((R)init[0], (R)init[1], (R)init[2], (R)init[3]);                                               \
+            if (init[0] == 0 && init[1] == 0 && init[2] == 0 && init[3] == 0)                                      \
+                t = qmul(qconj(w.bodies[b1].q), w.bodies[b2].q);                                                   \
+            angular_servo_init(j, t, (R)init[4]);                                                                  \
+        } else if (kind == JOR_CONSTRAINT_LINEARSERVO)                                                             \
+            linear_servo_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9]);       \
+        else if (kind == JOR_CONSTRAINT_LINEARAXISSERVO)                                                           \
+            linear_axis_servo_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9],  \
+                                   (R)init[10]);                                                                   \
+        else if (kind == JOR_CONSTRAINT_TWISTSERVO)                                                                \
+            twist_servo_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);              \
         w.joints.push_back(j);                                                                                     \
         return (int)w.joints.size() - 1;                                                                           \
     }                                                                                                              \
@@ -235,6 +251,39 @@ template <class R> struct Handle {
         TimeStep<R> ts((R)dt, 1);                                                                                  \
         joint_prepare(jt, w.bodies, ts);                                                                           \
         if (iterate) joint_iterate(jt, w.bodies, ts);                                                              \
+    }                                                                                                              \
+    /* one Prepare and `iterations` Iterates of joint j alone under TimeStep(dt, substeps), its own \
+       bias and softness: the Solve helper of the reference's ServoTests (ServoTests.cs:51-56) */    \
+    extern "C" void jor_world_joint_run_##SUF(void* h, int j, float dt, int substeps, int prepare, int iterations) { \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        TimeStep<R> ts((R)dt, substeps);                                                                           \
+        if (prepare) joint_prepare(w.joints[j], w.bodies, ts);                                                     \
+        for (int i = 0; i < iterations; i++) joint_iterate(w.joints[j], w.bodies, ts);                             \
+    }                                                                                                              \
+    /* a joint's accumulated impulse (acc xyz) */                                                                \
+    extern "C" void jor_world_joint_impulse_##SUF(void* h, int j, double* out) {                                   \
+        put3d(out, ((Handle<R>*)h)->w.joints[j].acc);                                                              \
+    }                                                                                                              \
+    /* a servo's target and maximum, as jg_set_servo: a changed target drops the warm start (and   \
+       the AngularServo's hemisphere) */                                                              \
+    extern "C" void jor_world_set_servo_##SUF(void* h, int j, const float* target, float maximum) {                \
+        Joint<R>& jt = ((Handle<R>*)h)->w.joints[j];                                                               \
+        bool changed;                                                                                              \
+        if (jt.kind == ANGULARSERVO) {                                                                             \
+            Q4<R> t((R)target[0], (R)target[1], (R)target[2], (R)target[3]);                                       \
+            changed = t.x != jt.q0.x || t.y != jt.q0.y || t.z != jt.q0.z || t.w != jt.q0.w;                        \
+            jt.q0 = t;                                                                                             \
+            if (changed) jt.hemisphere = 0;                                                                        \
+        } else if (jt.kind == LINEARSERVO) {                                                                       \
+            V3<R> t = get3<R>(target);                                                                             \
+            changed = t.x != jt.target_pos.x || t.y != jt.target_pos.y || t.z != jt.target_pos.z;                  \
+            jt.target_pos = t;                                                                                     \
+        } else {                                                                                                   \
+            changed = (R)target[0] != jt.target;                                                                   \
+            jt.target = (R)target[0];                                                                              \
+        }                                                                                                          \
+        if (changed) jt.acc = V3<R>();                                                                             \
+        jt.maximum = (R)maximum;                                                                                   \
     }                                                                                                              \
     /* one Iterate of joint j alone (after a Prepare) at step dt */                                              \
     extern "C" void jor_world_joint_iterate_##SUF(void* h, int j, float dt) {                                      \

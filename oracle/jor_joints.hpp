@@ -1,7 +1,8 @@
 // Oracle (test infrastructure only): CPU restatement of the joint kinds on the device:
 // BallSocket (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle
 // (Dynamics/Constraints/HingeAngle.cs:84-364), DistanceLimit (DistanceLimit.cs:92-391),
-// ConeLimit (ConeLimit.cs:92-404) and TwistAngle (TwistAngle.cs:85-323), with their math
+// ConeLimit (ConeLimit.cs:92-404), TwistAngle (TwistAngle.cs:85-323), FixedAngle, PointOnPlane,
+// the motors and the servos (AngularServo, LinearServo, LinearAxisServo, TwistServo), with their math
 // helpers (AngularConstraintMath.cs:13-95, QMatrix.cs:112-125, MathHelper.cs:282-372,
 // JMatrix.cs:391-478, JQuaternion.cs:84-101).
 #pragma once
@@ -198,7 +199,8 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
 }
 
 enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
-                 POINTONPLANE = 7, ANGULARMOTOR = 8, LINEARMOTOR = 9 };
+                 POINTONPLANE = 7, ANGULARMOTOR = 8, LINEARMOTOR = 9, ANGULARSERVO = 10, LINEARSERVO = 11,
+                 LINEARAXISSERVO = 12, TWISTSERVO = 13 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -219,9 +221,13 @@ template <class R> struct Joint {
     // one-row kinds (DistanceLimitData, ConeLimitData, TwistLimitData): limits in
     // min_angle / max_angle (and fixed_angle), the row's Jacobian blocks, its effective mass;
     // the accumulated impulse and bias in acc.x / bias.x
-    R target = 0;                     // DistanceLimit.Distance
+    R target = 0;                     // DistanceLimit.Distance; a servo's target position or angle
     V3<R> jr[4];
     R eff1 = 0;
+    // servos (AngularServoData, LinearServoData, LinearAxisServoData, TwistServoData):
+    // MaximumTorque / MaximumForce, LinearServo.TargetPosition
+    R maximum = 0;
+    V3<R> target_pos;
 };
 
 // BallSocket.Initialize (BallSocket.cs:120-138)
@@ -801,6 +807,234 @@ template <class R> void motor_iterate(Joint<R>& j, std::vector<Body<R>>& bodies,
     if (b2.motion == DYNAMIC) motor_push(b2, j2 * lambda, lin);
 }
 
+
+// ---- servos (Dynamics/Constraints/*Servo.cs, Internal/ServoMath.cs) --------------------------
+// ServoMath.MaximumImpulse (ServoMath.cs:30)
+template <class R> R servo_max_impulse(R maximum, R dt) { return dt > 0 ? maximum * dt : (R)0; }
+// Math.Clamp as .NET defines it (value < min -> min, value > max -> max, else value)
+template <class R> R net_clamp(R v, R lo, R hi) { return v < lo ? lo : (v > hi ? hi : v); }
+// ServoMath.ClampMagnitude (ServoMath.cs:32-38)
+template <class R> void servo_clamp_magnitude(V3<R>& imp, R maxi) {
+    if (std::isinf(maxi) && maxi > 0) return;
+    R l2 = dot(imp, imp);
+    if (l2 > maxi * maxi) imp = imp * (maxi / std::sqrt(l2));
+}
+// ServoMath.ClampAngular (ServoMath.cs:40-49): the applied angular impulse J^T imp limited
+template <class R> void servo_clamp_angular(V3<R>& imp, const Mat<R>& jac, R maxi) {
+    if (std::isinf(maxi) && maxi > 0) return;
+    V3<R> a = mtvec(jac, imp);
+    R l2 = dot(a, a);
+    if (l2 > maxi * maxi) imp = imp * (maxi / std::sqrt(l2));
+}
+
+// AngularServo.Initialize (AngularServo.cs:55-77): the target relative orientation (body 2 in
+// body 1's frame), MaximumTorque
+template <class R> void angular_servo_init(Joint<R>& j, Q4<R> target, R maximum) {
+    j.kind = ANGULARSERVO;
+    j.q0 = target;
+    j.maximum = maximum;
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    j.hemisphere = 0;
+}
+template <class R> void angular_servo_apply(Joint<R>& j, Body<R>& b1, Body<R>& b2, V3<R> imp) {
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, imp);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, imp);
+}
+// AngularServo.PrepareForIterationAngularServo (AngularServo.cs:125-149), ApplyImpulse (:164-172)
+template <class R> void angular_servo_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> err;
+    short hemi;
+    j.jac = mscale(-(R)2, calc_jacobian(qmul(qconj(j.q0), qconj(b1.q)), b2.q, err, hemi));
+    if (j.hemisphere != 0 && j.hemisphere != hemi) j.acc = V3<R>();
+    j.hemisphere = hemi;
+    Sym3<R> isum(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                 b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                 b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+    M3<R> jt3;
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) jt3.m[i][k] = j.jac.a[i][k];
+    j.eff = Mat<R>::from_sym(sym_transform(isum, jt3));
+    R soft = j.softness * ts.inv_sub_dt;
+    j.eff.a[0][0] += soft; j.eff.a[1][1] += soft; j.eff.a[2][2] += soft;
+    j.eff = inverse_symmetric(j.eff);
+    j.bias = -err * j.bias_factor * ts.inv_dt;
+    servo_clamp_angular(j.acc, j.jac, servo_max_impulse(j.maximum, ts.sub_dt));
+    angular_servo_apply(j, b1, b2, mtvec(j.jac, j.acc));
+}
+// AngularServo.IterateAngularServo (AngularServo.cs:151-162)
+template <class R> void angular_servo_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> jv = mvec(j.jac, b1.angvel - b2.angvel);
+    V3<R> soft = j.acc * (j.softness * ts.inv_sub_dt);
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, jv + j.bias + soft);
+    V3<R> prev = j.acc;
+    j.acc = j.acc + lambda;
+    servo_clamp_angular(j.acc, j.jac, servo_max_impulse(j.maximum, ts.sub_dt));
+    angular_servo_apply(j, b1, b2, mtvec(j.jac, j.acc - prev));
+}
+
+// LinearServo.Initialize (LinearServo.cs:60-73) with TargetPosition and MaximumForce: anchors on both bodies, the target offset of
+// anchor 2 from anchor 1 in body 1's frame, MaximumForce
+template <class R> void linear_servo_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> a1, V3<R> a2, V3<R> target,
+                                          R maximum) {
+    j.kind = LINEARSERVO;
+    j.la1 = rotate_inv(a1 - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(a2 - b[j.b2].pos, b[j.b2].q);
+    j.target_pos = target;
+    j.maximum = maximum;
+    j.softness = (R)0.00001;
+    j.bias_factor = (R)0.2;
+}
+template <class R> void linear_servo_apply(Joint<R>& j, Body<R>& b1, Body<R>& b2, V3<R> imp) {
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel - cmul(imp, b1.inv_mass_vec);
+        b1.angvel = b1.angvel - sym_mul(b1.inv_inertia_world, cross(j.r1, imp));
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(imp, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, cross(j.r2, imp));
+    }
+}
+// LinearServo.PrepareForIterationLinearServo (LinearServo.cs:149-171), ApplyImpulse (:189-201)
+template <class R> void linear_servo_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    j.r1 = rotate(j.la1 + j.target_pos, b1.q);
+    j.r2 = rotate(j.la2, b2.q);
+    Mat<R> e = ballsocket_mass(b1, j.r1, b2, j.r2);
+    R soft = j.softness * ts.inv_sub_dt;
+    e.a[0][0] += soft; e.a[1][1] += soft; e.a[2][2] += soft;
+    j.eff = inverse_symmetric(e);
+    j.bias = (((b2.pos + j.r2) - b1.pos) - j.r1) * (j.bias_factor * ts.inv_dt);
+    servo_clamp_magnitude(j.acc, servo_max_impulse(j.maximum, ts.sub_dt));
+    linear_servo_apply(j, b1, b2, j.acc);
+}
+// LinearServo.IterateLinearServo (LinearServo.cs:173-187)
+template <class R> void linear_servo_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> jv = ((-b1.vel - cross(b1.angvel, j.r1)) + b2.vel) + cross(b2.angvel, j.r2);
+    V3<R> soft = j.acc * (j.softness * ts.inv_sub_dt);
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, jv + j.bias + soft);
+    V3<R> prev = j.acc;
+    j.acc = j.acc + lambda;
+    servo_clamp_magnitude(j.acc, servo_max_impulse(j.maximum, ts.sub_dt));
+    linear_servo_apply(j, b1, b2, j.acc - prev);
+}
+
+// LinearAxisServo.Initialize (LinearAxisServo.cs:61-78) with MaximumForce: an axis fixed in body 1, anchors on
+// both bodies, the target signed position of anchor 2 along the axis, MaximumForce
+template <class R> void linear_axis_servo_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> axis, V3<R> a1, V3<R> a2,
+                                               R target, R maximum) {
+    j.kind = LINEARAXISSERVO;
+    axis = normalize(axis);
+    j.axis = rotate_inv(axis, b[j.b1].q);
+    j.la1 = rotate_inv(a1 - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(a2 - b[j.b2].pos, b[j.b2].q);
+    j.target = target;
+    j.maximum = maximum;
+    j.softness = (R)0.00001;
+    j.bias_factor = (R)0.2;
+}
+template <class R> void axis_servo_apply(Joint<R>& j, Body<R>& b1, Body<R>& b2, R a) {
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel + cmul(j.jr[0] * a, b1.inv_mass_vec);
+        b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, j.jr[1] * a);
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(j.jr[2] * a, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, j.jr[3] * a);
+    }
+}
+// LinearAxisServo.PrepareForIterationLinearAxisServo (LinearAxisServo.cs:169-194), ApplyImpulse (:211-224)
+template <class R> void linear_axis_servo_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> axis = rotate(j.axis, b1.q);
+    V3<R> r1 = rotate(j.la1, b1.q), r2 = rotate(j.la2, b2.q);
+    V3<R> sep = ((b2.pos + r2) - b1.pos) - r1;
+    j.jr[0] = -axis;
+    j.jr[1] = -cross(r1 + sep, axis);
+    j.jr[2] = axis;
+    j.jr[3] = cross(r2, axis);
+    R m = dot(cmul(j.jr[0], b1.inv_mass_vec), j.jr[0]) + dot(cmul(j.jr[2], b2.inv_mass_vec), j.jr[2]) +
+          dot(sym_mul(b1.inv_inertia_world, j.jr[1]), j.jr[1]) + dot(sym_mul(b2.inv_inertia_world, j.jr[3]), j.jr[3]) +
+          j.softness * ts.inv_sub_dt;
+    j.eff1 = m > 0 ? (R)1 / m : (R)0;
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = (dot(sep, axis) - j.target) * j.bias_factor * ts.inv_dt;
+    R maxi = servo_max_impulse(j.maximum, ts.sub_dt);
+    j.acc.x = net_clamp(j.acc.x, -maxi, maxi);
+    axis_servo_apply(j, b1, b2, j.acc.x);
+}
+// LinearAxisServo.IterateLinearAxisServo (LinearAxisServo.cs:196-209)
+template <class R> void linear_axis_servo_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(j.jr[0], b1.vel) + dot(j.jr[1], b1.angvel) + dot(j.jr[2], b2.vel) + dot(j.jr[3], b2.angvel);
+    R lambda = -(jv + j.bias.x + j.acc.x * j.softness * ts.inv_sub_dt) * j.eff1;
+    R prev = j.acc.x;
+    R maxi = servo_max_impulse(j.maximum, ts.sub_dt);
+    j.acc.x = net_clamp(prev + lambda, -maxi, maxi);
+    axis_servo_apply(j, b1, b2, j.acc.x - prev);
+}
+
+// TwistServo.Initialize (TwistServo.cs:69-87) with MaximumTorque: body 2's axis, the reference rotation that
+// turns body 1's axis onto it, the target twist angle in [-pi, pi], MaximumTorque
+template <class R> void twist_servo_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, R target,
+                                         R maximum) {
+    j.kind = TWISTSERVO;
+    ax1 = normalize(ax1);
+    ax2 = normalize(ax2);
+    const Q4<R> q1 = b[j.b1].q, q2 = b[j.b2].q;
+    j.axis = rotate_inv(ax2, q2);
+    V3<R> first = rotate_inv(ax1, q2);
+    j.q0 = qmul(from_to_rotation(first, j.axis), qmul(qconj(q2), q1));
+    j.target = target;
+    j.maximum = maximum;
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    j.hemisphere = 0;
+}
+template <class R> void twist_servo_apply(Joint<R>& j, Body<R>& b1, Body<R>& b2, R a) {
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, j.jr[0] * a);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, j.jr[0] * a);
+}
+// TwistServo.PrepareForIterationTwistServo (TwistServo.cs:150-170), ApplyImpulse (:184-192)
+template <class R> void twist_servo_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    short hemi;
+    R angle = calc_twist(qmul(j.q0, qconj(b1.q)), b2.q, j.axis, j.jr[0], hemi);
+    if (j.hemisphere != 0 && j.hemisphere != hemi) j.acc.x = 0;
+    j.hemisphere = hemi;
+    Sym3<R> isum(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                 b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                 b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+    R m = dot(sym_mul(isum, j.jr[0]), j.jr[0]) + j.softness * ts.inv_sub_dt;
+    j.eff1 = m > 0 ? (R)1 / m : (R)0;
+    if (j.eff1 == 0) j.acc.x = 0;
+    R error = angle - j.target;
+    j.bias.x = error * j.bias_factor * ts.inv_dt;
+    R maxi = servo_max_impulse(j.maximum, ts.sub_dt);
+    j.acc.x = net_clamp(j.acc.x, -maxi, maxi);
+    twist_servo_apply(j, b1, b2, j.acc.x);
+}
+// TwistServo.IterateTwistServo (TwistServo.cs:172-182)
+template <class R> void twist_servo_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(b1.angvel - b2.angvel, j.jr[0]);
+    R lambda = -j.eff1 * (jv + j.bias.x + j.acc.x * j.softness * ts.inv_sub_dt);
+    R prev = j.acc.x;
+    R maxi = servo_max_impulse(j.maximum, ts.sub_dt);
+    j.acc.x = net_clamp(prev + lambda, -maxi, maxi);
+    twist_servo_apply(j, b1, b2, j.acc.x - prev);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
@@ -810,6 +1044,10 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case FIXEDANGLE: fixed_prepare(j, b, ts); break;
         case POINTONPLANE: plane_prepare(j, b, ts); break;
         case ANGULARMOTOR: case LINEARMOTOR: motor_prepare(j, b, ts); break;
+        case ANGULARSERVO: angular_servo_prepare(j, b, ts); break;
+        case LINEARSERVO: linear_servo_prepare(j, b, ts); break;
+        case LINEARAXISSERVO: linear_axis_servo_prepare(j, b, ts); break;
+        case TWISTSERVO: twist_servo_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -822,6 +1060,10 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case FIXEDANGLE: fixed_iterate(j, b, ts); break;
         case POINTONPLANE: distance_iterate(j, b, ts); break;   // PointOnPlane.cs:218-256: the same one-row update
         case ANGULARMOTOR: case LINEARMOTOR: motor_iterate(j, b, ts); break;
+        case ANGULARSERVO: angular_servo_iterate(j, b, ts); break;
+        case LINEARSERVO: linear_servo_iterate(j, b, ts); break;
+        case LINEARAXISSERVO: linear_axis_servo_iterate(j, b, ts); break;
+        case TWISTSERVO: twist_servo_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }

@@ -44,6 +44,8 @@ def load():
             "jor_world_body_deactivation_time": (None, [P, I, D]), "jor_world_activate_body": (None, [P, I]),
             "jor_world_body_sleep_thresholds": (None, [P, I, D, D]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]), "jor_world_joint_iterate": (None, [P, I, F]),
+            "jor_world_joint_run": (None, [P, I, F, I, I, I]), "jor_world_joint_impulse": (None, [P, I, P]),
+            "jor_world_set_servo": (None, [P, I, P, F]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
             "jor_world_joint_limit_params": (None, [P, I, D, D]), "jor_world_joint_matrix": (None, [P, I, P]), "jor_world_set_orientation_d": (None, [P, I, P]),
@@ -272,6 +274,20 @@ class OracleWorld:
     def joint_solve(self, j, dt, bias, softness, iterate=True):
         """Prepare (and Iterate) one joint alone, bias factor and softness overridden."""
         self.fn("jor_world_joint_solve")(self.h, j, dt, bias, softness, 1 if iterate else 0)
+
+    def joint_run(self, j, dt, substeps=1, iterations=12, prepare=True):
+        """One Prepare (unless prepare is False) and `iterations` Iterates of joint j alone under
+        TimeStep(dt, substeps), with the joint's own bias and softness (ServoTests.cs:51-56)."""
+        self.fn("jor_world_joint_run")(self.h, j, dt, substeps, 1 if prepare else 0, iterations)
+
+    def joint_impulse(self, j):
+        out = np.zeros(3, np.float64)
+        self.fn("jor_world_joint_impulse")(self.h, j, out.ctypes.data)
+        return out
+
+    def set_servo(self, j, target, maximum):
+        v = np.ascontiguousarray(np.atleast_1d(target), np.float32)
+        self.fn("jor_world_set_servo")(self.h, j, v.ctypes.data, maximum)
 
     def joint_iterate(self, j, dt):
         """One Iterate of joint j alone."""
