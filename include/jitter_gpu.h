@@ -74,6 +74,7 @@ extern "C" {
 #define JG_CONSTRAINT_LINEARSERVO 11    /* Dynamics/Constraints/LinearServo.cs   */
 #define JG_CONSTRAINT_LINEARAXISSERVO 12 /* Dynamics/Constraints/LinearAxisServo.cs */
 #define JG_CONSTRAINT_TWISTSERVO 13     /* Dynamics/Constraints/TwistServo.cs    */
+#define JG_CONSTRAINT_POINTONLINE 14    /* Dynamics/Constraints/PointOnLine.cs   */
 
 /* ---- plain data structures ------------------------------------------------------- */
 
@@ -252,7 +253,8 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
 /* World.CreateConstraint<T> + Initialize (BallSocket.cs:120-138, HingeAngle.cs:84-110,
  * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128, FixedAngle.cs:72-85,
  * PointOnPlane.cs:89-126, AngularMotor.cs:62-82, LinearMotor.cs:97-115, AngularServo.cs:55-77,
- * LinearServo.cs:60-73, LinearAxisServo.cs:61-78, TwistServo.cs:69-87), world-space init:
+ * LinearServo.cs:60-73, LinearAxisServo.cs:61-78, TwistServo.cs:69-87, PointOnLine.cs:92-121),
+ * world-space init:
  *   BallSocket     anchor xyz
  *   HingeAngle     axis xyz, min, max (radians)
  *   DistanceLimit  anchor1 xyz, anchor2 xyz, min, max (offsets from the initial distance;
@@ -271,6 +273,9 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
  *   LinearAxisServo axis xyz (fixed in body 1), anchor1 xyz, anchor2 xyz, target position,
  *                  maximum force
  *   TwistServo     axis1 xyz, axis2 xyz, target angle (radians, in [-pi, pi]), maximum torque
+ *   PointOnLine    axis xyz (the line's direction, fixed in body 1), anchor1 xyz (on the line),
+ *                  anchor2 xyz, min, max (position along the line; min >= max fixes it,
+ *                  LinearLimit.Fixed = (1e-6, -1e-6))
  * A servo's maximum is >= 0 and may be +inf; 0 (the reference's default) applies no impulse.
  * Invalid arguments return JG_ERR_INVALID_ARG (the reference's ArgumentException). */
 int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,

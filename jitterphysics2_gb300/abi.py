@@ -37,6 +37,7 @@ WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
 CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE, CONSTRAINT_DISTANCELIMIT, CONSTRAINT_CONELIMIT, CONSTRAINT_TWISTANGLE = 1, 2, 3, 4, 5
 CONSTRAINT_FIXEDANGLE, CONSTRAINT_POINTONPLANE, CONSTRAINT_ANGULARMOTOR, CONSTRAINT_LINEARMOTOR = 6, 7, 8, 9
 CONSTRAINT_ANGULARSERVO, CONSTRAINT_LINEARSERVO, CONSTRAINT_LINEARAXISSERVO, CONSTRAINT_TWISTSERVO = 10, 11, 12, 13
+CONSTRAINT_POINTONLINE = 14
 
 ERROR_NAMES = {
     JG_ERR_INVALID_ARG: "JG_ERR_INVALID_ARG", JG_ERR_CAPACITY: "JG_ERR_CAPACITY",

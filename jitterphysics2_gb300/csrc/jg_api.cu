@@ -696,13 +696,13 @@ static int check_servo_init(int kind, const float* init) {
 
 int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
     if (!w || !init) return JG_ERR_INVALID_ARG;
-    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_TWISTSERVO) return JG_ERR_INVALID_ARG;
-    if (kind >= JG_CONSTRAINT_ANGULARSERVO) {
+    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_POINTONLINE) return JG_ERR_INVALID_ARG;
+    if (kind >= JG_CONSTRAINT_ANGULARSERVO && kind <= JG_CONSTRAINT_TWISTSERVO) {
         int r = check_servo_init(kind, init);
         if (r) return r;
-    } else if (kind == JG_CONSTRAINT_POINTONPLANE) {
-        // PointOnPlane.Initialize (PointOnPlane.cs:89-100): a non-zero finite axis, finite
-        // anchors, limits that are not NaN
+    } else if (kind == JG_CONSTRAINT_POINTONPLANE || kind == JG_CONSTRAINT_POINTONLINE) {
+        // PointOnPlane.Initialize (PointOnPlane.cs:89-100), PointOnLine.Initialize
+        // (PointOnLine.cs:92-100): a non-zero finite axis, finite anchors, limits that are not NaN
         for (int i = 0; i < 9; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
         if (len2(mk3(init[0], init[1], init[2])) == 0.f || std::isnan(init[9]) || std::isnan(init[10])) return JG_ERR_INVALID_ARG;
     } else if (kind == JG_CONSTRAINT_ANGULARMOTOR || kind == JG_CONSTRAINT_LINEARMOTOR) {
@@ -788,6 +788,14 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
         J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
         J.lim = make_float4(0.f, init[7], init[6], 0.f);
+    } else if (kind == JG_CONSTRAINT_POINTONLINE) {
+        // PointOnLine.Initialize (PointOnLine.cs:92-121)
+        v3 axis = normalize(mk3(init[0], init[1], init[2]));
+        J.la1 = f4(rotate_inv(mk3(init[3], init[4], init[5]) - p1, q1), 0.f);
+        J.la2 = f4(rotate_inv(mk3(init[6], init[7], init[8]) - p2, q2), 0.f);
+        J.axis = f4(rotate_inv(axis, q1), 0.f);
+        J.prm = make_float4(0.2f, 0.00001f, 0.2f, 0.0001f);
+        J.lim = make_float4(init[9], init[10], 0.f, 0.f);
     } else if (kind == JG_CONSTRAINT_ANGULARSERVO) {
         // AngularServo.Initialize (AngularServo.cs:55-77): the given target relative
         // orientation, or the current one (conj(q1) q2) when all four are zero

@@ -5,7 +5,8 @@
 // (PointOnPlane.cs:128-256), AngularMotor (AngularMotor.cs:128-180), LinearMotor
 // (LinearMotor.cs:152-231), AngularServo (AngularServo.cs:125-172), LinearServo
 // (LinearServo.cs:149-201), LinearAxisServo (LinearAxisServo.cs:169-224) and TwistServo
-// (TwistServo.cs:150-192).  Included by the solver translation unit.  Matrices are
+// (TwistServo.cs:150-192) and PointOnLine (PointOnLine.cs:149-465).  Included by the solver
+// translation unit.  Matrices are
 // row-major float[3][3].
 //
 // JointDev fields of the one-row kinds: la1/la2 anchors (DistanceLimit) or local axes
@@ -925,6 +926,142 @@ __device__ void twist_servo_iterate(const WorldDev& w, JointDev& J, const StepPa
     twist_servo_apply(w, J, b1, b2, J.acc.x - prev);
 }
 
+// ---- PointOnLine (PointOnLine.cs:149-465) ------------------------------------------------------
+// Math.Min / Math.Max as .NET defines them for floating point: NaN wins, and of two equal
+// values Min returns the negative zero, Max the positive one
+__device__ __forceinline__ float net_min(float a, float b) {
+    if (a != b) return isnan(a) ? a : (a < b ? a : b);
+    return signbit(b) ? b : a;
+}
+__device__ __forceinline__ float net_max(float a, float b) {
+    if (a != b) return isnan(a) ? a : (a > b ? a : b);
+    return signbit(b) ? a : b;
+}
+// The twelve Jacobian blocks (two rows across the line and one along it, each for v1, w1,
+// v2, w2) and the error, from the current poses (PointOnLine.cs:155-185, :378-408); the line's
+// direction (axis) and anchors (la1, la2) are local
+__device__ __forceinline__ v3 line_jacobian(const WorldDev& w, const JointDev& J, v3* jb) {
+    const int i1 = J.hdr.y, i2 = J.hdr.z;
+    const q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    const v3 aw = rotate(mk3(J.axis), q1);
+    const v3 n1 = rotate(create_orthonormal(mk3(J.axis)), q1);
+    const v3 n2 = cross(aw, n1);
+    const v3 r1 = rotate(mk3(J.la1), q1), r2 = rotate(mk3(J.la2), q2);
+    const v3 p1 = mk3(w.pos[i1]) + r1, p2 = mk3(w.pos[i2]) + r2;
+    const v3 u = p2 - p1;
+    jb[0] = -n1; jb[1] = -cross(r1 + u, n1); jb[2] = n1; jb[3] = cross(r2, n1);
+    jb[4] = -n2; jb[5] = -cross(r1 + u, n2); jb[6] = n2; jb[7] = cross(r2, n2);
+    jb[8] = -aw; jb[9] = -cross(r1 + u, aw); jb[10] = aw; jb[11] = cross(r2, aw);
+    return mk3(dot(u, n1), dot(u, n2), dot(u, aw));
+}
+__device__ __forceinline__ void line_apply(const WorldDev& w, const JointDev& J, LBody& b1, LBody& b2, const v3* jb, v3 a) {
+    if (b1.flags & SB_DYNAMIC) {
+        b1.v = b1.v + cmul(jb[0] * a.x + jb[4] * a.y + jb[8] * a.z, b1.im);
+        b1.w = b1.w + sym_mul(b1.I, jb[1] * a.x + jb[5] * a.y + jb[9] * a.z);
+        store_vel(w.body, J.hdr.y, b1);
+    }
+    if (b2.flags & SB_DYNAMIC) {
+        b2.v = b2.v + cmul(jb[2] * a.x + jb[6] * a.y + jb[10] * a.z, b2.im);
+        b2.w = b2.w + sym_mul(b2.I, jb[3] * a.x + jb[7] * a.y + jb[11] * a.z);
+        store_vel(w.body, J.hdr.z, b2);
+    }
+}
+// Prepare: prm = (bias, softness, limit bias, limit softness), lim = (min, max, -, clamp),
+// inverse effective mass in eff[0..2], bilateral block inverse in bil, couplings in cpl
+__device__ void line_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    LBody b1 = load_body(w.body, J.hdr.y), b2 = load_body(w.body, J.hdr.z);
+    v3 jb[12];
+    v3 err = line_jacobian(w, J, jb);
+    const sym6 I1 = b1.I, I2 = b2.I;
+    const v3 m1 = b1.im, m2 = b2.im;
+    M3x M = mzero();
+    M.a[0][0] = dot(cmul(jb[0], m1), jb[0]) + dot(cmul(jb[2], m2), jb[2]) + dot(sym_mul(I1, jb[1]), jb[1]) +
+                dot(sym_mul(I2, jb[3]), jb[3]);
+    M.a[1][1] = dot(cmul(jb[4], m1), jb[4]) + dot(cmul(jb[6], m2), jb[6]) + dot(sym_mul(I1, jb[5]), jb[5]) +
+                dot(sym_mul(I2, jb[7]), jb[7]);
+    M.a[2][2] = 1.0f;
+    M.a[0][1] = dot(sym_mul(I1, jb[1]), jb[5]) + dot(sym_mul(I2, jb[3]), jb[7]);
+    M.a[1][0] = dot(sym_mul(I1, jb[5]), jb[1]) + dot(sym_mul(I2, jb[7]), jb[3]);
+    const float c12 = dot(cmul(jb[0], m1), jb[4]) + dot(cmul(jb[2], m2), jb[6]);
+    M.a[0][1] += c12;
+    M.a[1][0] += c12;
+    v3 acc = mk3(J.acc);
+    const float lo = J.lim.x, hi = J.lim.y;
+    int clamp = 0;
+    if (lo >= hi) { err.z -= 0.5f * lo + 0.5f * hi; clamp = 3; }
+    else if (err.z >= hi) { err.z -= hi; clamp = 1; }
+    else if (err.z <= lo) { err.z -= lo; clamp = 2; }
+    else acc.z = 0.f;
+    if (clamp != 0) {
+        M.a[2][2] = dot(cmul(jb[8], m1), jb[8]) + dot(cmul(jb[10], m2), jb[10]) + dot(sym_mul(I1, jb[9]), jb[9]) +
+                    dot(sym_mul(I2, jb[11]), jb[11]);
+        M.a[0][2] = dot(sym_mul(I1, jb[1]), jb[9]) + dot(sym_mul(I2, jb[3]), jb[11]);
+        M.a[2][0] = dot(sym_mul(I1, jb[9]), jb[1]) + dot(sym_mul(I2, jb[11]), jb[3]);
+        M.a[1][2] = dot(sym_mul(I1, jb[5]), jb[9]) + dot(sym_mul(I2, jb[7]), jb[11]);
+        M.a[2][1] = dot(sym_mul(I1, jb[9]), jb[5]) + dot(sym_mul(I2, jb[11]), jb[7]);
+        const float c13 = dot(cmul(jb[0], m1), jb[8]) + dot(cmul(jb[2], m2), jb[10]);
+        const float c23 = dot(cmul(jb[4], m1), jb[8]) + dot(cmul(jb[6], m2), jb[10]);
+        M.a[0][2] += c13; M.a[2][0] += c13;
+        M.a[1][2] += c23; M.a[2][1] += c23;
+    }
+    M.a[0][0] += J.prm.y * sp.inv_sub_dt;
+    M.a[1][1] += J.prm.y * sp.inv_sub_dt;
+    M.a[2][2] += J.prm.w * sp.inv_sub_dt;
+    v3 bil = mk3(0.f);
+    float cx = 0.f, cy = 0.f;
+    if (clamp == 1 || clamp == 2) {
+        M3x blk = mzero();
+        blk.a[0][0] = M.a[0][0]; blk.a[0][1] = M.a[0][1]; blk.a[1][0] = M.a[0][1]; blk.a[1][1] = M.a[1][1];
+        M3x bi = inv_symmetric(blk);
+        bil = mk3(bi.a[0][0], bi.a[0][1], bi.a[1][1]);
+        cx = M.a[0][2];
+        cy = M.a[1][2];
+    }
+    if (clamp == 0) M.a[2][2] = 0.f;
+    jstore_m(J.eff, inv_symmetric(M));
+    v3 bias = err * sp.inv_dt;
+    bias.x *= J.prm.x; bias.y *= J.prm.x; bias.z *= J.prm.z;
+    if (clamp == 1) acc.z = net_min(0.f, acc.z);
+    else if (clamp == 2) acc.z = net_max(0.f, acc.z);
+    line_apply(w, J, b1, b2, jb, acc);
+    J.acc = f4(acc, 0.f);
+    J.bias = f4(bias, 0.f);
+    J.lim.w = (float)clamp;
+    J.bil = make_float4(bil.x, bil.y, bil.z, 0.f);
+    J.cpl = make_float4(cx, cy, 0.f, 0.f);
+}
+__device__ void line_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    LBody b1 = load_body(w.body, J.hdr.y), b2 = load_body(w.body, J.hdr.z);
+    v3 jb[12];
+    line_jacobian(w, J, jb);
+    v3 jv = mk3(dot(jb[0], b1.v) + dot(jb[1], b1.w) + dot(jb[2], b2.v) + dot(jb[3], b2.w),
+                dot(jb[4], b1.v) + dot(jb[5], b1.w) + dot(jb[6], b2.v) + dot(jb[7], b2.w),
+                dot(jb[8], b1.v) + dot(jb[9], b1.w) + dot(jb[10], b2.v) + dot(jb[11], b2.w));
+    v3 acc = mk3(J.acc);
+    v3 soft = acc * sp.inv_sub_dt;
+    soft.x *= J.prm.y; soft.y *= J.prm.y; soft.z *= J.prm.w;
+    v3 res = jv + mk3(J.bias) + soft;
+    v3 lambda = -1.0f * mv(jload_m(J.eff), res);
+    v3 orig = acc;
+    acc = acc + lambda;
+    const int clamp = (int)J.lim.w;
+    if ((clamp == 1 && acc.z > 0) || (clamp == 2 && acc.z < 0)) {
+        lambda.z = -orig.z;
+        float x = res.x + J.cpl.x * lambda.z;
+        float y = res.y + J.cpl.y * lambda.z;
+        lambda.x = -(J.bil.x * x + J.bil.y * y);
+        lambda.y = -(J.bil.y * x + J.bil.z * y);
+        acc.x = orig.x + lambda.x;
+        acc.y = orig.y + lambda.y;
+        acc.z = 0;
+    } else if (clamp == 0) {
+        acc.z = 0;
+        orig.z = 0;
+    }
+    J.acc = f4(acc, 0.f);
+    line_apply(w, J, b1, b2, jb, acc - orig);
+}
+
 __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
     switch (J.hdr.x) {
@@ -939,6 +1076,7 @@ __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_LINEARSERVO: linear_servo_prepare(w, J, sp); break;
         case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_prepare(w, J, sp); break;
         case JG_CONSTRAINT_TWISTSERVO: twist_servo_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_POINTONLINE: line_prepare(w, J, sp); break;
         default: twist_prepare(w, J, sp); break;
     }
 }
@@ -956,6 +1094,7 @@ __device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_LINEARSERVO: linear_servo_iterate(w, J, sp); break;
         case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_iterate(w, J, sp); break;
         case JG_CONSTRAINT_TWISTSERVO: twist_servo_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_POINTONLINE: line_iterate(w, J, sp); break;
         default: twist_iterate(w, J, sp); break;
     }
 }

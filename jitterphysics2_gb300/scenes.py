@@ -462,14 +462,15 @@ def mechanism_chains(n_chains=16, seed=12353, spacing=1.0):
 
 
 def servo_chains(n_chains=16, seed=12354, spacing=1.0):
-    """Chains of four boxes hanging from static anchors, one servo of each kind: link 1 hangs
+    """Chains of four boxes hanging from static anchors, one servo of each kind and a slider:
+    link 1 hangs
     on a BallSocket and is turned by an AngularServo towards a rotation of 0.3 rad about z
     (maximum torque 5); link 2 is held by a LinearServo at an offset of (1, 0.2, 0) from link
     1 in link 1's frame (maximum force 20); link 3 hangs on a BallSocket from link 2 and is
     twisted about the chain axis by a TwistServo towards 0.6 rad (maximum torque 3); link 4
-    is pushed along link 3's x axis by a LinearAxisServo towards 1.1 (maximum force 10) and
-    kept within reach by a DistanceLimit.  Links are 0.6 long with 0.4 gaps and the chains
-    are 8 apart: no contacts."""
+    slides on a PointOnLine along link 3's x axis (limited to 0.8-1.3) and is pushed along it
+    by a LinearAxisServo towards 1.1 (maximum force 10).  Links are 0.6 long with 0.4 gaps
+    and the chains are 8 apart: no contacts."""
     rng = np.random.Generator(np.random.PCG64(seed))
     per = 5
     n = n_chains * per
@@ -504,7 +505,7 @@ def servo_chains(n_chains=16, seed=12354, spacing=1.0):
         joints.append((abi.CONSTRAINT_BALLSOCKET, a + 2, a + 3, mid(3)))
         joints.append((abi.CONSTRAINT_TWISTSERVO, a + 2, a + 3, x_axis + x_axis + (0.6, 3.0)))
         joints.append((abi.CONSTRAINT_LINEARAXISSERVO, a + 3, a + 4, x_axis + pos(3) + pos(4) + (1.1 * spacing, 10.0)))
-        joints.append((abi.CONSTRAINT_DISTANCELIMIT, a + 3, a + 4, pos(3) + pos(4) + (-0.2, 0.2)))
+        joints.append((abi.CONSTRAINT_POINTONLINE, a + 3, a + 4, x_axis + pos(3) + pos(4) + (0.8, 1.3)))
     _finish_mass(bodies, shapes, np.zeros((0, 3), np.float32), 0, 0, n)
     return dict(bodies=bodies, shapes=shapes, hull=np.zeros((0, 3), np.float32),
                 triangles=np.zeros(0, abi.TRIANGLE_DTYPE), joints=joints,

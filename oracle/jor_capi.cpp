@@ -18,6 +18,7 @@ using namespace jor;
 #define JOR_CONSTRAINT_LINEARSERVO 11
 #define JOR_CONSTRAINT_LINEARAXISSERVO 12
 #define JOR_CONSTRAINT_TWISTSERVO 13
+#define JOR_CONSTRAINT_POINTONLINE 14
 
 namespace {
 
@@ -239,6 +240,8 @@ template <class R> struct Handle {
                                    (R)init[10]);                                                                   \
         else if (kind == JOR_CONSTRAINT_TWISTSERVO)                                                                \
             twist_servo_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);              \
+        else if (kind == JOR_CONSTRAINT_POINTONLINE)                                                               \
+            line_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9], (R)init[10]);  \
         w.joints.push_back(j);                                                                                     \
         return (int)w.joints.size() - 1;                                                                           \
     }                                                                                                              \
@@ -259,6 +262,13 @@ template <class R> struct Handle {
         TimeStep<R> ts((R)dt, substeps);                                                                           \
         if (prepare) joint_prepare(w.joints[j], w.bodies, ts);                                                     \
         for (int i = 0; i < iterations; i++) joint_iterate(w.joints[j], w.bodies, ts);                             \
+    }                                                                                                              \
+    /* PointOnLine.Distance (PointOnLine.cs:123-146): anchor 2's position along the line */                     \
+    extern "C" double jor_world_line_distance_##SUF(void* h, int j) {                                              \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        const Joint<R>& jt = w.joints[j];                                                                          \
+        V3<R> J[12];                                                                                               \
+        return (double)line_jacobian(jt, w.bodies[jt.b1], w.bodies[jt.b2], J).z;                                   \
     }                                                                                                              \
     /* a joint's accumulated impulse (acc xyz) */                                                                \
     extern "C" void jor_world_joint_impulse_##SUF(void* h, int j, double* out) {                                   \

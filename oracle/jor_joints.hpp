@@ -2,7 +2,8 @@
 // BallSocket (Dynamics/Constraints/BallSocket.cs:140-252), HingeAngle
 // (Dynamics/Constraints/HingeAngle.cs:84-364), DistanceLimit (DistanceLimit.cs:92-391),
 // ConeLimit (ConeLimit.cs:92-404), TwistAngle (TwistAngle.cs:85-323), FixedAngle, PointOnPlane,
-// the motors and the servos (AngularServo, LinearServo, LinearAxisServo, TwistServo), with their math
+// the motors, the servos (AngularServo, LinearServo, LinearAxisServo, TwistServo) and
+// PointOnLine, with their math
 // helpers (AngularConstraintMath.cs:13-95, QMatrix.cs:112-125, MathHelper.cs:282-372,
 // JMatrix.cs:391-478, JQuaternion.cs:84-101).
 #pragma once
@@ -200,7 +201,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
 
 enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
                  POINTONPLANE = 7, ANGULARMOTOR = 8, LINEARMOTOR = 9, ANGULARSERVO = 10, LINEARSERVO = 11,
-                 LINEARAXISSERVO = 12, TWISTSERVO = 13 };
+                 LINEARAXISSERVO = 12, TWISTSERVO = 13, POINTONLINE = 14 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -1035,6 +1036,140 @@ template <class R> void twist_servo_iterate(Joint<R>& j, std::vector<Body<R>>& b
     twist_servo_apply(j, b1, b2, j.acc.x - prev);
 }
 
+// ---- PointOnLine (Dynamics/Constraints/PointOnLine.cs) ---------------------------------------
+// Math.Min / Math.Max as .NET defines them for floating point: NaN wins, and of two equal
+// values Min returns the negative zero, Max the positive one
+template <class R> R net_min(R a, R b) {
+    if (a != b) return std::isnan(a) ? a : (a < b ? a : b);
+    return std::signbit(b) ? b : a;
+}
+template <class R> R net_max(R a, R b) {
+    if (a != b) return std::isnan(a) ? a : (a > b ? a : b);
+    return std::signbit(b) ? a : b;
+}
+// PointOnLine.Initialize (PointOnLine.cs:92-121): the line's direction fixed in body 1
+// through anchor 1, anchor 2 on body 2, the position along the line limited to [min, max]
+// (min >= max fixes it)
+template <class R> void line_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> axis, V3<R> a1, V3<R> a2, R lo, R hi) {
+    j.kind = POINTONLINE;
+    axis = normalize(axis);
+    j.la1 = rotate_inv(a1 - b[j.b1].pos, b[j.b1].q);
+    j.la2 = rotate_inv(a2 - b[j.b2].pos, b[j.b2].q);
+    j.axis = rotate_inv(axis, b[j.b1].q);
+    j.bias_factor = (R)0.2;
+    j.softness = (R)0.00001;
+    j.limit_softness = (R)0.0001;
+    j.limit_bias = (R)0.2;
+    j.min_angle = lo; j.max_angle = hi;
+}
+// the twelve Jacobian blocks (two perpendicular rows and the row along the line, each for
+// v1, w1, v2, w2) and the error (PointOnLine.cs:155-185, recomputed in :378-408)
+template <class R> V3<R> line_jacobian(const Joint<R>& j, const Body<R>& b1, const Body<R>& b2, V3<R>* J) {
+    V3<R> aw = rotate(j.axis, b1.q);
+    V3<R> n1 = rotate(create_orthonormal(j.axis), b1.q);
+    V3<R> n2 = cross(aw, n1);
+    V3<R> r1 = rotate(j.la1, b1.q), r2 = rotate(j.la2, b2.q);
+    V3<R> p1 = b1.pos + r1, p2 = b2.pos + r2;
+    V3<R> u = p2 - p1;
+    J[0] = -n1; J[1] = -cross(r1 + u, n1); J[2] = n1; J[3] = cross(r2, n1);
+    J[4] = -n2; J[5] = -cross(r1 + u, n2); J[6] = n2; J[7] = cross(r2, n2);
+    J[8] = -aw; J[9] = -cross(r1 + u, aw); J[10] = aw; J[11] = cross(r2, aw);
+    return V3<R>(dot(u, n1), dot(u, n2), dot(u, aw));
+}
+template <class R> void line_apply(Body<R>& b1, Body<R>& b2, const V3<R>* J, V3<R> a) {
+    if (b1.motion == DYNAMIC) {
+        b1.vel = b1.vel + cmul(J[0] * a.x + J[4] * a.y + J[8] * a.z, b1.inv_mass_vec);
+        b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, J[1] * a.x + J[5] * a.y + J[9] * a.z);
+    }
+    if (b2.motion == DYNAMIC) {
+        b2.vel = b2.vel + cmul(J[2] * a.x + J[6] * a.y + J[10] * a.z, b2.inv_mass_vec);
+        b2.angvel = b2.angvel + sym_mul(b2.inv_inertia_world, J[3] * a.x + J[7] * a.y + J[11] * a.z);
+    }
+}
+// PointOnLine.PrepareForIterationPointOnLine (PointOnLine.cs:149-300)
+template <class R> void line_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> J[12];
+    V3<R> err = line_jacobian(j, b1, b2, J);
+    const Sym3<R>& I1 = b1.inv_inertia_world;
+    const Sym3<R>& I2 = b2.inv_inertia_world;
+    const V3<R> m1 = b1.inv_mass_vec, m2 = b2.inv_mass_vec;
+    j.clamp = 0;
+    Mat<R> M = Mat<R>::ident();
+    M.a[0][0] = dot(cmul(J[0], m1), J[0]) + dot(cmul(J[2], m2), J[2]) + dot(sym_mul(I1, J[1]), J[1]) + dot(sym_mul(I2, J[3]), J[3]);
+    M.a[1][1] = dot(cmul(J[4], m1), J[4]) + dot(cmul(J[6], m2), J[6]) + dot(sym_mul(I1, J[5]), J[5]) + dot(sym_mul(I2, J[7]), J[7]);
+    M.a[0][1] = dot(sym_mul(I1, J[1]), J[5]) + dot(sym_mul(I2, J[3]), J[7]);
+    M.a[1][0] = dot(sym_mul(I1, J[5]), J[1]) + dot(sym_mul(I2, J[7]), J[3]);
+    R c12 = dot(cmul(J[0], m1), J[4]) + dot(cmul(J[2], m2), J[6]);
+    M.a[0][1] += c12;
+    M.a[1][0] += c12;
+    if (j.min_angle >= j.max_angle) { err.z -= (R)0.5 * j.min_angle + (R)0.5 * j.max_angle; j.clamp = 3; }
+    else if (err.z >= j.max_angle) { err.z -= j.max_angle; j.clamp = 1; }
+    else if (err.z <= j.min_angle) { err.z -= j.min_angle; j.clamp = 2; }
+    else j.acc.z = 0;
+    if (j.clamp != 0) {
+        M.a[2][2] = dot(cmul(J[8], m1), J[8]) + dot(cmul(J[10], m2), J[10]) + dot(sym_mul(I1, J[9]), J[9]) + dot(sym_mul(I2, J[11]), J[11]);
+        M.a[0][2] = dot(sym_mul(I1, J[1]), J[9]) + dot(sym_mul(I2, J[3]), J[11]);
+        M.a[2][0] = dot(sym_mul(I1, J[9]), J[1]) + dot(sym_mul(I2, J[11]), J[3]);
+        M.a[1][2] = dot(sym_mul(I1, J[5]), J[9]) + dot(sym_mul(I2, J[7]), J[11]);
+        M.a[2][1] = dot(sym_mul(I1, J[9]), J[5]) + dot(sym_mul(I2, J[11]), J[7]);
+        R c13 = dot(cmul(J[0], m1), J[8]) + dot(cmul(J[2], m2), J[10]);
+        R c23 = dot(cmul(J[4], m1), J[8]) + dot(cmul(J[6], m2), J[10]);
+        M.a[0][2] += c13; M.a[2][0] += c13;
+        M.a[1][2] += c23; M.a[2][1] += c23;
+    }
+    M.a[0][0] += j.softness * ts.inv_sub_dt;
+    M.a[1][1] += j.softness * ts.inv_sub_dt;
+    M.a[2][2] += j.limit_softness * ts.inv_sub_dt;
+    if (j.clamp == 1 || j.clamp == 2) {
+        j.bilateral = inverse_bilateral(M);
+        j.coupling_x = M.a[0][2];
+        j.coupling_y = M.a[1][2];
+    }
+    if (j.clamp == 0) M.a[2][2] = 0;
+    j.eff = inverse_symmetric(M);
+    j.bias = err * ts.inv_dt;
+    j.bias.x *= j.bias_factor;
+    j.bias.y *= j.bias_factor;
+    j.bias.z *= j.limit_bias;
+    if (j.clamp == 1) j.acc.z = net_min((R)0, j.acc.z);
+    else if (j.clamp == 2) j.acc.z = net_max((R)0, j.acc.z);
+    line_apply(b1, b2, J, j.acc);
+}
+// PointOnLine.IteratePointOnLine (PointOnLine.cs:372-465)
+template <class R> void line_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> J[12];
+    line_jacobian(j, b1, b2, J);
+    V3<R> jv(dot(J[0], b1.vel) + dot(J[1], b1.angvel) + dot(J[2], b2.vel) + dot(J[3], b2.angvel),
+             dot(J[4], b1.vel) + dot(J[5], b1.angvel) + dot(J[6], b2.vel) + dot(J[7], b2.angvel),
+             dot(J[8], b1.vel) + dot(J[9], b1.angvel) + dot(J[10], b2.vel) + dot(J[11], b2.angvel));
+    V3<R> sv = j.acc * ts.inv_sub_dt;
+    sv.x *= j.softness;
+    sv.y *= j.softness;
+    sv.z *= j.limit_softness;
+    V3<R> res = jv + j.bias + sv;
+    V3<R> lambda = -(R)1.0 * mvec(j.eff, res);
+    V3<R> orig = j.acc;
+    j.acc = j.acc + lambda;
+    if ((j.clamp == 1 && j.acc.z > 0) || (j.clamp == 2 && j.acc.z < 0)) {
+        lambda.z = -orig.z;
+        R x = res.x + j.coupling_x * lambda.z;
+        R y = res.y + j.coupling_y * lambda.z;
+        lambda.x = -(j.bilateral.x * x + j.bilateral.y * y);
+        lambda.y = -(j.bilateral.y * x + j.bilateral.z * y);
+        j.acc.x = orig.x + lambda.x;
+        j.acc.y = orig.y + lambda.y;
+        j.acc.z = 0;
+    } else if (j.clamp == 0) {
+        j.acc.z = 0;
+        orig.z = 0;
+    }
+    line_apply(b1, b2, J, j.acc - orig);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
@@ -1048,6 +1183,7 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case LINEARSERVO: linear_servo_prepare(j, b, ts); break;
         case LINEARAXISSERVO: linear_axis_servo_prepare(j, b, ts); break;
         case TWISTSERVO: twist_servo_prepare(j, b, ts); break;
+        case POINTONLINE: line_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -1064,6 +1200,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case LINEARSERVO: linear_servo_iterate(j, b, ts); break;
         case LINEARAXISSERVO: linear_axis_servo_iterate(j, b, ts); break;
         case TWISTSERVO: twist_servo_iterate(j, b, ts); break;
+        case POINTONLINE: line_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }

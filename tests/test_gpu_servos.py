@@ -1,5 +1,5 @@
-"""The servos on the device (AngularServo, LinearServo, LinearAxisServo, TwistServo), through
-the C ABI.
+"""The servos on the device (AngularServo, LinearServo, LinearAxisServo, TwistServo) and
+PointOnLine, through the C ABI.
 
 - One step of servo chains (scenes.servo_chains) from the GPU's state, replayed in the oracle
   in the GPU's order keys and warm-started with the GPU's impulses: velocities within 1e-3,
@@ -22,7 +22,7 @@ from jitterphysics2_gb300.world import world_for_scene
 pytestmark = pytest.mark.gpu
 
 SERVOS = (abi.CONSTRAINT_ANGULARSERVO, abi.CONSTRAINT_LINEARSERVO, abi.CONSTRAINT_LINEARAXISSERVO,
-          abi.CONSTRAINT_TWISTSERVO)
+          abi.CONSTRAINT_TWISTSERVO, abi.CONSTRAINT_POINTONLINE)
 KINDS = ["angular", "twist", "linear", "axis"]
 
 
@@ -68,9 +68,11 @@ def test_servo_chains_reach_their_targets():
         # link 2 sits at (1, 0.2, 0) from link 1 in link 1's frame
         off = _rotate(_conj(q[a + 1]), b["position"][a + 2] - b["position"][a + 1])
         assert np.abs(off - (1.0, 0.2, 0.0)).max() < 0.01, off
-        # link 4's centre is 1.1 along link 3's x axis
+        # link 4's centre is 1.1 along link 3's x axis, and on that line
         x3 = _rotate(q[a + 3], np.array([1.0, 0.0, 0.0]))
-        assert abs((b["position"][a + 4] - b["position"][a + 3]) @ x3 - 1.1) < 0.01
+        d = b["position"][a + 4] - b["position"][a + 3]
+        assert abs(d @ x3 - 1.1) < 0.01
+        assert np.linalg.norm(d - (d @ x3) * x3) < 0.01
 
 
 # ---- the reference's ServoTests on the device ---------------------------------------------
@@ -302,3 +304,41 @@ def test_angular_servo_rejects_a_non_unit_target():
     j = w.add_constraint(abi.CONSTRAINT_ANGULARSERVO, 0, 1, (0, 0, 0, 0, 1.0))   # the current orientation
     with pytest.raises(abi.JitterError):
         w.set_servo(j, (0, 0, 0, 2), 1.0)
+
+
+def test_point_on_line_reduces_the_distance_to_its_line():
+    # AdditionalConstraintBehaviorTests.PointOnLine_ReducesPerpendicularDistanceToLine
+    # (AdditionalConstraintBehaviorTests.cs:55-79): two unit spheres, the line along x through
+    # the static one's centre, the other starting 3.6 from it
+    sc = _scene(substeps=4)
+    b = sc["bodies"]
+    b["position"][1] = (0, 3, 2)
+    s = np.zeros(2, abi.SHAPE_DTYPE)
+    s["kind"] = abi.SHAPE_SPHERE
+    s["body"] = (0, 1)
+    s["dims"][:, 0] = 1.0
+    sc["shapes"] = s
+    b["inv_mass"][1] = 1.0 / (4.0 / 3.0 * np.pi)
+    sc["joints"] = [(abi.CONSTRAINT_POINTONLINE, 0, 1, (1, 0, 0, 0, 0, 0, 0, 3, 2, -np.inf, np.inf))]
+    w = world_for_scene(sc)
+    before = np.hypot(3.0, 2.0)
+    for _ in range(200):
+        w.step(0.01)
+    p = w.bodies()["position"][1]
+    after = np.hypot(p[1], p[2])
+    assert after < before and after < 2.1
+    _, imp = w.constraints()
+    assert np.linalg.norm(imp[0]) > 0
+
+
+@pytest.mark.parametrize("init", [
+    (0, 0, 0) + (0, 0, 0) + (1, 0, 0) + (0.0, 1.0),        # zero axis
+    (1, 0, 0) + (0, 0, 0) + (1, 0, 0) + (np.nan, 1.0),     # NaN limit
+    (1, 0, 0) + (np.inf, 0, 0) + (1, 0, 0) + (0.0, 1.0),   # infinite anchor
+])
+def test_invalid_point_on_line_arguments_raise(init):
+    # PointOnLine.Initialize (PointOnLine.cs:92-100): ArgumentCheck.NonZero, Finite, NotNaN
+    w = world_for_scene(_scene())
+    with pytest.raises(abi.JitterError) as e:
+        w.add_constraint(abi.CONSTRAINT_POINTONLINE, 0, 1, init)
+    assert e.value.code == abi.JG_ERR_INVALID_ARG
