@@ -75,6 +75,7 @@ extern "C" {
 #define JG_CONSTRAINT_LINEARAXISSERVO 12 /* Dynamics/Constraints/LinearAxisServo.cs */
 #define JG_CONSTRAINT_TWISTSERVO 13     /* Dynamics/Constraints/TwistServo.cs    */
 #define JG_CONSTRAINT_POINTONLINE 14    /* Dynamics/Constraints/PointOnLine.cs   */
+#define JG_CONSTRAINT_ELLIPTICALCONELIMIT 15 /* Dynamics/Constraints/EllipticalConeLimit.cs */
 
 /* ---- plain data structures ------------------------------------------------------- */
 
@@ -253,7 +254,8 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
 /* World.CreateConstraint<T> + Initialize (BallSocket.cs:120-138, HingeAngle.cs:84-110,
  * DistanceLimit.cs:92-117, ConeLimit.cs:92-118, TwistAngle.cs:85-128, FixedAngle.cs:72-85,
  * PointOnPlane.cs:89-126, AngularMotor.cs:62-82, LinearMotor.cs:97-115, AngularServo.cs:55-77,
- * LinearServo.cs:60-73, LinearAxisServo.cs:61-78, TwistServo.cs:69-87, PointOnLine.cs:92-121),
+ * LinearServo.cs:60-73, LinearAxisServo.cs:61-78, TwistServo.cs:69-87, PointOnLine.cs:92-121,
+ * EllipticalConeLimit.cs:92-126),
  * world-space init:
  *   BallSocket     anchor xyz
  *   HingeAngle     axis xyz, min, max (radians)
@@ -276,6 +278,9 @@ int jg_set_body(jg_world* world, int32_t body, int32_t field, const float* value
  *   PointOnLine    axis xyz (the line's direction, fixed in body 1), anchor1 xyz (on the line),
  *                  anchor2 xyz, min, max (position along the line; min >= max fixes it,
  *                  LinearLimit.Fixed = (1e-6, -1e-6))
+ *   EllipticalConeLimit axis1 xyz, axis2 xyz, reference xyz (body 1, not along axis1),
+ *                  min1, max1 (swing along the reference), min2, max2 (across it), radians:
+ *                  0 <= min <= max < pi, max > 0, min1 and min2 both zero or both positive
  * A servo's maximum is >= 0 and may be +inf; 0 (the reference's default) applies no impulse.
  * Invalid arguments return JG_ERR_INVALID_ARG (the reference's ArgumentException). */
 int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body2,
@@ -287,6 +292,13 @@ int jg_add_constraint(jg_world* world, int32_t kind, int32_t body1, int32_t body
  * (LinearServo) or one value (LinearAxisServo position, TwistServo angle).  A changed target
  * drops the servo's warm start; both wake its inactive dynamic bodies (ServoMath.cs:22-28). */
 int jg_set_servo(jg_world* world, int32_t constraint, const float* target, float maximum);
+
+/* A constraint's Bias, Softness, LimitBias and LimitSoftness setters (BallSocket.cs:192-222,
+ * HingeAngle.cs:250-312, PointOnLine.cs:308-374, EllipticalConeLimit.cs:226-252 and the like):
+ * NaN keeps a value; values are >= 0.  The limit pair exists for HingeAngle and PointOnLine only,
+ * and the motors have none of the four (JG_ERR_INVALID_ARG). */
+int jg_set_constraint_params(jg_world* world, int32_t constraint, float bias, float softness,
+                             float limit_bias, float limit_softness);
 
 /* ---- the step ------------------------------------------------------------------------- */
 

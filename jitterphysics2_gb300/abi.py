@@ -37,7 +37,7 @@ WARMSTART_ZERO, WARMSTART_CACHED, WARMSTART_MLP = 0, 1, 2
 CONSTRAINT_BALLSOCKET, CONSTRAINT_HINGEANGLE, CONSTRAINT_DISTANCELIMIT, CONSTRAINT_CONELIMIT, CONSTRAINT_TWISTANGLE = 1, 2, 3, 4, 5
 CONSTRAINT_FIXEDANGLE, CONSTRAINT_POINTONPLANE, CONSTRAINT_ANGULARMOTOR, CONSTRAINT_LINEARMOTOR = 6, 7, 8, 9
 CONSTRAINT_ANGULARSERVO, CONSTRAINT_LINEARSERVO, CONSTRAINT_LINEARAXISSERVO, CONSTRAINT_TWISTSERVO = 10, 11, 12, 13
-CONSTRAINT_POINTONLINE = 14
+CONSTRAINT_POINTONLINE, CONSTRAINT_ELLIPTICALCONELIMIT = 14, 15
 
 ERROR_NAMES = {
     JG_ERR_INVALID_ARG: "JG_ERR_INVALID_ARG", JG_ERR_CAPACITY: "JG_ERR_CAPACITY",
@@ -111,6 +111,7 @@ SIGNATURES = {
     "jg_set_body_sleep": (_I, [_P, _I, _F, _F, _F]),
     "jg_add_constraint": (_I, [_P, _I, _I, _I, _P, _PI]),
     "jg_set_servo": (_I, [_P, _I, _P, ctypes.c_float]),
+    "jg_set_constraint_params": (_I, [_P, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     "jg_step": (_I, [_P, _F]),
     "jg_step_host": (_I, [_P, _F, _P, _I]),
     "jg_stabilize": (_I, [_P, _F, _I, _I]),

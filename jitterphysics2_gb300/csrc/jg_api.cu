@@ -696,7 +696,28 @@ static int check_servo_init(int kind, const float* init) {
 
 int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const float* init, int32_t* out_id) {
     if (!w || !init) return JG_ERR_INVALID_ARG;
-    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_POINTONLINE) return JG_ERR_INVALID_ARG;
+    if (kind < JG_CONSTRAINT_BALLSOCKET || kind > JG_CONSTRAINT_ELLIPTICALCONELIMIT) return JG_ERR_INVALID_ARG;
+    v3 ell_ref = mk3(0.f);
+    if (kind == JG_CONSTRAINT_ELLIPTICALCONELIMIT) {
+        // EllipticalConeLimit.Initialize (EllipticalConeLimit.cs:92-113) and ValidateLimits
+        // (:178-200): finite non-zero directions, 0 <= min <= max < pi with max > 0 for both
+        // swings, the inner semiaxes both zero or both positive, and a reference direction
+        // that is not along body 1's axis
+        for (int i = 0; i < 9; i++) if (!std::isfinite(init[i])) return JG_ERR_INVALID_ARG;
+        for (int a = 0; a < 9; a += 3) if (len2(mk3(init[a], init[a + 1], init[a + 2])) == 0.f) return JG_ERR_INVALID_ARG;
+        const float PI = 3.14159265358979323846f;
+        for (int a = 9; a < 13; a += 2) {
+            const float lo = init[a], hi = init[a + 1];
+            if (!std::isfinite(lo) || !std::isfinite(hi) || lo < 0.f || hi <= 0.f || hi >= PI || lo > hi)
+                return JG_ERR_INVALID_ARG;
+        }
+        if ((init[9] == 0.f) != (init[11] == 0.f)) return JG_ERR_INVALID_ARG;
+        v3 ax1 = normalize(mk3(init[0], init[1], init[2]));
+        v3 r = normalize(mk3(init[6], init[7], init[8]));
+        r = r - ax1 * dot(ax1, r);
+        if (len2(r) < 1e-12f) return JG_ERR_INVALID_ARG;
+        ell_ref = normalize(r);
+    }
     if (kind >= JG_CONSTRAINT_ANGULARSERVO && kind <= JG_CONSTRAINT_TWISTSERVO) {
         int r = check_servo_init(kind, init);
         if (r) return r;
@@ -788,6 +809,13 @@ int jg_add_constraint(jg_world* w, int32_t kind, int32_t b1, int32_t b2, const f
         J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
         J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
         J.lim = make_float4(0.f, init[7], init[6], 0.f);
+    } else if (kind == JG_CONSTRAINT_ELLIPTICALCONELIMIT) {
+        // EllipticalConeLimit.Initialize (EllipticalConeLimit.cs:92-126)
+        J.la1 = f4(rotate_inv(normalize(mk3(init[0], init[1], init[2])), q1), 0.f);
+        J.la2 = f4(rotate_inv(normalize(mk3(init[3], init[4], init[5])), q2), 0.f);
+        J.axis = f4(rotate_inv(ell_ref, q1), 0.f);
+        J.prm = make_float4(0.2f, 0.001f, 0.f, 0.f);
+        J.lim = make_float4(init[9], init[10], init[11], init[12]);
     } else if (kind == JG_CONSTRAINT_POINTONLINE) {
         // PointOnLine.Initialize (PointOnLine.cs:92-121)
         v3 axis = normalize(mk3(init[0], init[1], init[2]));
@@ -997,6 +1025,31 @@ int jg_set_servo(jg_world* w, int32_t id, const float* target, float maximum) {
     }
     CK(cudaStreamSynchronize(w->stream));
     w->host_current = false;
+    return JG_OK;
+}
+
+// The constraints' Bias, Softness, LimitBias and LimitSoftness setters (e.g. BallSocket.cs:
+// 192-222, HingeAngle.cs:250-312, PointOnLine.cs:308-374, EllipticalConeLimit.cs:226-252): NaN
+// keeps a value, a negative one is refused (DebugCheck.IsNonNegative).  The limit pair applies to
+// HingeAngle and PointOnLine; the motors have none of the four.
+int jg_set_constraint_params(jg_world* w, int32_t id, float bias, float softness, float limit_bias, float limit_softness) {
+    if (!w || id < 0) return JG_ERR_INVALID_ARG;
+    const float v[4] = {bias, softness, limit_bias, limit_softness};
+    for (float x : v) if (!std::isnan(x) && !(x >= 0.f)) return JG_ERR_INVALID_ARG;
+    int r = flush_joints(w);
+    if (r) return r;
+    if (id >= w->nj_host) return JG_ERR_INVALID_ARG;
+    JointDev J;
+    CK(cudaMemcpy(&J, w->d.joints + id, sizeof(JointDev), cudaMemcpyDeviceToHost));
+    const int kind = J.hdr.x;
+    if (kind == JG_CONSTRAINT_ANGULARMOTOR || kind == JG_CONSTRAINT_LINEARMOTOR) return JG_ERR_INVALID_ARG;
+    const bool limits = kind == JG_CONSTRAINT_HINGEANGLE || kind == JG_CONSTRAINT_POINTONLINE;
+    if (!limits && (!std::isnan(limit_bias) || !std::isnan(limit_softness))) return JG_ERR_INVALID_ARG;
+    if (!std::isnan(bias)) J.prm.x = bias;
+    if (!std::isnan(softness)) J.prm.y = softness;
+    if (!std::isnan(limit_bias)) J.prm.z = limit_bias;
+    if (!std::isnan(limit_softness)) J.prm.w = limit_softness;
+    CK(cudaMemcpy(w->d.joints + id, &J, sizeof(JointDev), cudaMemcpyHostToDevice));
     return JG_OK;
 }
 

@@ -5,8 +5,8 @@
 // (PointOnPlane.cs:128-256), AngularMotor (AngularMotor.cs:128-180), LinearMotor
 // (LinearMotor.cs:152-231), AngularServo (AngularServo.cs:125-172), LinearServo
 // (LinearServo.cs:149-201), LinearAxisServo (LinearAxisServo.cs:169-224) and TwistServo
-// (TwistServo.cs:150-192) and PointOnLine (PointOnLine.cs:149-465).  Included by the solver
-// translation unit.  Matrices are
+// (TwistServo.cs:150-192), PointOnLine (PointOnLine.cs:149-465) and EllipticalConeLimit
+// (EllipticalConeLimit.cs:257-429).  Included by the solver translation unit.  Matrices are
 // row-major float[3][3].
 //
 // JointDev fields of the one-row kinds: la1/la2 anchors (DistanceLimit) or local axes
@@ -1062,6 +1062,103 @@ __device__ void line_iterate(const WorldDev& w, JointDev& J, const StepParams& s
     line_apply(w, J, b1, b2, jb, acc - orig);
 }
 
+// ---- EllipticalConeLimit (EllipticalConeLimit.cs:257-429) -----------------------------------------
+// la1, la2 the cone axes (local), axis body 1's reference direction (local), lim = (min1, max1,
+// min2, max2), prm = (bias factor, softness); the Jacobian row in jac[0] and the clamp state in
+// bil.w persist between steps, the effective mass is bil.x
+__device__ __forceinline__ float ellipse_radius(float a, float b, float c, float s, float& derivative) {
+    const float scale = net_min(a, b);
+    const float u = scale / a, v = scale / b;
+    const float sq = c * c * u * u + s * s * v * v;
+    derivative = c * s * (v * v - u * u) / sq;
+    return scale / sqrtf(sq);
+}
+__device__ __forceinline__ void elliptical_apply(const WorldDev& w, const JointDev& J, LBody& b1, LBody& b2, v3 jac, float a) {
+    if (b1.flags & SB_DYNAMIC) { b1.w = b1.w + sym_mul(b1.I, a * jac); store_vel(w.body, J.hdr.y, b1); }
+    if (b2.flags & SB_DYNAMIC) { b2.w = b2.w - sym_mul(b2.I, a * jac); store_vel(w.body, J.hdr.z, b2); }
+}
+__device__ void elliptical_prepare(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    int i1 = J.hdr.y, i2 = J.hdr.z;
+    LBody b1 = load_body(w.body, i1), b2 = load_body(w.body, i2);
+    const q4 q1 = mkq(w.q[i1]), q2 = mkq(w.q[i2]);
+    const v3 axis = rotate(mk3(J.la1), q1);
+    const v3 reference = rotate(mk3(J.axis), q1);
+    const v3 other = cross(axis, reference);
+    const v3 target = rotate(mk3(J.la2), q2);
+    const float x = dot(target, reference), y = dot(target, other), z = dot(target, axis);
+    const float sine = sqrtf(x * x + y * y);
+    const float angle = StableMathF::atan2(sine, z);
+    float ca, sa;
+    if (sine > 0.f) {
+        ca = x / sine;
+        sa = y / sine;
+    } else {
+        // no unique direction at either pole: the principal direction with the more
+        // responsive angular axis
+        const sym6 I = sym_add(b1.I, b2.I);
+        const bool use_ref = dot(sym_mul(I, other), other) >= dot(sym_mul(I, reference), reference);
+        ca = use_ref ? 1.f : 0.f;
+        sa = use_ref ? 0.f : 1.f;
+    }
+    float derivative;
+    const float outer = ellipse_radius(J.lim.y, J.lim.w, ca, sa, derivative);
+    const bool fixed_cone = J.lim.x == J.lim.y && J.lim.z == J.lim.w;
+    float boundary = outer;
+    int clamp = 0;
+    if (fixed_cone) clamp = 3;
+    else if (angle >= outer) clamp = 1;
+    else if (J.lim.x > 0.f) {
+        float inner_d;
+        const float inner = ellipse_radius(J.lim.x, J.lim.z, ca, sa, inner_d);
+        if (angle <= inner) {
+            clamp = 2;
+            boundary = inner;
+            derivative = inner_d;
+        }
+    }
+    const int previous = (int)J.bil.w;
+    J.bil.w = (float)clamp;
+    if (clamp == 0) {
+        J.acc.x = 0.f;
+        return;
+    }
+    const v3 tilt = ca * reference + sa * other;
+    const v3 azimuth = cross(axis, tilt);
+    const v3 angle_dir = z * tilt - sine * axis;
+    const float az = sine > 0.f ? angle / sine * derivative : 0.f;
+    const float scale = net_max(1.f, fabsf(az));
+    v3 jac = (-azimuth) * (1.f / scale) + (az / scale) * angle_dir;
+    float inv_len = 1.f / sqrtf(dot(jac, jac));
+    jac = jac * inv_len;
+    inv_len /= scale;
+    float acc = J.acc.x;
+    if (previous != clamp || dot(mk3(J.jac[0]), jac) < 0.f) acc = 0.f;
+    J.jac[0] = f4(jac, 0.f);
+    if (clamp == 1) acc = net_min(acc, 0.f);
+    else if (clamp == 2) acc = net_max(acc, 0.f);
+    const float mass = dot(sym_mul(b1.I, jac), jac) + dot(sym_mul(b2.I, jac), jac) + J.prm.y * sp.inv_sub_dt;
+    const float eff = mass > 0.f ? 1.f / mass : 0.f;
+    if (eff == 0.f) acc = 0.f;
+    J.bil.x = eff;
+    J.bias.x = (angle - boundary) * inv_len * J.prm.x * sp.inv_dt;
+    J.acc.x = acc;
+    elliptical_apply(w, J, b1, b2, jac, acc);
+}
+__device__ void elliptical_iterate(const WorldDev& w, JointDev& J, const StepParams& sp) {
+    const int clamp = (int)J.bil.w;
+    if (clamp == 0) return;
+    LBody b1 = load_body(w.body, J.hdr.y), b2 = load_body(w.body, J.hdr.z);
+    const v3 jac = mk3(J.jac[0]);
+    const float jv = dot(b1.w - b2.w, jac);
+    const float lambda = -J.bil.x * (jv + J.bias.x + J.acc.x * J.prm.y * sp.inv_sub_dt);
+    const float old = J.acc.x;
+    float acc = old + lambda;
+    if (clamp == 1) acc = net_min(acc, 0.f);
+    else if (clamp == 2) acc = net_max(acc, 0.f);
+    J.acc.x = acc;
+    elliptical_apply(w, J, b1, b2, jac, acc - old);
+}
+
 __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const StepParams& sp) {
     JointDev& J = w.joints[j];
     switch (J.hdr.x) {
@@ -1077,6 +1174,7 @@ __device__ __forceinline__ void joint_prepare(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_prepare(w, J, sp); break;
         case JG_CONSTRAINT_TWISTSERVO: twist_servo_prepare(w, J, sp); break;
         case JG_CONSTRAINT_POINTONLINE: line_prepare(w, J, sp); break;
+        case JG_CONSTRAINT_ELLIPTICALCONELIMIT: elliptical_prepare(w, J, sp); break;
         default: twist_prepare(w, J, sp); break;
     }
 }
@@ -1095,6 +1193,7 @@ __device__ __forceinline__ void joint_iterate(const WorldDev& w, int j, const St
         case JG_CONSTRAINT_LINEARAXISSERVO: linear_axis_servo_iterate(w, J, sp); break;
         case JG_CONSTRAINT_TWISTSERVO: twist_servo_iterate(w, J, sp); break;
         case JG_CONSTRAINT_POINTONLINE: line_iterate(w, J, sp); break;
+        case JG_CONSTRAINT_ELLIPTICALCONELIMIT: elliptical_iterate(w, J, sp); break;
         default: twist_iterate(w, J, sp); break;
     }
 }

@@ -88,6 +88,12 @@ class World:
         v = np.ascontiguousarray(np.atleast_1d(target), np.float32)
         check(self._lib.jg_set_servo(self._h, constraint, ptr(v), ctypes.c_float(maximum)), "jg_set_servo")
 
+    def set_constraint_params(self, constraint, bias=float("nan"), softness=float("nan"),
+                              limit_bias=float("nan"), limit_softness=float("nan")):
+        """A constraint's Bias / Softness / LimitBias / LimitSoftness (NaN keeps a value)."""
+        check(self._lib.jg_set_constraint_params(self._h, constraint, bias, softness, limit_bias, limit_softness),
+              "jg_set_constraint_params")
+
     def load_scene(self, scene):
         self.set_bodies(scene["bodies"])
         self.set_shapes(scene["shapes"], scene["hull"], scene["triangles"])

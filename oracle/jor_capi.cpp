@@ -19,6 +19,7 @@ using namespace jor;
 #define JOR_CONSTRAINT_LINEARAXISSERVO 12
 #define JOR_CONSTRAINT_TWISTSERVO 13
 #define JOR_CONSTRAINT_POINTONLINE 14
+#define JOR_CONSTRAINT_ELLIPTICALCONELIMIT 15
 
 namespace {
 
@@ -242,6 +243,9 @@ template <class R> struct Handle {
             twist_servo_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), (R)init[6], (R)init[7]);              \
         else if (kind == JOR_CONSTRAINT_POINTONLINE)                                                               \
             line_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9], (R)init[10]);  \
+        else if (kind == JOR_CONSTRAINT_ELLIPTICALCONELIMIT)                                                       \
+            elliptical_init(j, w.bodies, get3<R>(init), get3<R>(init + 3), get3<R>(init + 6), (R)init[9],        \
+                            (R)init[10], (R)init[11], (R)init[12]);                                                \
         w.joints.push_back(j);                                                                                     \
         return (int)w.joints.size() - 1;                                                                           \
     }                                                                                                              \
@@ -269,6 +273,13 @@ template <class R> struct Handle {
         const Joint<R>& jt = w.joints[j];                                                                          \
         V3<R> J[12];                                                                                               \
         return (double)line_jacobian(jt, w.bodies[jt.b1], w.bodies[jt.b2], J).z;                                   \
+    }                                                                                                              \
+    /* EllipticalConeLimit.GetSwing (EllipticalConeLimit.cs:206-221): out = along, across */                     \
+    extern "C" void jor_world_elliptical_swing_##SUF(void* h, int j, double* out) {                                \
+        World<R>& w = ((Handle<R>*)h)->w;                                                                          \
+        R x, y;                                                                                                    \
+        elliptical_swing(w.joints[j], w.bodies, x, y);                                                             \
+        out[0] = (double)x; out[1] = (double)y;                                                                    \
     }                                                                                                              \
     /* a joint's accumulated impulse (acc xyz) */                                                                \
     extern "C" void jor_world_joint_impulse_##SUF(void* h, int j, double* out) {                                   \

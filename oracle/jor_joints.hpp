@@ -3,7 +3,7 @@
 // (Dynamics/Constraints/HingeAngle.cs:84-364), DistanceLimit (DistanceLimit.cs:92-391),
 // ConeLimit (ConeLimit.cs:92-404), TwistAngle (TwistAngle.cs:85-323), FixedAngle, PointOnPlane,
 // the motors, the servos (AngularServo, LinearServo, LinearAxisServo, TwistServo) and
-// PointOnLine, with their math
+// PointOnLine and EllipticalConeLimit, with their math
 // helpers (AngularConstraintMath.cs:13-95, QMatrix.cs:112-125, MathHelper.cs:282-372,
 // JMatrix.cs:391-478, JQuaternion.cs:84-101).
 #pragma once
@@ -201,7 +201,7 @@ template <class R> Mat<R> calc_jacobian(Q4<R> left, Q4<R> right, V3<R>& err, sho
 
 enum JointKind { BALLSOCKET = 1, HINGEANGLE = 2, DISTANCELIMIT = 3, CONELIMIT = 4, TWISTANGLE = 5, FIXEDANGLE = 6,
                  POINTONPLANE = 7, ANGULARMOTOR = 8, LINEARMOTOR = 9, ANGULARSERVO = 10, LINEARSERVO = 11,
-                 LINEARAXISSERVO = 12, TWISTSERVO = 13, POINTONLINE = 14 };
+                 LINEARAXISSERVO = 12, TWISTSERVO = 13, POINTONLINE = 14, ELLIPTICALCONELIMIT = 15 };
 template <class R> struct Joint {
     int kind = BALLSOCKET;
     int b1 = 0, b2 = 0;
@@ -229,6 +229,9 @@ template <class R> struct Joint {
     // MaximumTorque / MaximumForce, LinearServo.TargetPosition
     R maximum = 0;
     V3<R> target_pos;
+    // EllipticalConeLimitData: MinAngle2 / MaxAngle2 (the first pair in min_angle / max_angle),
+    // LocalReference1 (in target_pos), the Jacobian kept from the last Prepare (jr[0])
+    R min_angle2 = 0, max_angle2 = 0;
 };
 
 // BallSocket.Initialize (BallSocket.cs:120-138)
@@ -1170,6 +1173,141 @@ template <class R> void line_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, 
     line_apply(b1, b2, J, j.acc - orig);
 }
 
+// ---- EllipticalConeLimit (Dynamics/Constraints/EllipticalConeLimit.cs) -----------------------
+// EllipticalConeLimit.Initialize (EllipticalConeLimit.cs:92-126) and SetLimits (:163-176): the
+// cone axes of both bodies, a reference direction of body 1 made perpendicular to its axis,
+// the swing limits along the reference [min1, max1] and across it [min2, max2]
+template <class R> void elliptical_init(Joint<R>& j, const std::vector<Body<R>>& b, V3<R> ax1, V3<R> ax2, V3<R> ref,
+                                        R min1, R max1, R min2, R max2) {
+    j.kind = ELLIPTICALCONELIMIT;
+    ax1 = normalize(ax1);
+    ax2 = normalize(ax2);
+    ref = normalize(ref);
+    ref = ref - ax1 * dot(ax1, ref);
+    ref = normalize(ref);
+    j.la1 = rotate_inv(ax1, b[j.b1].q);
+    j.la2 = rotate_inv(ax2, b[j.b2].q);
+    j.target_pos = rotate_inv(ref, b[j.b1].q);
+    j.softness = (R)0.001;
+    j.bias_factor = (R)0.2;
+    j.jr[0] = V3<R>();
+    j.min_angle = min1; j.max_angle = max1;
+    j.min_angle2 = min2; j.max_angle2 = max2;
+    j.acc.x = 0;
+    j.clamp = 0;
+}
+// EllipticalConeLimit.EllipseRadius (EllipticalConeLimit.cs:257-267): the radius of the
+// ellipse with semiaxes a, b at an azimuth, and its logarithmic azimuth derivative
+template <class R> R ellipse_radius(R a, R b, R c, R s, R& derivative) {
+    R scale = net_min(a, b);
+    R u = scale / a;
+    R v = scale / b;
+    R sq = c * c * u * u + s * s * v * v;
+    derivative = c * s * (v * v - u * u) / sq;
+    return scale / std::sqrt(sq);
+}
+// EllipticalConeLimit.GetSwing (EllipticalConeLimit.cs:206-221): the swing along the
+// reference and across it
+template <class R> void elliptical_swing(const Joint<R>& j, const std::vector<Body<R>>& bodies, R& along, R& across) {
+    const Body<R>& b1 = bodies[j.b1];
+    const Body<R>& b2 = bodies[j.b2];
+    V3<R> axis = rotate(j.la1, b1.q);
+    V3<R> reference = rotate(j.target_pos, b1.q);
+    V3<R> other = cross(axis, reference);
+    V3<R> target = rotate(j.la2, b2.q);
+    R x = dot(target, reference);
+    R y = dot(target, other);
+    R sine = std::sqrt(x * x + y * y);
+    R angle = StableMath<R>::atan2(sine, dot(target, axis));
+    R factor = sine > 0 ? angle / sine : (R)0;
+    along = sine > 0 ? x * factor : angle;
+    across = y * factor;
+}
+template <class R> void elliptical_apply(Body<R>& b1, Body<R>& b2, V3<R> jac, R a) {
+    if (b1.motion == DYNAMIC) b1.angvel = b1.angvel + sym_mul(b1.inv_inertia_world, a * jac);
+    if (b2.motion == DYNAMIC) b2.angvel = b2.angvel - sym_mul(b2.inv_inertia_world, a * jac);
+}
+// EllipticalConeLimit.PrepareForIterationEllipticalConeLimit (EllipticalConeLimit.cs:269-392)
+template <class R> void elliptical_prepare(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    V3<R> axis = rotate(j.la1, b1.q);
+    V3<R> reference = rotate(j.target_pos, b1.q);
+    V3<R> other = cross(axis, reference);
+    V3<R> target = rotate(j.la2, b2.q);
+    R x = dot(target, reference);
+    R y = dot(target, other);
+    R z = dot(target, axis);
+    R sine = std::sqrt(x * x + y * y);
+    R angle = StableMath<R>::atan2(sine, z);
+    R ca, sa;
+    if (sine > 0) {
+        ca = x / sine;
+        sa = y / sine;
+    } else {
+        Sym3<R> I(b1.inv_inertia_world.m11 + b2.inv_inertia_world.m11, b1.inv_inertia_world.m12 + b2.inv_inertia_world.m12,
+                  b1.inv_inertia_world.m13 + b2.inv_inertia_world.m13, b1.inv_inertia_world.m22 + b2.inv_inertia_world.m22,
+                  b1.inv_inertia_world.m23 + b2.inv_inertia_world.m23, b1.inv_inertia_world.m33 + b2.inv_inertia_world.m33);
+        bool use_ref = dot(sym_mul(I, other), other) >= dot(sym_mul(I, reference), reference);
+        ca = use_ref ? (R)1 : (R)0;
+        sa = use_ref ? (R)0 : (R)1;
+    }
+    R derivative;
+    R outer = ellipse_radius(j.max_angle, j.max_angle2, ca, sa, derivative);
+    bool fixed_cone = j.min_angle == j.max_angle && j.min_angle2 == j.max_angle2;
+    R boundary = outer;
+    int clamp = 0;
+    if (fixed_cone) clamp = 3;
+    else if (angle >= outer) clamp = 1;
+    else if (j.min_angle > 0) {
+        R inner_d;
+        R inner = ellipse_radius(j.min_angle, j.min_angle2, ca, sa, inner_d);
+        if (angle <= inner) {
+            clamp = 2;
+            boundary = inner;
+            derivative = inner_d;
+        }
+    }
+    int previous = j.clamp;
+    j.clamp = clamp;
+    if (clamp == 0) {
+        j.acc.x = 0;
+        return;
+    }
+    V3<R> tilt = ca * reference + sa * other;
+    V3<R> azimuth = cross(axis, tilt);
+    V3<R> angle_dir = z * tilt - sine * axis;
+    R az = sine > 0 ? angle / sine * derivative : (R)0;
+    R scale = net_max((R)1, std::fabs(az));
+    V3<R> jac = -azimuth * ((R)1 / scale) + (az / scale) * angle_dir;
+    R inv_len = (R)1 / std::sqrt(dot(jac, jac));
+    jac = jac * inv_len;
+    inv_len /= scale;
+    if (previous != clamp || dot(j.jr[0], jac) < 0) j.acc.x = 0;
+    j.jr[0] = jac;
+    if (clamp == 1) j.acc.x = net_min(j.acc.x, (R)0);
+    else if (clamp == 2) j.acc.x = net_max(j.acc.x, (R)0);
+    R mass = dot(sym_mul(b1.inv_inertia_world, jac), jac) + dot(sym_mul(b2.inv_inertia_world, jac), jac) +
+             j.softness * ts.inv_sub_dt;
+    j.eff1 = mass > 0 ? (R)1 / mass : (R)0;
+    if (j.eff1 == 0) j.acc.x = 0;
+    j.bias.x = (angle - boundary) * inv_len * j.bias_factor * ts.inv_dt;
+    elliptical_apply(b1, b2, jac, j.acc.x);
+}
+// EllipticalConeLimit.IterateEllipticalConeLimit (EllipticalConeLimit.cs:394-429)
+template <class R> void elliptical_iterate(Joint<R>& j, std::vector<Body<R>>& bodies, const TimeStep<R>& ts) {
+    if (j.clamp == 0) return;
+    Body<R>& b1 = bodies[j.b1];
+    Body<R>& b2 = bodies[j.b2];
+    R jv = dot(b1.angvel - b2.angvel, j.jr[0]);
+    R lambda = -j.eff1 * (jv + j.bias.x + j.acc.x * j.softness * ts.inv_sub_dt);
+    R old = j.acc.x;
+    j.acc.x = j.acc.x + lambda;
+    if (j.clamp == 1) j.acc.x = net_min(j.acc.x, (R)0);
+    else if (j.clamp == 2) j.acc.x = net_max(j.acc.x, (R)0);
+    elliptical_apply(b1, b2, j.jr[0], j.acc.x - old);
+}
+
 template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, const TimeStep<R>& ts) {
     switch (j.kind) {
         case BALLSOCKET: ballsocket_prepare(j, b, ts); break;
@@ -1184,6 +1322,7 @@ template <class R> void joint_prepare(Joint<R>& j, std::vector<Body<R>>& b, cons
         case LINEARAXISSERVO: linear_axis_servo_prepare(j, b, ts); break;
         case TWISTSERVO: twist_servo_prepare(j, b, ts); break;
         case POINTONLINE: line_prepare(j, b, ts); break;
+        case ELLIPTICALCONELIMIT: elliptical_prepare(j, b, ts); break;
         default: twist_prepare(j, b, ts); break;
     }
 }
@@ -1201,6 +1340,7 @@ template <class R> void joint_iterate(Joint<R>& j, std::vector<Body<R>>& b, cons
         case LINEARAXISSERVO: linear_axis_servo_iterate(j, b, ts); break;
         case TWISTSERVO: twist_servo_iterate(j, b, ts); break;
         case POINTONLINE: line_iterate(j, b, ts); break;
+        case ELLIPTICALCONELIMIT: elliptical_iterate(j, b, ts); break;
         default: twist_iterate(j, b, ts); break;
     }
 }

@@ -45,7 +45,7 @@ def load():
             "jor_world_body_sleep_thresholds": (None, [P, I, D, D]),
             "jor_world_shape_box": (None, [P, I, F, P]), "jor_world_joint_solve": (None, [P, I, F, F, F, I]), "jor_world_joint_iterate": (None, [P, I, F]),
             "jor_world_joint_run": (None, [P, I, F, I, I, I]), "jor_world_joint_impulse": (None, [P, I, P]),
-            "jor_world_set_servo": (None, [P, I, P, F]), "jor_world_line_distance": (D, [P, I]),
+            "jor_world_set_servo": (None, [P, I, P, F]), "jor_world_line_distance": (D, [P, I]), "jor_world_elliptical_swing": (None, [P, I, P]),
             "jor_world_joint_data": (None, [P, I, P]), "jor_world_joint_angle": (D, [P, I]),
             "jor_world_joint_set_limit": (None, [P, I, D, D]), "jor_world_joint_params": (None, [P, I, D, D]),
             "jor_world_joint_limit_params": (None, [P, I, D, D]), "jor_world_joint_matrix": (None, [P, I, P]), "jor_world_set_orientation_d": (None, [P, I, P]),
@@ -283,6 +283,12 @@ class OracleWorld:
     def line_distance(self, j):
         """PointOnLine.Distance: anchor 2's position along the line."""
         return self.fn("jor_world_line_distance")(self.h, j)
+
+    def elliptical_swing(self, j):
+        """EllipticalConeLimit.GetSwing: (along the reference, across it), radians."""
+        out = np.zeros(2, np.float64)
+        self.fn("jor_world_elliptical_swing")(self.h, j, out.ctypes.data)
+        return out
 
     def joint_impulse(self, j):
         out = np.zeros(3, np.float64)
