@@ -1360,7 +1360,7 @@ int jg_check_state(const void* buf, int64_t size, int32_t nb, int32_t ns, int32_
     for (int j = 0; j < h.nj; j++) {
         int4 hd;
         memcpy(&hd, jp + sizeof(JointDev) * (size_t)j, sizeof(hd));
-        if (hd.x < JG_CONSTRAINT_BALLSOCKET || hd.x > JG_CONSTRAINT_LINEARMOTOR || hd.y < 0 || hd.y >= nb || hd.z < 0 ||
+        if (hd.x < JG_CONSTRAINT_BALLSOCKET || hd.x > JG_CONSTRAINT_ELLIPTICALCONELIMIT || hd.y < 0 || hd.y >= nb || hd.z < 0 ||
             hd.z >= nb) {
             g_err = "state blob joint " + std::to_string(j) + " has an invalid kind or body";
             return JG_ERR_INVALID_ARG;

@@ -180,6 +180,9 @@ def test_state_blob_checks_without_a_device(built_lib):
     assert check(state_blob(nb, [(0, 1)], [(-1, 1)], [])) == abi.JG_ERR_INVALID_ARG   # negative body
     assert check(state_blob(nb, [], [], [(abi.CONSTRAINT_BALLSOCKET, 0, 9)])) == abi.JG_ERR_INVALID_ARG
     assert check(state_blob(nb, [], [], [(99, 0, 1)])) == abi.JG_ERR_INVALID_ARG       # unknown kind
+    for kind in range(abi.CONSTRAINT_BALLSOCKET, abi.CONSTRAINT_ELLIPTICALCONELIMIT + 1):  # every kind
+        assert check(state_blob(nb, [], [], [(kind, 0, 1)])) == 0, kind
+    assert check(state_blob(nb, [], [], [(abi.CONSTRAINT_ELLIPTICALCONELIMIT + 1, 0, 1)])) == abi.JG_ERR_INVALID_ARG
     assert check(state_blob(3, [], [], [])) == abi.JG_ERR_INVALID_ARG                   # other body count
     many = state_blob(nb, [(0, 1)] * 17, [(0, 1)] * 17, [])
     assert check(many) == abi.JG_ERR_CAPACITY
