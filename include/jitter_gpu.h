@@ -104,6 +104,9 @@ typedef struct jg_world_params {
     int32_t partitioned_solve;          /* 1 (default): spatial tasks in shared memory   */
     float   speculative_threshold;      /* SpeculativeVelocityThreshold, default 10      */
     int32_t allow_deactivation;         /* AllowDeactivation, default 1 (World.cs:333)   */
+    float   sched_cells_per_sm;         /* partitioned solve: column cells per grid and SM
+                                           (0 = 4.5; the cells never get narrower than three
+                                           times the widest arbiter); a speed knob only     */
 } jg_world_params;
 
 /* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the
@@ -429,8 +432,9 @@ int jg_collect_training(jg_world* world, float* features, float* targets, int32_
 int jg_batch_create(const jg_world_params* params, int32_t n_worlds, jg_world** out_world);
 int jg_batch_step(jg_world* world, float dt);
 /* Autotunes the solve for this world by timing a few steps of a copy of its state: the
- * solve's form (partitioned tasks or global colours) and its launch shape (threads per CTA,
- * CTAs per SM); writes the chosen values into params and keeps them. */
+ * solve's form (partitioned tasks or global colours), its launch shape (threads per CTA,
+ * CTAs per SM) and, for the partitioned solve, the cell density (sched_cells_per_sm);
+ * writes the chosen values into params and keeps them. */
 int jg_autotune(jg_world* world, float dt, int32_t steps, jg_world_params* chosen);
 
 /* ---- host utilities ------------------------------------------------------------------------- */

@@ -56,6 +56,7 @@ PARAMS_FIELDS = [
     ("deterministic", ctypes.c_int32),
     ("partitioned_solve", ctypes.c_int32), ("speculative_threshold", ctypes.c_float),
     ("allow_deactivation", ctypes.c_int32),
+    ("sched_cells_per_sm", ctypes.c_float),
 ]
 
 

@@ -158,6 +158,7 @@ int allocate(jg_world* w) {
     DA(d.sc_acount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_bcount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_task_of, 3 * JG_SCHED_MAXCELLS);
     DA(d.sc_task, JG_SCHED_MAXTASKS); DA(d.sc_cursor, JG_SCHED_MAXTASKS); DA(d.sc_tnc, JG_SCHED_MAXTASKS);
     DA(d.sc_tcell, JG_SCHED_MAXTASKS); DA(d.sc_tdep, 2 * JG_SCHED_MAXTASKS); DA(d.sc_done, JG_SCHED_MAXTASKS);
+    DA(d.sc_order, JG_SCHED_MAXTASKS);
     DA(d.sc_tcol, (size_t)JG_SCHED_MAXTASKS * (JG_TASK_MAXC + 1));
     DA(d.ev_created, d.cap_arb); DA(d.ev_removed, d.cap_arb); DA(d.remaining, 2); DA(d.dst_index, d.cap_arb);
     CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));
@@ -219,6 +220,9 @@ __global__ void k_reset_counters(DevCounters* c) {
     *c = z;
 }
 
+// The partition's cell density: 0 (the default) or a finite value in (0, 64].
+bool cells_per_sm_ok(float c) { return c == 0.f || (std::isfinite(c) && c > 0.f && c <= 64.f); }
+
 StepParams make_params(const jg_world* w, float dt) {
     StepParams sp;
     const jg_world_params& p = w->prm;
@@ -243,6 +247,7 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : JG_TASK_BLOCK,
                                        p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
+    sp.cells_per_sm = p.sched_cells_per_sm > 0 ? p.sched_cells_per_sm : JG_SCHED_CELLS_PER_SM;
     return sp;
 }
 
@@ -354,6 +359,7 @@ int jg_create(const jg_world_params* params, jg_world** out) {
     *out = nullptr;
     if (params->substeps < 1 || params->solver_iterations < 1 || params->relax_iterations < 0) return JG_ERR_INVALID_ARG;
     if (params->solver_iterations > 4096) return JG_ERR_INVALID_ARG;
+    if (!cells_per_sm_ok(params->sched_cells_per_sm)) return JG_ERR_INVALID_ARG;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) { g_err = "no CUDA device"; return JG_ERR_NOT_SUPPORTED; }
@@ -385,7 +391,7 @@ int jg_create(const jg_world_params* params, jg_world** out) {
 int jg_set_params(jg_world* w, const jg_world_params* p) {
     if (!w || !p) return JG_ERR_INVALID_ARG;
     if (p->substeps < 1 || p->solver_iterations < 1 || p->solver_iterations > 4096 || p->relax_iterations < 0 ||
-        !std::isfinite(p->gravity[0]) || !std::isfinite(p->gravity[1]) || !std::isfinite(p->gravity[2])) {
+        !cells_per_sm_ok(p->sched_cells_per_sm) || !std::isfinite(p->gravity[0]) || !std::isfinite(p->gravity[1]) || !std::isfinite(p->gravity[2])) {
         g_err = "jg_set_params: invalid solver settings";
         return JG_ERR_INVALID_ARG;
     }
@@ -1413,14 +1419,32 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     if (r) return r;
     std::vector<char> snap(size);
     if ((r = jg_export_state(w, snap.data(), size, &size))) return r;
-    // the solve's form (spatial tasks with their bodies in shared memory, or global colours)
-    // and its launch shape: threads per task CTA x task CTAs per SM (shared memory bound),
-    // or threads per CTA x CTAs per SM
+    jg_world_params saved = w->prm;
+    // steps from the snapshot under the current settings: milliseconds, or -1 on an error
+    auto trial = [&]() -> float {
+        w->prm.use_graph = 0;
+        jg_solver_reset_launch_cache(w->d);
+        if (jg_import_state(w, snap.data(), size)) return -1.f;
+        if (jg_step(w, dt)) return -1.f;  // warm-up
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0); cudaEventCreate(&e1);
+        cudaEventRecord(e0, w->stream);
+        bool ok = true;
+        for (int s = 0; s < steps && ok; s++) ok = jg_step(w, dt) == JG_OK;
+        cudaEventRecord(e1, w->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return ok ? ms : -1.f;
+    };
+    // 1. the solve's form (spatial tasks with their bodies in shared memory, or global
+    // colours) and its launch shape: threads per task CTA x task CTAs per SM (shared memory
+    // bound), or threads per CTA x CTAs per SM
     const int pblocks[] = {64, 96, 128}, gblocks[] = {128, 256, 512};
     const int pctas[] = {1, 2}, gctas[] = {1, 2, 4};
     float best = 1e30f;
     int bp = w->prm.partitioned_solve != 0, bb = bp ? JG_TASK_BLOCK : 256, bc = bp ? JG_TASK_CTAS : 2;
-    jg_world_params saved = w->prm;
     for (int part = 1; part >= 0; part--)
     for (int ib = 0; ib < 3; ib++)
         for (int ic = 0; ic < (part ? 2 : 3); ic++) {
@@ -1428,26 +1452,30 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
             w->prm.partitioned_solve = part;
             w->prm.solver_block = b;
             w->prm.solver_ctas_per_sm = c;
-            w->prm.use_graph = 0;
-            jg_solver_reset_launch_cache(w->d);
-            if ((r = jg_import_state(w, snap.data(), size))) return r;
-            if ((r = jg_step(w, dt))) continue;  // warm-up
-            cudaEvent_t e0, e1;
-            cudaEventCreate(&e0); cudaEventCreate(&e1);
-            cudaEventRecord(e0, w->stream);
-            bool ok = true;
-            for (int s = 0; s < steps && ok; s++) ok = jg_step(w, dt) == JG_OK;
-            cudaEventRecord(e1, w->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            cudaEventDestroy(e0); cudaEventDestroy(e1);
-            if (ok && ms < best) { best = ms; bb = b; bc = c; bp = part; }
+            const float ms = trial();
+            if (ms >= 0 && ms < best) { best = ms; bb = b; bc = c; bp = part; }
         }
-    w->prm = saved;
     w->prm.partitioned_solve = bp;
     w->prm.solver_block = bb;
     w->prm.solver_ctas_per_sm = bc;
+    // 2. for the spatial tasks, the partition's cell density (cells per grid and SM): more
+    // cells make the longest task shorter and add per-task latency
+    float bcell = saved.sched_cells_per_sm;
+    if (bp && w->d.nworlds <= 1) {  // (batched worlds: one cell per world)
+        const float cells[] = {2.f, 3.f, 4.5f, 6.f, 9.f};
+        float bcm = 1e30f;
+        for (float c : cells) {
+            w->prm.sched_cells_per_sm = c;
+            const float ms = trial();
+            if (ms >= 0 && ms < bcm) { bcm = ms; bcell = c; }
+        }
+    }
+    jg_world_params out = saved;
+    out.partitioned_solve = bp;
+    out.solver_block = bb;
+    out.solver_ctas_per_sm = bc;
+    out.sched_cells_per_sm = bcell;
+    w->prm = out;
     jg_solver_reset_launch_cache(w->d);
     invalidate_graphs(w);
     r = jg_import_state(w, snap.data(), size);

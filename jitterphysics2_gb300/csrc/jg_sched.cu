@@ -8,7 +8,9 @@
 //   1. three staggered column grids in x-z with cell size h > 3 x the largest horizontal
 //      distance between two dynamic bodies sharing an arbiter (offsets 0, h/3, 2h/3): an
 //      arbiter lies inside a cell of grid 0, else of grid 1, else of grid 2 (batched
-//      worlds use one cell per world, all in grid 0);
+//      worlds use one cell per world, all in grid 0).  Above that bound h gives about
+//      cells_per_sm cells per grid and SM: narrow columns keep the longest task short,
+//      which bounds every pass, at the price of more tasks;
 //   2. each non-empty cell of a grid is a task: its arbiters and the dynamic bodies they
 //      touch, which no other task of the same grid touches;
 //   3. inside a task, arbiters get local colours (Jones-Plassmann in shared memory) and
@@ -17,7 +19,9 @@
 //      (without a remainder a task waits only for the tasks of the two previous grid
 //      phases that may share its bodies; their list is built here);
 //   4. arbiters of cells too large for shared memory form the remainder, coloured
-//      globally and solved as before.
+//      globally and solved as before;
+//   5. each grid's tasks are queued longest first; the solver's blocks claim them in that
+//      order (list scheduling), which decides only which block runs a task.
 // The resulting order key of an arbiter (grid * 256 + local colour, or 768 + global
 // colour) describes a sequential order the oracle can replay.
 #include "jg_sync.cuh"
@@ -86,7 +90,7 @@ __global__ void k_sched_bounds(WorldDev w) {
 }
 
 // Cell size and grid extent (one thread).
-__global__ void k_sched_setup(WorldDev w, int nsm) {
+__global__ void k_sched_setup(WorldDev w, int nsm, float cells_per_sm) {
     SchedInfo* S = w.sc;
     if (w.nworlds > 1) {
         S->h = 0.f; S->x0 = S->z0 = 0.f; S->ncx = S->ncz = 1; S->ncells = min(w.nworlds, JG_SCHED_MAXCELLS);
@@ -96,7 +100,7 @@ __global__ void k_sched_setup(WorldDev w, int nsm) {
     float xmin = ord2f(S->bbox[0]), zmin = ord2f(S->bbox[1]), xmax = ord2f(S->bbox[2]), zmax = ord2f(S->bbox[3]);
     float ex = xmax - xmin, ez = zmax - zmin;
     float span = __uint_as_float(S->span_bits);
-    float h = fmaxf(3.0f * span * 1.001f + 1e-4f, sqrtf(ex * ez / (2.0f * (float)nsm)));
+    float h = fmaxf(3.0f * span * 1.001f + 1e-4f, sqrtf(ex * ez / (cells_per_sm * (float)nsm)));
     h = fmaxf(h, 1e-3f);
     float fx = 0.f, fz = 0.f;
     for (int k = 0; k < 256; k++) {
@@ -210,7 +214,9 @@ __global__ void __launch_bounds__(1024) k_sched_tasks(WorldDev w, StepParams sp)
     SchedInfo* S = w.sc;
     const int ncells = S->ncells;
     int t = 0, aoff = 0, boff = 0, over = 0;
+    int tb[JG_SCHED_GRIDS], nt[JG_SCHED_GRIDS];
     for (int g = 0; g < JG_SCHED_GRIDS; g++) {
+        tb[g] = t;
         if (threadIdx.x == 0) S->task_base[g] = t;
         for (int base = 0; base < ncells; base += blockDim.x) {
             int cell = base + threadIdx.x;
@@ -235,11 +241,34 @@ __global__ void __launch_bounds__(1024) k_sched_tasks(WorldDev w, StepParams sp)
             block_scan2(make_int2(ok2 ? 1 : 0, 0), nt);
             t += nt.x; aoff += tot.x; boff += tot.y;
         }
-        if (threadIdx.x == 0) S->ntask[g] = t - S->task_base[g];
+        nt[g] = t - tb[g];
+        if (threadIdx.x == 0) S->ntask[g] = nt[g];
     }
     if (threadIdx.x == 0) {
         S->ntasks = t; S->narb_task = aoff; S->overflow = over;
         w.ctr->ntasks = t; w.ctr->narb_task = aoff;
+    }
+    // Queue order of each grid's tasks, most arbiters first (buckets of 8 arbiters): the
+    // solve's blocks claim a grid phase's tasks in this order, so the longest tasks start
+    // first and a block running one takes no second task while other blocks idle
+    // (longest-processing-time-first list scheduling).  The order decides which block runs a
+    // task, never what the task computes.
+    __shared__ int s_hist[1024];
+    for (int g = 0; g < JG_SCHED_GRIDS; g++) {
+        s_hist[threadIdx.x] = 0;
+        __syncthreads();  // (also makes this block's task records visible to all its threads)
+        for (int i = threadIdx.x; i < nt[g]; i += blockDim.x)
+            atomicAdd(&s_hist[1023 - min(w.sc_task[tb[g] + i].y >> 3, 1023)], 1);
+        __syncthreads();
+        int2 tot;
+        const int2 pre = block_scan2(make_int2(s_hist[threadIdx.x], 0), tot);
+        s_hist[threadIdx.x] = pre.x;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nt[g]; i += blockDim.x) {
+            const int b = 1023 - min(w.sc_task[tb[g] + i].y >> 3, 1023);
+            w.sc_order[tb[g] + atomicAdd(&s_hist[b], 1)] = tb[g] + i;
+        }
+        __syncthreads();
     }
 }
 
@@ -448,7 +477,7 @@ void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int ns
     k_sched_reset<<<1, 1, 0, s>>>(w);
     if (p.partition) {
         k_sched_bounds<<<nsm * 4, 256, 0, s>>>(w);
-        k_sched_setup<<<1, 1, 0, s>>>(w, nsm);
+        k_sched_setup<<<1, 1, 0, s>>>(w, nsm, p.cells_per_sm);
         k_sched_cells<<<nsm * 4, 256, 0, s>>>(w);
         k_sched_assign<<<nsm * 4, 256, 0, s>>>(w);
         k_sched_tasks<<<1, 1024, 0, s>>>(w, p);

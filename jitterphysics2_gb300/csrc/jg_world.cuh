@@ -44,6 +44,7 @@ struct __align__(16) TriDev {
 #define JG_SCHED_GRIDS 3
 #define JG_SCHED_MAXCELLS 65536      // cells per grid
 #define JG_SCHED_MAXTASKS 32768
+#define JG_SCHED_CELLS_PER_SM 4.5f   // default cells per grid and SM (jg_world_params.sched_cells_per_sm)
 #define JG_TASK_MAXC 64              // local colours per task
 #define JG_TASK_MAXA 6144            // arbiters per task (local colouring in shared memory)
 #define JG_ORDER_REMAINDER 768       // order keys: task arbiters grid * 256 + colour, remainder 768 + colour
@@ -60,7 +61,8 @@ struct SchedInfo {
     int tag;                         // step counter for the body claim stamps
     int overflow;                    // cells pushed to the remainder (too large)
     int maxc;                        // most local colours of any task
-    int pad[3];
+    int pad;
+    unsigned long long qticket;      // the solve's task queue: next ticket to hand out
 };
 
 struct ArbStore {
@@ -211,6 +213,7 @@ struct WorldDev {
     int* sc_tcell;               // [MAXTASKS] cell of the task (in its grid)
     int4* sc_tdep;               // [2 * MAXTASKS] tasks of the previous two grid phases sharing bodies (-1: none)
     unsigned* sc_done;           // [MAXTASKS] levels (grid phases) the task has completed in the solve
+    int* sc_order;               // [MAXTASKS] each grid's tasks, most arbiters first (the queue order)
     int* sc_tcol;                // [MAXTASKS * (MAXC + 1)] colour offsets inside the task
     int* sc_tlist;               // [cap_arb] arbiters of each task (pre-permute ids)
     int* sc_tbody;               // [3 * cap_bodies] bodies of each task
@@ -256,6 +259,7 @@ struct StepParams {
     int allow_deact;             // World.AllowDeactivation: sleeping bodies and rows are skipped
     int stabilize;               // World.Stabilize: solve only, no force or velocity integration
     int task_maxb;               // bodies a task may hold in the solver's shared memory
+    float cells_per_sm;          // partition cells per grid and SM, before the span bound
 };
 
 // Partitioned-solve launch shape: threads per CTA and bytes of shared memory per

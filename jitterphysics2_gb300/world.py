@@ -234,7 +234,8 @@ class World:
     def autotune(self, dt, steps=3):
         chosen = abi.WorldParams()
         check(self._lib.jg_autotune(self._h, ctypes.c_float(dt), steps, ctypes.byref(chosen)), "jg_autotune")
-        return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile", "partitioned_solve")}
+        return {k: getattr(chosen, k) for k in ("solver_block", "solver_ctas_per_sm", "narrow_tile", "partitioned_solve",
+                                                "sched_cells_per_sm")}
 
     # -- learned warm start (no reference counterpart) ------------------------------------
     def mlp_load(self, params):

@@ -67,6 +67,7 @@ def test_autotune_picks_a_working_launch_shape():
         assert chosen["solver_block"] in (64, 96, 128) and chosen["solver_ctas_per_sm"] in (1, 2)
     else:
         assert chosen["solver_block"] in (128, 256, 512) and chosen["solver_ctas_per_sm"] in (1, 2, 4)
+    assert chosen["sched_cells_per_sm"] == 0.0   # batched worlds: one cell per world, not tuned
     # the tuner restores the state it timed from
     after = w.bodies()
     assert np.array_equal(before["position"], after["position"])

@@ -91,3 +91,13 @@ def test_first_invalid_body_decides_the_error():
     with pytest.raises(abi.JitterError) as e:
         w.set_bodies(bad)
     assert e.value.code == abi.JG_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("cells", [-1.0, float("nan"), float("inf"), 65.0])
+def test_invalid_cell_density_is_rejected(cells):
+    from jitterphysics2_gb300.world import World
+    with pytest.raises(abi.JitterError) as e:
+        World(max_bodies=16, sched_cells_per_sm=cells)
+    assert e.value.code == abi.JG_ERR_INVALID_ARG
+    w = World(max_bodies=16, sched_cells_per_sm=3.0)   # a valid density; 0 means the default
+    w.close()

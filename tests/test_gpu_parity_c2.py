@@ -54,3 +54,18 @@ def test_c2_one_step_velocities_match_oracle(settled_c2):
     err = _one_step_velocity_errors(sc, w)
     print("20k pile one-step velocity error: max %.3g, within 1e-3 %.5f" % (err.max(), np.mean(err < 1e-3)))
     assert np.mean(err < 1e-3) >= 0.999, (np.mean(err < 1e-3), np.sort(err)[-5:])
+
+
+def test_c2_one_step_velocities_with_more_tasks_than_blocks(settled_c2):
+    # a dense partition (9 cells per grid and SM, down to the floor of three arbiter widths)
+    # on one task CTA per SM: the blocks claim several tasks per grid phase from the solve's
+    # queue, longest first, and the result still replays in the oracle's order
+    sc, w = settled_c2
+    w2 = world_for_scene(sc, sched_cells_per_sm=9.0, solver_ctas_per_sm=1)
+    w2.import_state(w.export_state())
+    w2.step(sc["dt"])
+    c = w2.counters()
+    assert c["status"] == 0 and c["solver_tasks"] > 152 and c["task_arbiters"] == c["arbiters"], c
+    err = _one_step_velocity_errors(sc, w2)
+    print("20k pile, dense partition: max %.3g, within 1e-3 %.5f" % (err.max(), np.mean(err < 1e-3)))
+    assert np.mean(err < 1e-3) >= 0.999, (np.mean(err < 1e-3), np.sort(err)[-5:])
