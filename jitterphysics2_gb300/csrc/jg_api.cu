@@ -158,7 +158,6 @@ int allocate(jg_world* w) {
     DA(d.sc_acount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_bcount, 3 * JG_SCHED_MAXCELLS); DA(d.sc_task_of, 3 * JG_SCHED_MAXCELLS);
     DA(d.sc_task, JG_SCHED_MAXTASKS); DA(d.sc_cursor, JG_SCHED_MAXTASKS); DA(d.sc_tnc, JG_SCHED_MAXTASKS);
     DA(d.sc_tcell, JG_SCHED_MAXTASKS); DA(d.sc_tdep, 2 * JG_SCHED_MAXTASKS); DA(d.sc_done, JG_SCHED_MAXTASKS);
-    DA(d.sc_order, JG_SCHED_MAXTASKS);
     DA(d.sc_tcol, (size_t)JG_SCHED_MAXTASKS * (JG_TASK_MAXC + 1));
     DA(d.ev_created, d.cap_arb); DA(d.ev_removed, d.cap_arb); DA(d.remaining, 2); DA(d.dst_index, d.cap_arb);
     CK(cudaMallocHost((void**)&w->h_ctr, sizeof(DevCounters)));

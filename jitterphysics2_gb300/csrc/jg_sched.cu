@@ -19,9 +19,7 @@
 //      (without a remainder a task waits only for the tasks of the two previous grid
 //      phases that may share its bodies; their list is built here);
 //   4. arbiters of cells too large for shared memory form the remainder, coloured
-//      globally and solved as before;
-//   5. each grid's tasks are queued longest first; the solver's blocks claim them in that
-//      order (list scheduling), which decides only which block runs a task.
+//      globally and solved as before.
 // The resulting order key of an arbiter (grid * 256 + local colour, or 768 + global
 // colour) describes a sequential order the oracle can replay.
 #include "jg_sync.cuh"
@@ -214,9 +212,7 @@ __global__ void __launch_bounds__(1024) k_sched_tasks(WorldDev w, StepParams sp)
     SchedInfo* S = w.sc;
     const int ncells = S->ncells;
     int t = 0, aoff = 0, boff = 0, over = 0;
-    int tb[JG_SCHED_GRIDS], nt[JG_SCHED_GRIDS];
     for (int g = 0; g < JG_SCHED_GRIDS; g++) {
-        tb[g] = t;
         if (threadIdx.x == 0) S->task_base[g] = t;
         for (int base = 0; base < ncells; base += blockDim.x) {
             int cell = base + threadIdx.x;
@@ -241,34 +237,11 @@ __global__ void __launch_bounds__(1024) k_sched_tasks(WorldDev w, StepParams sp)
             block_scan2(make_int2(ok2 ? 1 : 0, 0), nt);
             t += nt.x; aoff += tot.x; boff += tot.y;
         }
-        nt[g] = t - tb[g];
-        if (threadIdx.x == 0) S->ntask[g] = nt[g];
+        if (threadIdx.x == 0) S->ntask[g] = t - S->task_base[g];
     }
     if (threadIdx.x == 0) {
         S->ntasks = t; S->narb_task = aoff; S->overflow = over;
         w.ctr->ntasks = t; w.ctr->narb_task = aoff;
-    }
-    // Queue order of each grid's tasks, most arbiters first (buckets of 8 arbiters): the
-    // solve's blocks claim a grid phase's tasks in this order, so the longest tasks start
-    // first and a block running one takes no second task while other blocks idle
-    // (longest-processing-time-first list scheduling).  The order decides which block runs a
-    // task, never what the task computes.
-    __shared__ int s_hist[1024];
-    for (int g = 0; g < JG_SCHED_GRIDS; g++) {
-        s_hist[threadIdx.x] = 0;
-        __syncthreads();  // (also makes this block's task records visible to all its threads)
-        for (int i = threadIdx.x; i < nt[g]; i += blockDim.x)
-            atomicAdd(&s_hist[1023 - min(w.sc_task[tb[g] + i].y >> 3, 1023)], 1);
-        __syncthreads();
-        int2 tot;
-        const int2 pre = block_scan2(make_int2(s_hist[threadIdx.x], 0), tot);
-        s_hist[threadIdx.x] = pre.x;
-        __syncthreads();
-        for (int i = threadIdx.x; i < nt[g]; i += blockDim.x) {
-            const int b = 1023 - min(w.sc_task[tb[g] + i].y >> 3, 1023);
-            w.sc_order[tb[g] + atomicAdd(&s_hist[b], 1)] = tb[g] + i;
-        }
-        __syncthreads();
     }
 }
 

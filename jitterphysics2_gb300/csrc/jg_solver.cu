@@ -598,8 +598,7 @@ __device__ __forceinline__ bool prepare_task(const WorldDev& w, const ArbStore& 
 // (JG_ERR_TIMEOUT recorded).
 __device__ __forceinline__ bool run_task(const WorldDev& w, const ArbStore& A, const StepParams& sp, int t, int kind,
                                          float4* sbody, float4* ring, volatile int* sver, volatile int* abort_flag,
-                                         float& d2, float& l2, unsigned long long* queue = nullptr,
-                                         unsigned long long* s_next = nullptr) {
+                                         float& d2, float& l2) {
     const int4 T = w.sc_task[t];
     const int bs = blockDim.x, tid = threadIdx.x;
     const int sst = sp.task_maxb;  // stride of the staged body arrays
@@ -640,17 +639,11 @@ __device__ __forceinline__ bool run_task(const WorldDev& w, const ArbStore& A, c
     }
     cp_async_wait_0();  // no copy into shared memory outlives the task
     __syncthreads();
-    // with a queue, the block's next ticket is claimed here, its latency hidden behind the
-    // write-back (claimed any earlier, a block would commit to its next task while still
-    // running a long one)
-    unsigned long long next = 0;
-    if (queue && tid == 0) next = atomicAdd(queue, 1ull);
     for (int i = tid; i < T.w; i += bs) {
         float4* dst = (float4*)&w.body[w.sc_tbody[T.z + i]];
         dst[0] = sbody[i];
         dst[1] = sbody[sst + i];
     }
-    if (queue && tid == 0) *s_next = next;
     __syncthreads();
     return ok && !*abort_flag;
 }
@@ -723,61 +716,31 @@ __global__ void k_solve_tasks(WorldDev w, StepParams sp) {
     // a grid barrier: a task waits only for the tasks of the two phases before it that may
     // share its bodies (their completion counters), so a slow task delays its neighbours,
     // not the whole pass.  Grid barriers stay around the whole-body integration steps.
-    // Blocks take their tasks from one queue of tickets: pass after pass (over the
-    // substeps), grid phase after grid phase, each grid's tasks longest first.  A block
-    // claims its next ticket while it writes back the current task; a ticket of the segment
-    // after the next grid barrier is kept across that barrier.  Tickets are handed out in
-    // order and every awaited task has a smaller ticket, so the smallest unfinished ticket
-    // can always run: the waits end.
+    // Every block runs its tasks in phase order and each awaited task belongs to an earlier
+    // phase, so the waits end.  (Tasks go to blocks in cell order: a longest-first order,
+    // static or claimed from a queue, measured slower.)
     if (w.ctr->ncolors == 0) {
-        __shared__ unsigned long long s_ticket;
-        unsigned long long* const queue = &w.sc->qticket;
-        if (blockIdx.x == 0 && threadIdx.x == 0) *queue = 0ull;  // ordered before every claim by the barrier below
-        const unsigned long long per_pass = (unsigned long long)ntasks;
-        unsigned long long ticket = 0;
-        bool held = false;
+        unsigned level = 0;  // grid phases started so far in this launch
         for (int s = 0; s < sp.substeps; s++) {
             if (!sp.stabilize) integrate_forces_all(w, sp, tid, nth);
             if (!grid_sync(w.bar_count, w.bar_gen, status)) return;
-            // segment 0: the prepare pass and the iterations; segment 1: the relaxation
-            for (int seg = 0; seg < 2; seg++) {
-                const int pass_end = seg == 0 ? sp.iterations + 1 : npass;
-                const unsigned long long seg_end = ((unsigned long long)s * npass + pass_end) * per_pass;
-                int cur = -1;  // the pass the residual sums belong to
+            for (int pass = 0; pass < npass; pass++) {
+                const bool relax = pass > sp.iterations;
+                const int kind = pass == 0 ? PASS_PREPARE : (relax ? PASS_RELAX : PASS_ITERATE);
                 float d2 = 0.f, l2 = 0.f;
-                auto flush = [&]() {
-                    if (sp.record_residual && s == 0 && cur > 0 && cur <= sp.iterations && cur <= JG_RESID_MAX)
-                        block_reduce_add(d2, l2, w.resid + 2 * (cur - 1));
-                    d2 = l2 = 0.f;
-                };
-                for (;;) {
-                    if (!held) {
-                        if (threadIdx.x == 0) s_ticket = atomicAdd(queue, 1ull);
-                        __syncthreads();
-                        ticket = s_ticket;
-                        held = true;
+                for (int g = 0; g < JG_SCHED_GRIDS; g++, level++) {
+                    for (int t = tbase[g] + blockIdx.x; t < tbase[g] + ntask[g]; t += gridDim.x) {
+                        if (!wait_deps(w, t, level, status)) return;
+                        if (!run_task(w, A, sp, t, kind, sbody, ring, sver, &s_abort, d2, l2)) return;
+                        if (threadIdx.x == 0) {  // run_task ended with a block barrier
+                            __threadfence();
+                            st_release_u32(&w.sc_done[t], level + 1);
+                        }
                     }
-                    if (ticket >= seg_end) break;  // after the next grid barrier: kept
-                    held = false;
-                    const unsigned long long P = ticket / per_pass;  // pass over the whole launch
-                    int r = (int)(ticket - P * per_pass), g = 0;
-                    while (g + 1 < JG_SCHED_GRIDS && r >= ntask[g]) { r -= ntask[g]; g++; }
-                    const int pass = (int)(P % (unsigned long long)npass);
-                    if (pass != cur) { flush(); cur = pass; }
-                    const int t = w.sc_order[tbase[g] + r];
-                    const unsigned level = (unsigned)(P * JG_SCHED_GRIDS + g);
-                    const int kind = pass == 0 ? PASS_PREPARE : (pass > sp.iterations ? PASS_RELAX : PASS_ITERATE);
-                    if (!wait_deps(w, t, level, status)) return;
-                    if (!run_task(w, A, sp, t, kind, sbody, ring, sver, &s_abort, d2, l2, queue, &s_ticket)) return;
-                    if (threadIdx.x == 0) {  // run_task ended with a block barrier
-                        __threadfence();
-                        st_release_u32(&w.sc_done[t], level + 1);
-                    }
-                    ticket = s_ticket;  // claimed during the write-back
-                    held = true;
                 }
-                flush();
-                if (seg == 0) {  // after the last biased iteration (World.Step.cs:244-246)
+                if (sp.record_residual && s == 0 && pass > 0 && !relax && pass <= JG_RESID_MAX)
+                    block_reduce_add(d2, l2, w.resid + 2 * (pass - 1));
+                if (pass == sp.iterations) {  // after the last biased iteration (World.Step.cs:244-246)
                     if (!grid_sync(w.bar_count, w.bar_gen, status)) return;  // every task of the pass
                     if (w.rec_on && s == 0) record_targets(w, A, tid, nth);
                     if (!sp.stabilize) integrate_velocities_all(w, sp, tid, nth);

@@ -61,8 +61,7 @@ struct SchedInfo {
     int tag;                         // step counter for the body claim stamps
     int overflow;                    // cells pushed to the remainder (too large)
     int maxc;                        // most local colours of any task
-    int pad;
-    unsigned long long qticket;      // the solve's task queue: next ticket to hand out
+    int pad[3];
 };
 
 struct ArbStore {
@@ -213,7 +212,6 @@ struct WorldDev {
     int* sc_tcell;               // [MAXTASKS] cell of the task (in its grid)
     int4* sc_tdep;               // [2 * MAXTASKS] tasks of the previous two grid phases sharing bodies (-1: none)
     unsigned* sc_done;           // [MAXTASKS] levels (grid phases) the task has completed in the solve
-    int* sc_order;               // [MAXTASKS] each grid's tasks, most arbiters first (the queue order)
     int* sc_tcol;                // [MAXTASKS * (MAXC + 1)] colour offsets inside the task
     int* sc_tlist;               // [cap_arb] arbiters of each task (pre-permute ids)
     int* sc_tbody;               // [3 * cap_bodies] bodies of each task

@@ -58,8 +58,8 @@ def test_c2_one_step_velocities_match_oracle(settled_c2):
 
 def test_c2_one_step_velocities_with_more_tasks_than_blocks(settled_c2):
     # a dense partition (9 cells per grid and SM, down to the floor of three arbiter widths)
-    # on one task CTA per SM: the blocks claim several tasks per grid phase from the solve's
-    # queue, longest first, and the result still replays in the oracle's order
+    # on one task CTA per SM: each block runs several tasks per grid phase, and the result
+    # still replays in the oracle's order
     sc, w = settled_c2
     w2 = world_for_scene(sc, sched_cells_per_sm=9.0, solver_ctas_per_sm=1)
     w2.import_state(w.export_state())
