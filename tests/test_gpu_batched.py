@@ -106,3 +106,19 @@ def test_batched_graph_step_equals_stream_steps():
     assert a.counters()["status"] == 0 and a.counters()["contacts"] > 0
     assert np.array_equal(ba["position"], bb["position"]) and np.array_equal(ba["velocity"], bb["velocity"])
     assert a.timings()["total"] > 0
+
+
+def test_autotune_on_a_single_world_picks_a_cell_density():
+    sc = scenes.mixed_pile(n=2000, box=(30.0, 10.0, 30.0), y0=0.0, cells=16, seed=23, lattice=2.0)
+    w = world_for_scene(sc)
+    for _ in range(30):
+        w.step(sc["dt"])
+    before = w.bodies()
+    chosen = w.autotune(sc["dt"], steps=1)
+    if chosen["partitioned_solve"]:
+        assert chosen["sched_cells_per_sm"] in (2.0, 3.0, 4.5, 6.0, 9.0), chosen
+    after = w.bodies()
+    assert np.array_equal(before["position"], after["position"])
+    for _ in range(3):
+        w.step(sc["dt"])
+    assert w.counters()["status"] == 0
