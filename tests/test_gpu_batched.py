@@ -116,7 +116,7 @@ def test_autotune_on_a_single_world_picks_a_cell_density():
     before = w.bodies()
     chosen = w.autotune(sc["dt"], steps=1)
     if chosen["partitioned_solve"]:
-        assert chosen["sched_cells_per_sm"] in (2.0, 3.0, 4.5, 6.0, 9.0), chosen
+        assert chosen["sched_cells_per_sm"] in (0.0, 1.0, 2.0, 3.0, 4.5, 6.0, 9.0), chosen
     after = w.bodies()
     assert np.array_equal(before["position"], after["position"])
     for _ in range(3):
