@@ -105,9 +105,10 @@ typedef struct jg_world_params {
     float   speculative_threshold;      /* SpeculativeVelocityThreshold, default 10      */
     int32_t allow_deactivation;         /* AllowDeactivation, default 1 (World.cs:333)   */
     float   sched_cells_per_sm;         /* partitioned solve: column cells per grid and SM
-                                           (0 = about 160 arbiters per cell; the cells never
-                                           get narrower than three times the widest
-                                           arbiter); a speed knob only                      */
+                                           (0 = the narrowest cells when they are no more
+                                           than the solve's blocks, else about 250 arbiters
+                                           per cell; the cells never get narrower than three
+                                           times the widest arbiter); a speed knob only     */
 } jg_world_params;
 
 /* One rigid body: the fields of RigidBodyData (RigidBody.cs:107-250) plus the

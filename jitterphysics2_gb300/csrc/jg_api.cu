@@ -246,7 +246,8 @@ StepParams make_params(const jg_world* w, float dt) {
     sp.task_maxb = jg_solver_task_maxb(p.solver_block > 0 ? p.solver_block : JG_TASK_BLOCK,
                                        p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     if (sp.task_maxb < 64) sp.partition = 0;  // a block too large for a useful task
-    sp.cells_per_sm = p.sched_cells_per_sm;  // 0: chosen on the device from the arbiter count
+    sp.cells_per_sm = p.sched_cells_per_sm;  // 0: chosen on the device (cell count and arbiter count)
+    sp.solve_blocks = w->nsm * (p.solver_ctas_per_sm > 0 ? p.solver_ctas_per_sm : JG_TASK_CTAS);
     return sp;
 }
 
@@ -1461,7 +1462,7 @@ int jg_autotune(jg_world* w, float dt, int32_t steps, jg_world_params* chosen) {
     // cells make the longest task shorter and add per-task latency
     float bcell = saved.sched_cells_per_sm;
     if (bp && w->d.nworlds <= 1) {  // (batched worlds: one cell per world)
-        const float cells[] = {0.f, 1.f, 2.f, 3.f, 4.5f, 6.f, 9.f};  // 0: the arbiter-count rule
+        const float cells[] = {0.f, 1.f, 2.f, 3.f, 4.5f, 6.f, 9.f};  // 0: the default rule
         float bcm = 1e30f;
         for (float c : cells) {
             w->prm.sched_cells_per_sm = c;

@@ -9,9 +9,10 @@
 //      distance between two dynamic bodies sharing an arbiter (offsets 0, h/3, 2h/3): an
 //      arbiter lies inside a cell of grid 0, else of grid 1, else of grid 2 (batched
 //      worlds use one cell per world, all in grid 0).  Above that bound h gives about
-//      cells_per_sm cells per grid and SM (by default as many as make about 160 arbiters a
-//      cell): narrow columns keep the longest task short, which bounds every pass, at the
-//      price of more tasks, each with a fixed latency;
+//      cells_per_sm cells per grid and SM (by default the narrowest cells when there are
+//      no more of them than solve blocks, else as many as make about 250 arbiters a cell):
+//      narrow columns keep the longest task short, which bounds every pass, at the price of
+//      more tasks, each with a fixed latency;
 //   2. each non-empty cell of a grid is a task: its arbiters and the dynamic bodies they
 //      touch, which no other task of the same grid touches;
 //   3. inside a task, arbiters get local colours (Jones-Plassmann in shared memory) and
@@ -89,7 +90,7 @@ __global__ void k_sched_bounds(WorldDev w) {
 }
 
 // Cell size and grid extent (one thread).
-__global__ void k_sched_setup(WorldDev w, int nsm, float cells_per_sm) {
+__global__ void k_sched_setup(WorldDev w, int nsm, float cells_per_sm, int blocks) {
     SchedInfo* S = w.sc;
     if (w.nworlds > 1) {
         S->h = 0.f; S->x0 = S->z0 = 0.f; S->ncx = S->ncz = 1; S->ncells = min(w.nworlds, JG_SCHED_MAXCELLS);
@@ -99,12 +100,19 @@ __global__ void k_sched_setup(WorldDev w, int nsm, float cells_per_sm) {
     float xmin = ord2f(S->bbox[0]), zmin = ord2f(S->bbox[1]), xmax = ord2f(S->bbox[2]), zmax = ord2f(S->bbox[3]);
     float ex = xmax - xmin, ez = zmax - zmin;
     float span = __uint_as_float(S->span_bits);
-    // cells per grid and SM: the caller's, or (0) about JG_SCHED_CELL_ARBITERS arbiters per
-    // cell on average, so that dense piles get narrow columns (their longest task bounds a
-    // pass) and sparse scenes few tasks (each task costs a fixed latency)
-    if (!(cells_per_sm > 0.f))
-        cells_per_sm = fminf(fmaxf((float)min(w.ctr->narb, w.cap_arb) / (JG_SCHED_CELL_ARBITERS * (float)nsm), 0.5f), 16.f);
-    float h = fmaxf(3.0f * span * 1.001f + 1e-4f, sqrtf(ex * ez / (cells_per_sm * (float)nsm)));
+    const float h_min = 3.0f * span * 1.001f + 1e-4f;
+    float h;
+    if (cells_per_sm > 0.f) {
+        h = fmaxf(h_min, sqrtf(ex * ez / (cells_per_sm * (float)nsm)));
+    } else if ((floorf(ex / h_min) + 3.0f) * (floorf(ez / h_min) + 3.0f) <= (float)blocks) {
+        h = h_min;  // the narrowest cells still give each solve block at most one task per grid
+    } else {
+        // more cells than blocks: about JG_SCHED_CELL_ARBITERS arbiters per cell on average,
+        // so that dense piles get narrow columns (their longest task bounds a pass) and
+        // sparse scenes few tasks per block (each task costs a fixed latency)
+        const float c = fminf(fmaxf((float)min(w.ctr->narb, w.cap_arb) / (JG_SCHED_CELL_ARBITERS * (float)nsm), 0.5f), 16.f);
+        h = fmaxf(h_min, sqrtf(ex * ez / (c * (float)nsm)));
+    }
     h = fmaxf(h, 1e-3f);
     float fx = 0.f, fz = 0.f;
     for (int k = 0; k < 256; k++) {
@@ -456,7 +464,7 @@ void jg_launch_schedule(WorldDev& w, const StepParams& p, cudaStream_t s, int ns
     k_sched_reset<<<1, 1, 0, s>>>(w);
     if (p.partition) {
         k_sched_bounds<<<nsm * 4, 256, 0, s>>>(w);
-        k_sched_setup<<<1, 1, 0, s>>>(w, nsm, p.cells_per_sm);
+        k_sched_setup<<<1, 1, 0, s>>>(w, nsm, p.cells_per_sm, p.solve_blocks);
         k_sched_cells<<<nsm * 4, 256, 0, s>>>(w);
         k_sched_assign<<<nsm * 4, 256, 0, s>>>(w);
         k_sched_tasks<<<1, 1024, 0, s>>>(w, p);

@@ -44,7 +44,7 @@ struct __align__(16) TriDev {
 #define JG_SCHED_GRIDS 3
 #define JG_SCHED_MAXCELLS 65536      // cells per grid
 #define JG_SCHED_MAXTASKS 32768
-#define JG_SCHED_CELL_ARBITERS 160.f // default partition density: arbiters per cell on average
+#define JG_SCHED_CELL_ARBITERS 250.f // default partition density: arbiters per cell on average
 #define JG_TASK_MAXC 64              // local colours per task
 #define JG_TASK_MAXA 6144            // arbiters per task (local colouring in shared memory)
 #define JG_ORDER_REMAINDER 768       // order keys: task arbiters grid * 256 + colour, remainder 768 + colour
@@ -257,7 +257,8 @@ struct StepParams {
     int allow_deact;             // World.AllowDeactivation: sleeping bodies and rows are skipped
     int stabilize;               // World.Stabilize: solve only, no force or velocity integration
     int task_maxb;               // bodies a task may hold in the solver's shared memory
-    float cells_per_sm;          // partition cells per grid and SM, before the span bound (0: by arbiter count)
+    float cells_per_sm;          // partition cells per grid and SM, before the span bound (0: chosen on the device)
+    int solve_blocks;            // persistent blocks of the task solve (the default density rule)
 };
 
 // Partitioned-solve launch shape: threads per CTA and bytes of shared memory per
