@@ -59,10 +59,10 @@ STATE_CACHE = os.environ.get("JG_BENCH_CACHE", "/tmp/jitter_gb300_bench")
 
 # Figures from ncu captures (profiles/), labelled with the commit they were taken at:
 # they do not follow later code changes.
-CAPTURE = {"k_solve_tasks_dram_bytes": 0.076e9, "k_mpr_fma_pipe_pct": 33.2,
-           "source": "ncu captures of the formed 100k pile: k_solve_tasks at commit 00f0da0 "
-                     "(profiles/k_solve_tasks_pile100k.md), k_mpr at commit 20319af "
-                     "(profiles/k_mpr_k_epa_pile100k.md); solver and narrowphase unchanged since"}
+CAPTURE = {"k_solve_tasks_dram_bytes": 0.067e9, "k_mpr_fma_pipe_pct": 33.2,
+           "source": "ncu captures of the formed 100k pile: k_solve_tasks at commit 0e4443c "
+                     "(profiles/k_solve_tasks_pile100k.md; later commits keep its partition of this pile), "
+                     "k_mpr at commit 20319af (profiles/k_mpr_k_epa_pile100k.md); narrowphase unchanged since"}
 
 
 def peaks():
