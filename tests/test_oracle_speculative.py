@@ -302,3 +302,43 @@ def test_linear_only_contact_ignores_angular_surface_velocity(gap, target):
     b = w.bodies()
     assert b["velocity"][1][0] == pytest.approx(target, abs=1e-5)
     np.testing.assert_array_equal(b["angular_velocity"][1], (0, 0, 10))
+
+
+@pytest.mark.parametrize("speculative", [True, False])
+def test_bullet_stops_on_a_triangle_mesh_only_with_speculative_contacts(speculative):
+    # the sweep against triangle shapes (NarrowPhase.Sweep on a TriangleShape's support map,
+    # World.Detect.cs:168-196): a 0.1 sphere 0.8 above a flat 4 x 4-cell mesh at 100 m/s, one
+    # step of 0.01 (1.0 of travel): with the flag it stops on the mesh, without it passes
+    tris = scenes.heightfield(cells=4, extent=8.0, amplitude=0.0, base=0.0)
+    nt = len(tris)
+    b = np.zeros(2, abi.BODY_DTYPE)
+    b["orientation"][:, 3] = 1.0
+    b["linear_damping"] = 0.998
+    b["angular_damping"] = 0.995
+    b["flags"] = abi.BODY_ACTIVE | abi.BODY_NO_GRAVITY
+    b["friction"] = 0.2
+    b["motion_type"][0] = abi.MOTION_STATIC
+    b["position"][1] = (0.3, 0.8, 0.3)
+    b["inv_mass"][1] = 1.0
+    b["inv_inertia"][1] = (1, 0, 0, 1, 0, 1)
+    b["velocity"][1] = (0, -100, 0)
+    if speculative:
+        b["flags"][1] |= abi.BODY_SPECULATIVE
+    s = np.zeros(nt + 1, abi.SHAPE_DTYPE)
+    s["kind"][:nt] = abi.SHAPE_TRIANGLE
+    s["body"][:nt] = 0
+    s["data_offset"][:nt] = np.arange(nt)
+    s["kind"][nt] = abi.SHAPE_SPHERE
+    s["body"][nt] = 1
+    s["dims"][nt, 0] = 0.1
+    sc = dict(bodies=b, shapes=s, hull=np.zeros((0, 3), np.float32), triangles=tris,
+              params=dict(gravity=(0.0, 0.0, 0.0)))
+    o = O.OracleWorld(sc)
+    o.step(0.01)
+    y = o.bodies()["position"][1, 1]
+    if speculative:
+        assert o.counters()["speculative"] >= 1
+        assert y > 0.0
+    else:
+        assert o.counters()["speculative"] == 0
+        assert y < -0.1
